@@ -1,0 +1,184 @@
+/*
+ * quest_gb300.h -- C ABI of the GB300 (sm_103a) gate-application backend.
+ *
+ * Each entry point replaces one GPU backend function of QuEST v4.1.0, named in
+ * its comment (file:line within the QuEST project).  A QuEST build reaches these
+ * through a thin shim that keeps the signatures of quest/src/gpu/gpu_subroutines.hpp
+ * and quest/src/gpu/gpu_config.hpp; the localiser and the
+ * accelerator above it are unchanged.
+ *
+ * Conventions
+ *  - amps: DEVICE pointer to interleaved complex amplitudes, FP64 (qg_cplx, the
+ *    layout of qcomp at FLOAT_PRECISION=2) unless the name ends in _f32.
+ *  - numQubits: qubits of the amplitude vector; for a density matrix routine
+ *    (qg_dm_*) numKetQubits is the Qureg's qubit count and the vector holds
+ *    4^numKetQubits amps (column-major Choi vector: row = low bits).
+ *  - ctrls / ctrlStates / targs / qubits: HOST int arrays.  ctrlStates may be
+ *    NULL, meaning every control must be 1 (the reference's default,
+ *    quest/src/core/localiser.cpp:58-67).
+ *  - matrices and factors: HOST pointers, read during the call.
+ *  - stream: a cudaStream_t (NULL = the legacy default stream).  Amplitude
+ *    routines are asynchronous like the reference's kernel launches; reductions
+ *    return a host value and therefore synchronise the stream, as the reference's
+ *    Thrust reductions do.
+ *  - Every function returns QG_OK (0) or a negative QG_ERR_* code; the message
+ *    of the last failure on the calling thread is in qg_get_last_error().
+ */
+#ifndef QUEST_GB300_H
+#define QUEST_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct { double re, im; } qg_cplx;   /* = qcomp at FLOAT_PRECISION=2 */
+typedef struct { float re, im; } qg_cplxf;   /* = qcomp at FLOAT_PRECISION=1 */
+
+#define QG_OK            0
+#define QG_ERR_CUDA     -1   /* a CUDA runtime call failed (reference: error_cudaCallFailed, errors.cpp:630) */
+#define QG_ERR_ARG      -2   /* invalid argument (qubit out of range, overlapping qubits, bad size ...) */
+#define QG_ERR_OOM      -3   /* device allocation failed (reference: gpu_allocArray returns nullptr, gpu_config.cpp:407-412) */
+#define QG_ERR_TIMEOUT  -4   /* a bounded device-side wait gave up */
+#define QG_ERR_NOTSUP   -5   /* configuration not supported by this build */
+
+const char* qg_get_last_error(void);
+const char* qg_get_error_string(int code);
+int  qg_get_version(void);                 /* 100*major + minor */
+
+/* ------------------------------------------------------------------ runtime
+ * replaces quest/src/gpu/gpu_config.hpp (gpu_config.cpp:124-663)            */
+
+int qg_init(int device);                                   /* gpu_bindLocalGPUsToNodes (gpu_config.cpp:332) + queries */
+int qg_get_num_devices(int* out);                          /* gpu_getNumberOfLocalGpus (gpu_config.cpp:124) */
+int qg_get_device_info(int* numSMs, int64_t* totalMem, int64_t* freeMem, int* ccMajor, int* ccMinor);
+int qg_alloc(void** out, int64_t numBytes);                /* gpu_allocArray (gpu_config.cpp:399-421) */
+int qg_free(void* ptr);                                    /* gpu_deallocArray (gpu_config.cpp:424-436) */
+int qg_copy_h2d(void* dst, const void* src, int64_t numBytes, void* stream);   /* gpu_copyCpuToGpu (gpu_config.cpp:535) */
+int qg_copy_d2h(void* dst, const void* src, int64_t numBytes, void* stream);   /* gpu_copyGpuToCpu (gpu_config.cpp:449-533) */
+int qg_copy_d2d(void* dst, const void* src, int64_t numBytes, void* stream);   /* gpu_copyArray (gpu_config.cpp:521-532) */
+int qg_sync(void);                                         /* gpu_sync (gpu_config.cpp:382-390) */
+int qg_stream_sync(void* stream);
+int qg_get_cache_size(int64_t* out);                       /* getGpuCacheSize (quest/src/api/debug.cpp:180) */
+int qg_clear_cache(void);                                  /* gpu_clearCache (gpu_config.cpp:665) */
+int qg_get_launch_count(int64_t* out);                     /* kernels launched by this library so far */
+
+/* ------------------------------------------------------------------ initialisation
+ * replaces gpu_statevec_initUniformState_sub / initDebugState_sub
+ * (gpu_subroutines.hpp:189-193; gpu_thrust.cuh:1053-1070)                    */
+
+int qg_sv_initUniformState(void* amps, int numQubits, qg_cplx amp, void* stream);
+int qg_sv_initClassicalState(void* amps, int numQubits, int64_t index, void* stream);   /* initZeroState / initClassicalState */
+int qg_sv_initDebugState(void* amps, int numQubits, void* stream);
+
+/* ------------------------------------------------------------------ statevector gates
+ * (a density matrix's Choi vector is passed here too, with numQubits = 2*numKetQubits) */
+
+/* gpu_statevec_anyCtrlSwap_subA (gpu_subroutines.hpp:50; gpu_subroutines.cpp:197-222) */
+int qg_sv_anyCtrlSwap(void* amps, int numQubits, const int* ctrls, const int* ctrlStates, int numCtrls,
+                      int targ1, int targ2, void* stream);
+
+/* gpu_statevec_anyCtrlOneTargDenseMatr_subA (gpu_subroutines.hpp:59; gpu_subroutines.cpp:286-315)
+ * matr: 2x2 row-major */
+int qg_sv_anyCtrlOneTargDenseMatr(void* amps, int numQubits, const int* ctrls, const int* ctrlStates, int numCtrls,
+                                  int targ, const qg_cplx* matr, void* stream);
+
+/* gpu_statevec_anyCtrlTwoTargDenseMatr_sub (gpu_subroutines.hpp:62; gpu_subroutines.cpp:354-385)
+ * matr: 4x4 row-major; matrix index bit 0 is targ1 */
+int qg_sv_anyCtrlTwoTargDenseMatr(void* amps, int numQubits, const int* ctrls, const int* ctrlStates, int numCtrls,
+                                  int targ1, int targ2, const qg_cplx* matr, void* stream);
+
+/* gpu_statevec_anyCtrlAnyTargDenseMatr_sub<NumCtrls,NumTargs,ApplyConj> (gpu_subroutines.hpp:64;
+ * gpu_subroutines.cpp:396-507).  matr: 2^k x 2^k row-major HOST elements; matrix
+ * index bit i is targs[i].  applyConj conjugates every element. */
+int qg_sv_anyCtrlAnyTargDenseMatr(void* amps, int numQubits, const int* ctrls, const int* ctrlStates, int numCtrls,
+                                  const int* targs, int numTargs, const qg_cplx* matr, int applyConj, void* stream);
+
+/* gpu_statevec_anyCtrlOneTargDiagMatr_sub (gpu_subroutines.hpp:71; gpu_subroutines.cpp:516-572) */
+int qg_sv_anyCtrlOneTargDiagMatr(void* amps, int numQubits, const int* ctrls, const int* ctrlStates, int numCtrls,
+                                 int targ, const qg_cplx* elems, void* stream);
+
+/* gpu_statevec_anyCtrlTwoTargDiagMatr_sub (gpu_subroutines.hpp:73; gpu_subroutines.cpp:584-641)
+ * elems index = (bit targ2) * 2 + (bit targ1) */
+int qg_sv_anyCtrlTwoTargDiagMatr(void* amps, int numQubits, const int* ctrls, const int* ctrlStates, int numCtrls,
+                                 int targ1, int targ2, const qg_cplx* elems, void* stream);
+
+/* gpu_statevec_anyCtrlAnyTargDiagMatr_sub<C,T,ApplyConj,HasPower> (gpu_subroutines.hpp:75;
+ * gpu_subroutines.cpp:653-709).  exponent == NULL (or 1+0i) means no power; the power
+ * is applied before the conjugation, as in the reference. */
+int qg_sv_anyCtrlAnyTargDiagMatr(void* amps, int numQubits, const int* ctrls, const int* ctrlStates, int numCtrls,
+                                 const int* targs, int numTargs, const qg_cplx* elems, int applyConj,
+                                 const qg_cplx* exponent, void* stream);
+
+/* gpu_statevector_anyCtrlPauliTensorOrGadget_subA<C,T> (gpu_subroutines.hpp:86;
+ * gpu_subroutines.cpp:779-820): amp pairs (iA, iA ^ maskXY) mixed as
+ * a'A = ampFac*aA + pairAmpFac*i^#Y*sign(iB)*aB */
+int qg_sv_anyCtrlPauliTensorOrGadget(void* amps, int numQubits, const int* ctrls, const int* ctrlStates, int numCtrls,
+                                     const int* targsX, int numX, const int* targsY, int numY, const int* targsZ, int numZ,
+                                     qg_cplx ampFac, qg_cplx pairAmpFac, void* stream);
+
+/* gpu_statevector_anyCtrlAnyTargZOrPhaseGadget_sub<C> (gpu_subroutines.hpp:90;
+ * gpu_subroutines.cpp:864-887): a *= (parity of targs even) ? fac0 : fac1 */
+int qg_sv_anyCtrlAnyTargZOrPhaseGadget(void* amps, int numQubits, const int* ctrls, const int* ctrlStates, int numCtrls,
+                                       const int* targs, int numTargs, qg_cplx fac0, qg_cplx fac1, void* stream);
+
+/* gpu_statevec_multiQubitProjector_sub<N> (gpu_subroutines.hpp:183; gpu_thrust.cuh:1014-1030) */
+int qg_sv_multiQubitProjector(void* amps, int numQubits, const int* qubits, const int* outcomes, int numQubitsProj,
+                              double prob, void* stream);
+
+/* ------------------------------------------------------------------ density-matrix channels */
+
+/* gpu_densmatr_multiQubitProjector_sub<N> (gpu_subroutines.hpp:184; gpu_thrust.cuh:1033-1048) */
+int qg_dm_multiQubitProjector(void* amps, int numKetQubits, const int* qubits, const int* outcomes, int numQubitsProj,
+                              double prob, void* stream);
+/* gpu_densmatr_oneQubitDepolarising_subA (gpu_subroutines.hpp:114; gpu_subroutines.cpp:1069-1086) */
+int qg_dm_oneQubitDepolarising(void* amps, int numKetQubits, int qubit, double prob, void* stream);
+/* gpu_densmatr_twoQubitDepolarising_subA + subB (gpu_subroutines.hpp:117-118), fused into one pass */
+int qg_dm_twoQubitDepolarising(void* amps, int numKetQubits, int qubit1, int qubit2, double prob, void* stream);
+/* gpu_densmatr_oneQubitDephasing_subA (gpu_subroutines.hpp:108) */
+int qg_dm_oneQubitDephasing(void* amps, int numKetQubits, int qubit, double prob, void* stream);
+/* gpu_densmatr_twoQubitDephasing_subA (gpu_subroutines.hpp:111) */
+int qg_dm_twoQubitDephasing(void* amps, int numKetQubits, int qubit1, int qubit2, double prob, void* stream);
+/* gpu_densmatr_oneQubitDamping_subA (gpu_subroutines.hpp:127) */
+int qg_dm_oneQubitDamping(void* amps, int numKetQubits, int qubit, double prob, void* stream);
+/* gpu_densmatr_oneQubitPauliChannel_subA (gpu_subroutines.hpp:124); probI = 1 - pX - pY - pZ */
+int qg_dm_oneQubitPauliChannel(void* amps, int numKetQubits, int qubit, double probX, double probY, double probZ, void* stream);
+
+/* ------------------------------------------------------------------ reductions (FP64 accumulation,
+ * fixed reduction tree: the same input gives the same bits on every run) */
+
+/* gpu_statevec_calcTotalProb_sub (gpu_subroutines.hpp:144; gpu_thrust.cuh:745-764) */
+int qg_sv_calcTotalProb(const void* amps, int numQubits, double* out, void* stream);
+/* gpu_densmatr_calcTotalProb_sub (gpu_subroutines.hpp:145; gpu_thrust.cuh:767-785) */
+int qg_dm_calcTotalProb(const void* amps, int numKetQubits, double* out, void* stream);
+/* gpu_statevec_calcProbOfMultiQubitOutcome_sub<N> (gpu_subroutines.hpp:147; gpu_thrust.cuh:788-805) */
+int qg_sv_calcProbOfMultiQubitOutcome(const void* amps, int numQubits, const int* qubits, const int* outcomes, int num,
+                                      double* out, void* stream);
+/* gpu_densmatr_calcProbOfMultiQubitOutcome_sub<N> (gpu_subroutines.hpp:148; gpu_thrust.cuh:808-832) */
+int qg_dm_calcProbOfMultiQubitOutcome(const void* amps, int numKetQubits, const int* qubits, const int* outcomes, int num,
+                                      double* out, void* stream);
+/* gpu_statevec_calcProbsOfAllMultiQubitOutcomes_sub<N> (gpu_subroutines.hpp:150; gpu_kernels.cuh:1145-1171);
+ * deterministic (no atomics on the probabilities). outProbs: HOST array of 2^num */
+int qg_sv_calcProbsOfAllMultiQubitOutcomes(double* outProbs, const void* amps, int numQubits, const int* qubits, int num,
+                                           void* stream);
+/* gpu_statevec_calcExpecAnyTargZ_sub (gpu_subroutines.hpp:169; gpu_thrust.cuh:888-900) */
+int qg_sv_calcExpecAnyTargZ(const void* amps, int numQubits, const int* targs, int numTargs, double* out, void* stream);
+/* gpu_densmatr_calcExpecAnyTargZ_sub (gpu_subroutines.hpp:170; gpu_thrust.cuh:903-915) */
+int qg_dm_calcExpecAnyTargZ(const void* amps, int numKetQubits, const int* targs, int numTargs, qg_cplx* out, void* stream);
+/* gpu_statevec_calcExpecPauliStr_subA (gpu_subroutines.hpp:173; gpu_thrust.cuh:918-932) */
+int qg_sv_calcExpecPauliStr(const void* amps, int numQubits, const int* targsX, int numX, const int* targsY, int numY,
+                            const int* targsZ, int numZ, qg_cplx* out, void* stream);
+/* gpu_densmatr_calcExpecPauliStr_sub (gpu_subroutines.hpp:175; gpu_thrust.cuh:953-974) */
+int qg_dm_calcExpecPauliStr(const void* amps, int numKetQubits, const int* targsX, int numX, const int* targsY, int numY,
+                            const int* targsZ, int numZ, qg_cplx* out, void* stream);
+/* Many Pauli strings in ONE pass over a statevector (batched calcExpecPauliStr, the
+ * per-term loop of localiser_statevec_calcExpecPauliStrSum, localiser.cpp:2052-2148).
+ * Strings are given as (maskXY, maskYZ, numY) triples; out[s] is string s's value. */
+int qg_sv_calcExpecPauliStrBatch(const void* amps, int numQubits, const int64_t* masksXY, const int64_t* masksYZ,
+                                 const int* numsY, int numStrings, qg_cplx* out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* QUEST_GB300_H */

@@ -1,0 +1,286 @@
+// Runtime services of the backend: device binding, allocation, copies, error
+// reporting and the library-owned scratch cache.  Replaces the role of QuEST's
+// quest/src/gpu/gpu_config.cpp for the gate path (allocation gpu_config.cpp:399-436,
+// copies :449-633, sync :382-390, the scratch cache :639-669).
+#include "qg_common.cuh"
+
+#include <algorithm>
+#include <atomic>
+#include <cstdarg>
+#include <cstdio>
+#include <mutex>
+#include <vector>
+
+namespace {
+thread_local std::string g_last_error;
+std::atomic<long long> g_launches{0};
+
+struct DeviceCache {
+    void* scratch = nullptr;
+    size_t scratchBytes = 0;
+    void* pinned = nullptr;
+    size_t pinnedBytes = 0;
+    int numSMs = 0;
+};
+std::mutex g_cache_mutex;
+std::vector<DeviceCache> g_caches;
+
+DeviceCache& cache_for_current() {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(g_cache_mutex);
+    if ((int)g_caches.size() <= dev) g_caches.resize(dev + 1);
+    return g_caches[dev];
+}
+}  // namespace
+
+void qg_set_error(const char* fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+}
+
+int qg_fail(int code, const char* fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+int qg_check_cuda(cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return QG_OK;
+    if (e == cudaErrorMemoryAllocation) {
+        cudaGetLastError();
+        return qg_fail(QG_ERR_OOM, "%s: %s", what, cudaGetErrorString(e));
+    }
+    return qg_fail(QG_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+int qg_check_launch(const char* what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return qg_fail(QG_ERR_CUDA, "launch of %s failed: %s", what, cudaGetErrorString(e));
+    return QG_OK;
+}
+
+void qg_note_launch(int n) { g_launches += n; }
+
+int qg_num_sms() {
+    DeviceCache& c = cache_for_current();
+    if (c.numSMs == 0) {
+        int dev = 0, n = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        c.numSMs = n > 0 ? n : 1;
+    }
+    return c.numSMs;
+}
+
+int qg_scratch_get(void** out, size_t bytes) {
+    DeviceCache& c = cache_for_current();
+    if (c.scratchBytes < bytes) {
+        if (c.scratch) {
+            // the old cache may still be read by queued kernels on any stream
+            QG_CUDA(cudaDeviceSynchronize());
+            QG_CUDA(cudaFree(c.scratch));
+            c.scratch = nullptr;
+            c.scratchBytes = 0;
+        }
+        size_t want = std::max(bytes, (size_t)1 << 20);
+        QG_CUDA(cudaMalloc(&c.scratch, want));
+        QG_CUDA(cudaMemset(c.scratch, 0, want));
+        c.scratchBytes = want;
+    }
+    *out = c.scratch;
+    return QG_OK;
+}
+
+int qg_pinned_result(void** out, size_t bytes) {
+    DeviceCache& c = cache_for_current();
+    if (c.pinnedBytes < bytes) {
+        if (c.pinned) QG_CUDA(cudaFreeHost(c.pinned));
+        c.pinned = nullptr;
+        size_t want = std::max(bytes, (size_t)4096);
+        QG_CUDA(cudaMallocHost(&c.pinned, want));
+        c.pinnedBytes = want;
+    }
+    *out = c.pinned;
+    return QG_OK;
+}
+
+int qg_check_qubits(int numQubits, const int* qubits, int num, const char* what) {
+    if (num < 0) return qg_fail(QG_ERR_ARG, "%s: negative count", what);
+    if (num > 0 && qubits == nullptr) return qg_fail(QG_ERR_ARG, "%s: null qubit list", what);
+    unsigned long long seen = 0;
+    for (int i = 0; i < num; i++) {
+        int q = qubits[i];
+        if (q < 0 || q >= numQubits) return qg_fail(QG_ERR_ARG, "%s: qubit %d is outside [0, %d)", what, q, numQubits);
+        if (seen & (1ULL << q)) return qg_fail(QG_ERR_ARG, "%s: qubit %d appears twice", what, q);
+        seen |= 1ULL << q;
+    }
+    return QG_OK;
+}
+
+int qg_check_amps(const void* amps, int numQubits) {
+    if (amps == nullptr) return qg_fail(QG_ERR_ARG, "null amplitude pointer");
+    if (numQubits < 1 || numQubits > QG_MAX_QUBITS) return qg_fail(QG_ERR_ARG, "numQubits %d outside [1, %d]", numQubits, QG_MAX_QUBITS);
+    if (((uintptr_t)amps) & 15) return qg_fail(QG_ERR_ARG, "amplitude pointer is not 16-byte aligned");
+    return QG_OK;
+}
+
+int qg_make_plan(int numQubits, const int* ctrls, const int* ctrlStates, int numCtrls,
+                 const int* extraQubits, const int* extraValues, int numExtra, QubitPlan* plan) {
+    int all[64];
+    int n = numCtrls + numExtra;
+    if (n > QG_MAX_INSERT) return qg_fail(QG_ERR_NOTSUP, "%d controls+targets exceed the supported %d", n, QG_MAX_INSERT);
+    if (n > numQubits) return qg_fail(QG_ERR_ARG, "%d controls+targets exceed %d qubits", n, numQubits);
+    plan->stateMask = 0;
+    for (int i = 0; i < numCtrls; i++) {
+        all[i] = ctrls[i];
+        int st = ctrlStates ? ctrlStates[i] : 1;
+        if (st != 0 && st != 1) return qg_fail(QG_ERR_ARG, "control state %d is not 0 or 1", st);
+        if (st) plan->stateMask |= (qidx)1 << ctrls[i];
+    }
+    for (int i = 0; i < numExtra; i++) {
+        all[numCtrls + i] = extraQubits[i];
+        if (extraValues && extraValues[i]) plan->stateMask |= (qidx)1 << extraQubits[i];
+    }
+    QG_TRY(qg_check_qubits(numQubits, all, n, "controls/targets"));
+    std::sort(all, all + n);
+    plan->ins.num = n;
+    for (int i = 0; i < n; i++) plan->ins.low[i] = ((qidx)1 << all[i]) - 1;
+    plan->numFixed = n;
+    return QG_OK;
+}
+
+extern "C" {
+
+const char* qg_get_last_error(void) { return g_last_error.c_str(); }
+
+const char* qg_get_error_string(int code) {
+    switch (code) {
+        case QG_OK: return "success";
+        case QG_ERR_CUDA: return "CUDA runtime error";
+        case QG_ERR_ARG: return "invalid argument";
+        case QG_ERR_OOM: return "device allocation failed";
+        case QG_ERR_TIMEOUT: return "device-side wait timed out";
+        case QG_ERR_NOTSUP: return "not supported";
+        default: return "unknown error";
+    }
+}
+
+int qg_get_version(void) { return 100; }
+
+int qg_init(int device) {
+    int n = 0;
+    QG_CUDA(cudaGetDeviceCount(&n));
+    if (device < 0 || device >= n) return qg_fail(QG_ERR_ARG, "device %d outside [0, %d)", device, n);
+    QG_CUDA(cudaSetDevice(device));
+    QG_CUDA(cudaFree(0));  // create the primary context now
+    qg_num_sms();
+    return QG_OK;
+}
+
+int qg_get_num_devices(int* out) {
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        n = 0;
+    }
+    *out = n;
+    return QG_OK;
+}
+
+int qg_get_device_info(int* numSMs, int64_t* totalMem, int64_t* freeMem, int* ccMajor, int* ccMinor) {
+    int dev = 0;
+    QG_CUDA(cudaGetDevice(&dev));
+    cudaDeviceProp p;
+    QG_CUDA(cudaGetDeviceProperties(&p, dev));
+    size_t fr = 0, tot = 0;
+    QG_CUDA(cudaMemGetInfo(&fr, &tot));
+    if (numSMs) *numSMs = p.multiProcessorCount;
+    if (totalMem) *totalMem = (int64_t)tot;
+    if (freeMem) *freeMem = (int64_t)fr;
+    if (ccMajor) *ccMajor = p.major;
+    if (ccMinor) *ccMinor = p.minor;
+    return QG_OK;
+}
+
+int qg_alloc(void** out, int64_t numBytes) {
+    if (!out) return qg_fail(QG_ERR_ARG, "null output pointer");
+    *out = nullptr;
+    if (numBytes <= 0) return qg_fail(QG_ERR_ARG, "allocation of %lld bytes", (long long)numBytes);
+    cudaError_t e = cudaMalloc(out, (size_t)numBytes);
+    if (e != cudaSuccess) {
+        *out = nullptr;
+        return qg_check_cuda(e, "cudaMalloc");
+    }
+    return QG_OK;
+}
+
+int qg_free(void* ptr) {
+    if (ptr) QG_CUDA(cudaFree(ptr));
+    return QG_OK;
+}
+
+int qg_copy_h2d(void* dst, const void* src, int64_t numBytes, void* stream) {
+    if (numBytes < 0 || (numBytes > 0 && (!dst || !src))) return qg_fail(QG_ERR_ARG, "bad copy arguments");
+    if (numBytes == 0) return QG_OK;
+    QG_CUDA(cudaMemcpyAsync(dst, src, (size_t)numBytes, cudaMemcpyHostToDevice, qg_stream(stream)));
+    return QG_OK;
+}
+
+int qg_copy_d2h(void* dst, const void* src, int64_t numBytes, void* stream) {
+    if (numBytes < 0 || (numBytes > 0 && (!dst || !src))) return qg_fail(QG_ERR_ARG, "bad copy arguments");
+    if (numBytes == 0) return QG_OK;
+    QG_CUDA(cudaMemcpyAsync(dst, src, (size_t)numBytes, cudaMemcpyDeviceToHost, qg_stream(stream)));
+    QG_CUDA(cudaStreamSynchronize(qg_stream(stream)));
+    return QG_OK;
+}
+
+int qg_copy_d2d(void* dst, const void* src, int64_t numBytes, void* stream) {
+    if (numBytes < 0 || (numBytes > 0 && (!dst || !src))) return qg_fail(QG_ERR_ARG, "bad copy arguments");
+    if (numBytes == 0) return QG_OK;
+    QG_CUDA(cudaMemcpyAsync(dst, src, (size_t)numBytes, cudaMemcpyDeviceToDevice, qg_stream(stream)));
+    return QG_OK;
+}
+
+int qg_sync(void) {
+    QG_CUDA(cudaDeviceSynchronize());
+    return QG_OK;
+}
+
+int qg_stream_sync(void* stream) {
+    QG_CUDA(cudaStreamSynchronize(qg_stream(stream)));
+    return QG_OK;
+}
+
+int qg_get_cache_size(int64_t* out) {
+    DeviceCache& c = cache_for_current();
+    *out = (int64_t)c.scratchBytes;
+    return QG_OK;
+}
+
+int qg_clear_cache(void) {
+    DeviceCache& c = cache_for_current();
+    if (c.scratch) {
+        QG_CUDA(cudaDeviceSynchronize());
+        QG_CUDA(cudaFree(c.scratch));
+    }
+    c.scratch = nullptr;
+    c.scratchBytes = 0;
+    return QG_OK;
+}
+
+int qg_get_launch_count(int64_t* out) {
+    *out = (int64_t)g_launches.load();
+    return QG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,681 @@
+// Statevector amplitude kernels of the sm_103a backend (FP64).
+//
+// One thread owns one amplitude group (a pair for one-target gates, a quad for
+// two-target gates, a 2^k block for k-target dense matrices, a single amplitude
+// for diagonals).  Group bases come from bit insertion over the sorted control
+// and target positions (qg_common.cuh), so a warp reads 32 consecutive groups:
+// coalesced 16-byte loads for every target position.  Matrices of up to five
+// targets travel in the kernel's parameter space, which the whole warp reads
+// with uniform (broadcast) constant-bank loads.  Gates whose structure permits
+// it (real matrices, gadgets with a real diagonal factor, permutations, unit
+// diagonal entries) run reduced-arithmetic variants, because FP64 issue rate
+// rather than HBM bandwidth bounds general complex gates on this part.
+//
+// Reference algorithms: quest/src/cpu/cpu_subroutines.cpp (index maps and
+// arithmetic of each cpu_statevec_* routine) and quest/src/gpu/gpu_kernels.cuh.
+#include "qg_common.cuh"
+
+#include <cmath>
+#include <complex>
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+// ============================================================== initialisation
+
+__global__ void k_init_uniform(double2* __restrict__ a, qidx n, double2 v) {
+    qidx i = blockIdx.x * (qidx)blockDim.x + threadIdx.x;
+    if (i < n) st_amp(a + i, v);
+}
+
+__global__ void k_set_one(double2* __restrict__ a, qidx index, double2 v) { a[index] = v; }
+
+// initDebugState: amp_k = (2k + i(2k+1)) / 10 (cpu_subroutines.cpp:2364-2376)
+__global__ void k_init_debug(double2* __restrict__ a, qidx n) {
+    qidx i = blockIdx.x * (qidx)blockDim.x + threadIdx.x;
+    if (i < n) st_amp(a + i, make_double2((2.0 * i) / 10.0, (2.0 * i + 1.0) / 10.0));
+}
+
+// ============================================================== swap
+// cpu_statevec_anyCtrlSwap_subA (cpu_subroutines.cpp:255-280): i01 has the higher
+// target at 0 and the lower at 1; it trades places with i10.
+
+template <int NB>
+__global__ void k_swap(double2* __restrict__ a, qidx numIts, Ins ins, qidx mask, qidx flip) {
+    qidx n = blockIdx.x * (qidx)blockDim.x + threadIdx.x;
+    if (n >= numIts) return;
+    qidx i01 = insert_bits<NB>(n, ins) | mask;
+    qidx i10 = i01 ^ flip;
+    double2 x = ld_amp(a + i01), y = ld_amp(a + i10);
+    st_amp(a + i01, y);
+    st_amp(a + i10, x);
+}
+
+// ============================================================== one-target dense
+
+struct Mat1 { double2 m[4]; };
+
+// MODE 0: general complex 2x2; MODE 1: real 2x2 (imaginary parts all zero)
+template <int NB, int MODE>
+__global__ void k_dense1(double2* __restrict__ a, qidx numIts, Ins ins, qidx mask, qidx tbit, Mat1 M) {
+    qidx n = blockIdx.x * (qidx)blockDim.x + threadIdx.x;
+    if (n >= numIts) return;
+    qidx i0 = insert_bits<NB>(n, ins) | mask;
+    qidx i1 = i0 | tbit;
+    double2 x = ld_amp(a + i0), y = ld_amp(a + i1);
+    double2 o0, o1;
+    if (MODE == 1) {
+        o0 = make_double2(fma(M.m[0].x, x.x, M.m[1].x * y.x), fma(M.m[0].x, x.y, M.m[1].x * y.y));
+        o1 = make_double2(fma(M.m[2].x, x.x, M.m[3].x * y.x), fma(M.m[2].x, x.y, M.m[3].x * y.y));
+    } else {
+        o0 = cfma(M.m[0], x, cmul(M.m[1], y));
+        o1 = cfma(M.m[2], x, cmul(M.m[3], y));
+    }
+    st_amp(a + i0, o0);
+    st_amp(a + i1, o1);
+}
+
+// ============================================================== two-target dense
+
+struct Mat2 { double2 m[16]; };
+
+template <int NB>
+__global__ void k_dense2(double2* __restrict__ a, qidx numIts, Ins ins, qidx mask, qidx b1, qidx b2, Mat2 M) {
+    qidx n = blockIdx.x * (qidx)blockDim.x + threadIdx.x;
+    if (n >= numIts) return;
+    qidx i00 = insert_bits<NB>(n, ins) | mask;
+    qidx idx[4] = {i00, i00 | b1, i00 | b2, i00 | b1 | b2};
+    double2 v[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) v[j] = ld_amp(a + idx[j]);
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        double2 acc = cmul(M.m[4 * r], v[0]);
+#pragma unroll
+        for (int j = 1; j < 4; j++) acc = cfma(M.m[4 * r + j], v[j], acc);
+        st_amp(a + idx[r], acc);
+    }
+}
+
+// ============================================================== few-target dense (3..5 targets)
+// Each thread caches its 2^K amplitudes in registers; the matrix (already
+// conjugated if requested) sits in parameter space.
+
+template <int K>
+struct MatK {
+    double2 m[1 << (2 * K)];
+    qidx off[1 << K];   // offset of matrix index j from the group base
+};
+
+template <int K, int NB>
+__global__ void __launch_bounds__(128) k_denseK(double2* __restrict__ a, qidx numIts, Ins ins, qidx mask, MatK<K> M) {
+    qidx n = blockIdx.x * (qidx)blockDim.x + threadIdx.x;
+    if (n >= numIts) return;
+    constexpr int D = 1 << K;
+    qidx base = insert_bits<NB>(n, ins) | mask;
+    double2 v[D];
+#pragma unroll
+    for (int j = 0; j < D; j++) v[j] = ld_amp(a + base + M.off[j]);
+#pragma unroll
+    for (int r = 0; r < D; r++) {
+        double2 acc = cmul(M.m[r * D], v[0]);
+#pragma unroll
+        for (int j = 1; j < D; j++) acc = cfma(M.m[r * D + j], v[j], acc);
+        st_amp(a + base + M.off[r], acc);
+    }
+}
+
+// ============================================================== many-target dense (>= 6 targets)
+// One CTA per 2^K block: the block's amplitudes are staged in `cache` (shared
+// memory, or a per-CTA slot of global scratch beyond shared capacity), then each
+// thread forms whole output rows from the column-major matrix in global memory.
+
+__global__ void k_denseMany(double2* __restrict__ a, qidx numBlocks, int K, Ins ins, qidx mask,
+                            const qidx* __restrict__ off, const double2* __restrict__ McolMajor,
+                            double2* __restrict__ globalCache) {
+    extern __shared__ double2 smem[];
+    const int D = 1 << K;
+    double2* cache = globalCache ? globalCache + (qidx)blockIdx.x * D : smem;
+    for (qidx blk = blockIdx.x; blk < numBlocks; blk += gridDim.x) {
+        qidx base = insert_bits<-1>(blk, ins) | mask;
+        for (int j = threadIdx.x; j < D; j += blockDim.x) cache[j] = a[base + off[j]];
+        __syncthreads();
+        for (int r = threadIdx.x; r < D; r += blockDim.x) {
+            double2 acc = make_double2(0, 0);
+            for (int j = 0; j < D; j++) acc = cfma(McolMajor[(qidx)j * D + r], cache[j], acc);
+            a[base + off[r]] = acc;
+        }
+        __syncthreads();
+    }
+}
+
+// ============================================================== diagonals
+
+// MODE 0: factor d[bit t]; MODE 1: single factor d0 on every visited amplitude
+template <int NB, int MODE>
+__global__ void k_diag1(double2* __restrict__ a, qidx numIts, Ins ins, qidx mask, qidx tbit, double2 d0, double2 d1) {
+    qidx n = blockIdx.x * (qidx)blockDim.x + threadIdx.x;
+    if (n >= numIts) return;
+    qidx i = insert_bits<NB>(n, ins) | mask;
+    double2 f = (MODE == 1) ? d0 : ((i & tbit) ? d1 : d0);
+    st_amp(a + i, cmul(f, ld_amp(a + i)));
+}
+
+struct Diag4 { double2 d[4]; };
+
+template <int NB>
+__global__ void k_diag2(double2* __restrict__ a, qidx numIts, Ins ins, qidx mask, int t1, int t2, Diag4 D) {
+    qidx n = blockIdx.x * (qidx)blockDim.x + threadIdx.x;
+    if (n >= numIts) return;
+    qidx i = insert_bits<NB>(n, ins) | mask;
+    int k = (int)(((i >> t2) & 1) << 1 | ((i >> t1) & 1));
+    st_amp(a + i, cmul(D.d[k], ld_amp(a + i)));
+}
+
+#define QG_DIAG_PARAM_MAX 10   // up to 2^10 diagonal elements in parameter space
+
+struct DiagK {
+    double2 d[1 << QG_DIAG_PARAM_MAX];
+    int t[QG_DIAG_PARAM_MAX];
+    int k;
+};
+struct DiagKDev {
+    const double2* d;
+    int t[QG_MAX_QUBITS];
+    int k;
+};
+
+template <int NB, typename DT>
+__device__ __forceinline__ double2 diagk_elem(const DT& D, qidx i);
+
+template <int NB>
+__global__ void k_diagK(double2* __restrict__ a, qidx numIts, Ins ins, qidx mask, DiagK D) {
+    qidx n = blockIdx.x * (qidx)blockDim.x + threadIdx.x;
+    if (n >= numIts) return;
+    qidx i = insert_bits<NB>(n, ins) | mask;
+    int v = 0;
+    for (int b = 0; b < D.k; b++) v |= (int)((i >> D.t[b]) & 1) << b;
+    st_amp(a + i, cmul(D.d[v], ld_amp(a + i)));
+}
+
+template <int NB>
+__global__ void k_diagKdev(double2* __restrict__ a, qidx numIts, Ins ins, qidx mask, DiagKDev D) {
+    qidx n = blockIdx.x * (qidx)blockDim.x + threadIdx.x;
+    if (n >= numIts) return;
+    qidx i = insert_bits<NB>(n, ins) | mask;
+    qidx v = 0;
+    for (int b = 0; b < D.k; b++) v |= ((i >> D.t[b]) & 1) << b;
+    st_amp(a + i, cmul(__ldg(D.d + v), ld_amp(a + i)));
+}
+
+// ============================================================== Pauli tensors and gadgets
+// Pairs (iA, iB = iA ^ maskXY), enumerated by fixing the highest X/Y target of
+// iA to zero: the same set of pairs as cpu_statevector_anyCtrlPauliTensorOrGadget_subA
+// (cpu_subroutines.cpp:802-906), each visited once.
+//   a'A = f0*aA + f1*sign(iB)*aB,  a'B = f0*aB + f1*sign(iA)*aA
+// with sign(i) = (-1)^parity(i & maskYZ) and f1 already scaled by i^numY.
+
+__device__ __forceinline__ double neg_if(double x, int s) {
+    return __longlong_as_double(__double_as_longlong(x) ^ ((long long)s << 63));
+}
+
+// MODE 0: general complex f0, f1.  MODE 1: f0 real, f1 real (f1.y == 0).
+// MODE 2: f0 real, f1 imaginary (f1.x == 0).  MODE 3: f0 == 0, f1 in {1,i,-1,-i}: pure permutation.
+template <int NB, int MODE>
+__global__ void k_pauli(double2* __restrict__ a, qidx numIts, Ins ins, qidx mask, qidx maskXY, qidx maskYZ,
+                        double2 f0, double2 f1) {
+    qidx n = blockIdx.x * (qidx)blockDim.x + threadIdx.x;
+    if (n >= numIts) return;
+    qidx iA = insert_bits<NB>(n, ins) | mask;
+    qidx iB = iA ^ maskXY;
+    int sA = parity64(iA & maskYZ), sB = parity64(iB & maskYZ);   // 1 means minus
+    double2 x = ld_amp(a + iA), y = ld_amp(a + iB);
+    double2 oA, oB;
+    if (MODE == 0) {
+        double2 gA = make_double2(neg_if(f1.x, sB), neg_if(f1.y, sB));
+        double2 gB = make_double2(neg_if(f1.x, sA), neg_if(f1.y, sA));
+        oA = cfma(f0, x, cmul(gA, y));
+        oB = cfma(f0, y, cmul(gB, x));
+    } else if (MODE == 1) {
+        double gA = neg_if(f1.x, sB), gB = neg_if(f1.x, sA);
+        oA = make_double2(fma(f0.x, x.x, gA * y.x), fma(f0.x, x.y, gA * y.y));
+        oB = make_double2(fma(f0.x, y.x, gB * x.x), fma(f0.x, y.y, gB * x.y));
+    } else if (MODE == 2) {
+        // f1 = i*g: (i g) * (yr + i yi) = (-g yi, g yr)
+        double gA = neg_if(f1.y, sB), gB = neg_if(f1.y, sA);
+        oA = make_double2(fma(f0.x, x.x, -gA * y.y), fma(f0.x, x.y, gA * y.x));
+        oB = make_double2(fma(f0.x, y.x, -gB * x.y), fma(f0.x, y.y, gB * x.x));
+    } else {
+        // f1 in {1, i, -1, -i}: multiply by a unit of the Gaussian integers without FP work
+        bool imag = (f1.y != 0.0);
+        int neg = imag ? (f1.y < 0) : (f1.x < 0);
+        if (imag) {   // (i s)(yr + i yi) = (-s yi, s yr)
+            oA = make_double2(neg_if(y.y, !(neg ^ sB)), neg_if(y.x, neg ^ sB));
+            oB = make_double2(neg_if(x.y, !(neg ^ sA)), neg_if(x.x, neg ^ sA));
+        } else {
+            oA = make_double2(neg_if(y.x, neg ^ sB), neg_if(y.y, neg ^ sB));
+            oB = make_double2(neg_if(x.x, neg ^ sA), neg_if(x.y, neg ^ sA));
+        }
+    }
+    st_amp(a + iA, oA);
+    st_amp(a + iB, oB);
+}
+
+// cpu_statevector_anyCtrlAnyTargZOrPhaseGadget_sub (cpu_subroutines.cpp:962-990).
+// MODE 0: general complex factors.  MODE 1: f0 = 1 and f1 = -1 (Z tensor): only
+// odd-parity amplitudes change, by a sign flip.
+template <int NB, int MODE>
+__global__ void k_zphase(double2* __restrict__ a, qidx numIts, Ins ins, qidx mask, qidx tmask, double2 f0, double2 f1) {
+    qidx n = blockIdx.x * (qidx)blockDim.x + threadIdx.x;
+    if (n >= numIts) return;
+    qidx i = insert_bits<NB>(n, ins) | mask;
+    int p = parity64(i & tmask);
+    double2 x = ld_amp(a + i);
+    if (MODE == 1) {
+        st_amp(a + i, make_double2(neg_if(x.x, p), neg_if(x.y, p)));
+    } else {
+        st_amp(a + i, cmul(p ? f1 : f0, x));
+    }
+}
+
+// cpu_statevec_multiQubitProjector_sub (cpu_subroutines.cpp:2281-2306)
+__global__ void k_projector(double2* __restrict__ a, qidx numAmps, qidx qmask, qidx retainBits, double renorm) {
+    qidx i = blockIdx.x * (qidx)blockDim.x + threadIdx.x;
+    if (i >= numAmps) return;
+    if ((i & qmask) == retainBits) {
+        double2 x = ld_amp(a + i);
+        st_amp(a + i, make_double2(renorm * x.x, renorm * x.y));
+    } else {
+        st_amp(a + i, make_double2(0.0, 0.0));
+    }
+}
+
+// ============================================================== host side
+
+namespace {
+
+double2 d2(qg_cplx c) { return make_double2(c.re, c.im); }
+
+#define QG_LAUNCH_PLAIN(KERNEL, NBV, ...) \
+    KERNEL<NBV><<<qg_blocks(numIts), QG_THREADS, 0, st>>>(__VA_ARGS__)
+
+}  // namespace
+
+extern "C" {
+
+int qg_sv_initUniformState(void* amps, int numQubits, qg_cplx amp, void* stream) {
+    QG_TRY(qg_check_amps(amps, numQubits));
+    qidx n = (qidx)1 << numQubits;
+    k_init_uniform<<<qg_blocks(n), QG_THREADS, 0, qg_stream(stream)>>>((double2*)amps, n, d2(amp));
+    qg_note_launch();
+    return qg_check_launch("init_uniform");
+}
+
+int qg_sv_initClassicalState(void* amps, int numQubits, int64_t index, void* stream) {
+    QG_TRY(qg_check_amps(amps, numQubits));
+    qidx n = (qidx)1 << numQubits;
+    if (index < 0 || index >= n) return qg_fail(QG_ERR_ARG, "basis index %lld outside [0, %lld)", (long long)index, n);
+    k_init_uniform<<<qg_blocks(n), QG_THREADS, 0, qg_stream(stream)>>>((double2*)amps, n, make_double2(0, 0));
+    k_set_one<<<1, 1, 0, qg_stream(stream)>>>((double2*)amps, index, make_double2(1, 0));
+    qg_note_launch(2);
+    return qg_check_launch("init_classical");
+}
+
+int qg_sv_initDebugState(void* amps, int numQubits, void* stream) {
+    QG_TRY(qg_check_amps(amps, numQubits));
+    qidx n = (qidx)1 << numQubits;
+    k_init_debug<<<qg_blocks(n), QG_THREADS, 0, qg_stream(stream)>>>((double2*)amps, n);
+    qg_note_launch();
+    return qg_check_launch("init_debug");
+}
+
+int qg_sv_anyCtrlSwap(void* amps, int numQubits, const int* ctrls, const int* ctrlStates, int numCtrls,
+                      int targ1, int targ2, void* stream) {
+    QG_TRY(qg_check_amps(amps, numQubits));
+    if (targ1 == targ2) return qg_fail(QG_ERR_ARG, "swap targets must differ");
+    if (targ1 > targ2) { int t = targ1; targ1 = targ2; targ2 = t; }
+    int tq[2] = {targ2, targ1}, tv[2] = {0, 1};
+    QubitPlan p;
+    QG_TRY(qg_make_plan(numQubits, ctrls, ctrlStates, numCtrls, tq, tv, 2, &p));
+    qidx numIts = ((qidx)1 << numQubits) >> p.numFixed;
+    qidx flip = ((qidx)1 << targ1) | ((qidx)1 << targ2);
+    cudaStream_t st = qg_stream(stream);
+#define L(NBV) QG_LAUNCH_PLAIN(k_swap, NBV, (double2*)amps, numIts, p.ins, p.stateMask, flip)
+    QG_DISPATCH_NB(p.numFixed, L)
+#undef L
+    qg_note_launch();
+    return qg_check_launch("swap");
+}
+
+int qg_sv_anyCtrlOneTargDenseMatr(void* amps, int numQubits, const int* ctrls, const int* ctrlStates, int numCtrls,
+                                  int targ, const qg_cplx* matr, void* stream) {
+    QG_TRY(qg_check_amps(amps, numQubits));
+    if (!matr) return qg_fail(QG_ERR_ARG, "null matrix");
+    int tv = 0;
+    QubitPlan p;
+    QG_TRY(qg_make_plan(numQubits, ctrls, ctrlStates, numCtrls, &targ, &tv, 1, &p));
+    Mat1 M;
+    bool real = true;
+    for (int i = 0; i < 4; i++) {
+        M.m[i] = d2(matr[i]);
+        if (matr[i].im != 0.0) real = false;
+    }
+    qidx numIts = ((qidx)1 << numQubits) >> p.numFixed;
+    qidx tbit = (qidx)1 << targ;
+    cudaStream_t st = qg_stream(stream);
+    if (real) {
+#define L(NBV) k_dense1<NBV, 1><<<qg_blocks(numIts), QG_THREADS, 0, st>>>((double2*)amps, numIts, p.ins, p.stateMask, tbit, M)
+        QG_DISPATCH_NB(p.numFixed, L)
+#undef L
+    } else {
+#define L(NBV) k_dense1<NBV, 0><<<qg_blocks(numIts), QG_THREADS, 0, st>>>((double2*)amps, numIts, p.ins, p.stateMask, tbit, M)
+        QG_DISPATCH_NB(p.numFixed, L)
+#undef L
+    }
+    qg_note_launch();
+    return qg_check_launch("dense1");
+}
+
+int qg_sv_anyCtrlTwoTargDenseMatr(void* amps, int numQubits, const int* ctrls, const int* ctrlStates, int numCtrls,
+                                  int targ1, int targ2, const qg_cplx* matr, void* stream) {
+    QG_TRY(qg_check_amps(amps, numQubits));
+    if (!matr) return qg_fail(QG_ERR_ARG, "null matrix");
+    int tq[2] = {targ1, targ2}, tv[2] = {0, 0};
+    QubitPlan p;
+    QG_TRY(qg_make_plan(numQubits, ctrls, ctrlStates, numCtrls, tq, tv, 2, &p));
+    Mat2 M;
+    for (int i = 0; i < 16; i++) M.m[i] = d2(matr[i]);
+    qidx numIts = ((qidx)1 << numQubits) >> p.numFixed;
+    qidx b1 = (qidx)1 << targ1, b2 = (qidx)1 << targ2;
+    cudaStream_t st = qg_stream(stream);
+#define L(NBV) QG_LAUNCH_PLAIN(k_dense2, NBV, (double2*)amps, numIts, p.ins, p.stateMask, b1, b2, M)
+    QG_DISPATCH_NB(p.numFixed, L)
+#undef L
+    qg_note_launch();
+    return qg_check_launch("dense2");
+}
+
+}  // extern "C"
+
+namespace {
+
+template <int K>
+int launch_denseK(double2* amps, qidx numIts, const QubitPlan& p, const qg_cplx* matr, const int* targs, int conj, cudaStream_t st) {
+    MatK<K> M;
+    constexpr int D = 1 << K;
+    for (int i = 0; i < D * D; i++) M.m[i] = make_double2(matr[i].re, conj ? -matr[i].im : matr[i].im);
+    for (int j = 0; j < D; j++) {
+        qidx o = 0;
+        for (int b = 0; b < K; b++)
+            if ((j >> b) & 1) o |= (qidx)1 << targs[b];
+        M.off[j] = o;
+    }
+    unsigned blocks = (unsigned)((numIts + 127) / 128);
+#define L(NBV) k_denseK<K, NBV><<<blocks, 128, 0, st>>>(amps, numIts, p.ins, p.stateMask, M)
+    QG_DISPATCH_NB(p.numFixed, L)
+#undef L
+    return QG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int qg_sv_anyCtrlAnyTargDenseMatr(void* amps, int numQubits, const int* ctrls, const int* ctrlStates, int numCtrls,
+                                  const int* targs, int numTargs, const qg_cplx* matr, int applyConj, void* stream) {
+    QG_TRY(qg_check_amps(amps, numQubits));
+    if (!matr) return qg_fail(QG_ERR_ARG, "null matrix");
+    if (numTargs < 1) return qg_fail(QG_ERR_ARG, "at least one target is required");
+    if (numTargs <= 2) {
+        // the bespoke one- and two-target kernels (as localiser.cpp:1051-1076 diverts)
+        int D = 1 << numTargs;
+        qg_cplx m[16];
+        for (int i = 0; i < D * D; i++) m[i] = {matr[i].re, applyConj ? -matr[i].im : matr[i].im};
+        if (numTargs == 1) return qg_sv_anyCtrlOneTargDenseMatr(amps, numQubits, ctrls, ctrlStates, numCtrls, targs[0], m, stream);
+        return qg_sv_anyCtrlTwoTargDenseMatr(amps, numQubits, ctrls, ctrlStates, numCtrls, targs[0], targs[1], m, stream);
+    }
+    std::vector<int> zeros(numTargs, 0);
+    QubitPlan p;
+    QG_TRY(qg_make_plan(numQubits, ctrls, ctrlStates, numCtrls, targs, zeros.data(), numTargs, &p));
+    qidx numIts = ((qidx)1 << numQubits) >> p.numFixed;
+    cudaStream_t st = qg_stream(stream);
+    switch (numTargs) {
+        case 3: QG_TRY(launch_denseK<3>((double2*)amps, numIts, p, matr, targs, applyConj, st)); break;
+        case 4: QG_TRY(launch_denseK<4>((double2*)amps, numIts, p, matr, targs, applyConj, st)); break;
+        case 5: QG_TRY(launch_denseK<5>((double2*)amps, numIts, p, matr, targs, applyConj, st)); break;
+        default: {
+            // matrix (column-major, conjugated if asked) and target offsets in stream-ordered device memory
+            int K = numTargs;
+            qidx D = (qidx)1 << K;
+            std::vector<double2> colMajor((size_t)(D * D));
+            for (qidx r = 0; r < D; r++)
+                for (qidx c = 0; c < D; c++) {
+                    qg_cplx e = matr[r * D + c];
+                    colMajor[(size_t)(c * D + r)] = make_double2(e.re, applyConj ? -e.im : e.im);
+                }
+            std::vector<qidx> off((size_t)D);
+            for (qidx j = 0; j < D; j++) {
+                qidx o = 0;
+                for (int b = 0; b < K; b++)
+                    if ((j >> b) & 1) o |= (qidx)1 << targs[b];
+                off[(size_t)j] = o;
+            }
+            size_t matBytes = sizeof(double2) * (size_t)(D * D), offBytes = sizeof(qidx) * (size_t)D;
+            int sms = qg_num_sms();
+            bool useSmem = (size_t)D * sizeof(double2) <= 96 * 1024;
+            qidx grid = std::min<qidx>(numIts, (qidx)sms * 8);
+            size_t cacheBytes = useSmem ? 0 : sizeof(double2) * (size_t)(D * grid);
+            char* dev = nullptr;
+            QG_CUDA(cudaMallocAsync((void**)&dev, matBytes + offBytes + cacheBytes, st));
+            QG_CUDA(cudaMemcpyAsync(dev, colMajor.data(), matBytes, cudaMemcpyHostToDevice, st));
+            QG_CUDA(cudaMemcpyAsync(dev + matBytes, off.data(), offBytes, cudaMemcpyHostToDevice, st));
+            size_t smemBytes = useSmem ? (size_t)D * sizeof(double2) : 0;
+            if (smemBytes > 48 * 1024)
+                QG_CUDA(cudaFuncSetAttribute(k_denseMany, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemBytes));
+            k_denseMany<<<(unsigned)grid, 256, smemBytes, st>>>((double2*)amps, numIts, K, p.ins, p.stateMask,
+                                                                 (const qidx*)(dev + matBytes), (const double2*)dev,
+                                                                 useSmem ? nullptr : (double2*)(dev + matBytes + offBytes));
+            QG_TRY(qg_check_launch("denseMany"));
+            QG_CUDA(cudaFreeAsync(dev, st));
+        }
+    }
+    qg_note_launch();
+    return qg_check_launch("denseK");
+}
+
+int qg_sv_anyCtrlOneTargDiagMatr(void* amps, int numQubits, const int* ctrls, const int* ctrlStates, int numCtrls,
+                                 int targ, const qg_cplx* elems, void* stream) {
+    QG_TRY(qg_check_amps(amps, numQubits));
+    if (!elems) return qg_fail(QG_ERR_ARG, "null diagonal");
+    QG_TRY(qg_check_qubits(numQubits, &targ, 1, "target"));
+    for (int i = 0; i < numCtrls; i++)
+        if (ctrls[i] == targ) return qg_fail(QG_ERR_ARG, "control %d is also the target", targ);
+    bool one0 = elems[0].re == 1.0 && elems[0].im == 0.0;
+    bool one1 = elems[1].re == 1.0 && elems[1].im == 0.0;
+    cudaStream_t st = qg_stream(stream);
+    if (one0 && one1) return QG_OK;   // the identity: nothing changes
+    if (one0 || one1) {
+        // only amplitudes whose factor differs from 1 are visited
+        int tv = one0 ? 1 : 0;
+        QubitPlan p;
+        QG_TRY(qg_make_plan(numQubits, ctrls, ctrlStates, numCtrls, &targ, &tv, 1, &p));
+        qidx numIts = ((qidx)1 << numQubits) >> p.numFixed;
+        double2 f = d2(one0 ? elems[1] : elems[0]);
+#define L(NBV) k_diag1<NBV, 1><<<qg_blocks(numIts), QG_THREADS, 0, st>>>((double2*)amps, numIts, p.ins, p.stateMask, 0, f, f)
+        QG_DISPATCH_NB(p.numFixed, L)
+#undef L
+    } else {
+        QubitPlan p;
+        QG_TRY(qg_make_plan(numQubits, ctrls, ctrlStates, numCtrls, nullptr, nullptr, 0, &p));
+        qidx numIts = ((qidx)1 << numQubits) >> p.numFixed;
+        qidx tbit = (qidx)1 << targ;
+#define L(NBV) k_diag1<NBV, 0><<<qg_blocks(numIts), QG_THREADS, 0, st>>>((double2*)amps, numIts, p.ins, p.stateMask, tbit, d2(elems[0]), d2(elems[1]))
+        QG_DISPATCH_NB(p.numFixed, L)
+#undef L
+    }
+    qg_note_launch();
+    return qg_check_launch("diag1");
+}
+
+int qg_sv_anyCtrlTwoTargDiagMatr(void* amps, int numQubits, const int* ctrls, const int* ctrlStates, int numCtrls,
+                                 int targ1, int targ2, const qg_cplx* elems, void* stream) {
+    QG_TRY(qg_check_amps(amps, numQubits));
+    if (!elems) return qg_fail(QG_ERR_ARG, "null diagonal");
+    int tq[2] = {targ1, targ2};
+    QG_TRY(qg_check_qubits(numQubits, tq, 2, "targets"));
+    QubitPlan p;
+    QG_TRY(qg_make_plan(numQubits, ctrls, ctrlStates, numCtrls, nullptr, nullptr, 0, &p));
+    for (int i = 0; i < numCtrls; i++)
+        if (ctrls[i] == targ1 || ctrls[i] == targ2) return qg_fail(QG_ERR_ARG, "control %d is also a target", ctrls[i]);
+    Diag4 D;
+    for (int i = 0; i < 4; i++) D.d[i] = d2(elems[i]);
+    qidx numIts = ((qidx)1 << numQubits) >> p.numFixed;
+    cudaStream_t st = qg_stream(stream);
+#define L(NBV) QG_LAUNCH_PLAIN(k_diag2, NBV, (double2*)amps, numIts, p.ins, p.stateMask, targ1, targ2, D)
+    QG_DISPATCH_NB(p.numFixed, L)
+#undef L
+    qg_note_launch();
+    return qg_check_launch("diag2");
+}
+
+int qg_sv_anyCtrlAnyTargDiagMatr(void* amps, int numQubits, const int* ctrls, const int* ctrlStates, int numCtrls,
+                                 const int* targs, int numTargs, const qg_cplx* elems, int applyConj,
+                                 const qg_cplx* exponent, void* stream) {
+    QG_TRY(qg_check_amps(amps, numQubits));
+    if (!elems) return qg_fail(QG_ERR_ARG, "null diagonal");
+    QG_TRY(qg_check_qubits(numQubits, targs, numTargs, "targets"));
+    for (int i = 0; i < numCtrls; i++)
+        for (int j = 0; j < numTargs; j++)
+            if (ctrls[i] == targs[j]) return qg_fail(QG_ERR_ARG, "control %d is also a target", ctrls[i]);
+    QubitPlan p;
+    QG_TRY(qg_make_plan(numQubits, ctrls, ctrlStates, numCtrls, nullptr, nullptr, 0, &p));
+    // the 2^k elements are prepared once on the host: the power (std::pow on qcomp, as
+    // cpu_subroutines.cpp:663-701 evaluates it per amplitude) then the conjugation
+    qidx D = (qidx)1 << numTargs;
+    bool hasPower = exponent && !(exponent->re == 1.0 && exponent->im == 0.0);
+    std::vector<double2> el((size_t)D);
+    for (qidx v = 0; v < D; v++) {
+        std::complex<double> e(elems[v].re, elems[v].im);
+        if (hasPower) e = std::pow(e, std::complex<double>(exponent->re, exponent->im));
+        if (applyConj) e = std::conj(e);
+        el[(size_t)v] = make_double2(e.real(), e.imag());
+    }
+    qidx numIts = ((qidx)1 << numQubits) >> p.numFixed;
+    cudaStream_t st = qg_stream(stream);
+    if (numTargs <= QG_DIAG_PARAM_MAX) {
+        DiagK Dk;
+        Dk.k = numTargs;
+        for (int b = 0; b < numTargs; b++) Dk.t[b] = targs[b];
+        for (qidx v = 0; v < D; v++) Dk.d[v] = el[(size_t)v];
+#define L(NBV) QG_LAUNCH_PLAIN(k_diagK, NBV, (double2*)amps, numIts, p.ins, p.stateMask, Dk)
+        QG_DISPATCH_NB(p.numFixed, L)
+#undef L
+    } else {
+        double2* dev = nullptr;
+        QG_CUDA(cudaMallocAsync((void**)&dev, sizeof(double2) * (size_t)D, st));
+        QG_CUDA(cudaMemcpyAsync(dev, el.data(), sizeof(double2) * (size_t)D, cudaMemcpyHostToDevice, st));
+        DiagKDev Dk;
+        Dk.d = dev;
+        Dk.k = numTargs;
+        for (int b = 0; b < numTargs; b++) Dk.t[b] = targs[b];
+#define L(NBV) QG_LAUNCH_PLAIN(k_diagKdev, NBV, (double2*)amps, numIts, p.ins, p.stateMask, Dk)
+        QG_DISPATCH_NB(p.numFixed, L)
+#undef L
+        QG_TRY(qg_check_launch("diagKdev"));
+        QG_CUDA(cudaFreeAsync(dev, st));
+    }
+    qg_note_launch();
+    return qg_check_launch("diagK");
+}
+
+int qg_sv_anyCtrlPauliTensorOrGadget(void* amps, int numQubits, const int* ctrls, const int* ctrlStates, int numCtrls,
+                                     const int* targsX, int numX, const int* targsY, int numY, const int* targsZ, int numZ,
+                                     qg_cplx ampFac, qg_cplx pairAmpFac, void* stream) {
+    QG_TRY(qg_check_amps(amps, numQubits));
+    if (numX + numY == 0) return qg_fail(QG_ERR_ARG, "a Pauli tensor or gadget needs an X or Y target");
+    std::vector<int> all;
+    qidx maskXY = 0, maskYZ = 0;
+    int top = -1;
+    for (int i = 0; i < numX; i++) { all.push_back(targsX[i]); maskXY |= (qidx)1 << targsX[i]; top = std::max(top, targsX[i]); }
+    for (int i = 0; i < numY; i++) { all.push_back(targsY[i]); maskXY |= (qidx)1 << targsY[i]; maskYZ |= (qidx)1 << targsY[i]; top = std::max(top, targsY[i]); }
+    for (int i = 0; i < numZ; i++) { all.push_back(targsZ[i]); maskYZ |= (qidx)1 << targsZ[i]; }
+    for (int i = 0; i < numCtrls; i++) all.push_back(ctrls[i]);
+    QG_TRY(qg_check_qubits(numQubits, all.data(), (int)all.size(), "Pauli targets and controls"));
+    int tv = 0;
+    QubitPlan p;
+    QG_TRY(qg_make_plan(numQubits, ctrls, ctrlStates, numCtrls, &top, &tv, 1, &p));
+    // scale the pair factor by i^numY (util_getPowerOfI, utilities.cpp:333-338)
+    static const double pr[4] = {1, 0, -1, 0}, pi[4] = {0, 1, 0, -1};
+    int r = numY % 4;
+    double2 f1 = make_double2(pairAmpFac.re * pr[r] - pairAmpFac.im * pi[r], pairAmpFac.re * pi[r] + pairAmpFac.im * pr[r]);
+    double2 f0 = d2(ampFac);
+    qidx numIts = ((qidx)1 << numQubits) >> p.numFixed;
+    cudaStream_t st = qg_stream(stream);
+    int mode = 0;
+    bool unit1 = (std::fabs(f1.x) == 1.0 && f1.y == 0.0) || (f1.x == 0.0 && std::fabs(f1.y) == 1.0);
+    if (f0.x == 0.0 && f0.y == 0.0 && unit1) mode = 3;
+    else if (f0.y == 0.0 && f1.y == 0.0) mode = 1;
+    else if (f0.y == 0.0 && f1.x == 0.0) mode = 2;
+#define L0(NBV) k_pauli<NBV, 0><<<qg_blocks(numIts), QG_THREADS, 0, st>>>((double2*)amps, numIts, p.ins, p.stateMask, maskXY, maskYZ, f0, f1)
+#define L1(NBV) k_pauli<NBV, 1><<<qg_blocks(numIts), QG_THREADS, 0, st>>>((double2*)amps, numIts, p.ins, p.stateMask, maskXY, maskYZ, f0, f1)
+#define L2(NBV) k_pauli<NBV, 2><<<qg_blocks(numIts), QG_THREADS, 0, st>>>((double2*)amps, numIts, p.ins, p.stateMask, maskXY, maskYZ, f0, f1)
+#define L3(NBV) k_pauli<NBV, 3><<<qg_blocks(numIts), QG_THREADS, 0, st>>>((double2*)amps, numIts, p.ins, p.stateMask, maskXY, maskYZ, f0, f1)
+    switch (mode) {
+        case 0: QG_DISPATCH_NB(p.numFixed, L0) break;
+        case 1: QG_DISPATCH_NB(p.numFixed, L1) break;
+        case 2: QG_DISPATCH_NB(p.numFixed, L2) break;
+        default: QG_DISPATCH_NB(p.numFixed, L3) break;
+    }
+#undef L0
+#undef L1
+#undef L2
+#undef L3
+    qg_note_launch();
+    return qg_check_launch("pauli");
+}
+
+int qg_sv_anyCtrlAnyTargZOrPhaseGadget(void* amps, int numQubits, const int* ctrls, const int* ctrlStates, int numCtrls,
+                                       const int* targs, int numTargs, qg_cplx fac0, qg_cplx fac1, void* stream) {
+    QG_TRY(qg_check_amps(amps, numQubits));
+    QG_TRY(qg_check_qubits(numQubits, targs, numTargs, "targets"));
+    for (int i = 0; i < numCtrls; i++)
+        for (int j = 0; j < numTargs; j++)
+            if (ctrls[i] == targs[j]) return qg_fail(QG_ERR_ARG, "control %d is also a target", ctrls[i]);
+    QubitPlan p;
+    QG_TRY(qg_make_plan(numQubits, ctrls, ctrlStates, numCtrls, nullptr, nullptr, 0, &p));
+    qidx tmask = 0;
+    for (int j = 0; j < numTargs; j++) tmask |= (qidx)1 << targs[j];
+    qidx numIts = ((qidx)1 << numQubits) >> p.numFixed;
+    cudaStream_t st = qg_stream(stream);
+    bool ztensor = fac0.re == 1.0 && fac0.im == 0.0 && fac1.re == -1.0 && fac1.im == 0.0;
+    if (ztensor) {
+#define L(NBV) k_zphase<NBV, 1><<<qg_blocks(numIts), QG_THREADS, 0, st>>>((double2*)amps, numIts, p.ins, p.stateMask, tmask, d2(fac0), d2(fac1))
+        QG_DISPATCH_NB(p.numFixed, L)
+#undef L
+    } else {
+#define L(NBV) k_zphase<NBV, 0><<<qg_blocks(numIts), QG_THREADS, 0, st>>>((double2*)amps, numIts, p.ins, p.stateMask, tmask, d2(fac0), d2(fac1))
+        QG_DISPATCH_NB(p.numFixed, L)
+#undef L
+    }
+    qg_note_launch();
+    return qg_check_launch("zphase");
+}
+
+int qg_sv_multiQubitProjector(void* amps, int numQubits, const int* qubits, const int* outcomes, int num,
+                              double prob, void* stream) {
+    QG_TRY(qg_check_amps(amps, numQubits));
+    QG_TRY(qg_check_qubits(numQubits, qubits, num, "projector qubits"));
+    qidx qmask = 0, retain = 0;
+    for (int i = 0; i < num; i++) {
+        if (outcomes[i] != 0 && outcomes[i] != 1) return qg_fail(QG_ERR_ARG, "outcome %d is not 0 or 1", outcomes[i]);
+        qmask |= (qidx)1 << qubits[i];
+        if (outcomes[i]) retain |= (qidx)1 << qubits[i];
+    }
+    qidx n = (qidx)1 << numQubits;
+    double renorm = 1 / std::sqrt(prob);
+    k_projector<<<qg_blocks(n), QG_THREADS, 0, qg_stream(stream)>>>((double2*)amps, n, qmask, retain, renorm);
+    qg_note_launch();
+    return qg_check_launch("projector");
+}
+
+}  // extern "C"

@@ -1,0 +1,949 @@
+// QuEST v4 API functions of the gate-application path, on the GB300 backend.
+//
+// This file is the host side above the C ABI (include/quest_gb300.h).  It keeps
+// the reference's observable behaviour: the same validation (and error handler
+// contract), the same decomposition of each API call into backend calls
+// (quest/src/api/operations.cpp, decoherence.cpp, calculations.cpp and the
+// single-node branches of quest/src/core/localiser.cpp), the same gate
+// constants, and the same host random-number stream for measurements
+// (std::mt19937_64 seeded through std::seed_seq, a uniform double in [0,1)
+// compared with the zero-outcome probability; quest/src/core/randomiser.cpp:59-137).
+// Every Qureg lives on the GPU; nothing here evaluates amplitudes on the CPU.
+#include "quest_gb300_api.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <random>
+#include <string>
+#include <vector>
+
+using std::vector;
+typedef std::complex<double> cd;
+
+namespace {
+
+const int QG_MAX_QUBITS_API = 40;    // 2^40 FP64 amplitudes = 16 TiB: far above one GPU
+const double DEFAULT_EPS = 1e-12;            // precision.h:131-140 at FLOAT_PRECISION=2
+const double REDUCTION_EPS_FACTOR = 100;     // validation.cpp:1137
+double g_eps = DEFAULT_EPS;
+bool g_envInit = false;
+thread_local void* g_stream = nullptr;
+std::mt19937_64 g_rng;
+
+void default_handler(const char* func, const char* msg) {
+    std::fprintf(stderr, "\nQuEST encountered a validation error during function '%s':\n%s\nExiting...\n", func, msg);
+    std::exit(EXIT_FAILURE);
+}
+void (*g_handler)(const char*, const char*) = default_handler;
+
+// Reports a failed check; returns false so callers can `if (!check(...)) return;`
+bool fail(const char* func, const std::string& msg) {
+    g_handler(func, msg.c_str());
+    return false;
+}
+bool check(bool cond, const char* func, const std::string& msg) { return cond ? true : fail(func, msg); }
+bool backend(int rc, const char* func) {
+    if (rc == QG_OK) return true;
+    std::string m = std::string("GPU backend call failed in ") + func + ": " + qg_get_last_error();
+    g_handler("qg_backend", m.c_str());
+    return false;
+}
+
+inline int nsv(const Qureg& q) { return q.isDensityMatrix ? 2 * q.numQubits : q.numQubits; }
+inline cd C(qcomp_t c) { return cd(c.re, c.im); }
+inline qcomp_t Q(cd c) { return qcomp_t{c.real(), c.imag()}; }
+
+bool checkEnv(const char* func) { return check(g_envInit, func, "The QuEST environment has not been initialised."); }
+
+bool checkQureg(const Qureg& q, const char* func) {
+    if (!checkEnv(func)) return false;
+    return check(q.gpuAmps != nullptr && q.numQubits >= 1, func, "Invalid Qureg; it was not created, or was destroyed.");
+}
+
+bool checkQubits(const Qureg& q, const int* qs, int n, const char* func, const char* what) {
+    if (!check(n >= 0, func, std::string("Invalid number of ") + what + ".")) return false;
+    if (n > 0 && !check(qs != nullptr, func, std::string("Null list of ") + what + ".")) return false;
+    for (int i = 0; i < n; i++) {
+        if (!check(qs[i] >= 0 && qs[i] < q.numQubits, func,
+                   std::string("Invalid ") + what + " index " + std::to_string(qs[i]) + ". Must be >=0 and <" +
+                       std::to_string(q.numQubits) + "."))
+            return false;
+        for (int j = 0; j < i; j++)
+            if (!check(qs[i] != qs[j], func, std::string("The ") + what + " contain a duplicate qubit."))
+                return false;
+    }
+    return true;
+}
+
+bool checkCtrlsTargs(const Qureg& q, const int* c, int nc, const int* t, int nt, const char* func) {
+    if (!checkQubits(q, c, nc, func, "control qubits")) return false;
+    if (!checkQubits(q, t, nt, func, "target qubits")) return false;
+    for (int i = 0; i < nc; i++)
+        for (int j = 0; j < nt; j++)
+            if (!check(c[i] != t[j], func, "A control qubit was also a target qubit.")) return false;
+    return true;
+}
+
+bool checkStates(const int* s, int n, const char* func) {
+    if (!s) return true;
+    for (int i = 0; i < n; i++)
+        if (!check(s[i] == 0 || s[i] == 1, func, "Invalid control-qubit state; must be 0 or 1.")) return false;
+    return true;
+}
+
+bool isUnitaryDense(const qcomp_t* m, qindex dim) {
+    for (qindex r = 0; r < dim; r++)
+        for (qindex c = 0; c < dim; c++) {
+            cd e = 0;
+            for (qindex i = 0; i < dim; i++) e += C(m[r * dim + i]) * std::conj(C(m[c * dim + i]));
+            if (std::norm(e - cd(r == c, 0)) > g_eps) return false;
+        }
+    return true;
+}
+bool isUnitaryDiag(const qcomp_t* d, qindex dim) {
+    for (qindex i = 0; i < dim; i++)
+        if (std::abs(std::abs(C(d[i])) - 1) > g_eps) return false;
+    return true;
+}
+
+vector<int> V(const int* p, int n) { return p ? vector<int>(p, p + n) : vector<int>(); }
+vector<int> braOf(const Qureg& q, vector<int> v) { for (auto& x : v) x += q.numQubits; return v; }
+const int* P(const vector<int>& v) { return v.empty() ? nullptr : v.data(); }
+const int* S(const vector<int>& s) { return s.empty() ? nullptr : s.data(); }
+
+// ------------------------------------------------------------------ dense / diagonal on the Choi or state vector
+
+bool denseSV(const Qureg& q, const vector<int>& c, const vector<int>& s, const vector<int>& t, const qcomp_t* m, bool conj, const char* func) {
+    int k = (int)t.size();
+    qindex D = (qindex)1 << k;
+    if (k <= 2) {
+        vector<qcomp_t> mm(m, m + D * D);
+        if (conj) for (auto& e : mm) e.im = -e.im;
+        if (k == 1) return backend(qg_sv_anyCtrlOneTargDenseMatr(q.gpuAmps, nsv(q), P(c), S(s), (int)c.size(), t[0], mm.data(), g_stream), func);
+        return backend(qg_sv_anyCtrlTwoTargDenseMatr(q.gpuAmps, nsv(q), P(c), S(s), (int)c.size(), t[0], t[1], mm.data(), g_stream), func);
+    }
+    return backend(qg_sv_anyCtrlAnyTargDenseMatr(q.gpuAmps, nsv(q), P(c), S(s), (int)c.size(), t.data(), k, m, conj ? 1 : 0, g_stream), func);
+}
+
+// validateAndApplyAnyCtrlAnyTargUnitaryMatrix: operations.cpp:36-63
+void applyDense(const Qureg& q, const int* ctrls, const int* states, int nc, const int* targs, int nt, const qcomp_t* m, bool checkUnitary, const char* func) {
+    if (!checkQureg(q, func)) return;
+    if (!checkCtrlsTargs(q, ctrls, nc, targs, nt, func)) return;
+    if (!checkStates(states, nc, func)) return;
+    if (!check(nt >= 1, func, "At least one target qubit is required.")) return;
+    if (checkUnitary && !check(isUnitaryDense(m, (qindex)1 << nt), func, "The given matrix was not (approximately) unitary.")) return;
+    vector<int> c = V(ctrls, nc), s = V(states, nc), t = V(targs, nt);
+    if (!denseSV(q, c, s, t, m, false, func)) return;
+    if (!q.isDensityMatrix) return;
+    denseSV(q, braOf(q, c), s, braOf(q, t), m, true, func);
+}
+
+bool diagSV(const Qureg& q, const vector<int>& c, const vector<int>& s, const vector<int>& t, const qcomp_t* d, bool conj, const qcomp_t* ex, bool anyTarg, const char* func) {
+    int k = (int)t.size();
+    if (!anyTarg && !ex && k <= 2) {
+        qcomp_t dd[4];
+        for (int i = 0; i < (1 << k); i++) dd[i] = qcomp_t{d[i].re, conj ? -d[i].im : d[i].im};
+        if (k == 1) return backend(qg_sv_anyCtrlOneTargDiagMatr(q.gpuAmps, nsv(q), P(c), S(s), (int)c.size(), t[0], dd, g_stream), func);
+        return backend(qg_sv_anyCtrlTwoTargDiagMatr(q.gpuAmps, nsv(q), P(c), S(s), (int)c.size(), t[0], t[1], dd, g_stream), func);
+    }
+    return backend(qg_sv_anyCtrlAnyTargDiagMatr(q.gpuAmps, nsv(q), P(c), S(s), (int)c.size(), t.data(), k, d, conj ? 1 : 0, ex, g_stream), func);
+}
+
+void applyDiag(const Qureg& q, const int* ctrls, const int* states, int nc, const int* targs, int nt, const qcomp_t* d,
+               const qcomp_t* ex, bool anyTarg, const char* func) {
+    if (!checkQureg(q, func)) return;
+    if (!checkCtrlsTargs(q, ctrls, nc, targs, nt, func)) return;
+    if (!checkStates(states, nc, func)) return;
+    if (!check(nt >= 1, func, "At least one target qubit is required.")) return;
+    if (!check(isUnitaryDiag(d, (qindex)1 << nt), func, "The given matrix was not (approximately) unitary.")) return;
+    if (ex && !check(std::abs(ex->im) <= g_eps, func, "The exponent of a unitary diagonal matrix must be real.")) return;
+    vector<int> c = V(ctrls, nc), s = V(states, nc), t = V(targs, nt);
+    if (!diagSV(q, c, s, t, d, false, ex, anyTarg, func)) return;
+    if (!q.isDensityMatrix) return;
+    diagSV(q, braOf(q, c), s, braOf(q, t), d, true, ex, anyTarg, func);
+}
+
+// ------------------------------------------------------------------ Pauli strings (paulis.h:53-60)
+
+int pauliAt(const PauliStr& p, int q) {
+    return q < 32 ? (int)((p.lowPaulis >> (2 * q)) & 3) : (int)((p.highPaulis >> (2 * (q - 32))) & 3);
+}
+vector<int> codesOf(const PauliStr& p, int n) { vector<int> v(n); for (int q = 0; q < n; q++) v[q] = pauliAt(p, q); return v; }
+bool strFits(const PauliStr& p, int n) {
+    for (int q = n; q < 64; q++) if (pauliAt(p, q)) return false;
+    return true;
+}
+void splitXYZ(const vector<int>& codes, vector<int>& x, vector<int>& y, vector<int>& z) {
+    for (size_t q = 0; q < codes.size(); q++) {
+        if (codes[q] == 1) x.push_back((int)q);
+        else if (codes[q] == 2) y.push_back((int)q);
+        else if (codes[q] == 3) z.push_back((int)q);
+    }
+}
+int numY(const vector<int>& codes) { int k = 0; for (int v : codes) k += v == 2; return k; }
+
+// localiser_statevec_anyCtrlPauliTensor (localiser.cpp:1319-1339) on codes over the whole vector
+bool pauliTensorSV(const Qureg& q, const vector<int>& c, const vector<int>& s, const vector<int>& codes, cd factor, const char* func) {
+    vector<int> x, y, z;
+    splitXYZ(codes, x, y, z);
+    if (!x.empty() || !y.empty())
+        return backend(qg_sv_anyCtrlPauliTensorOrGadget(q.gpuAmps, nsv(q), P(c), S(s), (int)c.size(), P(x), (int)x.size(), P(y), (int)y.size(),
+                                                         P(z), (int)z.size(), Q(0.0 * factor), Q(1.0 * factor), g_stream), func);
+    return backend(qg_sv_anyCtrlAnyTargZOrPhaseGadget(q.gpuAmps, nsv(q), P(c), S(s), (int)c.size(), P(z), (int)z.size(),
+                                                       qcomp_t{1, 0}, qcomp_t{-1, 0}, g_stream), func);
+}
+
+// localiser_statevec_anyCtrlPhaseGadget / PauliGadget (localiser.cpp:1342-1360)
+bool phaseGadgetSV(const Qureg& q, const vector<int>& c, const vector<int>& s, const vector<int>& t, double phase, const char* func) {
+    cd f0 = std::exp(cd(0, +phase)), f1 = std::exp(cd(0, -phase));
+    return backend(qg_sv_anyCtrlAnyTargZOrPhaseGadget(q.gpuAmps, nsv(q), P(c), S(s), (int)c.size(), P(t), (int)t.size(), Q(f0), Q(f1), g_stream), func);
+}
+bool pauliGadgetSV(const Qureg& q, const vector<int>& c, const vector<int>& s, const vector<int>& codes, double phase, const char* func) {
+    vector<int> x, y, z;
+    splitXYZ(codes, x, y, z);
+    if (x.empty() && y.empty()) return phaseGadgetSV(q, c, s, z, phase, func);
+    cd f0 = std::cos(phase), f1 = std::sin(phase) * cd(0, 1);
+    return backend(qg_sv_anyCtrlPauliTensorOrGadget(q.gpuAmps, nsv(q), P(c), S(s), (int)c.size(), P(x), (int)x.size(), P(y), (int)y.size(),
+                                                     P(z), (int)z.size(), Q(f0), Q(f1), g_stream), func);
+}
+
+vector<int> shiftedCodes(const Qureg& q, const vector<int>& ket) {
+    vector<int> v(nsv(q), 0);
+    for (int i = 0; i < q.numQubits; i++) v[i + q.numQubits] = ket[i];
+    return v;
+}
+vector<int> paddedCodes(const Qureg& q, const vector<int>& ket) {
+    vector<int> v(nsv(q), 0);
+    for (int i = 0; i < q.numQubits; i++) v[i] = ket[i];
+    return v;
+}
+
+bool checkPauliTargs(const Qureg& q, const int* ctrls, int nc, const PauliStr& str, const char* func) {
+    if (!check(strFits(str, q.numQubits), func, "The Pauli string targets a qubit beyond the Qureg.")) return false;
+    if (!checkQubits(q, ctrls, nc, func, "control qubits")) return false;
+    for (int i = 0; i < nc; i++)
+        if (!check(pauliAt(str, ctrls[i]) == 0, func, "A control qubit was also a target qubit.")) return false;
+    return true;
+}
+
+// ------------------------------------------------------------------ probabilities
+
+bool probOf(const Qureg& q, const vector<int>& qs, const vector<int>& os, double* out, const char* func) {
+    if (q.isDensityMatrix)
+        return backend(qg_dm_calcProbOfMultiQubitOutcome(q.gpuAmps, q.numQubits, P(qs), P(os), (int)qs.size(), out, g_stream), func);
+    return backend(qg_sv_calcProbOfMultiQubitOutcome(q.gpuAmps, q.numQubits, P(qs), P(os), (int)qs.size(), out, g_stream), func);
+}
+bool project(const Qureg& q, const vector<int>& qs, const vector<int>& os, double prob, const char* func) {
+    if (q.isDensityMatrix)
+        return backend(qg_dm_multiQubitProjector(q.gpuAmps, q.numQubits, P(qs), P(os), (int)qs.size(), prob, g_stream), func);
+    return backend(qg_sv_multiQubitProjector(q.gpuAmps, q.numQubits, P(qs), P(os), (int)qs.size(), prob, g_stream), func);
+}
+
+bool checkDensMatr(const Qureg& q, const char* func) {
+    return check(q.isDensityMatrix, func, "Expected a density matrix Qureg but received a statevector.");
+}
+bool checkProb(double p, double maxP, const char* func) {
+    if (!check(p >= 0 && p <= 1, func, "The given probability is invalid; it must lie in [0, 1].")) return false;
+    return check(p <= maxP, func, "The given probability exceeds the maximal mixing of this channel.");
+}
+
+}  // namespace
+
+extern "C" {
+
+// ====================================================================== environment
+
+void initQuESTEnv(void) { initCustomQuESTEnv(0, 1, 0); }
+
+void initCustomQuESTEnv(int useDistrib, int useGpuAccel, int useMultithread) {
+    (void)useMultithread;
+    const char* func = "initCustomQuESTEnv";
+    if (!check(!g_envInit, func, "The QuEST environment has already been initialised.")) return;
+    if (!check(useDistrib == 0 || useDistrib == -1, func, "This build runs on one GPU; distribution is compiled out.")) return;
+    if (!check(useGpuAccel != 0, func, "This build has no CPU backend; GPU acceleration cannot be disabled.")) return;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (!backend(qg_init(dev), func)) return;
+    std::random_device rd;   // rand_setSeedsToDefault (randomiser.cpp:89-106)
+    vector<unsigned> seeds(4);
+    for (auto& s : seeds) s = rd();
+    std::seed_seq seq(seeds.begin(), seeds.end());
+    g_rng.seed(seq);
+    g_envInit = true;
+}
+
+void finalizeQuESTEnv(void) {
+    if (!g_envInit) return;
+    qg_sync();
+    g_envInit = false;
+}
+
+int isQuESTEnvInit(void) { return g_envInit ? 1 : 0; }
+
+void syncQuESTEnv(void) { backend(qg_sync(), "syncQuESTEnv"); }
+
+void setInputErrorHandler(void (*callback)(const char*, const char*)) { g_handler = callback ? callback : default_handler; }
+
+void setSeeds(unsigned* seeds, int numSeeds) {
+    if (!check(numSeeds > 0 && seeds != nullptr, "setSeeds", "Invalid number of seeds.")) return;
+    std::seed_seq seq(seeds, seeds + numSeeds);
+    g_rng.seed(seq);
+}
+
+void setValidationEpsilon(qreal eps) {
+    if (!check(eps >= 0, "setValidationEpsilon", "The validation epsilon must be non-negative.")) return;
+    g_eps = eps;
+}
+void setValidationEpsilonToDefault(void) { g_eps = DEFAULT_EPS; }
+void setQuESTStream(void* s) { g_stream = s; }
+
+// ====================================================================== qureg lifecycle
+
+Qureg createCustomQureg(int numQubits, int isDensMatr, int useDistrib, int useGpuAccel, int useMultithread) {
+    (void)useMultithread;
+    const char* func = "createCustomQureg";
+    Qureg q;
+    std::memset(&q, 0, sizeof(q));
+    if (!checkEnv(func)) return q;
+    if (!check(numQubits >= 1, func, "Invalid number of qubits; must be >= 1.")) return q;
+    if (!check(useDistrib == 0 || useDistrib == -1, func, "This build runs on one GPU; distribution is compiled out.")) return q;
+    if (!check(useGpuAccel != 0, func, "This build has no CPU backend; GPU acceleration cannot be disabled.")) return q;
+    int n = isDensMatr ? 2 * numQubits : numQubits;
+    if (!check(n <= QG_MAX_QUBITS_API, func, "Too many qubits for one GPU.")) return q;
+    qindex numAmps = (qindex)1 << n;
+    size_t bytes = sizeof(qcomp_t) * (size_t)numAmps;
+    // qureg_populateNonHeapFields (qureg.cpp:37-88), single node
+    q.isMultithreaded = 0;
+    q.isGpuAccelerated = 1;
+    q.isDistributed = 0;
+    q.rank = 0;
+    q.numNodes = 1;
+    q.logNumNodes = 0;
+    q.isDensityMatrix = isDensMatr ? 1 : 0;
+    q.numQubits = numQubits;
+    q.numAmps = numAmps;
+    q.logNumAmps = n;
+    q.numAmpsPerNode = numAmps;
+    q.logNumAmpsPerNode = n;
+    q.logNumColsPerNode = isDensMatr ? numQubits : 0;
+    void* dev = nullptr;
+    int rc = qg_alloc(&dev, (int64_t)bytes);
+    if (rc != QG_OK) {
+        fail(func, std::string("Could not allocate ") + std::to_string(bytes) + " bytes of GPU memory: " + qg_get_last_error());
+        std::memset(&q, 0, sizeof(q));
+        return q;
+    }
+    void* host = nullptr;
+    if (cudaMallocHost(&host, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        host = std::calloc(1, bytes);
+    }
+    if (!host) {
+        qg_free(dev);
+        fail(func, "Could not allocate the host copy of the amplitudes.");
+        std::memset(&q, 0, sizeof(q));
+        return q;
+    }
+    q.gpuAmps = (qcomp_t*)dev;
+    q.cpuAmps = (qcomp_t*)host;
+    initZeroState(q);
+    return q;
+}
+
+Qureg createQureg(int numQubits) { return createCustomQureg(numQubits, 0, 0, 1, 0); }
+Qureg createDensityQureg(int numQubits) { return createCustomQureg(numQubits, 1, 0, 1, 0); }
+
+Qureg createCloneQureg(Qureg qureg) {
+    Qureg q;
+    std::memset(&q, 0, sizeof(q));
+    if (!checkQureg(qureg, "createCloneQureg")) return q;
+    q = createCustomQureg(qureg.numQubits, qureg.isDensityMatrix, 0, 1, 0);
+    if (q.gpuAmps) backend(qg_copy_d2d(q.gpuAmps, qureg.gpuAmps, (int64_t)(sizeof(qcomp_t) * qureg.numAmps), g_stream), "createCloneQureg");
+    return q;
+}
+
+void destroyQureg(Qureg qureg) {
+    if (!checkQureg(qureg, "destroyQureg")) return;
+    qg_sync();
+    qg_free(qureg.gpuAmps);
+    if (cudaFreeHost(qureg.cpuAmps) != cudaSuccess) {
+        cudaGetLastError();
+        std::free(qureg.cpuAmps);
+    }
+}
+
+void syncQuregToGpu(Qureg q) {
+    if (!checkQureg(q, "syncQuregToGpu")) return;
+    backend(qg_copy_h2d(q.gpuAmps, q.cpuAmps, (int64_t)(sizeof(qcomp_t) * q.numAmps), g_stream), "syncQuregToGpu");
+}
+
+void syncQuregFromGpu(Qureg q) {
+    if (!checkQureg(q, "syncQuregFromGpu")) return;
+    backend(qg_copy_d2h(q.cpuAmps, q.gpuAmps, (int64_t)(sizeof(qcomp_t) * q.numAmps), g_stream), "syncQuregFromGpu");
+}
+
+void getQuregAmps(qcomp_t* out, Qureg q, qindex start, qindex num) {
+    const char* func = "getQuregAmps";
+    if (!checkQureg(q, func)) return;
+    if (!check(start >= 0 && num >= 0 && start + num <= q.numAmps, func, "Invalid amplitude range.")) return;
+    backend(qg_copy_d2h(out, q.gpuAmps + start, (int64_t)(sizeof(qcomp_t) * num), g_stream), func);
+}
+
+qcomp_t getQuregAmp(Qureg q, qindex index) {
+    qcomp_t v{0, 0};
+    getQuregAmps(&v, q, index, 1);
+    return v;
+}
+
+// ====================================================================== initialisations
+
+void initZeroState(Qureg q) { initClassicalState(q, 0); }
+
+void initPlusState(Qureg q) {
+    const char* func = "initPlusState";
+    if (!checkQureg(q, func)) return;
+    double v = q.isDensityMatrix ? 1.0 / (double)((qindex)1 << q.numQubits) : 1.0 / std::sqrt((double)((qindex)1 << q.numQubits));
+    backend(qg_sv_initUniformState(q.gpuAmps, nsv(q), qcomp_t{v, 0}, g_stream), func);
+}
+
+void initClassicalState(Qureg q, qindex ind) {
+    const char* func = "initClassicalState";
+    if (!checkQureg(q, func)) return;
+    qindex dim = (qindex)1 << q.numQubits;
+    if (!check(ind >= 0 && ind < dim, func, "Invalid basis state index.")) return;
+    qindex flat = q.isDensityMatrix ? ind * (dim + 1) : ind;
+    backend(qg_sv_initClassicalState(q.gpuAmps, nsv(q), flat, g_stream), func);
+}
+
+void initDebugState(Qureg q) {
+    if (!checkQureg(q, "initDebugState")) return;
+    backend(qg_sv_initDebugState(q.gpuAmps, nsv(q), g_stream), "initDebugState");
+}
+
+void setQuregAmps(Qureg q, qindex start, qcomp_t* amps, qindex num) {
+    const char* func = "setQuregAmps";
+    if (!checkQureg(q, func)) return;
+    if (!check(start >= 0 && num >= 0 && start + num <= q.numAmps, func, "Invalid amplitude range.")) return;
+    backend(qg_copy_h2d(q.gpuAmps + start, amps, (int64_t)(sizeof(qcomp_t) * num), g_stream), func);
+}
+
+void setDensityQuregFlatAmps(Qureg q, qindex start, qcomp_t* amps, qindex num) {
+    const char* func = "setDensityQuregFlatAmps";
+    if (!checkQureg(q, func) || !checkDensMatr(q, func)) return;
+    if (!check(start >= 0 && num >= 0 && start + num <= q.numAmps, func, "Invalid amplitude range.")) return;
+    backend(qg_copy_h2d(q.gpuAmps + start, amps, (int64_t)(sizeof(qcomp_t) * num), g_stream), func);
+}
+
+// ====================================================================== matrices and channels
+
+CompMatr createCompMatr(int k) {
+    CompMatr m;
+    std::memset(&m, 0, sizeof(m));
+    if (!check(k >= 1 && k <= 16, "createCompMatr", "Invalid number of qubits for a CompMatr.")) return m;
+    qindex D = (qindex)1 << k;
+    m.numQubits = k;
+    m.numRows = D;
+    m.isApproxUnitary = (int*)std::malloc(sizeof(int));
+    m.isApproxHermitian = (int*)std::malloc(sizeof(int));
+    m.wasGpuSynced = (int*)std::malloc(sizeof(int));
+    *m.isApproxUnitary = -1;
+    *m.isApproxHermitian = -1;
+    *m.wasGpuSynced = 0;
+    m.cpuElemsFlat = (qcomp_t*)std::calloc((size_t)(D * D), sizeof(qcomp_t));
+    m.cpuElems = (qcomp_t**)std::malloc(sizeof(qcomp_t*) * (size_t)D);
+    for (qindex r = 0; r < D; r++) m.cpuElems[r] = m.cpuElemsFlat + r * D;
+    m.gpuElemsFlat = nullptr;   // the backend stages dense matrices itself
+    return m;
+}
+
+void destroyCompMatr(CompMatr m) {
+    std::free(m.isApproxUnitary);
+    std::free(m.isApproxHermitian);
+    std::free(m.wasGpuSynced);
+    std::free(m.cpuElems);
+    std::free(m.cpuElemsFlat);
+}
+
+void syncCompMatr(CompMatr m) {
+    *m.wasGpuSynced = 1;
+    *m.isApproxUnitary = -1;
+}
+
+void setCompMatrFlat(CompMatr m, const qcomp_t* elems) {
+    std::memcpy(m.cpuElemsFlat, elems, sizeof(qcomp_t) * (size_t)(m.numRows * m.numRows));
+    syncCompMatr(m);
+}
+
+DiagMatr createDiagMatr(int k) {
+    DiagMatr m;
+    std::memset(&m, 0, sizeof(m));
+    if (!check(k >= 1 && k <= 30, "createDiagMatr", "Invalid number of qubits for a DiagMatr.")) return m;
+    m.numQubits = k;
+    m.numElems = (qindex)1 << k;
+    int** flags[] = {&m.isApproxUnitary, &m.isApproxHermitian, &m.isApproxNonZero, &m.isStrictlyNonNegative, &m.wasGpuSynced};
+    for (auto f : flags) { *f = (int*)std::malloc(sizeof(int)); **f = -1; }
+    *m.wasGpuSynced = 0;
+    m.cpuElems = (qcomp_t*)std::calloc((size_t)m.numElems, sizeof(qcomp_t));
+    m.gpuElems = nullptr;
+    return m;
+}
+
+void destroyDiagMatr(DiagMatr m) {
+    std::free(m.isApproxUnitary);
+    std::free(m.isApproxHermitian);
+    std::free(m.isApproxNonZero);
+    std::free(m.isStrictlyNonNegative);
+    std::free(m.wasGpuSynced);
+    std::free(m.cpuElems);
+}
+
+void syncDiagMatr(DiagMatr m) {
+    *m.wasGpuSynced = 1;
+    *m.isApproxUnitary = -1;
+}
+
+void setDiagMatrFlat(DiagMatr m, const qcomp_t* elems) {
+    std::memcpy(m.cpuElems, elems, sizeof(qcomp_t) * (size_t)m.numElems);
+    syncDiagMatr(m);
+}
+
+KrausMap createKrausMap(int k, int numOps) {
+    KrausMap m;
+    std::memset(&m, 0, sizeof(m));
+    if (!check(k >= 1 && k <= 8 && numOps >= 1, "createKrausMap", "Invalid Kraus map dimensions.")) return m;
+    qindex D = (qindex)1 << k, SD = D * D;
+    m.numQubits = k;
+    m.numMatrices = numOps;
+    m.numRows = D;
+    m.matrices = (qcomp_t***)std::malloc(sizeof(qcomp_t**) * numOps);
+    for (int n = 0; n < numOps; n++) {
+        m.matrices[n] = (qcomp_t**)std::malloc(sizeof(qcomp_t*) * (size_t)D);
+        for (qindex r = 0; r < D; r++) m.matrices[n][r] = (qcomp_t*)std::calloc((size_t)D, sizeof(qcomp_t));
+    }
+    m.superop.numQubits = 2 * k;
+    m.superop.numRows = SD;
+    m.superop.cpuElemsFlat = (qcomp_t*)std::calloc((size_t)(SD * SD), sizeof(qcomp_t));
+    m.superop.cpuElems = (qcomp_t**)std::malloc(sizeof(qcomp_t*) * (size_t)SD);
+    for (qindex r = 0; r < SD; r++) m.superop.cpuElems[r] = m.superop.cpuElemsFlat + r * SD;
+    m.superop.gpuElemsFlat = nullptr;
+    m.superop.wasGpuSynced = (int*)std::malloc(sizeof(int));
+    *m.superop.wasGpuSynced = 0;
+    m.isApproxCPTP = (int*)std::malloc(sizeof(int));
+    *m.isApproxCPTP = -1;
+    return m;
+}
+
+// syncKrausMap: rebuilds the superoperator sum_n conj(K_n) (x) K_n on the host
+// (channels.cpp:228-240, util_setSuperoperator utilities.cpp:770-801)
+void syncKrausMap(KrausMap m) {
+    qindex D = m.numRows, SD = D * D;
+    for (qindex i = 0; i < SD * SD; i++) m.superop.cpuElemsFlat[i] = qcomp_t{0, 0};
+    for (int n = 0; n < m.numMatrices; n++)
+        for (qindex i = 0; i < D; i++)
+            for (qindex j = 0; j < D; j++)
+                for (qindex k = 0; k < D; k++)
+                    for (qindex l = 0; l < D; l++) {
+                        qindex r = i * D + k, c = j * D + l;
+                        cd v = C(m.superop.cpuElemsFlat[r * SD + c]) + std::conj(C(m.matrices[n][i][j])) * C(m.matrices[n][k][l]);
+                        m.superop.cpuElemsFlat[r * SD + c] = Q(v);
+                    }
+    *m.superop.wasGpuSynced = 1;
+    *m.isApproxCPTP = -1;
+}
+
+void setKrausMapFlat(KrausMap m, const qcomp_t* ops) {
+    qindex D = m.numRows;
+    for (int n = 0; n < m.numMatrices; n++)
+        for (qindex r = 0; r < D; r++)
+            for (qindex c = 0; c < D; c++) m.matrices[n][r][c] = ops[(n * D + r) * D + c];
+    syncKrausMap(m);
+}
+
+void destroyKrausMap(KrausMap m) {
+    for (int n = 0; n < m.numMatrices; n++) {
+        for (qindex r = 0; r < m.numRows; r++) std::free(m.matrices[n][r]);
+        std::free(m.matrices[n]);
+    }
+    std::free(m.matrices);
+    std::free(m.superop.cpuElems);
+    std::free(m.superop.cpuElemsFlat);
+    std::free(m.superop.wasGpuSynced);
+    std::free(m.isApproxCPTP);
+}
+
+PauliStr getPauliStrFromCodes(const int* paulis, const int* indices, int num) {
+    PauliStr p{0, 0};
+    for (int i = 0; i < num; i++) {
+        if (!check(paulis[i] >= 0 && paulis[i] <= 3, "getPauliStr", "Invalid Pauli code; must be 0 (I), 1 (X), 2 (Y) or 3 (Z).")) return PauliStr{0, 0};
+        if (!check(indices[i] >= 0 && indices[i] < 64, "getPauliStr", "Invalid Pauli index.")) return PauliStr{0, 0};
+        int q = indices[i];
+        PAULI_MASK_TYPE code = (PAULI_MASK_TYPE)paulis[i];
+        if (q < 32) p.lowPaulis |= code << (2 * q);
+        else p.highPaulis |= code << (2 * (q - 32));
+    }
+    return p;
+}
+
+// ====================================================================== operations
+
+void applyCompMatr1(Qureg q, int t, CompMatr1 m) { applyDense(q, nullptr, nullptr, 0, &t, 1, &m.elems[0][0], true, "applyCompMatr1"); }
+void applyControlledCompMatr1(Qureg q, int c, int t, CompMatr1 m) { applyDense(q, &c, nullptr, 1, &t, 1, &m.elems[0][0], true, "applyControlledCompMatr1"); }
+void applyMultiControlledCompMatr1(Qureg q, int* c, int nc, int t, CompMatr1 m) { applyDense(q, c, nullptr, nc, &t, 1, &m.elems[0][0], true, "applyMultiControlledCompMatr1"); }
+void applyMultiStateControlledCompMatr1(Qureg q, int* c, int* s, int nc, int t, CompMatr1 m) { applyDense(q, c, s, nc, &t, 1, &m.elems[0][0], true, "applyMultiStateControlledCompMatr1"); }
+
+void applyCompMatr2(Qureg q, int t1, int t2, CompMatr2 m) { int t[2] = {t1, t2}; applyDense(q, nullptr, nullptr, 0, t, 2, &m.elems[0][0], true, "applyCompMatr2"); }
+void applyControlledCompMatr2(Qureg q, int c, int t1, int t2, CompMatr2 m) { int t[2] = {t1, t2}; applyDense(q, &c, nullptr, 1, t, 2, &m.elems[0][0], true, "applyControlledCompMatr2"); }
+void applyMultiStateControlledCompMatr2(Qureg q, int* c, int* s, int nc, int t1, int t2, CompMatr2 m) { int t[2] = {t1, t2}; applyDense(q, c, s, nc, t, 2, &m.elems[0][0], true, "applyMultiStateControlledCompMatr2"); }
+
+void applyCompMatr(Qureg q, int* t, int nt, CompMatr m) {
+    if (!check(m.cpuElemsFlat && m.numQubits == nt, "applyCompMatr", "The matrix size does not match the number of targets.")) return;
+    applyDense(q, nullptr, nullptr, 0, t, nt, m.cpuElemsFlat, true, "applyCompMatr");
+}
+void applyMultiStateControlledCompMatr(Qureg q, int* c, int* s, int nc, int* t, int nt, CompMatr m) {
+    if (!check(m.cpuElemsFlat && m.numQubits == nt, "applyMultiStateControlledCompMatr", "The matrix size does not match the number of targets.")) return;
+    applyDense(q, c, s, nc, t, nt, m.cpuElemsFlat, true, "applyMultiStateControlledCompMatr");
+}
+
+void applyDiagMatr1(Qureg q, int t, DiagMatr1 m) { applyDiag(q, nullptr, nullptr, 0, &t, 1, m.elems, nullptr, false, "applyDiagMatr1"); }
+void applyMultiStateControlledDiagMatr1(Qureg q, int* c, int* s, int nc, int t, DiagMatr1 m) { applyDiag(q, c, s, nc, &t, 1, m.elems, nullptr, false, "applyMultiStateControlledDiagMatr1"); }
+void applyDiagMatr2(Qureg q, int t1, int t2, DiagMatr2 m) { int t[2] = {t1, t2}; applyDiag(q, nullptr, nullptr, 0, t, 2, m.elems, nullptr, false, "applyDiagMatr2"); }
+void applyMultiStateControlledDiagMatr2(Qureg q, int* c, int* s, int nc, int t1, int t2, DiagMatr2 m) { int t[2] = {t1, t2}; applyDiag(q, c, s, nc, t, 2, m.elems, nullptr, false, "applyMultiStateControlledDiagMatr2"); }
+void applyDiagMatr(Qureg q, int* t, int nt, DiagMatr m) {
+    if (!check(m.cpuElems && m.numQubits == nt, "applyDiagMatr", "The matrix size does not match the number of targets.")) return;
+    applyDiag(q, nullptr, nullptr, 0, t, nt, m.cpuElems, nullptr, true, "applyDiagMatr");
+}
+void applyMultiStateControlledDiagMatr(Qureg q, int* c, int* s, int nc, int* t, int nt, DiagMatr m) {
+    if (!check(m.cpuElems && m.numQubits == nt, "applyMultiStateControlledDiagMatr", "The matrix size does not match the number of targets.")) return;
+    applyDiag(q, c, s, nc, t, nt, m.cpuElems, nullptr, true, "applyMultiStateControlledDiagMatr");
+}
+void applyDiagMatrPower(Qureg q, int* t, int nt, DiagMatr m, qcomp_t ex) {
+    if (!check(m.cpuElems && m.numQubits == nt, "applyDiagMatrPower", "The matrix size does not match the number of targets.")) return;
+    applyDiag(q, nullptr, nullptr, 0, t, nt, m.cpuElems, &ex, true, "applyDiagMatrPower");
+}
+void applyMultiStateControlledDiagMatrPower(Qureg q, int* c, int* s, int nc, int* t, int nt, DiagMatr m, qcomp_t ex) {
+    if (!check(m.cpuElems && m.numQubits == nt, "applyMultiStateControlledDiagMatrPower", "The matrix size does not match the number of targets.")) return;
+    applyDiag(q, c, s, nc, t, nt, m.cpuElems, &ex, true, "applyMultiStateControlledDiagMatrPower");
+}
+
+// S = diag(1, i) (operations.cpp:614-618); T = diag(1, 1/sqrt2 + i/sqrt2) (:665-669)
+void applyS(Qureg q, int t) { qcomp_t d[2] = {{1, 0}, {0, 1}}; applyDiag(q, nullptr, nullptr, 0, &t, 1, d, nullptr, false, "applyS"); }
+void applyT(Qureg q, int t) { double r = 1 / std::sqrt(2); qcomp_t d[2] = {{1, 0}, {r, r}}; applyDiag(q, nullptr, nullptr, 0, &t, 1, d, nullptr, false, "applyT"); }
+
+// operations.cpp:716-723: a = 1/sqrt(2)
+void applyMultiStateControlledHadamard(Qureg q, int* c, int* s, int nc, int t) {
+    double a = 1 / std::sqrt(2);
+    qcomp_t m[4] = {{a, 0}, {a, 0}, {a, 0}, {-a, 0}};
+    applyDense(q, c, s, nc, &t, 1, m, false, "applyHadamard");
+}
+void applyHadamard(Qureg q, int t) { applyMultiStateControlledHadamard(q, nullptr, nullptr, 0, t); }
+
+// operations.cpp:778-796
+void applyMultiStateControlledSwap(Qureg q, int* c, int* s, int nc, int a, int b) {
+    const char* func = "applySwap";
+    if (!checkQureg(q, func)) return;
+    int t[2] = {a, b};
+    if (!checkCtrlsTargs(q, c, nc, t, 2, func) || !checkStates(s, nc, func)) return;
+    vector<int> cv = V(c, nc), sv = V(s, nc);
+    if (!backend(qg_sv_anyCtrlSwap(q.gpuAmps, nsv(q), P(cv), S(sv), nc, a, b, g_stream), func)) return;
+    if (!q.isDensityMatrix) return;
+    vector<int> bc = braOf(q, cv);
+    backend(qg_sv_anyCtrlSwap(q.gpuAmps, nsv(q), P(bc), S(sv), nc, a + q.numQubits, b + q.numQubits, g_stream), func);
+}
+void applySwap(Qureg q, int a, int b) { applyMultiStateControlledSwap(q, nullptr, nullptr, 0, a, b); }
+
+// applyMultiStateControlledPauliStr: operations.cpp:1061-1090
+void applyMultiStateControlledPauliStr(Qureg q, int* c, int* s, int nc, PauliStr str) {
+    const char* func = "applyPauliStr";
+    if (!checkQureg(q, func) || !checkPauliTargs(q, c, nc, str, func) || !checkStates(s, nc, func)) return;
+    vector<int> cv = V(c, nc), sv = V(s, nc);
+    vector<int> ket = codesOf(str, q.numQubits);
+    bool oddY = numY(ket) % 2;
+    if (q.isDensityMatrix && nc == 0) {
+        vector<int> both = paddedCodes(q, ket), sh = shiftedCodes(q, ket);
+        for (size_t i = 0; i < both.size(); i++) both[i] |= sh[i];
+        pauliTensorSV(q, cv, sv, both, oddY ? -1.0 : 1.0, func);
+        return;
+    }
+    if (!pauliTensorSV(q, cv, sv, q.isDensityMatrix ? paddedCodes(q, ket) : ket, 1.0, func)) return;
+    if (q.isDensityMatrix) pauliTensorSV(q, braOf(q, cv), sv, shiftedCodes(q, ket), oddY ? -1.0 : 1.0, func);
+}
+void applyPauliStr(Qureg q, PauliStr str) { applyMultiStateControlledPauliStr(q, nullptr, nullptr, 0, str); }
+
+void applyPauliX(Qureg q, int t) {
+    if (!checkQureg(q, "applyPauliX") || !checkQubits(q, &t, 1, "applyPauliX", "target qubits")) return;
+    int code = 1; applyPauliStr(q, getPauliStrFromCodes(&code, &t, 1));
+}
+void applyPauliY(Qureg q, int t) {
+    if (!checkQureg(q, "applyPauliY") || !checkQubits(q, &t, 1, "applyPauliY", "target qubits")) return;
+    int code = 2; applyPauliStr(q, getPauliStrFromCodes(&code, &t, 1));
+}
+// Z = DiagMatr1 {1, -1} (operations.cpp:977-985)
+void applyPauliZ(Qureg q, int t) { qcomp_t d[2] = {{1, 0}, {-1, 0}}; applyDiag(q, nullptr, nullptr, 0, &t, 1, d, nullptr, false, "applyPauliZ"); }
+void applyControlledPauliX(Qureg q, int c, int t) {
+    if (!checkQureg(q, "applyControlledPauliX") || !checkCtrlsTargs(q, &c, 1, &t, 1, "applyControlledPauliX")) return;
+    int code = 1; applyMultiStateControlledPauliStr(q, &c, nullptr, 1, getPauliStrFromCodes(&code, &t, 1));
+}
+void applyControlledPauliZ(Qureg q, int c, int t) { qcomp_t d[2] = {{1, 0}, {-1, 0}}; applyDiag(q, &c, nullptr, 1, &t, 1, d, nullptr, false, "applyControlledPauliZ"); }
+
+// applyMultiStateControlledPauliGadget: operations.cpp:1449-1476 (phase = -angle/2, utilities.cpp:911-914)
+void applyMultiStateControlledPauliGadget(Qureg q, int* c, int* s, int nc, PauliStr str, qreal angle) {
+    const char* func = "applyPauliGadget";
+    if (!checkQureg(q, func) || !checkPauliTargs(q, c, nc, str, func) || !checkStates(s, nc, func)) return;
+    vector<int> ket = codesOf(str, q.numQubits);
+    bool isId = std::all_of(ket.begin(), ket.end(), [](int v) { return v == 0; });
+    if (isId && nc == 0 && q.isDensityMatrix) return;
+    double phase = -angle / 2;
+    vector<int> cv = V(c, nc), sv = V(s, nc);
+    if (!pauliGadgetSV(q, cv, sv, q.isDensityMatrix ? paddedCodes(q, ket) : ket, phase, func)) return;
+    if (!q.isDensityMatrix) return;
+    phase *= (numY(ket) % 2) ? 1 : -1;
+    pauliGadgetSV(q, braOf(q, cv), sv, shiftedCodes(q, ket), phase, func);
+}
+void applyPauliGadget(Qureg q, PauliStr str, qreal angle) { applyMultiStateControlledPauliGadget(q, nullptr, nullptr, 0, str, angle); }
+
+void applyRotateX(Qureg q, int t, qreal a) { if (!checkQureg(q, "applyRotateX") || !checkQubits(q, &t, 1, "applyRotateX", "target qubits")) return; int p = 1; applyPauliGadget(q, getPauliStrFromCodes(&p, &t, 1), a); }
+void applyRotateY(Qureg q, int t, qreal a) { if (!checkQureg(q, "applyRotateY") || !checkQubits(q, &t, 1, "applyRotateY", "target qubits")) return; int p = 2; applyPauliGadget(q, getPauliStrFromCodes(&p, &t, 1), a); }
+void applyRotateZ(Qureg q, int t, qreal a) { if (!checkQureg(q, "applyRotateZ") || !checkQubits(q, &t, 1, "applyRotateZ", "target qubits")) return; int p = 3; applyPauliGadget(q, getPauliStrFromCodes(&p, &t, 1), a); }
+void applyControlledRotateX(Qureg q, int c, int t, qreal a) { if (!checkQureg(q, "applyControlledRotateX") || !checkCtrlsTargs(q, &c, 1, &t, 1, "applyControlledRotateX")) return; int p = 1; applyMultiStateControlledPauliGadget(q, &c, nullptr, 1, getPauliStrFromCodes(&p, &t, 1), a); }
+void applyControlledRotateY(Qureg q, int c, int t, qreal a) { if (!checkQureg(q, "applyControlledRotateY") || !checkCtrlsTargs(q, &c, 1, &t, 1, "applyControlledRotateY")) return; int p = 2; applyMultiStateControlledPauliGadget(q, &c, nullptr, 1, getPauliStrFromCodes(&p, &t, 1), a); }
+void applyControlledRotateZ(Qureg q, int c, int t, qreal a) { if (!checkQureg(q, "applyControlledRotateZ") || !checkCtrlsTargs(q, &c, 1, &t, 1, "applyControlledRotateZ")) return; int p = 3; applyMultiStateControlledPauliGadget(q, &c, nullptr, 1, getPauliStrFromCodes(&p, &t, 1), a); }
+
+// applyMultiStateControlledPhaseGadget: operations.cpp:1532-1549
+void applyMultiStateControlledPhaseGadget(Qureg q, int* c, int* s, int nc, int* t, int nt, qreal angle) {
+    const char* func = "applyPhaseGadget";
+    if (!checkQureg(q, func) || !checkCtrlsTargs(q, c, nc, t, nt, func) || !checkStates(s, nc, func)) return;
+    double phase = -angle / 2;
+    vector<int> cv = V(c, nc), sv = V(s, nc), tv = V(t, nt);
+    if (!phaseGadgetSV(q, cv, sv, tv, phase, func)) return;
+    if (!q.isDensityMatrix) return;
+    phaseGadgetSV(q, braOf(q, cv), sv, braOf(q, tv), -phase, func);
+}
+void applyPhaseGadget(Qureg q, int* t, int nt, qreal angle) { applyMultiStateControlledPhaseGadget(q, nullptr, nullptr, 0, t, nt, angle); }
+
+// applyMultiQubitPhaseShift: a (n-1)-controlled DiagMatr1 {1, e^(i angle)} (operations.cpp:1605-1613)
+void applyMultiQubitPhaseShift(Qureg q, int* t, int nt, qreal angle) {
+    const char* func = "applyMultiQubitPhaseShift";
+    if (!checkQureg(q, func) || !checkQubits(q, t, nt, func, "target qubits")) return;
+    if (!check(nt >= 1, func, "At least one target qubit is required.")) return;
+    cd e = std::exp(cd(0, 1) * angle);
+    qcomp_t d[2] = {{1, 0}, Q(e)};
+    applyDiag(q, t + 1, nullptr, nt - 1, &t[0], 1, d, nullptr, false, func);
+}
+void applyPhaseShift(Qureg q, int t, qreal a) { applyMultiQubitPhaseShift(q, &t, 1, a); }
+void applyTwoQubitPhaseShift(Qureg q, int t1, int t2, qreal a) { int t[2] = {t1, t2}; applyMultiQubitPhaseShift(q, t, 2, a); }
+void applyPhaseFlip(Qureg q, int t) { qcomp_t d[2] = {{1, 0}, {-1, 0}}; applyDiag(q, nullptr, nullptr, 0, &t, 1, d, nullptr, false, "applyPhaseFlip"); }
+void applyTwoQubitPhaseFlip(Qureg q, int t1, int t2) { qcomp_t d[2] = {{1, 0}, {-1, 0}}; applyDiag(q, &t2, nullptr, 1, &t1, 1, d, nullptr, false, "applyTwoQubitPhaseFlip"); }
+
+// applyQuantumFourierTransform: operations.cpp:1934-1952
+void applyQuantumFourierTransform(Qureg q, int* t, int nt) {
+    const char* func = "applyQuantumFourierTransform";
+    if (!checkQureg(q, func) || !checkQubits(q, t, nt, func, "target qubits")) return;
+    const double PI = 3.141592653589793238462643383279502884;
+    for (int n = nt - 1; n >= 0; n--) {
+        applyHadamard(q, t[n]);
+        for (int m = 0; m < n; m++) {
+            double arg = PI / (double)((qindex)1 << (m + 1));
+            applyTwoQubitPhaseShift(q, t[n], t[n - m - 1], arg);
+        }
+    }
+    for (int n = 0; n < nt / 2; n++) applySwap(q, t[n], t[nt - 1 - n]);
+}
+void applyFullQuantumFourierTransform(Qureg q) {
+    if (!checkQureg(q, "applyFullQuantumFourierTransform")) return;
+    vector<int> t(q.numQubits);
+    for (int i = 0; i < q.numQubits; i++) t[i] = i;
+    applyQuantumFourierTransform(q, t.data(), (int)t.size());
+}
+
+// projectors and measurement: operations.cpp:1754-1826, localiser.cpp:2295-2322
+void applyMultiQubitProjector(Qureg q, int* qs, int* os, int n) {
+    const char* func = "applyMultiQubitProjector";
+    if (!checkQureg(q, func) || !checkQubits(q, qs, n, func, "target qubits")) return;
+    for (int i = 0; i < n; i++)
+        if (!check(os[i] == 0 || os[i] == 1, func, "Invalid measurement outcome; must be 0 or 1.")) return;
+    project(q, V(qs, n), V(os, n), 1.0, func);
+}
+void applyQubitProjector(Qureg q, int t, int o) { applyMultiQubitProjector(q, &t, &o, 1); }
+
+int applyQubitMeasurementAndGetProb(Qureg q, int t, qreal* probability) {
+    const char* func = "applyQubitMeasurement";
+    if (!checkQureg(q, func) || !checkQubits(q, &t, 1, func, "target qubits")) return -1;
+    double p[2];
+    if (!probOf(q, {t}, {0}, &p[0], func) || !probOf(q, {t}, {1}, &p[1], func)) return -1;
+    if (!check(std::abs(p[0] + p[1] - 1) <= g_eps, func, "The outcome probabilities do not sum to one; the state is not normalised.")) return -1;
+    std::uniform_real_distribution<double> distrib(0, 1);
+    double sample = distrib(g_rng);
+    int outcome = sample > p[0];
+    if (probability) *probability = p[outcome];
+    project(q, {t}, {outcome}, p[outcome], func);
+    return outcome;
+}
+int applyQubitMeasurement(Qureg q, int t) { qreal p = 0; return applyQubitMeasurementAndGetProb(q, t, &p); }
+
+// ====================================================================== decoherence (decoherence.cpp:31-131)
+
+void mixDephasing(Qureg q, int qubit, qreal prob) {
+    const char* func = "mixDephasing";
+    if (!checkQureg(q, func) || !checkQubits(q, &qubit, 1, func, "target qubits") || !checkProb(prob, 0.5, func)) return;
+    if (prob == 0) return;
+    if (!checkDensMatr(q, func)) return;
+    backend(qg_dm_oneQubitDephasing(q.gpuAmps, q.numQubits, qubit, prob, g_stream), func);
+}
+void mixTwoQubitDephasing(Qureg q, int a, int b, qreal prob) {
+    const char* func = "mixTwoQubitDephasing";
+    int t[2] = {a, b};
+    if (!checkQureg(q, func) || !checkQubits(q, t, 2, func, "target qubits") || !checkProb(prob, 0.75, func)) return;
+    if (prob == 0) return;
+    if (!checkDensMatr(q, func)) return;
+    backend(qg_dm_twoQubitDephasing(q.gpuAmps, q.numQubits, a, b, prob, g_stream), func);
+}
+void mixDepolarising(Qureg q, int qubit, qreal prob) {
+    const char* func = "mixDepolarising";
+    if (!checkQureg(q, func) || !checkQubits(q, &qubit, 1, func, "target qubits") || !checkProb(prob, 0.75, func)) return;
+    if (prob == 0) return;
+    if (!checkDensMatr(q, func)) return;
+    backend(qg_dm_oneQubitDepolarising(q.gpuAmps, q.numQubits, qubit, prob, g_stream), func);
+}
+void mixTwoQubitDepolarising(Qureg q, int a, int b, qreal prob) {
+    const char* func = "mixTwoQubitDepolarising";
+    int t[2] = {a, b};
+    if (!checkQureg(q, func) || !checkQubits(q, t, 2, func, "target qubits") || !checkProb(prob, 15.0 / 16, func)) return;
+    if (prob == 0) return;
+    if (!checkDensMatr(q, func)) return;
+    backend(qg_dm_twoQubitDepolarising(q.gpuAmps, q.numQubits, a, b, prob, g_stream), func);
+}
+void mixDamping(Qureg q, int qubit, qreal prob) {
+    const char* func = "mixDamping";
+    if (!checkQureg(q, func) || !checkQubits(q, &qubit, 1, func, "target qubits") || !checkProb(prob, 1.0, func)) return;
+    if (prob == 0) return;
+    if (!checkDensMatr(q, func)) return;
+    backend(qg_dm_oneQubitDamping(q.gpuAmps, q.numQubits, qubit, prob, g_stream), func);
+}
+void mixPaulis(Qureg q, int qubit, qreal px, qreal py, qreal pz) {
+    const char* func = "mixPaulis";
+    if (!checkQureg(q, func) || !checkQubits(q, &qubit, 1, func, "target qubits")) return;
+    if (!checkProb(px, 1, func) || !checkProb(py, 1, func) || !checkProb(pz, 1, func)) return;
+    if (px == 0 && py == 0 && pz == 0) return;
+    if (!checkDensMatr(q, func)) return;
+    backend(qg_dm_oneQubitPauliChannel(q.gpuAmps, q.numQubits, qubit, px, py, pz, g_stream), func);
+}
+
+// mixKrausMap: the superoperator as a dense matrix on targets {ket..., bra...}
+// (localiser_densmatr_superoperator, localiser.cpp:1670-1686), not conjugated
+void mixKrausMap(Qureg q, int* qubits, int n, KrausMap map) {
+    const char* func = "mixKrausMap";
+    if (!checkQureg(q, func) || !checkDensMatr(q, func) || !checkQubits(q, qubits, n, func, "target qubits")) return;
+    if (!check(map.numQubits == n && map.superop.cpuElemsFlat, func, "The Kraus map size does not match the number of targets.")) return;
+    // util_isCPTP (utilities.cpp:729-768): sum_n K_n^dagger K_n = I within eps (squared distance)
+    if (*map.isApproxCPTP == -1) {
+        int ok = 1;
+        for (qindex r = 0; r < map.numRows && ok; r++)
+            for (qindex c = 0; c < map.numRows && ok; c++) {
+                cd e = 0;
+                for (int k = 0; k < map.numMatrices; k++)
+                    for (qindex i = 0; i < map.numRows; i++) e += std::conj(C(map.matrices[k][i][r])) * C(map.matrices[k][i][c]);
+                if (std::norm(e - cd(r == c, 0)) > g_eps) ok = 0;
+            }
+        *map.isApproxCPTP = ok;
+    }
+    if (!check(*map.isApproxCPTP == 1, func, "The Kraus map is not (approximately) completely positive and trace preserving.")) return;
+    vector<int> t(qubits, qubits + n);
+    for (int i = 0; i < n; i++) t.push_back(qubits[i] + q.numQubits);
+    denseSV(q, {}, {}, t, map.superop.cpuElemsFlat, false, func);
+}
+
+// ====================================================================== calculations
+
+qreal calcTotalProb(Qureg q) {
+    const char* func = "calcTotalProb";
+    if (!checkQureg(q, func)) return 0;
+    double v = 0;
+    if (q.isDensityMatrix) backend(qg_dm_calcTotalProb(q.gpuAmps, q.numQubits, &v, g_stream), func);
+    else backend(qg_sv_calcTotalProb(q.gpuAmps, q.numQubits, &v, g_stream), func);
+    return v;
+}
+
+// calcPurity: calculations.cpp:293-300
+qreal calcPurity(Qureg q) {
+    const char* func = "calcPurity";
+    if (!checkQureg(q, func)) return 0;
+    double v = 0;
+    backend(qg_sv_calcTotalProb(q.gpuAmps, nsv(q), &v, g_stream), func);
+    return q.isDensityMatrix ? v : v * v;
+}
+
+qreal calcProbOfMultiQubitOutcome(Qureg q, int* qs, int* os, int n) {
+    const char* func = "calcProbOfMultiQubitOutcome";
+    if (!checkQureg(q, func) || !checkQubits(q, qs, n, func, "target qubits")) return 0;
+    for (int i = 0; i < n; i++)
+        if (!check(os[i] == 0 || os[i] == 1, func, "Invalid measurement outcome; must be 0 or 1.")) return 0;
+    double v = 0;
+    probOf(q, V(qs, n), V(os, n), &v, func);
+    return v;
+}
+qreal calcProbOfQubitOutcome(Qureg q, int qubit, int outcome) { return calcProbOfMultiQubitOutcome(q, &qubit, &outcome, 1); }
+
+void calcProbsOfAllMultiQubitOutcomes(qreal* out, Qureg q, int* qs, int n) {
+    const char* func = "calcProbsOfAllMultiQubitOutcomes";
+    if (!checkQureg(q, func) || !checkQubits(q, qs, n, func, "target qubits")) return;
+    if (!q.isDensityMatrix) {
+        backend(qg_sv_calcProbsOfAllMultiQubitOutcomes(out, q.gpuAmps, q.numQubits, qs, n, g_stream), func);
+        return;
+    }
+    // density matrix: one diagonal reduction per outcome
+    vector<int> qv(qs, qs + n), ov(n);
+    for (qindex b = 0; b < ((qindex)1 << n); b++) {
+        for (int i = 0; i < n; i++) ov[i] = (int)((b >> i) & 1);
+        if (!probOf(q, qv, ov, &out[b], func)) return;
+    }
+}
+
+// calcExpecPauliStr: calculations.cpp:133-144 and localiser.cpp:1963-2049
+qreal calcExpecPauliStr(Qureg q, PauliStr str) {
+    const char* func = "calcExpecPauliStr";
+    if (!checkQureg(q, func)) return 0;
+    if (!check(strFits(str, q.numQubits), func, "The Pauli string targets a qubit beyond the Qureg.")) return 0;
+    vector<int> x, y, z;
+    splitXYZ(codesOf(str, q.numQubits), x, y, z);
+    qcomp_t v{0, 0};
+    bool ok = q.isDensityMatrix
+                  ? backend(qg_dm_calcExpecPauliStr(q.gpuAmps, q.numQubits, P(x), (int)x.size(), P(y), (int)y.size(), P(z), (int)z.size(), &v, g_stream), func)
+                  : backend(qg_sv_calcExpecPauliStr(q.gpuAmps, q.numQubits, P(x), (int)x.size(), P(y), (int)y.size(), P(z), (int)z.size(), &v, g_stream), func);
+    if (!ok) return 0;
+    if (!check(std::abs(v.im) <= REDUCTION_EPS_FACTOR * g_eps, func, "The expectation value was not approximately real.")) return 0;
+    return v.re;
+}
+
+void calcExpecPauliStrs(qreal* out, Qureg q, const PauliStr* strs, int num) {
+    const char* func = "calcExpecPauliStrs";
+    if (!checkQureg(q, func)) return;
+    if (q.isDensityMatrix) {
+        for (int s = 0; s < num; s++) out[s] = calcExpecPauliStr(q, strs[s]);
+        return;
+    }
+    vector<int64_t> mxy(num), myz(num);
+    vector<int> ny(num);
+    for (int s = 0; s < num; s++) {
+        if (!check(strFits(strs[s], q.numQubits), func, "A Pauli string targets a qubit beyond the Qureg.")) return;
+        vector<int> codes = codesOf(strs[s], q.numQubits);
+        int64_t a = 0, b = 0;
+        for (int i = 0; i < q.numQubits; i++) {
+            if (codes[i] == 1 || codes[i] == 2) a |= (int64_t)1 << i;
+            if (codes[i] == 2 || codes[i] == 3) b |= (int64_t)1 << i;
+        }
+        mxy[s] = a;
+        myz[s] = b;
+        ny[s] = numY(codes);
+    }
+    vector<qcomp_t> v(num);
+    if (!backend(qg_sv_calcExpecPauliStrBatch(q.gpuAmps, q.numQubits, mxy.data(), myz.data(), ny.data(), num, v.data(), g_stream), func)) return;
+    for (int s = 0; s < num; s++) out[s] = v[s].re;
+}
+
+}  // extern "C"

@@ -1,0 +1,264 @@
+"""GPU parity: the GB300 path (QuEST-named API over the C ABI) against the
+CPU oracle and the reference's golden fixtures.
+
+Bar (FP64): max-abs difference per amplitude and per reduction <= 1e-12;
+index/permutation work and sampled measurement outcomes bit-exact."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+import qcircuits as qc
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-12
+GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+
+
+def run_gpu(env, text, nq, is_dm, amps):
+    from quest_gb300.circuit import run_text
+    Q = env.Q
+    q = Q.createDensityQureg(nq) if is_dm else Q.createQureg(nq)
+    try:
+        env.set_amps(q, amps)
+        res, outs = run_text("SEED 0\n" + text, q)
+        out = env.get_amps(q)
+    finally:
+        Q.destroyQureg(q)
+    return out, res, outs
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[:-4] for p in GOLDEN])
+def test_golden_fixture_on_gpu(env, path):
+    z = np.load(path)
+    out, res, outs = run_gpu(env, str(z["text"]), int(z["nq"]), int(z["is_dm"]), z["amps_in"])
+    assert np.max(np.abs(out - z["amps_out"])) <= TOL
+    assert np.max(np.abs(res - z["results"]), initial=0) <= TOL
+    assert outs.tolist() == z["outcomes"].tolist()
+
+
+@pytest.mark.parametrize("nq,is_dm,seed", [(3, 0, 1), (4, 0, 2), (7, 0, 3), (10, 0, 4), (13, 0, 5), (16, 0, 6),
+                                           (3, 1, 7), (5, 1, 8), (7, 1, 9)])
+def test_every_op_vs_oracle(env, nq, is_dm, seed):
+    text = qc.every_op_circuit(nq, is_dm, seed)
+    amps = qc.random_density_matrix(nq, seed) if is_dm else qc.random_statevector(nq, seed)
+    a1, r1, o1 = qc.oracle().run(text, nq, is_dm, amps)
+    a2, r2, o2 = run_gpu(env, text, nq, is_dm, amps)
+    assert np.max(np.abs(a1 - a2)) <= TOL
+    assert np.max(np.abs(r1 - r2)) <= TOL
+    assert o1.tolist() == o2.tolist()
+
+
+def test_config1_shape_vs_oracle(env):
+    """The plain method's circuit shape at 14 qubits, 4 layers."""
+    nq = 14
+    text = qc.config1_circuit(nq, 4, 77)
+    amps = qc.random_statevector(nq, 77)
+    a1, r1, _ = qc.oracle().run(text, nq, 0, amps)
+    a2, r2, _ = run_gpu(env, text, nq, 0, amps)
+    assert np.max(np.abs(a1 - a2)) <= TOL
+    assert np.max(np.abs(r1 - r2)) <= TOL
+
+
+def _all_ctrl_targ_cases(n, rng):
+    """Every target (and target pair) with 0, 1 and 2 controls in random states."""
+    cases = []
+    for t in range(n):
+        others = [q for q in range(n) if q != t]
+        cases.append(([], [], [t]))
+        for c in others:
+            cases.append(([c], [int(rng.integers(2))], [t]))
+        c2 = [int(v) for v in rng.choice(others, 2, replace=False)]
+        cases.append((c2, [int(v) for v in rng.integers(0, 2, 2)], [t]))
+    for t1 in range(n):
+        for t2 in range(n):
+            if t1 != t2:
+                others = [q for q in range(n) if q not in (t1, t2)]
+                c = [int(rng.choice(others))]
+                cases.append(([], [], [t1, t2]))
+                cases.append((c, [int(rng.integers(2))], [t1, t2]))
+    return cases
+
+
+def test_every_ctrl_and_target_permutation(env):
+    """All single/pair target placements with controls, for dense, diagonal,
+    swap and Pauli ops, at 7 qubits (the reference's unit tests enumerate
+    ctrl/target permutations the same way)."""
+    n = 7
+    rng = np.random.default_rng(2024)
+    lines = []
+    for c, s, t in _all_ctrl_targ_cases(n, rng):
+        nc = len(c)
+        pre = f"{nc} {' '.join(map(str, c))} {' '.join(map(str, s))}".replace("  ", " ")
+        if len(t) == 1:
+            m = qc.mat_tokens(qc.haar_unitary(2, rng))
+            lines.append(f"CU1 {pre} {t[0]} {m}" if nc else f"U1 {t[0]} {m}")
+            d = qc.mat_tokens(np.exp(1j * rng.uniform(0, 6.3, 2)))
+            lines.append(f"CDK {pre} 1 {t[0]} {d}" if nc else f"D1 {t[0]} {d}")
+            codes = [0] * n
+            codes[t[0]] = int(rng.integers(1, 4))
+            lines.append(f"CPSTR {pre} {qc.pauli_text(codes)}" if nc else f"PSTR {qc.pauli_text(codes)}")
+            lines.append(f"CPG {pre} {qc.pauli_text(codes)} {qc.fmt(rng.uniform(0, 6.3))}" if nc else f"PG {qc.pauli_text(codes)} {qc.fmt(rng.uniform(0, 6.3))}")
+        else:
+            m = qc.mat_tokens(qc.haar_unitary(4, rng))
+            lines.append(f"CU2 {pre} {t[0]} {t[1]} {m}" if nc else f"U2 {t[0]} {t[1]} {m}")
+            lines.append(f"CSWAP {pre} {t[0]} {t[1]}" if nc else f"SWAP {t[0]} {t[1]}")
+            d = qc.mat_tokens(np.exp(1j * rng.uniform(0, 6.3, 4)))
+            lines.append(f"CDK {pre} 2 {t[0]} {t[1]} {d}" if nc else f"D2 {t[0]} {t[1]} {d}")
+    lines.append("TOTALPROB")
+    text = "\n".join(lines) + "\n"
+    for is_dm, nq in ((0, n), (1, 3)):
+        if is_dm:
+            # density matrices use only qubits < 3 from the same op kinds
+            sub = [l for l in lines if all(int(tok) < 3 for tok in _qubit_tokens(l))]
+            text_dm = "\n".join(sub) + "\n"
+            amps = qc.random_density_matrix(nq, 9)
+            a1, r1, _ = qc.oracle().run(text_dm, nq, 1, amps)
+            a2, r2, _ = run_gpu(env, text_dm, nq, 1, amps)
+        else:
+            amps = qc.random_statevector(nq, 9)
+            a1, r1, _ = qc.oracle().run(text, nq, 0, amps)
+            a2, r2, _ = run_gpu(env, text, nq, 0, amps)
+        assert np.max(np.abs(a1 - a2)) <= TOL
+        assert np.max(np.abs(r1 - r2)) <= TOL
+
+
+def _qubit_tokens(line):
+    tok = line.split()
+    op = tok[0]
+    if op in ("U1", "D1"):
+        return [tok[1]]
+    if op in ("U2", "SWAP", "D2"):
+        return tok[1:3]
+    if op in ("PSTR", "PG"):
+        return [str(i) for i, ch in enumerate(tok[1]) if ch != "I"]
+    if op.startswith("C"):
+        nc = int(tok[1])
+        qs = tok[2:2 + nc]
+        rest = tok[2 + 2 * nc:]
+        if op in ("CU1",):
+            return qs + [rest[0]]
+        if op in ("CU2", "CSWAP"):
+            return qs + rest[:2]
+        if op == "CDK":
+            k = int(rest[0])
+            return qs + rest[1:1 + k]
+        if op in ("CPSTR", "CPG"):
+            return qs + [str(i) for i, ch in enumerate(rest[0]) if ch != "I"]
+    return []
+
+
+def test_dense_many_targets_vs_oracle(env):
+    """Dense matrices of 3..8 targets (register, parameter-space and shared-memory paths)."""
+    rng = np.random.default_rng(11)
+    n = 10
+    lines = []
+    for k in (3, 4, 5, 6, 7, 8):
+        t = [int(v) for v in rng.choice(n, k, replace=False)]
+        lines.append(f"UK {k} {' '.join(map(str, t))} {qc.mat_tokens(qc.haar_unitary(1 << k, rng))}")
+    c = [int(v) for v in rng.choice(n, 7, replace=False)]
+    lines.append(f"CUK 1 {c[0]} 0 6 {' '.join(map(str, c[1:]))} {qc.mat_tokens(qc.haar_unitary(64, rng))}")
+    text = "\n".join(lines) + "\nTOTALPROB\n"
+    amps = qc.random_statevector(n, 12)
+    a1, r1, _ = qc.oracle().run(text, n, 0, amps)
+    a2, r2, _ = run_gpu(env, text, n, 0, amps)
+    assert np.max(np.abs(a1 - a2)) <= TOL
+    assert np.max(np.abs(r1 - r2)) <= TOL
+
+
+def test_measurement_outcomes_bit_exact_under_shared_seed(env):
+    nq = 12
+    rng = np.random.default_rng(5)
+    lines = [f"SEED {int(rng.integers(1 << 30))} {int(rng.integers(1 << 30))}"]
+    for _ in range(3):
+        for t in range(nq):
+            lines.append(f"U1 {t} {qc.mat_tokens(qc.haar_unitary(2, rng))}")
+        for t in range(0, nq - 1, 2):
+            lines.append(f"CZ {t} {t + 1}")
+        for t in rng.choice(nq, 3, replace=False):
+            lines.append(f"MEAS {int(t)}")
+    text = "\n".join(lines) + "\nTOTALPROB\n"
+    amps = qc.random_statevector(nq, 6)
+    a1, r1, o1 = qc.oracle().run(text, nq, 0, amps)
+    a2, r2, o2 = run_gpu(env, text, nq, 0, amps)
+    assert o1.tolist() == o2.tolist() and len(o1) == 9
+    assert np.max(np.abs(a1 - a2)) <= TOL
+
+
+def test_reductions_are_deterministic(env):
+    Q = env.Q
+    nq = 22
+    q = Q.createQureg(nq)
+    try:
+        env.set_amps(q, qc.random_statevector(nq, 3))
+        p = env.pauli_str("XYZI" * 5 + "XY")
+        vals = [(Q.calcTotalProb(q), Q.calcExpecPauliStr(q, p), Q.calcProbOfQubitOutcome(q, 17, 1)) for _ in range(3)]
+        assert vals[0] == vals[1] == vals[2]
+    finally:
+        Q.destroyQureg(q)
+
+
+def test_large_state_properties(env):
+    """Size-independent properties at 26 qubits (1 GiB): involutions and
+    permutations are bit-exact, unitary layers keep the norm."""
+    Q = env.Q
+    nq = 26
+    amps = qc.random_statevector(nq, 42)
+    q = Q.createQureg(nq)
+    try:
+        env.set_amps(q, amps)
+        for t in (0, 5, 13, 25):
+            Q.applyPauliX(q, t)
+            Q.applyPauliX(q, t)
+        Q.applySwap(q, 3, 24)
+        Q.applySwap(q, 24, 3)
+        Q.applyControlledPauliX(q, 25, 0)
+        Q.applyControlledPauliX(q, 25, 0)
+        out = env.get_amps(q)
+        assert np.array_equal(out, amps)
+        # CNOT 0 -> 25 permutes amplitudes exactly like the numpy index map
+        Q.applyControlledPauliX(q, 0, 25)
+        out = env.get_amps(q)
+        idx = np.arange(1 << nq)
+        perm = np.where(idx & 1, idx ^ (1 << 25), idx)
+        assert np.array_equal(out, amps[perm])
+        rng = np.random.default_rng(1)
+        for t in range(nq):
+            Q.applyCompMatr1(q, t, env.comp_matr1(qc.haar_unitary(2, rng)))
+        assert abs(Q.calcTotalProb(q) - 1) < 1e-11
+    finally:
+        Q.destroyQureg(q)
+
+
+def test_invalid_input_raises(env):
+    Q = env.Q
+    q = Q.createQureg(4)
+    try:
+        with pytest.raises(env.QuESTError):
+            Q.applyHadamard(q, 4)
+        with pytest.raises(env.QuESTError):
+            Q.applyControlledPauliX(q, 2, 2)
+        with pytest.raises(env.QuESTError):
+            Q.applyCompMatr1(q, 0, env.comp_matr1([[1, 1], [0, 1]]))   # not unitary
+        with pytest.raises(env.QuESTError):
+            Q.mixDepolarising(q, 0, 0.1)   # statevector
+        d = Q.createDensityQureg(2)
+        with pytest.raises(env.QuESTError):
+            Q.mixDepolarising(d, 0, 0.8)   # beyond maximal mixing
+        Q.destroyQureg(d)
+    finally:
+        Q.destroyQureg(q)
+
+
+def test_abi_rejects_bad_arguments(env):
+    from quest_gb300 import _lib
+    L = _lib.lib()
+    q = env.Q.createQureg(3)
+    try:
+        m = _lib.cplx_array([1, 0, 0, 1])
+        assert L.qg_sv_anyCtrlOneTargDenseMatr(q.gpuAmps, 3, None, None, 0, 3, m, None) == -2
+        assert L.qg_sv_anyCtrlSwap(q.gpuAmps, 3, None, None, 0, 1, 1, None) == -2
+        assert L.qg_sv_anyCtrlOneTargDenseMatr(None, 3, None, None, 0, 0, m, None) == -2
+    finally:
+        env.Q.destroyQureg(q)
