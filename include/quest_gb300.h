@@ -63,6 +63,11 @@ int qg_stream_sync(void* stream);
 int qg_get_cache_size(int64_t* out);                       /* getGpuCacheSize (quest/src/api/debug.cpp:180) */
 int qg_clear_cache(void);                                  /* gpu_clearCache (gpu_config.cpp:665) */
 int qg_get_launch_count(int64_t* out);                     /* kernels launched by this library so far */
+/* CUDA events on the launching stream, for timing kernels from a host harness */
+int qg_event_create(void** out);
+int qg_event_destroy(void* event);
+int qg_event_record(void* event, void* stream);
+int qg_event_elapsed_ms(void* start, void* stop, float* ms); /* waits for `stop` */
 
 /* ------------------------------------------------------------------ initialisation
  * replaces gpu_statevec_initUniformState_sub / initDebugState_sub
@@ -177,6 +182,38 @@ int qg_dm_calcExpecPauliStr(const void* amps, int numKetQubits, const int* targs
  * Strings are given as (maskXY, maskYZ, numY) triples; out[s] is string s's value. */
 int qg_sv_calcExpecPauliStrBatch(const void* amps, int numQubits, const int64_t* masksXY, const int64_t* masksYZ,
                                  const int* numsY, int numStrings, qg_cplx* out, void* stream);
+
+/* ------------------------------------------------------------------ FP32 fused-block path
+ * A circuit of small dense unitaries is fused on the host into blocks of at most
+ * k <= 5 qubits (each block's matrix formed in FP64), then applied to an FP32
+ * (complex64) statevector one block per pass.  A block is the few-target dense
+ * primitive of gpu_statevec_anyCtrlAnyTargDenseMatr_sub (gpu_kernels.cuh:296-356)
+ * in FP32; 5-qubit blocks can run on the tensor cores as 3xTF32 GEMM tiles. */
+
+typedef struct qg_circuit qg_circuit;
+
+int qg_circuit_create(qg_circuit** out, int numQubits);
+int qg_circuit_destroy(qg_circuit* circuit);
+/* appends a dense unitary on 1..5 qubits; matr row-major 2^k x 2^k, index bit i <-> targs[i] */
+int qg_circuit_add_matrix(qg_circuit* circuit, const int* targs, int numTargs, const qg_cplx* matr);
+/* greedy fusion into blocks of at most maxFusedQubits (1..5) qubits; matrices upload at the first apply */
+int qg_circuit_fuse(qg_circuit* circuit, int maxFusedQubits);
+int qg_circuit_get_num_gates(const qg_circuit* circuit, int* out);
+int qg_circuit_get_num_blocks(const qg_circuit* circuit, int* out);
+/* block i: its ascending targets and (if matr != NULL) its 2^k x 2^k FP64 matrix */
+int qg_circuit_get_block(const qg_circuit* circuit, int i, int* targs, int* numTargs, qg_cplx* matr);
+/* impl: 0 automatic (tensor cores for 5-qubit blocks on >= 12 qubits), 1 SIMT FP32, 2 tensor cores */
+int qg_sv32_apply_circuit(qg_circuit* circuit, void* amps32, int numQubits, int impl, void* stream);
+int qg_tc_get_error_flag(int* out);    /* 1 if a tensor-core kernel's bounded wait ran out */
+
+int qg_sv32_initUniformState(void* amps32, int numQubits, qg_cplxf amp, void* stream);
+int qg_sv32_initClassicalState(void* amps32, int numQubits, int64_t index, void* stream);
+int qg_sv_convert_f64_to_f32(void* dst32, const void* src64, int numQubits, void* stream);
+int qg_sv_convert_f32_to_f64(void* dst64, const void* src32, int numQubits, void* stream);
+/* FP64-accumulated reductions of an FP32 statevector */
+int qg_sv32_calcTotalProb(const void* amps32, int numQubits, double* out, void* stream);
+int qg_sv32_calcExpecPauliStrBatch(const void* amps32, int numQubits, const int64_t* masksXY, const int64_t* masksYZ,
+                                   const int* numsY, int numStrings, qg_cplx* out, void* stream);
 
 #ifdef __cplusplus
 }

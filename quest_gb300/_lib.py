@@ -32,6 +32,10 @@ class qg_cplx(ctypes.Structure):
     _fields_ = [("re", ctypes.c_double), ("im", ctypes.c_double)]
 
 
+class qg_cplxf(ctypes.Structure):
+    _fields_ = [("re", ctypes.c_float), ("im", ctypes.c_float)]
+
+
 c_int_p = ctypes.POINTER(ctypes.c_int)
 c_dbl_p = ctypes.POINTER(ctypes.c_double)
 c_i64_p = ctypes.POINTER(ctypes.c_int64)
@@ -56,6 +60,10 @@ ABI = {
     "qg_get_cache_size": [c_i64_p],
     "qg_clear_cache": [],
     "qg_get_launch_count": [c_i64_p],
+    "qg_event_create": [ctypes.POINTER(vp)],
+    "qg_event_destroy": [vp],
+    "qg_event_record": [vp, vp],
+    "qg_event_elapsed_ms": [vp, vp, ctypes.POINTER(ctypes.c_float)],
     "qg_sv_initUniformState": [vp, I, qg_cplx, vp],
     "qg_sv_initClassicalState": [vp, I, I64, vp],
     "qg_sv_initDebugState": [vp, I, vp],
@@ -86,6 +94,21 @@ ABI = {
     "qg_sv_calcExpecPauliStr": [vp, I, c_int_p, I, c_int_p, I, c_int_p, I, c_cplx_p, vp],
     "qg_dm_calcExpecPauliStr": [vp, I, c_int_p, I, c_int_p, I, c_int_p, I, c_cplx_p, vp],
     "qg_sv_calcExpecPauliStrBatch": [vp, I, c_i64_p, c_i64_p, c_int_p, I, c_cplx_p, vp],
+    "qg_circuit_create": [ctypes.POINTER(vp), I],
+    "qg_circuit_destroy": [vp],
+    "qg_circuit_add_matrix": [vp, c_int_p, I, c_cplx_p],
+    "qg_circuit_fuse": [vp, I],
+    "qg_circuit_get_num_gates": [vp, c_int_p],
+    "qg_circuit_get_num_blocks": [vp, c_int_p],
+    "qg_circuit_get_block": [vp, I, c_int_p, c_int_p, c_cplx_p],
+    "qg_sv32_apply_circuit": [vp, vp, I, I, vp],
+    "qg_tc_get_error_flag": [c_int_p],
+    "qg_sv32_initUniformState": [vp, I, qg_cplxf, vp],
+    "qg_sv32_initClassicalState": [vp, I, I64, vp],
+    "qg_sv_convert_f64_to_f32": [vp, vp, I, vp],
+    "qg_sv_convert_f32_to_f64": [vp, vp, I, vp],
+    "qg_sv32_calcTotalProb": [vp, I, c_dbl_p, vp],
+    "qg_sv32_calcExpecPauliStrBatch": [vp, I, c_i64_p, c_i64_p, c_int_p, I, c_cplx_p, vp],
 }
 
 

@@ -1,0 +1,531 @@
+// FP32 fused-block path: circuits compiled into dense blocks of up to k qubits
+// and applied to FP32 (complex64) statevectors.
+//
+// The gate path of QuEST applies one kernel per gate.  Here a circuit (a list of
+// small dense unitaries) is first fused on the host: gates are greedily merged
+// into blocks acting on at most k qubits, each block's 2^k x 2^k matrix is
+// formed in FP64 (the product of its gates, in order), and the matrices are
+// uploaded once.  Applying a block is the dense-matrix primitive of
+// quest/src/gpu/gpu_kernels.cuh:296-356 (anyCtrlFewTargDenseMatr) on FP32
+// amplitudes; each pass reads and writes every amplitude once, so a circuit
+// costs (number of blocks) passes instead of (number of gates).
+//
+// Two block kernels: a SIMT kernel (each thread holds one 2^k-amplitude group
+// in registers and the matrix is read from shared memory as warp broadcasts),
+// and the tensor-core kernel of qg_fused_tc.cu (k = 5, 3xTF32 on tcgen05).
+// Norms and expectation values of FP32 states accumulate in FP64.
+#include "qg_reduce.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstring>
+#include <vector>
+
+typedef std::complex<double> cd;
+
+// ============================================================== circuit object (host)
+
+struct QgGate {
+    std::vector<int> targs;   // matrix index bit i <-> targs[i]
+    std::vector<cd> m;        // row-major 2^k x 2^k
+};
+
+struct QgBlock {
+    std::vector<int> targs;   // ascending
+    std::vector<cd> m;        // row-major, index bit i <-> targs[i]
+    size_t off32 = 0;         // offset (in float2) of the FP32 matrix in devF32
+    size_t offTC = 0;         // offset (in floats) of the tensor-core operand pair in devTC (k == 5 only)
+};
+
+struct qg_circuit {
+    int numQubits = 0;
+    std::vector<QgGate> gates;
+    std::vector<QgBlock> blocks;
+    int fusedK = 0;
+    float2* devF32 = nullptr;   // concatenated FP32 block matrices
+    float* devTC = nullptr;     // per k=5 block: Bhi, Blo (64x64 real each) in tensor-core layout
+    size_t tcFloats = 0;
+    bool uploaded = false;      // block matrices are copied to the device at the first apply
+};
+
+// tensor-core operand builder, defined in qg_fused_tc.cu
+size_t qg_tc_operand_floats();
+void qg_tc_build_operands(const std::complex<double>* m32x32, float* out);
+int qg_tc_apply_block(float2* amps, int numQubits, const int* targs, const float* devOperands, cudaStream_t st);
+bool qg_tc_supported(int numQubits);
+
+namespace {
+
+// y = G x on the space of `qs` (sorted); G acts on gate qubits `gq` (a subset of qs)
+void apply_gate_to_columns(std::vector<cd>& M, const std::vector<int>& qs, const QgGate& g) {
+    int m = (int)qs.size();
+    size_t D = (size_t)1 << m;
+    int gk = (int)g.targs.size();
+    size_t GD = (size_t)1 << gk;
+    std::vector<int> pos(gk);
+    for (int i = 0; i < gk; i++) pos[i] = (int)(std::find(qs.begin(), qs.end(), g.targs[i]) - qs.begin());
+    size_t gmask = 0;
+    for (int i = 0; i < gk; i++) gmask |= (size_t)1 << pos[i];
+    std::vector<cd> in(GD), out(GD);
+    // rows of M are indexed by output basis states; apply G to every column
+    for (size_t col = 0; col < D; col++) {
+        for (size_t base = 0; base < D; base++) {
+            if (base & gmask) continue;
+            for (size_t j = 0; j < GD; j++) {
+                size_t r = base;
+                for (int i = 0; i < gk; i++) if ((j >> i) & 1) r |= (size_t)1 << pos[i];
+                in[j] = M[r * D + col];
+            }
+            for (size_t r2 = 0; r2 < GD; r2++) {
+                cd acc = 0;
+                for (size_t j = 0; j < GD; j++) acc += g.m[r2 * GD + j] * in[j];
+                out[r2] = acc;
+            }
+            for (size_t j = 0; j < GD; j++) {
+                size_t r = base;
+                for (int i = 0; i < gk; i++) if ((j >> i) & 1) r |= (size_t)1 << pos[i];
+                M[r * D + col] = out[j];
+            }
+        }
+    }
+}
+
+// re-express M (over qs) on the larger sorted set qs2 (M tensor identity)
+std::vector<cd> expand(const std::vector<cd>& M, const std::vector<int>& qs, const std::vector<int>& qs2) {
+    int m = (int)qs.size(), m2 = (int)qs2.size();
+    size_t D = (size_t)1 << m, D2 = (size_t)1 << m2;
+    std::vector<int> pos(m);
+    for (int i = 0; i < m; i++) pos[i] = (int)(std::find(qs2.begin(), qs2.end(), qs[i]) - qs2.begin());
+    size_t inMask = 0;
+    for (int i = 0; i < m; i++) inMask |= (size_t)1 << pos[i];
+    std::vector<cd> out(D2 * D2, cd(0, 0));
+    auto sub = [&](size_t x) { size_t v = 0; for (int i = 0; i < m; i++) if ((x >> pos[i]) & 1) v |= (size_t)1 << i; return v; };
+    for (size_t r = 0; r < D2; r++)
+        for (size_t c = 0; c < D2; c++) {
+            if ((r & ~inMask) != (c & ~inMask)) continue;
+            out[r * D2 + c] = M[sub(r) * D + sub(c)];
+        }
+    return out;
+}
+
+struct OpenBlock {
+    std::vector<int> qs;   // sorted
+    std::vector<cd> m;
+    int order;             // creation order, for deterministic emission
+};
+
+void absorb(OpenBlock& b, const QgGate& g) {
+    std::vector<int> u = b.qs;
+    for (int q : g.targs) if (std::find(u.begin(), u.end(), q) == u.end()) u.push_back(q);
+    std::sort(u.begin(), u.end());
+    if (u != b.qs) {
+        b.m = expand(b.m, b.qs, u);
+        b.qs = u;
+    }
+    apply_gate_to_columns(b.m, b.qs, g);
+}
+
+OpenBlock block_from(const QgGate& g, int order) {
+    OpenBlock b;
+    b.qs = g.targs;
+    std::sort(b.qs.begin(), b.qs.end());
+    size_t D = (size_t)1 << b.qs.size();
+    b.m.assign(D * D, cd(0, 0));
+    for (size_t i = 0; i < D; i++) b.m[i * D + i] = 1;
+    b.order = order;
+    apply_gate_to_columns(b.m, b.qs, g);
+    return b;
+}
+
+void emit(std::vector<QgBlock>& out, OpenBlock& b) {
+    QgBlock q;
+    q.targs = b.qs;
+    q.m = b.m;
+    out.push_back(q);
+}
+
+}  // namespace
+
+// Greedy fusion: open blocks have pairwise disjoint qubits (so they commute).
+// A gate joins the single open block it overlaps if the union still fits in k
+// qubits, merges the blocks it overlaps when they fit together, joins a block
+// with room when it overlaps none, and otherwise closes what it overlaps.
+static void fuse_gates(const std::vector<QgGate>& gates, int k, std::vector<QgBlock>& out) {
+    std::vector<OpenBlock> open;
+    int order = 0;
+    for (const QgGate& g : gates) {
+        std::vector<int> hit;
+        for (int i = 0; i < (int)open.size(); i++)
+            for (int q : g.targs)
+                if (std::find(open[i].qs.begin(), open[i].qs.end(), q) != open[i].qs.end()) { hit.push_back(i); break; }
+        std::vector<int> uni = g.targs;
+        for (int i : hit)
+            for (int q : open[i].qs)
+                if (std::find(uni.begin(), uni.end(), q) == uni.end()) uni.push_back(q);
+        if (!hit.empty() && (int)uni.size() <= k) {
+            // merge every hit block into the first, then absorb the gate
+            OpenBlock& b0 = open[hit[0]];
+            for (size_t h = 1; h < hit.size(); h++) {
+                OpenBlock& bh = open[hit[h]];
+                QgGate as;
+                as.targs = bh.qs;
+                as.m = bh.m;
+                absorb(b0, as);
+            }
+            absorb(b0, g);
+            for (int h = (int)hit.size() - 1; h >= 1; h--) open.erase(open.begin() + hit[h]);
+            continue;
+        }
+        if (hit.empty()) {
+            int best = -1;
+            for (int i = 0; i < (int)open.size(); i++)
+                if ((int)(open[i].qs.size() + g.targs.size()) <= k && (best < 0 || open[i].qs.size() > open[best].qs.size())) best = i;
+            if (best >= 0) {
+                absorb(open[best], g);
+                continue;
+            }
+            open.push_back(block_from(g, order++));
+            continue;
+        }
+        // overlapping blocks that cannot merge: close them (in creation order), start anew
+        std::sort(hit.begin(), hit.end(), [&](int a, int b) { return open[a].order < open[b].order; });
+        for (int i : hit) emit(out, open[i]);
+        std::sort(hit.begin(), hit.end());
+        for (int h = (int)hit.size() - 1; h >= 0; h--) open.erase(open.begin() + hit[h]);
+        open.push_back(block_from(g, order++));
+    }
+    std::sort(open.begin(), open.end(), [](const OpenBlock& a, const OpenBlock& b) { return a.order < b.order; });
+    for (auto& b : open) emit(out, b);
+}
+
+// ============================================================== FP32 kernels
+
+__device__ __forceinline__ float2 ld32(const float2* p) { return __ldcs(p); }
+__device__ __forceinline__ void st32(float2* p, float2 v) { __stcs(p, v); }
+
+__global__ void k32_init_uniform(float2* __restrict__ a, qidx n, float2 v) {
+    qidx i = blockIdx.x * (qidx)blockDim.x + threadIdx.x;
+    if (i < n) st32(a + i, v);
+}
+__global__ void k32_set_one(float2* __restrict__ a, qidx i, float2 v) { a[i] = v; }
+
+__global__ void k_f64_to_f32(float2* __restrict__ dst, const double2* __restrict__ src, qidx n) {
+    qidx i = blockIdx.x * (qidx)blockDim.x + threadIdx.x;
+    if (i < n) { double2 v = __ldcs(src + i); st32(dst + i, make_float2((float)v.x, (float)v.y)); }
+}
+__global__ void k_f32_to_f64(double2* __restrict__ dst, const float2* __restrict__ src, qidx n) {
+    qidx i = blockIdx.x * (qidx)blockDim.x + threadIdx.x;
+    if (i < n) { float2 v = ld32(src + i); __stcs(dst + i, make_double2(v.x, v.y)); }
+}
+
+// One 2^K-amplitude group per thread.  off[j]: offset of matrix index j from the
+// group base.  The FP32 matrix is staged in shared memory (warp-uniform reads).
+template <int K, int NB>
+__global__ void __launch_bounds__(128) k32_fused(float2* __restrict__ a, qidx numIts, Ins ins, const float2* __restrict__ M, InsertList<8> offs) {
+    constexpr int D = 1 << K;
+    __shared__ float2 sm[D * D];
+    __shared__ qidx soff[D];
+    for (int i = threadIdx.x; i < D * D; i += blockDim.x) sm[i] = M[i];
+    if (threadIdx.x < D) {
+        qidx o = 0;
+        for (int b = 0; b < K; b++) if ((threadIdx.x >> b) & 1) o |= offs.low[b];
+        soff[threadIdx.x] = o;
+    }
+    __syncthreads();
+    qidx n = blockIdx.x * (qidx)blockDim.x + threadIdx.x;
+    if (n >= numIts) return;
+    qidx base = insert_bits<NB>(n, ins);
+    float2 v[D];
+#pragma unroll
+    for (int j = 0; j < D; j++) v[j] = ld32(a + base + soff[j]);
+#pragma unroll
+    for (int r = 0; r < D; r++) {
+        float2 acc = cmulf(sm[r * D], v[0]);
+#pragma unroll
+        for (int j = 1; j < D; j++) acc = cfmaf(sm[r * D + j], v[j], acc);
+        st32(a + base + soff[r], acc);
+    }
+}
+
+// sum |a_i|^2 in FP64 over an FP32 vector
+__global__ void __launch_bounds__(RED_THREADS) k32_sum_norm(const float2* __restrict__ a, qidx n, RedOut out) {
+    double v[1] = {0.0};
+    qidx stride = (qidx)gridDim.x * RED_THREADS;
+    for (qidx i = blockIdx.x * (qidx)RED_THREADS + threadIdx.x; i < n; i += stride) {
+        float2 x = ld32(a + i);
+        v[0] += (double)x.x * x.x + (double)x.y * x.y;
+    }
+    block_reduce_and_finish<1>(v, out);
+}
+
+// batched Pauli expectation (FP64 accumulation), the reference's per-n term
+template <int NS>
+__global__ void __launch_bounds__(RED_THREADS) k32_expec_pauli_batch(const float2* __restrict__ a, qidx n,
+                                                                    const qidx* __restrict__ mXY, const qidx* __restrict__ mYZ,
+                                                                    int numStrings, RedOut out) {
+    double v[2 * NS];
+#pragma unroll
+    for (int k = 0; k < 2 * NS; k++) v[k] = 0.0;
+    __shared__ qidx sXY[NS], sYZ[NS];
+    if (threadIdx.x < NS) {
+        sXY[threadIdx.x] = threadIdx.x < numStrings ? mXY[threadIdx.x] : 0;
+        sYZ[threadIdx.x] = threadIdx.x < numStrings ? mYZ[threadIdx.x] : 0;
+    }
+    __syncthreads();
+    qidx stride = (qidx)gridDim.x * RED_THREADS;
+    for (qidx i = blockIdx.x * (qidx)RED_THREADS + threadIdx.x; i < n; i += stride) {
+        float2 an = __ldg(a + i);
+#pragma unroll
+        for (int s = 0; s < NS; s++) {
+            if (s < numStrings) {
+                qidx j = i ^ sXY[s];
+                float2 aj = __ldg(a + j);
+                double sg = parity64(j & sYZ[s]) ? -1.0 : 1.0;
+                v[2 * s] += sg * ((double)an.x * aj.x + (double)an.y * aj.y);
+                v[2 * s + 1] += sg * ((double)an.x * aj.y - (double)an.y * aj.x);
+            }
+        }
+    }
+    block_reduce_and_finish<2 * NS>(v, out);
+}
+
+// ============================================================== host side
+
+namespace {
+
+int check32(const void* amps, int nq) {
+    if (amps == nullptr) return qg_fail(QG_ERR_ARG, "null amplitude pointer");
+    if (nq < 1 || nq > QG_MAX_QUBITS) return qg_fail(QG_ERR_ARG, "numQubits %d outside [1, %d]", nq, QG_MAX_QUBITS);
+    if (((uintptr_t)amps) & 7) return qg_fail(QG_ERR_ARG, "FP32 amplitude pointer is not 8-byte aligned");
+    return QG_OK;
+}
+
+int launch_fused_simt(float2* amps, int nq, const std::vector<int>& targs, const float2* devM, cudaStream_t st) {
+    int k = (int)targs.size();
+    std::vector<int> zeros(k, 0);
+    QubitPlan p;
+    QG_TRY(qg_make_plan(nq, nullptr, nullptr, 0, targs.data(), zeros.data(), k, &p));
+    InsertList<8> offs;
+    offs.num = k;
+    for (int b = 0; b < k; b++) offs.low[b] = (qidx)1 << targs[b];
+    qidx numIts = ((qidx)1 << nq) >> k;
+    unsigned blocks = (unsigned)((numIts + 127) / 128);
+#define LK(KV, NBV) k32_fused<KV, NBV><<<blocks, 128, 0, st>>>(amps, numIts, p.ins, devM, offs)
+    switch (k) {
+        case 1: LK(1, 1); break;
+        case 2: LK(2, 2); break;
+        case 3: LK(3, 3); break;
+        case 4: LK(4, 4); break;
+        case 5: LK(5, 5); break;
+        default: return qg_fail(QG_ERR_NOTSUP, "FP32 fused blocks of %d qubits are not supported (max 5)", k);
+    }
+#undef LK
+    qg_note_launch();
+    return qg_check_launch("k32_fused");
+}
+
+int upload_blocks(qg_circuit* c) {
+    if (c->devF32) { cudaFree(c->devF32); c->devF32 = nullptr; }
+    if (c->devTC) { cudaFree(c->devTC); c->devTC = nullptr; }
+    size_t n32 = 0, nTC = 0;
+    size_t tcPer = qg_tc_operand_floats();
+    for (auto& b : c->blocks) {
+        size_t D = (size_t)1 << b.targs.size();
+        b.off32 = n32;
+        n32 += D * D;
+        if (b.targs.size() == 5) { b.offTC = nTC; nTC += tcPer; }
+    }
+    std::vector<float2> h32(n32);
+    std::vector<float> hTC(nTC);
+    for (auto& b : c->blocks) {
+        size_t D = (size_t)1 << b.targs.size();
+        for (size_t i = 0; i < D * D; i++) h32[b.off32 + i] = make_float2((float)b.m[i].real(), (float)b.m[i].imag());
+        if (b.targs.size() == 5) qg_tc_build_operands(b.m.data(), hTC.data() + b.offTC);
+    }
+    if (n32) {
+        QG_CUDA(cudaMalloc(&c->devF32, n32 * sizeof(float2)));
+        QG_CUDA(cudaMemcpy(c->devF32, h32.data(), n32 * sizeof(float2), cudaMemcpyHostToDevice));
+    }
+    if (nTC) {
+        QG_CUDA(cudaMalloc(&c->devTC, nTC * sizeof(float)));
+        QG_CUDA(cudaMemcpy(c->devTC, hTC.data(), nTC * sizeof(float), cudaMemcpyHostToDevice));
+    }
+    c->tcFloats = nTC;
+    return QG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int qg_circuit_create(qg_circuit** out, int numQubits) {
+    if (!out) return qg_fail(QG_ERR_ARG, "null output");
+    if (numQubits < 1 || numQubits > QG_MAX_QUBITS) return qg_fail(QG_ERR_ARG, "numQubits %d outside [1, %d]", numQubits, QG_MAX_QUBITS);
+    *out = new qg_circuit();
+    (*out)->numQubits = numQubits;
+    return QG_OK;
+}
+
+int qg_circuit_destroy(qg_circuit* c) {
+    if (!c) return QG_OK;
+    if (c->devF32) cudaFree(c->devF32);
+    if (c->devTC) cudaFree(c->devTC);
+    delete c;
+    return QG_OK;
+}
+
+int qg_circuit_add_matrix(qg_circuit* c, const int* targs, int numTargs, const qg_cplx* matr) {
+    if (!c || !matr) return qg_fail(QG_ERR_ARG, "null circuit or matrix");
+    if (numTargs < 1 || numTargs > 5) return qg_fail(QG_ERR_ARG, "a circuit gate acts on 1..5 qubits, not %d", numTargs);
+    QG_TRY(qg_check_qubits(c->numQubits, targs, numTargs, "gate targets"));
+    QgGate g;
+    g.targs.assign(targs, targs + numTargs);
+    size_t D = (size_t)1 << numTargs;
+    g.m.resize(D * D);
+    for (size_t i = 0; i < D * D; i++) g.m[i] = cd(matr[i].re, matr[i].im);
+    c->gates.push_back(std::move(g));
+    c->blocks.clear();
+    c->uploaded = false;
+    return QG_OK;
+}
+
+int qg_circuit_fuse(qg_circuit* c, int maxFusedQubits) {
+    if (!c) return qg_fail(QG_ERR_ARG, "null circuit");
+    if (maxFusedQubits < 1 || maxFusedQubits > 5) return qg_fail(QG_ERR_ARG, "fusion width %d outside [1, 5]", maxFusedQubits);
+    for (auto& g : c->gates)
+        if ((int)g.targs.size() > maxFusedQubits) return qg_fail(QG_ERR_ARG, "a gate is wider than the fusion width");
+    c->blocks.clear();
+    fuse_gates(c->gates, maxFusedQubits, c->blocks);
+    c->fusedK = maxFusedQubits;
+    c->uploaded = false;
+    return QG_OK;
+}
+
+int qg_circuit_get_num_gates(const qg_circuit* c, int* out) {
+    if (!c || !out) return qg_fail(QG_ERR_ARG, "null argument");
+    *out = (int)c->gates.size();
+    return QG_OK;
+}
+
+int qg_circuit_get_num_blocks(const qg_circuit* c, int* out) {
+    if (!c || !out) return qg_fail(QG_ERR_ARG, "null argument");
+    *out = (int)c->blocks.size();
+    return QG_OK;
+}
+
+int qg_circuit_get_block(const qg_circuit* c, int i, int* targs, int* numTargs, qg_cplx* matr) {
+    if (!c || i < 0 || i >= (int)c->blocks.size()) return qg_fail(QG_ERR_ARG, "block index out of range");
+    const QgBlock& b = c->blocks[i];
+    *numTargs = (int)b.targs.size();
+    for (size_t j = 0; j < b.targs.size(); j++) targs[j] = b.targs[j];
+    if (matr)
+        for (size_t j = 0; j < b.m.size(); j++) matr[j] = qg_cplx{b.m[j].real(), b.m[j].imag()};
+    return QG_OK;
+}
+
+// impl: 0 = automatic (tensor cores for 5-qubit blocks on large states), 1 = SIMT FP32, 2 = tensor cores
+int qg_sv32_apply_circuit(qg_circuit* c, void* amps, int numQubits, int impl, void* stream) {
+    QG_TRY(check32(amps, numQubits));
+    if (!c) return qg_fail(QG_ERR_ARG, "null circuit");
+    if (!c->uploaded) {
+        QG_TRY(upload_blocks(c));
+        c->uploaded = true;
+    }
+    if (numQubits != c->numQubits) return qg_fail(QG_ERR_ARG, "circuit has %d qubits, state has %d", c->numQubits, numQubits);
+    if (c->blocks.empty() && !c->gates.empty()) return qg_fail(QG_ERR_ARG, "circuit was not fused (qg_circuit_fuse)");
+    cudaStream_t st = qg_stream(stream);
+    for (const QgBlock& b : c->blocks) {
+        bool tc = b.targs.size() == 5 && (impl == 2 || (impl == 0 && qg_tc_supported(numQubits)));
+        if (tc) {
+            QG_TRY(qg_tc_apply_block((float2*)amps, numQubits, b.targs.data(), c->devTC + b.offTC, st));
+        } else {
+            QG_TRY(launch_fused_simt((float2*)amps, numQubits, b.targs, c->devF32 + b.off32, st));
+        }
+    }
+    return QG_OK;
+}
+
+int qg_sv32_initUniformState(void* amps, int numQubits, qg_cplxf amp, void* stream) {
+    QG_TRY(check32(amps, numQubits));
+    qidx n = (qidx)1 << numQubits;
+    k32_init_uniform<<<qg_blocks(n), QG_THREADS, 0, qg_stream(stream)>>>((float2*)amps, n, make_float2(amp.re, amp.im));
+    qg_note_launch();
+    return qg_check_launch("k32_init_uniform");
+}
+
+int qg_sv32_initClassicalState(void* amps, int numQubits, int64_t index, void* stream) {
+    QG_TRY(check32(amps, numQubits));
+    qidx n = (qidx)1 << numQubits;
+    if (index < 0 || index >= n) return qg_fail(QG_ERR_ARG, "basis index outside the state");
+    k32_init_uniform<<<qg_blocks(n), QG_THREADS, 0, qg_stream(stream)>>>((float2*)amps, n, make_float2(0, 0));
+    k32_set_one<<<1, 1, 0, qg_stream(stream)>>>((float2*)amps, index, make_float2(1, 0));
+    qg_note_launch(2);
+    return qg_check_launch("k32_init_classical");
+}
+
+int qg_sv_convert_f64_to_f32(void* dst32, const void* src64, int numQubits, void* stream) {
+    QG_TRY(check32(dst32, numQubits));
+    QG_TRY(qg_check_amps(src64, numQubits));
+    qidx n = (qidx)1 << numQubits;
+    k_f64_to_f32<<<qg_blocks(n), QG_THREADS, 0, qg_stream(stream)>>>((float2*)dst32, (const double2*)src64, n);
+    qg_note_launch();
+    return qg_check_launch("k_f64_to_f32");
+}
+
+int qg_sv_convert_f32_to_f64(void* dst64, const void* src32, int numQubits, void* stream) {
+    QG_TRY(check32(src32, numQubits));
+    QG_TRY(qg_check_amps(dst64, numQubits));
+    qidx n = (qidx)1 << numQubits;
+    k_f32_to_f64<<<qg_blocks(n), QG_THREADS, 0, qg_stream(stream)>>>((double2*)dst64, (const float2*)src32, n);
+    qg_note_launch();
+    return qg_check_launch("k_f32_to_f64");
+}
+
+int qg_sv32_calcTotalProb(const void* amps, int numQubits, double* out, void* stream) {
+    QG_TRY(check32(amps, numQubits));
+    qidx n = (qidx)1 << numQubits;
+    int grid = red_grid(n);
+    RedOut r;
+    QG_TRY(red_setup(grid, 1, &r));
+    cudaStream_t st = qg_stream(stream);
+    k32_sum_norm<<<grid, RED_THREADS, 0, st>>>((const float2*)amps, n, r);
+    return red_fetch(r, 1, out, st);
+}
+
+int qg_sv32_calcExpecPauliStrBatch(const void* amps, int numQubits, const int64_t* masksXY, const int64_t* masksYZ,
+                                   const int* numsY, int numStrings, qg_cplx* out, void* stream) {
+    QG_TRY(check32(amps, numQubits));
+    if (numStrings < 0) return qg_fail(QG_ERR_ARG, "negative string count");
+    qidx lim = ((qidx)1 << numQubits) - 1;
+    for (int s = 0; s < numStrings; s++)
+        if ((masksXY[s] & ~lim) || (masksYZ[s] & ~lim)) return qg_fail(QG_ERR_ARG, "Pauli string %d targets a qubit beyond %d", s, numQubits);
+    cudaStream_t st = qg_stream(stream);
+    const int NS = 16;
+    qidx n = (qidx)1 << numQubits;
+    for (int s0 = 0; s0 < numStrings; s0 += NS) {
+        int cnt = std::min(NS, numStrings - s0);
+        int grid = red_grid(n);
+        void* s = nullptr;
+        QG_TRY(qg_scratch_get(&s, red_scratch_bytes(grid, 2 * NS) + 512));
+        RedOut r;
+        red_setup_at((char*)s + 512, grid, 2 * NS, &r);
+        r.ticket = (unsigned int*)s;              // the ticket stays at the start of scratch
+        qidx* dm = (qidx*)((char*)s + 256);       // masks right after it
+        std::vector<qidx> hm(2 * NS, 0);
+        for (int k = 0; k < cnt; k++) { hm[k] = masksXY[s0 + k]; hm[NS + k] = masksYZ[s0 + k]; }
+        QG_CUDA(cudaMemcpyAsync(dm, hm.data(), 8 * 2 * NS, cudaMemcpyHostToDevice, st));
+        k32_expec_pauli_batch<NS><<<grid, RED_THREADS, 0, st>>>((const float2*)amps, n, dm, dm + NS, cnt, r);
+        double v[2 * NS];
+        QG_TRY(red_fetch(r, 2 * NS, v, st));
+        for (int k = 0; k < cnt; k++) {
+            double re = v[2 * k], im = v[2 * k + 1];
+            times_power_of_i(&re, &im, numsY[s0 + k]);
+            out[s0 + k].re = re;
+            out[s0 + k].im = im;
+        }
+    }
+    return QG_OK;
+}
+
+}  // extern "C"

@@ -9,67 +9,10 @@
 // an atomic ticket after a memory fence) adds the partials in block order and
 // resets the ticket.  The grid, the assignment of terms to threads and every
 // addition order are fixed, so the same input always gives the same bits.
-#include "qg_common.cuh"
+#include "qg_reduce.cuh"
 
 #include <algorithm>
 #include <vector>
-
-#define RED_THREADS 256
-#define RED_MAX_VALUES 34   // up to 17 complex values per launch
-
-struct RedOut {
-    double* partials;        // [NV][gridDim.x]
-    unsigned int* ticket;
-    double* result;          // [NV]
-};
-
-template <int NV>
-__device__ __forceinline__ void block_reduce_and_finish(double (&v)[NV], const RedOut& out) {
-    __shared__ double sh[NV][RED_THREADS / 32];
-    __shared__ bool amLast;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-    for (int k = 0; k < NV; k++) {
-        double x = v[k];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-        if (lane == 0) sh[k][warp] = x;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-#pragma unroll
-        for (int k = 0; k < NV; k++) {
-            double s = 0;
-            for (int w = 0; w < RED_THREADS / 32; w++) s += sh[k][w];
-            out.partials[k * gridDim.x + blockIdx.x] = s;
-        }
-        __threadfence();
-        unsigned int t = atomicAdd(out.ticket, 1u);
-        amLast = (t == gridDim.x - 1);
-    }
-    __syncthreads();
-    if (!amLast) return;
-    __threadfence();
-    // the last block adds every block's partial in a fixed order
-#pragma unroll
-    for (int k = 0; k < NV; k++) {
-        double s = 0;
-        for (unsigned b = threadIdx.x; b < gridDim.x; b += RED_THREADS) s += ((volatile double*)out.partials)[k * gridDim.x + b];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-        if (lane == 0) sh[k][warp] = s;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-#pragma unroll
-        for (int k = 0; k < NV; k++) {
-            double s = 0;
-            for (int w = 0; w < RED_THREADS / 32; w++) s += sh[k][w];
-            out.result[k] = s;
-        }
-        *out.ticket = 0;
-    }
-}
 
 // ----------------------------------------------------------------- kernels
 
@@ -237,36 +180,6 @@ __global__ void k_probs_all_finish(const double* __restrict__ partials, int perB
 
 namespace {
 
-int red_grid(qidx work) {
-    qidx g = (qidx)qg_num_sms() * 4;
-    qidx need = (work + RED_THREADS - 1) / RED_THREADS;
-    if (need < g) g = std::max<qidx>(1, need);
-    return (int)g;
-}
-
-// scratch layout: [ticket (256 B)] [results (NV doubles, 256 B aligned)] [partials]
-int red_setup(int grid, int nv, RedOut* out) {
-    void* s = nullptr;
-    size_t bytes = 512 + 8 * (size_t)nv + 8 * (size_t)nv * grid + 256;
-    QG_TRY(qg_scratch_get(&s, bytes));
-    char* base = (char*)s;
-    out->ticket = (unsigned int*)base;
-    out->result = (double*)(base + 256);
-    out->partials = (double*)(base + 256 + ((8 * (size_t)nv + 255) / 256) * 256);
-    return QG_OK;
-}
-
-int red_fetch(const RedOut& out, int nv, double* host, cudaStream_t st) {
-    QG_TRY(qg_check_launch("reduction"));
-    void* pinned = nullptr;
-    QG_TRY(qg_pinned_result(&pinned, 8 * (size_t)nv));
-    QG_CUDA(cudaMemcpyAsync(pinned, out.result, 8 * (size_t)nv, cudaMemcpyDeviceToHost, st));
-    QG_CUDA(cudaStreamSynchronize(st));
-    std::copy((double*)pinned, (double*)pinned + nv, host);
-    qg_note_launch();
-    return QG_OK;
-}
-
 int sum_norm(const void* amps, int numQubits, const QubitPlan& p, double* out, cudaStream_t st) {
     qidx numIts = ((qidx)1 << numQubits) >> p.numFixed;
     int grid = red_grid(numIts);
@@ -293,17 +206,6 @@ int sum_diag(const void* amps, int nKet, const QubitPlan& p, double* out, cudaSt
 int check_dm_amps(const void* amps, int nKet) {
     if (nKet < 1 || 2 * nKet > QG_MAX_QUBITS) return qg_fail(QG_ERR_ARG, "density matrix of %d qubits is unsupported", nKet);
     return qg_check_amps(amps, 2 * nKet);
-}
-
-// i^k
-void times_power_of_i(double* re, double* im, int k) {
-    double r = *re, i = *im;
-    switch (k % 4) {
-        case 0: break;
-        case 1: *re = -i; *im = r; break;
-        case 2: *re = -r; *im = -i; break;
-        default: *re = i; *im = -r; break;
-    }
 }
 
 int pauli_masks(int limit, const int* x, int nx, const int* y, int ny, const int* z, int nz, qidx* mXY, qidx* mYZ, int* top) {

@@ -278,6 +278,29 @@ int qg_clear_cache(void) {
     return QG_OK;
 }
 
+int qg_event_create(void** out) {
+    cudaEvent_t e;
+    QG_CUDA(cudaEventCreate(&e));
+    *out = (void*)e;
+    return QG_OK;
+}
+
+int qg_event_destroy(void* ev) {
+    if (ev) QG_CUDA(cudaEventDestroy((cudaEvent_t)ev));
+    return QG_OK;
+}
+
+int qg_event_record(void* ev, void* stream) {
+    QG_CUDA(cudaEventRecord((cudaEvent_t)ev, qg_stream(stream)));
+    return QG_OK;
+}
+
+int qg_event_elapsed_ms(void* start, void* stop, float* ms) {
+    QG_CUDA(cudaEventSynchronize((cudaEvent_t)stop));
+    QG_CUDA(cudaEventElapsedTime(ms, (cudaEvent_t)start, (cudaEvent_t)stop));
+    return QG_OK;
+}
+
 int qg_get_launch_count(int64_t* out) {
     *out = (int64_t)g_launches.load();
     return QG_OK;

@@ -1,0 +1,109 @@
+"""FP32 fused-block path on the GPU (SIMT and tcgen05 3xTF32 kernels) against the
+FP64 oracle applying the same gates one by one.
+
+Bar (precision form): fidelity |<psi32|psi64>|^2 >= 1 - 1e-6 and max-abs
+amplitude error <= 2e-6 x max|psi|; the two FP32 kernels agree to 2e-6 x max|psi|."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import qcircuits as qc
+
+pytestmark = pytest.mark.gpu
+CZ = np.diag([1, 1, 1, -1]).astype(np.complex128)
+
+
+def run_oracle(n, amps, gates):
+    lines = []
+    for t, m in gates:
+        if len(t) == 1:
+            lines.append(f"U1 {t[0]} {qc.mat_tokens(m)}")
+        elif len(t) == 2:
+            lines.append(f"U2 {t[0]} {t[1]} {qc.mat_tokens(m)}")
+        else:
+            lines.append(f"UK {len(t)} {' '.join(map(str, t))} {qc.mat_tokens(m)}")
+    out, _, _ = qc.oracle().run("\n".join(lines) + "\n", n, 0, amps)
+    return out
+
+
+def run_fused(env, n, amps, gates, k, impl):
+    from quest_gb300.fused import Circuit, StateVector32
+    c = Circuit(n)
+    for t, m in gates:
+        c.add(t, m)
+    c.fuse(k)
+    s = StateVector32(n)
+    try:
+        s.set(amps)
+        c.apply(s, impl=impl)
+        return s.get().astype(np.complex128), c.num_blocks
+    finally:
+        s.free()
+
+
+def brickwork(n, depth, rng):
+    gates = []
+    for d in range(depth):
+        for t in range(n):
+            gates.append(([t], qc.haar_unitary(2, rng)))
+        for t in range(d % 2, n - 1, 2):
+            gates.append(([t, t + 1], CZ))
+    return gates
+
+
+def fidelity(a, b):
+    return abs(np.vdot(a, b)) ** 2 / (np.vdot(a, a).real * np.vdot(b, b).real)
+
+
+@pytest.mark.parametrize("n,depth", [(12, 6), (15, 8), (18, 10)])
+@pytest.mark.parametrize("impl", [1, 2])
+def test_fused_brickwork_vs_fp64_oracle(env, n, depth, impl):
+    rng = np.random.default_rng(n * 10 + depth)
+    gates = brickwork(n, depth, rng)
+    amps = qc.random_statevector(n, n)
+    ref = run_oracle(n, amps, gates)
+    got, nblocks = run_fused(env, n, amps, gates, 5, impl)
+    scale = np.max(np.abs(ref))
+    assert fidelity(got, ref) >= 1 - 1e-6
+    assert np.max(np.abs(got - ref)) <= 2e-6 * scale
+    assert nblocks < len(gates) / 3
+    from quest_gb300 import _lib
+    flag = ctypes.c_int(0)
+    _lib.lib().qg_tc_get_error_flag(ctypes.byref(flag))
+    assert flag.value == 0
+
+
+@pytest.mark.parametrize("targs", [[0, 1, 2, 3, 4], [7, 8, 9, 10, 11], [11, 0, 6, 3, 9], [2, 5, 6, 10, 13],
+                                   [13, 12, 1, 0, 7]])
+def test_single_5qubit_block_every_layout(env, targs):
+    n = 14
+    rng = np.random.default_rng(sum(targs))
+    u = qc.haar_unitary(32, rng)
+    amps = qc.random_statevector(n, 3)
+    ref = run_oracle(n, amps, [(targs, u)])
+    scale = np.max(np.abs(ref))
+    simt, _ = run_fused(env, n, amps, [(targs, u)], 5, 1)
+    tc, _ = run_fused(env, n, amps, [(targs, u)], 5, 2)
+    assert np.max(np.abs(simt - ref)) <= 2e-6 * scale
+    assert np.max(np.abs(tc - ref)) <= 2e-6 * scale
+    assert np.max(np.abs(tc - simt)) <= 2e-6 * scale
+
+
+def test_fp32_reductions_accumulate_in_fp64(env):
+    from quest_gb300.fused import StateVector32
+    n = 16
+    amps = qc.random_statevector(n, 8).astype(np.complex64)
+    s = StateVector32(n)
+    try:
+        s.set(amps)
+        a64 = amps.astype(np.complex128)
+        assert abs(s.total_prob() - np.vdot(a64, a64).real) < 1e-12
+        rng = np.random.default_rng(1)
+        codes = [[int(v) for v in rng.integers(0, 4, n)] for _ in range(20)]
+        got = s.expec_paulis(codes)
+        text = "".join(f"EXPEC {qc.pauli_text(c)}\n" for c in codes)
+        _, want, _ = qc.oracle().run(text, n, 0, a64)
+        assert np.max(np.abs(got - want)) < 1e-12
+    finally:
+        s.free()
