@@ -330,10 +330,17 @@ def run_gb300(args, world, rank, local, dist):
     peak_src = "measured" if peak else "fallback"
     peak = peak or 6800.0
     achieved = dense_bytes / avg_dense / 1e9
+    # the general complex 2x2 gate needs 16 FP64 FMAs per amplitude pair (64 B): its
+    # FP64 issue ceiling in bandwidth terms, from a live probe of the FMA rate
+    fma_rate = C.c_double(0)
+    _lib.check(L.qg_measure_fp64_fma_rate(C.byref(fma_rate)))
+    fp64_ceiling_gbs = fma_rate.value / 16 * 64 / 1e9
     roofline = {"bound": "hbm", "kernel": "k_dense1 (applyCompMatr1, general complex 2x2, FP64)",
                 "achieved": round(achieved, 1), "peak": peak, "peak_source": peak_src, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": args.traffic,
-                "launches_timed": len(dense_ms), "avg_launch_ms": round(avg_dense * 1e3, 4)}
+                "launches_timed": len(dense_ms), "avg_launch_ms": round(avg_dense * 1e3, 4),
+                "fp64_fma_per_s": round(fma_rate.value, -8), "fp64_ceiling_gbs": round(fp64_ceiling_gbs, 1),
+                "fp64_ceiling_frac": round(achieved / fp64_ceiling_gbs, 4)}
 
     cpu = None
     if rank == 0 and args.cpu_sample > 0:

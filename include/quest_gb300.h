@@ -68,6 +68,9 @@ int qg_event_create(void** out);
 int qg_event_destroy(void* event);
 int qg_event_record(void* event, void* stream);
 int qg_event_elapsed_ms(void* start, void* stop, float* ms); /* waits for `stop` */
+/* FP64 fused multiply-adds per second this GPU sustains (a short probe kernel);
+ * the issue rate that bounds the general complex FP64 gates */
+int qg_measure_fp64_fma_rate(double* fmaPerSecond);
 
 /* ------------------------------------------------------------------ initialisation
  * replaces gpu_statevec_initUniformState_sub / initDebugState_sub

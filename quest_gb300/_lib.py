@@ -64,6 +64,7 @@ ABI = {
     "qg_event_destroy": [vp],
     "qg_event_record": [vp, vp],
     "qg_event_elapsed_ms": [vp, vp, ctypes.POINTER(ctypes.c_float)],
+    "qg_measure_fp64_fma_rate": [c_dbl_p],
     "qg_sv_initUniformState": [vp, I, qg_cplx, vp],
     "qg_sv_initClassicalState": [vp, I, I64, vp],
     "qg_sv_initDebugState": [vp, I, vp],

@@ -307,3 +307,37 @@ int qg_get_launch_count(int64_t* out) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------- FP64 issue-rate probe
+// Eight independent FMA chains per thread, enough warps to fill every SM: the
+// kernel's FP64 throughput is the rate that bounds the general complex gates.
+__global__ void k_fp64_fma_rate(double* out, int iters, double a, double b) {
+    double x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+    for (int i = 0; i < iters; i++) {
+        x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+        x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+    }
+    out[blockIdx.x * (size_t)blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
+extern "C" int qg_measure_fp64_fma_rate(double* fmaPerSecond) {
+    int blocks = qg_num_sms() * 8, threads = 256, iters = 1 << 13;
+    double* out = nullptr;
+    QG_CUDA(cudaMalloc(&out, sizeof(double) * blocks * threads));
+    cudaEvent_t e0, e1;
+    QG_CUDA(cudaEventCreate(&e0));
+    QG_CUDA(cudaEventCreate(&e1));
+    k_fp64_fma_rate<<<blocks, threads>>>(out, 64, 1.0000001, 1e-9);   // warm-up
+    QG_CUDA(cudaEventRecord(e0));
+    k_fp64_fma_rate<<<blocks, threads>>>(out, iters, 1.0000001, 1e-9);
+    QG_CUDA(cudaEventRecord(e1));
+    QG_CUDA(cudaEventSynchronize(e1));
+    float ms = 0;
+    QG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    QG_CUDA(cudaFree(out));
+    qg_note_launch(2);
+    *fmaPerSecond = (double)blocks * threads * iters * 8 / (ms * 1e-3);
+    return QG_OK;
+}
