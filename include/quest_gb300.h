@@ -186,6 +186,20 @@ int qg_dm_calcExpecPauliStr(const void* amps, int numKetQubits, const int* targs
 int qg_sv_calcExpecPauliStrBatch(const void* amps, int numQubits, const int64_t* masksXY, const int64_t* masksYZ,
                                  const int* numsY, int numStrings, qg_cplx* out, void* stream);
 
+/* The same batched Pauli expectation values, for callers that cannot allocate
+ * device or pinned memory during the call (their HBM is reserved up front by
+ * another allocator, or they cannot afford cudaMalloc's implicit
+ * synchronisation).  No counterpart in the reference.  Allocates nothing: its
+ * scratch is a fixed device array inside the library (about 264 KiB per GPU
+ * that loads the library, held until exit).  At most QG_NOALLOC_MAX_STRINGS
+ * strings per call; more is rejected with QG_ERR_ARG.  The first call on a
+ * device looks up the array's device address (cudaGetSymbolAddress) and should
+ * come before any stream capture.  Calls share the array: calls that overlap on
+ * the GPU race. */
+#define QG_NOALLOC_MAX_STRINGS 64
+int qg_sv_calcExpecPauliStrBatch_noalloc(const void* amps, int numQubits, const int64_t* masksXY, const int64_t* masksYZ,
+                                         const int* numsY, int numStrings, qg_cplx* out, void* stream);
+
 /* ------------------------------------------------------------------ FP32 fused-block path
  * A circuit of small dense unitaries is fused on the host into blocks of at most
  * k <= 5 qubits (each block's matrix formed in FP64), then applied to an FP32
