@@ -403,6 +403,246 @@ def run_reference(args, world, rank, dist):
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------------ precision form (FP32 fused blocks)
+
+def brickwork_gates(nq, depth, seed):
+    """Haar 1q on every qubit + CZ on alternating neighbour pairs, per layer."""
+    rng = np.random.default_rng(seed)
+    cz = np.diag([1, 1, 1, -1]).astype(np.complex128)
+    gates = []
+    for d in range(depth):
+        for t in range(nq):
+            gates.append(([t], haar_2x2(rng)))
+        for t in range(d % 2, nq - 1, 2):
+            gates.append(([t, t + 1], cz))
+    return gates
+
+
+def run_precision(args, world, rank, local, dist):
+    """FP32 statevector, brickwork circuit fused into 5-qubit blocks applied as 3xTF32
+    tensor-core GEMM tiles.  Accuracy against the FP64 per-gate path (which is pinned
+    to the FP64 oracle) at `--acc-qubits`; throughput at `--qubits`."""
+    import ctypes as C
+    from quest_gb300 import _lib, api
+    from quest_gb300.api import Q, comp_matr1
+    from quest_gb300.fused import Circuit, StateVector32, IMPL_TC, IMPL_SIMT
+    L = _lib.lib()
+    _lib.check(L.qg_init(local))
+    api.init_env()
+    nq, na, depth = args.qubits, args.acc_qubits, args.depth
+    impl = IMPL_SIMT if args.fused_impl == "simt" else IMPL_TC
+
+    # ---- accuracy at na qubits
+    gates = brickwork_gates(na, depth, seed=0x5155455354 + 4)
+    psi0 = random_state(na, seed=0x5155455354 + 4)
+    q = Q.createQureg(na)
+    api.set_amps(q, psi0)
+    for t, m in gates:
+        if len(t) == 1:
+            Q.applyCompMatr1(q, t[0], comp_matr1(m))
+        else:
+            Q.applyControlledPauliZ(q, t[0], t[1])
+    psi64 = api.get_amps(q)
+    rng = np.random.default_rng(7)
+    codes = [[int(v) for v in rng.integers(0, 4, na)] for _ in range(16)]
+    strs = (api.PauliStr * 16)(*[api.pauli_str(c) for c in codes])
+    e64 = (C.c_double * 16)()
+    Q.calcExpecPauliStrs(e64, q, strs, 16)
+    Q.destroyQureg(q)
+    circ = Circuit(na)
+    for t, m in gates:
+        circ.add(t, m)
+    circ.fuse(5)
+    s = StateVector32(na)
+    s.set(psi0)
+    circ.apply(s, impl=impl)
+    e32 = s.expec_paulis(codes)
+    psi32 = s.get().astype(np.complex128)
+    s.free()
+    fid = float(abs(np.vdot(psi32, psi64)) ** 2 / (np.vdot(psi32, psi32).real * np.vdot(psi64, psi64).real))
+    maxabs = float(np.max(np.abs(psi32 - psi64)))
+    experr = float(np.max(np.abs(np.array(e32) - np.array(list(e64)))))
+    del psi0, psi64, psi32
+
+    # ---- throughput at nq qubits
+    gates = brickwork_gates(nq, depth, seed=0x5155455354 + 4)
+    circ = Circuit(nq)
+    for t, m in gates:
+        circ.add(t, m)
+    circ.fuse(5)
+    nblocks = circ.num_blocks
+    s = StateVector32(nq)
+    s.init_zero()
+    for _ in range(args.warmup):
+        circ.apply(s, impl=impl)
+    L.qg_sync()
+    ev0, ev1 = C.c_void_p(), C.c_void_p()
+    L.qg_event_create(C.byref(ev0))
+    L.qg_event_create(C.byref(ev1))
+    launches0 = C.c_int64(0)
+    L.qg_get_launch_count(C.byref(launches0))
+    with ClockSampler(local) as clocks:
+        barrier(dist)
+        L.qg_event_record(ev0, None)
+        for _ in range(args.steps):
+            circ.apply(s, impl=impl)
+        L.qg_event_record(ev1, None)
+        L.qg_sync()
+        barrier(dist)
+    launches1 = C.c_int64(0)
+    L.qg_get_launch_count(C.byref(launches1))
+    ms = C.c_float(0)
+    L.qg_event_elapsed_ms(ev0, ev1, C.byref(ms))
+    t = max_over_ranks(dist, ms.value / 1e3)
+    norm = s.total_prob()
+    flag = C.c_int(0)
+    L.qg_tc_get_error_flag(C.byref(flag))
+    s.free()
+    pass_bytes = 2 * 8 * (1 << nq)
+    eff = world * args.steps * nblocks * pass_bytes / t / 1e9
+    per_pass_ms = t / (args.steps * nblocks) * 1e3
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    peak = peaks.get("hbm_gbs", 6800.0)
+    tensor_flops = nblocks * 3 * 2 * (1 << (nq - 5)) * 64 * 64   # 3 real 64x64 products per 32-amplitude group
+    line = {"metric": "precision form: FP32 fused-block circuit throughput (effective HBM GB/s) and fidelity vs FP64",
+            "value": round(eff, 1), "unit": "GB/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(t / args.steps * 1e3, 2), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 (3xTF32 tensor-core products)" if impl == IMPL_TC else "f32 (SIMT FFMA)",
+            "data": "synthetic (|0> start for throughput; seeded Gaussian state for accuracy)",
+            "config": {"workload": f"{nq}-qubit FP32 statevector, depth-{depth} Haar 1q + CZ brickwork fused into "
+                                   f"<=5-qubit blocks", "qubits": nq, "depth": depth, "gates": len(gates),
+                       "blocks": nblocks, "impl": args.fused_impl},
+            "circuits_per_s": round(world * args.steps / t, 3), "ms_per_block_pass": round(per_pass_ms, 3),
+            "roofline": {"bound": "hbm", "kernel": "k32_fused_tc" if impl == IMPL_TC else "k32_fused",
+                         "achieved": round(eff / world, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(eff / world / peak, 4), "traffic": None,
+                         "tensor_tflops": round(tensor_flops * args.steps / t / 1e12, 1)},
+            "accuracy": {"qubits": na, "fidelity": fid, "one_minus_fidelity": 1 - fid, "max_abs_amp_err": maxabs,
+                         "max_pauli_expec_err": experr, "reference": "FP64 per-gate GPU path (parity-pinned to the oracle)"},
+            "gpu_launches": int(launches1.value - launches0.value), "tc_error_flag": flag.value,
+            "final_total_prob": norm, "clocks": clocks.summary()}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ serving form
+
+def run_serve(args, world, rank, local, dist):
+    """Poisson stream of hardware-efficient-ansatz requests (8-26 qubits, depth 10-100,
+    16 Pauli expectations each).  Served: FP32 fused blocks through the continuous-
+    batching server (circuits fused on a host thread pool as they arrive).  Plain:
+    QuEST's per-gate FP64 path through the API, one request at a time in arrival order."""
+    import concurrent.futures as cf
+    import ctypes as C
+    from quest_gb300 import _lib, api
+    from quest_gb300.api import Q
+    from quest_gb300.serve import Server, circuit_of, hea_request
+    L = _lib.lib()
+    _lib.check(L.qg_init(local))
+    api.init_env()
+    rng = np.random.default_rng(0x5155455354 + 5 + rank)
+    reqs = []
+    for _ in range(args.requests):
+        n = int(rng.integers(args.min_qubits, args.max_qubits + 1))
+        depth = int(rng.integers(10, 101))
+        ops, codes = hea_request(n, depth, rng)
+        reqs.append((n, depth, ops, codes))
+    ngates = sum(len(r[2]) for r in reqs)
+
+    def plain_one(n, ops, codes):
+        q = Q.createQureg(n)
+        for op in ops:
+            if op[0] == "RY":
+                Q.applyRotateY(q, op[1], op[2])
+            elif op[0] == "RZ":
+                Q.applyRotateZ(q, op[1], op[2])
+            else:
+                Q.applyControlledPauliZ(q, op[1], op[2])
+        strs = (api.PauliStr * len(codes))(*[api.pauli_str(c) for c in codes])
+        vals = (C.c_double * len(codes))()
+        Q.calcExpecPauliStrs(vals, q, strs, len(codes))
+        Q.destroyQureg(q)
+        return np.array(list(vals))
+
+    def run_plain(arrivals):
+        t0 = time.perf_counter()
+        lat, vals = [], []
+        for (n, depth, ops, codes), ta in zip(reqs, arrivals):
+            while time.perf_counter() - t0 < ta:
+                time.sleep(1e-4)
+            vals.append(plain_one(n, ops, codes))
+            lat.append(time.perf_counter() - t0 - ta)
+        return time.perf_counter() - t0, lat, vals
+
+    def run_served(arrivals):
+        server = Server(args.hbm_budget_gib << 30, max_in_flight=max(64, len(reqs)))
+        pool = cf.ThreadPoolExecutor(max_workers=args.fuse_threads)
+        t0 = time.perf_counter()
+        nxt, futs, live, lat, vals = 0, {}, {}, [None] * len(reqs), [None] * len(reqs)
+        done = 0
+        while done < len(reqs):
+            now = time.perf_counter() - t0
+            while nxt < len(reqs) and arrivals[nxt] <= now:
+                n, depth, ops, codes = reqs[nxt]
+                futs[nxt] = pool.submit(circuit_of, n, ops)
+                nxt += 1
+            for i in [i for i, f in futs.items() if f.done()]:
+                live[server.submit(futs.pop(i).result(), reqs[i][3])] = i
+            server.poll()
+            for rid in list(live):
+                ok, v = server.result(rid)
+                if ok:
+                    i = live.pop(rid)
+                    lat[i] = time.perf_counter() - t0 - arrivals[i]
+                    vals[i] = v
+                    server.release(rid)
+                    done += 1
+            if not futs and not live and nxt < len(reqs):
+                time.sleep(max(0.0, min(1e-3, arrivals[nxt] - (time.perf_counter() - t0))))
+        makespan = time.perf_counter() - t0
+        pool.shutdown()
+        server.close()
+        return makespan, lat, vals
+
+    # warm-up: compile kernels, create contexts
+    small = [(10, 5, *hea_request(10, 5, np.random.default_rng(1)))]
+    run_served_small = Server(1 << 30)
+    run_served_small.run_all([(circuit_of(10, small[0][2]), small[0][3])])
+    run_served_small.close()
+    plain_one(10, small[0][2], small[0][3])
+
+    zero = [0.0] * len(reqs)
+    # saturation: every request queued at t = 0
+    ms_plain, lat_p0, vals_plain = run_plain(zero)
+    ms_served, lat_s0, vals_served = run_served(zero)
+    err = max(float(np.max(np.abs(a - b))) for a, b in zip(vals_plain, vals_served))
+    cps_plain = len(reqs) / ms_plain
+    cps_served = len(reqs) / ms_served
+    # Poisson arrivals at `load` x the plain path's capacity, the same stream for both
+    lam = args.load * cps_plain
+    arrivals = list(np.cumsum(np.random.default_rng(11).exponential(1.0 / lam, len(reqs))))
+    _, lat_p, _ = run_plain(arrivals)
+    _, lat_s, _ = run_served(arrivals)
+    pct = lambda xs, q: float(np.percentile(np.array(xs) * 1e3, q))
+    line = {"metric": "serving: circuits/s and p50/p99 latency, served FP32 fused batched vs plain per-gate FP64",
+            "value": round(world * cps_served, 3), "unit": "circuits/s", "n_gpus": world,
+            "steps": 1, "warmup": args.warmup, "ms_per_step": round(ms_served * 1e3, 1), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 served / f64 plain",
+            "data": f"synthetic: {len(reqs)} hardware-efficient ansatz requests, {args.min_qubits}-{args.max_qubits} qubits, "
+                    f"depth 10-100, 16 Pauli strings each ({ngates} gates)",
+            "config": {"workload": "Poisson stream of HEA circuits (RY/RZ + CZ ladder), 16 Pauli expectations each",
+                       "requests": len(reqs), "hbm_budget_gib": args.hbm_budget_gib, "fuse_threads": args.fuse_threads},
+            "saturation": {"served_circuits_per_s": round(cps_served, 3), "plain_circuits_per_s": round(cps_plain, 3),
+                           "speedup": round(cps_served / cps_plain, 2),
+                           "served_makespan_s": round(ms_served, 3), "plain_makespan_s": round(ms_plain, 3)},
+            "poisson": {"rate_per_s": round(lam, 3), "load_vs_plain_capacity": args.load,
+                        "served_p50_ms": round(pct(lat_s, 50), 2), "served_p99_ms": round(pct(lat_s, 99), 2),
+                        "plain_p50_ms": round(pct(lat_p, 50), 2), "plain_p99_ms": round(pct(lat_p, 99), 2)},
+            "max_abs_expec_err_served_vs_fp64": err}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -413,9 +653,28 @@ def main():
     ap.add_argument("--depth", type=int, default=20)
     ap.add_argument("--cpu-sample", type=int, default=45, help="gates of the circuit timed on the host CPU")
     ap.add_argument("--traffic", type=float, default=None, help="ncu DRAM bytes per dense launch, if captured")
+    ap.add_argument("--config", default="plain", choices=["plain", "precision", "serve"],
+                    help="plain: the 30-qubit FP64 per-gate circuit (default); precision: FP32 fused blocks; "
+                         "serve: request stream, served vs plain")
+    ap.add_argument("--requests", type=int, default=48)
+    ap.add_argument("--min-qubits", type=int, default=8)
+    ap.add_argument("--max-qubits", type=int, default=26)
+    ap.add_argument("--hbm-budget-gib", type=int, default=64)
+    ap.add_argument("--fuse-threads", type=int, default=8)
+    ap.add_argument("--load", type=float, default=0.8, help="Poisson rate as a fraction of the plain path's capacity")
+    ap.add_argument("--acc-qubits", type=int, default=28, help="precision form: qubits of the accuracy check")
+    ap.add_argument("--fused-impl", default="tc", choices=["tc", "simt"])
     args = ap.parse_args()
     world, rank, local, dist = dist_setup()
-    if args.impl == "reference":
+    if args.config == "serve":
+        run_serve(args, world, rank, local, dist)
+    elif args.config == "precision":
+        if args.qubits == 30 and "--qubits" not in sys.argv:
+            args.qubits = 32
+        if "--depth" not in sys.argv:
+            args.depth = 40
+        run_precision(args, world, rank, local, dist)
+    elif args.impl == "reference":
         run_reference(args, world, rank, dist)
     else:
         run_gb300(args, world, rank, local, dist)

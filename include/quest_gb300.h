@@ -232,6 +232,27 @@ int qg_sv32_calcTotalProb(const void* amps32, int numQubits, double* out, void* 
 int qg_sv32_calcExpecPauliStrBatch(const void* amps32, int numQubits, const int64_t* masksXY, const int64_t* masksYZ,
                                    const int* numsY, int numStrings, qg_cplx* out, void* stream);
 
+/* ------------------------------------------------------------------ continuous-batching server
+ * Requests are fused circuits on FP32 registers starting in |0>, each returning up to
+ * 16 Pauli expectation values.  Registers of <= 14 qubits run whole in shared memory,
+ * one thread block per request, all admitted small requests in one launch; larger
+ * registers are admitted against an HBM byte budget (sub-allocated from one arena) and
+ * run on a pool of non-blocking streams.  poll() is one non-blocking scheduling step. */
+
+typedef struct qg_server qg_server;
+
+int qg_server_create(qg_server** out, int64_t hbmBudgetBytes, int maxInFlight, int impl);
+int qg_server_destroy(qg_server* server);
+/* queues a request (the fused circuit must outlive it); returns its id */
+int qg_server_submit(qg_server* server, qg_circuit* circuit, const int64_t* masksXY, const int64_t* masksYZ,
+                     const int* numsY, int numStrings, int64_t* id);
+/* retires finished requests, admits queued ones in arrival order as slots and memory free up, launches their work */
+int qg_server_poll(qg_server* server, int* numDone);
+/* *done = 1 once finished; values = the request's expectation values */
+int qg_server_result(qg_server* server, int64_t id, double* values, int* done);
+int qg_server_release(qg_server* server, int64_t id);
+int qg_server_stats(qg_server* server, int64_t* queued, int64_t* inFlight, int64_t* hbmInUse, int64_t* finished);
+
 #ifdef __cplusplus
 }
 #endif

@@ -111,6 +111,13 @@ ABI = {
     "qg_sv_convert_f32_to_f64": [vp, vp, I, vp],
     "qg_sv32_calcTotalProb": [vp, I, c_dbl_p, vp],
     "qg_sv32_calcExpecPauliStrBatch": [vp, I, c_i64_p, c_i64_p, c_int_p, I, c_cplx_p, vp],
+    "qg_server_create": [ctypes.POINTER(vp), I64, I, I],
+    "qg_server_destroy": [vp],
+    "qg_server_submit": [vp, vp, c_i64_p, c_i64_p, c_int_p, I, c_i64_p],
+    "qg_server_poll": [vp, c_int_p],
+    "qg_server_result": [vp, I64, c_dbl_p, c_int_p],
+    "qg_server_release": [vp, I64],
+    "qg_server_stats": [vp, c_i64_p, c_i64_p, c_i64_p, c_i64_p],
 }
 
 

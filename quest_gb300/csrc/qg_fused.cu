@@ -22,32 +22,9 @@
 #include <cstring>
 #include <vector>
 
-typedef std::complex<double> cd;
-
 // ============================================================== circuit object (host)
 
-struct QgGate {
-    std::vector<int> targs;   // matrix index bit i <-> targs[i]
-    std::vector<cd> m;        // row-major 2^k x 2^k
-};
-
-struct QgBlock {
-    std::vector<int> targs;   // ascending
-    std::vector<cd> m;        // row-major, index bit i <-> targs[i]
-    size_t off32 = 0;         // offset (in float2) of the FP32 matrix in devF32
-    size_t offTC = 0;         // offset (in floats) of the tensor-core operand pair in devTC (k == 5 only)
-};
-
-struct qg_circuit {
-    int numQubits = 0;
-    std::vector<QgGate> gates;
-    std::vector<QgBlock> blocks;
-    int fusedK = 0;
-    float2* devF32 = nullptr;   // concatenated FP32 block matrices
-    float* devTC = nullptr;     // per k=5 block: Bhi, Blo (64x64 real each) in tensor-core layout
-    size_t tcFloats = 0;
-    bool uploaded = false;      // block matrices are copied to the device at the first apply
-};
+#include "qg_circuit.cuh"
 
 // tensor-core operand builder, defined in qg_fused_tc.cu
 size_t qg_tc_operand_floats();
@@ -325,37 +302,85 @@ int launch_fused_simt(float2* amps, int nq, const std::vector<int>& targs, const
     return qg_check_launch("k32_fused");
 }
 
-int upload_blocks(qg_circuit* c) {
-    if (c->devF32) { cudaFree(c->devF32); c->devF32 = nullptr; }
-    if (c->devTC) { cudaFree(c->devTC); c->devTC = nullptr; }
-    size_t n32 = 0, nTC = 0;
-    size_t tcPer = qg_tc_operand_floats();
+}  // namespace
+
+namespace {
+
+size_t round256(size_t x) { return (x + 255) / 256 * 256; }
+
+// assigns each block its matrix offsets; returns (info, f32, tc) byte sizes
+void layout_blocks(qg_circuit* c, size_t* infoBytes, size_t* f32Bytes, size_t* tcBytes) {
+    size_t n32 = 0, nTC = 0, tcPer = qg_tc_operand_floats();
     for (auto& b : c->blocks) {
         size_t D = (size_t)1 << b.targs.size();
         b.off32 = n32;
         n32 += D * D;
         if (b.targs.size() == 5) { b.offTC = nTC; nTC += tcPer; }
     }
-    std::vector<float2> h32(n32);
-    std::vector<float> hTC(nTC);
-    for (auto& b : c->blocks) {
-        size_t D = (size_t)1 << b.targs.size();
-        for (size_t i = 0; i < D * D; i++) h32[b.off32 + i] = make_float2((float)b.m[i].real(), (float)b.m[i].imag());
-        if (b.targs.size() == 5) qg_tc_build_operands(b.m.data(), hTC.data() + b.offTC);
-    }
-    if (n32) {
-        QG_CUDA(cudaMalloc(&c->devF32, n32 * sizeof(float2)));
-        QG_CUDA(cudaMemcpy(c->devF32, h32.data(), n32 * sizeof(float2), cudaMemcpyHostToDevice));
-    }
-    if (nTC) {
-        QG_CUDA(cudaMalloc(&c->devTC, nTC * sizeof(float)));
-        QG_CUDA(cudaMemcpy(c->devTC, hTC.data(), nTC * sizeof(float), cudaMemcpyHostToDevice));
-    }
+    *infoBytes = round256(c->blocks.size() * sizeof(QgBlockInfo));
+    *f32Bytes = round256(n32 * sizeof(float2));
+    *tcBytes = round256(nTC * sizeof(float));
     c->tcFloats = nTC;
-    return QG_OK;
+}
+
+void free_owned(qg_circuit* c) {
+    if (c->ownsDevice && c->devInfo) cudaFree(c->devInfo);
+    c->devInfo = nullptr;
+    c->devF32 = nullptr;
+    c->devTC = nullptr;
+    c->ownsDevice = false;
+    c->uploaded = false;
 }
 
 }  // namespace
+
+size_t qg_circuit_device_bytes(qg_circuit* c) {
+    size_t a, b, t;
+    layout_blocks(c, &a, &b, &t);
+    return a + b + t;
+}
+
+// Writes the block descriptors, FP32 matrices and tensor-core operands into `dev`
+// (qg_circuit_device_bytes bytes) with copies on `st`, in stream order.
+int qg_circuit_upload_to(qg_circuit* c, char* dev, cudaStream_t st) {
+    free_owned(c);
+    size_t infoBytes, f32Bytes, tcBytes;
+    layout_blocks(c, &infoBytes, &f32Bytes, &tcBytes);
+    std::vector<QgBlockInfo> hInfo(c->blocks.size());
+    std::vector<float2> h32(f32Bytes / sizeof(float2));
+    std::vector<float> hTC(tcBytes / sizeof(float));
+    for (size_t i = 0; i < c->blocks.size(); i++) {
+        auto& b = c->blocks[i];
+        size_t D = (size_t)1 << b.targs.size();
+        for (size_t j = 0; j < D * D; j++) h32[b.off32 + j] = make_float2((float)b.m[j].real(), (float)b.m[j].imag());
+        if (b.targs.size() == 5) qg_tc_build_operands(b.m.data(), hTC.data() + b.offTC);
+        hInfo[i].k = (int)b.targs.size();
+        for (int j = 0; j < 5; j++) hInfo[i].t[j] = j < hInfo[i].k ? b.targs[j] : 0;
+        hInfo[i].off32 = (int)b.off32;
+        hInfo[i].pad = 0;
+    }
+    c->devInfo = (QgBlockInfo*)dev;
+    c->devF32 = (float2*)(dev + infoBytes);
+    c->devTC = (float*)(dev + infoBytes + f32Bytes);
+    if (!hInfo.empty()) QG_CUDA(cudaMemcpyAsync(c->devInfo, hInfo.data(), hInfo.size() * sizeof(QgBlockInfo), cudaMemcpyHostToDevice, st));
+    if (!h32.empty()) QG_CUDA(cudaMemcpyAsync(c->devF32, h32.data(), h32.size() * sizeof(float2), cudaMemcpyHostToDevice, st));
+    if (!hTC.empty()) QG_CUDA(cudaMemcpyAsync(c->devTC, hTC.data(), hTC.size() * sizeof(float), cudaMemcpyHostToDevice, st));
+    // copies from pageable memory are staged by the driver before cudaMemcpyAsync returns,
+    // so the vectors may die now; the device copy is complete in stream order
+    c->uploaded = true;
+    return QG_OK;
+}
+
+int qg_circuit_upload(qg_circuit* c, cudaStream_t st) {
+    free_owned(c);
+    size_t bytes = qg_circuit_device_bytes(c);
+    char* dev = nullptr;
+    QG_CUDA(cudaMalloc(&dev, std::max<size_t>(bytes, 256)));
+    QG_TRY(qg_circuit_upload_to(c, dev, st));
+    c->ownsDevice = true;
+    QG_CUDA(cudaStreamSynchronize(st));
+    return QG_OK;
+}
 
 extern "C" {
 
@@ -369,8 +394,7 @@ int qg_circuit_create(qg_circuit** out, int numQubits) {
 
 int qg_circuit_destroy(qg_circuit* c) {
     if (!c) return QG_OK;
-    if (c->devF32) cudaFree(c->devF32);
-    if (c->devTC) cudaFree(c->devTC);
+    free_owned(c);
     delete c;
     return QG_OK;
 }
@@ -386,7 +410,7 @@ int qg_circuit_add_matrix(qg_circuit* c, const int* targs, int numTargs, const q
     for (size_t i = 0; i < D * D; i++) g.m[i] = cd(matr[i].re, matr[i].im);
     c->gates.push_back(std::move(g));
     c->blocks.clear();
-    c->uploaded = false;
+    free_owned(c);
     return QG_OK;
 }
 
@@ -398,7 +422,7 @@ int qg_circuit_fuse(qg_circuit* c, int maxFusedQubits) {
     c->blocks.clear();
     fuse_gates(c->gates, maxFusedQubits, c->blocks);
     c->fusedK = maxFusedQubits;
-    c->uploaded = false;
+    free_owned(c);
     return QG_OK;
 }
 
@@ -428,10 +452,7 @@ int qg_circuit_get_block(const qg_circuit* c, int i, int* targs, int* numTargs, 
 int qg_sv32_apply_circuit(qg_circuit* c, void* amps, int numQubits, int impl, void* stream) {
     QG_TRY(check32(amps, numQubits));
     if (!c) return qg_fail(QG_ERR_ARG, "null circuit");
-    if (!c->uploaded) {
-        QG_TRY(upload_blocks(c));
-        c->uploaded = true;
-    }
+    if (!c->uploaded) QG_TRY(qg_circuit_upload(c, qg_stream(stream)));
     if (numQubits != c->numQubits) return qg_fail(QG_ERR_ARG, "circuit has %d qubits, state has %d", c->numQubits, numQubits);
     if (c->blocks.empty() && !c->gates.empty()) return qg_fail(QG_ERR_ARG, "circuit was not fused (qg_circuit_fuse)");
     cudaStream_t st = qg_stream(stream);

@@ -15,9 +15,10 @@
 // 8-byte loads: consecutive threads own consecutive groups), split them into
 // TF32 hi/lo parts and store both into shared memory in the no-swizzle K-major
 // core-matrix layout (8 rows x 16 bytes per core matrix); one thread issues the
-// 24 MMAs (3 products x 8 K-steps of 8) into a 128-lane x 64-column TMEM
-// accumulator and commits them to an mbarrier; every warp then reads its 32
-// TMEM lanes (tcgen05.ld 32x32b) and writes its groups' 32 outputs back.
+// 24 MMAs (3 products x 8 K-steps of 8) into two 128-lane x 64-column TMEM
+// accumulators (large term, small terms) and commits them to an mbarrier; every
+// warp then reads its 32 TMEM lanes (tcgen05.ld 32x32b), adds the two
+// accumulators in FP32 and writes its groups' 32 outputs back.
 // Every wait is bounded: a wait that runs out sets the error flag, frees the
 // TMEM and returns.
 #include "qg_common.cuh"
@@ -30,7 +31,7 @@
 #define TC_K 64               // real K (32 complex amplitudes)
 #define TC_N 64               // real N
 #define TC_THREADS 128
-#define TC_TMEM_COLS 64
+#define TC_TMEM_COLS 128          // two 64-column accumulators: the large and the small 3xTF32 terms
 #define TC_WAIT_NS 2000000000ull   // a tile's MMAs take microseconds; 2 s means they never completed
 
 // shared-memory operand sizes (bytes)
@@ -190,13 +191,17 @@ __global__ void __launch_bounds__(TC_THREADS, 2) k32_fused_tc(TcArgs args) {
     const uint32_t barAddr = smem_addr(bar);
     uint32_t phase = 0;
 
-    for (qidx tile = blockIdx.x; tile < args.numTiles; tile += gridDim.x) {
-        // ---- load the tile's 128 groups: thread tid owns group (tile*128 + tid)
-        qidx g = tile * TC_M + tid;
-        qidx base = insert_bits<5>(g, args.ins);
-        float2 x[32];
+    // Software pipeline: the next tile's 32 amplitudes per thread are loaded into
+    // registers while this tile's MMAs run and its results are written back.
+    qidx tile = blockIdx.x;
+    float2 x[32];
+    qidx base = 0;
+    if (tile < args.numTiles) {
+        base = insert_bits<5>(tile * TC_M + tid, args.ins);
 #pragma unroll
         for (int j = 0; j < 32; j++) x[j] = __ldcs(args.amps + base + args.off[j]);
+    }
+    for (; tile < args.numTiles; tile += gridDim.x) {
         // ---- split into TF32 hi/lo and store in the K-major core layout (kk = 2j + c)
 #pragma unroll
         for (int q = 0; q < 16; q++) {
@@ -214,24 +219,37 @@ __global__ void __launch_bounds__(TC_THREADS, 2) k32_fused_tc(TcArgs args) {
         __syncthreads();
         asm volatile("tcgen05.fence::after_thread_sync;");
 
-        // ---- one thread issues D = Al*Bh + Ah*Bl + Ah*Bh (8 K-steps each) and commits
+        // ---- one thread issues the 24 MMAs (8 K-steps per product) and commits them:
+        //      columns 64..127 accumulate the small terms Al*Bh + Ah*Bl, columns 0..63 the
+        //      large term Ah*Bh; the epilogue adds the two in FP32
         if (tid == 0) {
             const uint32_t lboA = (TC_M / 8) * 128, lboB = (TC_N / 8) * 128, sbo = 128;
-            uint32_t acc = 0;
             for (int part = 0; part < 3; part++) {
                 uint32_t a = (part == 0) ? aL : aH;
                 uint32_t b = (part == 1) ? bL : bH;
+                uint32_t d = (part == 2) ? tmem : tmem + TC_N;
+                uint32_t acc = (part == 1) ? 1u : 0u;
 #pragma unroll
                 for (int s = 0; s < TC_K / 8; s++) {
                     uint64_t ad = make_desc(a + s * 2 * lboA, lboA, sbo);
                     uint64_t bd = make_desc(b + s * 2 * lboB, lboB, sbo);
-                    mma_tf32(tmem, ad, bd, idesc, acc);
+                    mma_tf32(d, ad, bd, idesc, acc);
                     acc = 1;
                 }
             }
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" :: "r"(barAddr) : "memory");
         }
-        // ---- every thread waits for the MMAs (bounded)
+
+        // ---- while the MMAs run: load the next tile (registers only; shared memory is busy)
+        const qidx cur = base;
+        const qidx next = tile + gridDim.x;
+        if (next < args.numTiles) {
+            base = insert_bits<5>(next * TC_M + tid, args.ins);
+#pragma unroll
+            for (int j = 0; j < 32; j++) x[j] = __ldcs(args.amps + base + args.off[j]);
+        }
+
+        // ---- every thread waits for the MMAs (bounded by %globaltimer)
         {
             const uint64_t t0 = globaltimer_ns();
             while (!mbar_try_wait(barAddr, phase)) {
@@ -246,17 +264,22 @@ __global__ void __launch_bounds__(TC_THREADS, 2) k32_fused_tc(TcArgs args) {
         }
         asm volatile("tcgen05.fence::after_thread_sync;");
 
-        // ---- epilogue: warp w reads TMEM lanes 32w..32w+31 (its groups), 64 columns
-        uint32_t r[64];
+        // ---- epilogue: warp w reads TMEM lanes 32w..32w+31 (its groups), 16 columns of
+        //      each accumulator at a time, and writes 8 amplitudes per chunk
         const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
-        TMEM_LD16(taddr + 0, (r + 0));
-        TMEM_LD16(taddr + 16, (r + 16));
-        TMEM_LD16(taddr + 32, (r + 32));
-        TMEM_LD16(taddr + 48, (r + 48));
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-        for (int k = 0; k < 32; k++)
-            __stcs(args.amps + base + args.off[k], make_float2(__uint_as_float(r[2 * k]), __uint_as_float(r[2 * k + 1])));
+        for (int c = 0; c < 4; c++) {
+            uint32_t big[16], small[16];
+            TMEM_LD16(taddr + 16 * c, big);
+            TMEM_LD16(taddr + TC_N + 16 * c, small);
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+            for (int k = 0; k < 8; k++) {
+                float re = __uint_as_float(small[2 * k]) + __uint_as_float(big[2 * k]);
+                float im = __uint_as_float(small[2 * k + 1]) + __uint_as_float(big[2 * k + 1]);
+                __stcs(args.amps + cur + args.off[8 * c + k], make_float2(re, im));
+            }
+        }
         asm volatile("tcgen05.fence::before_thread_sync;");
         __syncthreads();   // TMEM and the A buffers may now be overwritten
         asm volatile("tcgen05.fence::after_thread_sync;");

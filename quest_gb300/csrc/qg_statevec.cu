@@ -42,28 +42,38 @@ __global__ void k_init_debug(double2* __restrict__ a, qidx n) {
 
 template <int NB>
 __global__ void k_swap(double2* __restrict__ a, qidx numIts, Ins ins, qidx mask, qidx flip) {
+    const qidx stride = (qidx)gridDim.x * blockDim.x;
     qidx n = blockIdx.x * (qidx)blockDim.x + threadIdx.x;
     if (n >= numIts) return;
     qidx i01 = insert_bits<NB>(n, ins) | mask;
-    qidx i10 = i01 ^ flip;
-    double2 x = ld_amp(a + i01), y = ld_amp(a + i10);
-    st_amp(a + i01, y);
-    st_amp(a + i10, x);
+    double2 x = ld_amp(a + i01), y = ld_amp(a + (i01 ^ flip));
+    for (;;) {
+        // software pipeline: the next group's loads are in flight while this one is stored
+        const qidx nn = n + stride;
+        const bool more = nn < numIts;
+        qidx j01 = 0;
+        double2 xn, yn;
+        if (more) {
+            j01 = insert_bits<NB>(nn, ins) | mask;
+            xn = ld_amp(a + j01);
+            yn = ld_amp(a + (j01 ^ flip));
+        }
+        st_amp(a + i01, y);
+        st_amp(a + (i01 ^ flip), x);
+        if (!more) break;
+        n = nn; i01 = j01; x = xn; y = yn;
+    }
 }
 
 // ============================================================== one-target dense
 
 struct Mat1 { double2 m[4]; };
 
-// MODE 0: general complex 2x2; MODE 1: real 2x2 (imaginary parts all zero)
-template <int NB, int MODE>
-__global__ void k_dense1(double2* __restrict__ a, qidx numIts, Ins ins, qidx mask, qidx tbit, Mat1 M) {
-    qidx n = blockIdx.x * (qidx)blockDim.x + threadIdx.x;
-    if (n >= numIts) return;
-    qidx i0 = insert_bits<NB>(n, ins) | mask;
-    qidx i1 = i0 | tbit;
-    double2 x = ld_amp(a + i0), y = ld_amp(a + i1);
-    double2 o0, o1;
+// MODE 0: general complex 2x2; MODE 1: real 2x2 (imaginary parts all zero).
+// Persistent grid-stride loop with the next pair's loads issued before this
+// pair's FP64 work, so the FP64 pipe is not left idle while warps wait on memory.
+template <int MODE>
+__device__ __forceinline__ void dense1_pair(const Mat1& M, double2 x, double2 y, double2& o0, double2& o1) {
     if (MODE == 1) {
         o0 = make_double2(fma(M.m[0].x, x.x, M.m[1].x * y.x), fma(M.m[0].x, x.y, M.m[1].x * y.y));
         o1 = make_double2(fma(M.m[2].x, x.x, M.m[3].x * y.x), fma(M.m[2].x, x.y, M.m[3].x * y.y));
@@ -71,8 +81,32 @@ __global__ void k_dense1(double2* __restrict__ a, qidx numIts, Ins ins, qidx mas
         o0 = cfma(M.m[0], x, cmul(M.m[1], y));
         o1 = cfma(M.m[2], x, cmul(M.m[3], y));
     }
-    st_amp(a + i0, o0);
-    st_amp(a + i1, o1);
+}
+
+template <int NB, int MODE>
+__global__ void k_dense1(double2* __restrict__ a, qidx numIts, Ins ins, qidx mask, qidx tbit, Mat1 M) {
+    const qidx stride = (qidx)gridDim.x * blockDim.x;
+    qidx n = blockIdx.x * (qidx)blockDim.x + threadIdx.x;
+    if (n >= numIts) return;
+    qidx i0 = insert_bits<NB>(n, ins) | mask;
+    double2 x = ld_amp(a + i0), y = ld_amp(a + (i0 | tbit));
+    for (;;) {
+        const qidx nn = n + stride;
+        const bool more = nn < numIts;
+        qidx j0 = 0;
+        double2 xn, yn;
+        if (more) {
+            j0 = insert_bits<NB>(nn, ins) | mask;
+            xn = ld_amp(a + j0);
+            yn = ld_amp(a + (j0 | tbit));
+        }
+        double2 o0, o1;
+        dense1_pair<MODE>(M, x, y, o0, o1);
+        st_amp(a + i0, o0);
+        st_amp(a + (i0 | tbit), o1);
+        if (!more) break;
+        n = nn; i0 = j0; x = xn; y = yn;
+    }
 }
 
 // ============================================================== two-target dense
@@ -154,11 +188,25 @@ __global__ void k_denseMany(double2* __restrict__ a, qidx numBlocks, int K, Ins 
 // MODE 0: factor d[bit t]; MODE 1: single factor d0 on every visited amplitude
 template <int NB, int MODE>
 __global__ void k_diag1(double2* __restrict__ a, qidx numIts, Ins ins, qidx mask, qidx tbit, double2 d0, double2 d1) {
+    const qidx stride = (qidx)gridDim.x * blockDim.x;
     qidx n = blockIdx.x * (qidx)blockDim.x + threadIdx.x;
     if (n >= numIts) return;
     qidx i = insert_bits<NB>(n, ins) | mask;
-    double2 f = (MODE == 1) ? d0 : ((i & tbit) ? d1 : d0);
-    st_amp(a + i, cmul(f, ld_amp(a + i)));
+    double2 x = ld_amp(a + i);
+    for (;;) {
+        const qidx nn = n + stride;
+        const bool more = nn < numIts;
+        qidx j = 0;
+        double2 xn;
+        if (more) {
+            j = insert_bits<NB>(nn, ins) | mask;
+            xn = ld_amp(a + j);
+        }
+        double2 f = (MODE == 1) ? d0 : ((i & tbit) ? d1 : d0);
+        st_amp(a + i, cmul(f, x));
+        if (!more) break;
+        n = nn; i = j; x = xn;
+    }
 }
 
 struct Diag4 { double2 d[4]; };
@@ -221,16 +269,8 @@ __device__ __forceinline__ double neg_if(double x, int s) {
 
 // MODE 0: general complex f0, f1.  MODE 1: f0 real, f1 real (f1.y == 0).
 // MODE 2: f0 real, f1 imaginary (f1.x == 0).  MODE 3: f0 == 0, f1 in {1,i,-1,-i}: pure permutation.
-template <int NB, int MODE>
-__global__ void k_pauli(double2* __restrict__ a, qidx numIts, Ins ins, qidx mask, qidx maskXY, qidx maskYZ,
-                        double2 f0, double2 f1) {
-    qidx n = blockIdx.x * (qidx)blockDim.x + threadIdx.x;
-    if (n >= numIts) return;
-    qidx iA = insert_bits<NB>(n, ins) | mask;
-    qidx iB = iA ^ maskXY;
-    int sA = parity64(iA & maskYZ), sB = parity64(iB & maskYZ);   // 1 means minus
-    double2 x = ld_amp(a + iA), y = ld_amp(a + iB);
-    double2 oA, oB;
+template <int MODE>
+__device__ __forceinline__ void pauli_pair(double2 f0, double2 f1, int sA, int sB, double2 x, double2 y, double2& oA, double2& oB) {
     if (MODE == 0) {
         double2 gA = make_double2(neg_if(f1.x, sB), neg_if(f1.y, sB));
         double2 gB = make_double2(neg_if(f1.x, sA), neg_if(f1.y, sA));
@@ -257,8 +297,35 @@ __global__ void k_pauli(double2* __restrict__ a, qidx numIts, Ins ins, qidx mask
             oB = make_double2(neg_if(x.x, neg ^ sA), neg_if(x.y, neg ^ sA));
         }
     }
-    st_amp(a + iA, oA);
-    st_amp(a + iB, oB);
+}
+
+template <int NB, int MODE>
+__global__ void k_pauli(double2* __restrict__ a, qidx numIts, Ins ins, qidx mask, qidx maskXY, qidx maskYZ,
+                        double2 f0, double2 f1) {
+    const qidx stride = (qidx)gridDim.x * blockDim.x;
+    qidx n = blockIdx.x * (qidx)blockDim.x + threadIdx.x;
+    if (n >= numIts) return;
+    qidx iA = insert_bits<NB>(n, ins) | mask;
+    double2 x = ld_amp(a + iA), y = ld_amp(a + (iA ^ maskXY));
+    for (;;) {
+        const qidx nn = n + stride;
+        const bool more = nn < numIts;
+        qidx jA = 0;
+        double2 xn, yn;
+        if (more) {
+            jA = insert_bits<NB>(nn, ins) | mask;
+            xn = ld_amp(a + jA);
+            yn = ld_amp(a + (jA ^ maskXY));
+        }
+        const qidx iB = iA ^ maskXY;
+        const int sA = parity64(iA & maskYZ), sB = parity64(iB & maskYZ);   // 1 means minus
+        double2 oA, oB;
+        pauli_pair<MODE>(f0, f1, sA, sB, x, y, oA, oB);
+        st_amp(a + iA, oA);
+        st_amp(a + iB, oB);
+        if (!more) break;
+        n = nn; iA = jA; x = xn; y = yn;
+    }
 }
 
 // cpu_statevector_anyCtrlAnyTargZOrPhaseGadget_sub (cpu_subroutines.cpp:962-990).
@@ -266,15 +333,25 @@ __global__ void k_pauli(double2* __restrict__ a, qidx numIts, Ins ins, qidx mask
 // odd-parity amplitudes change, by a sign flip.
 template <int NB, int MODE>
 __global__ void k_zphase(double2* __restrict__ a, qidx numIts, Ins ins, qidx mask, qidx tmask, double2 f0, double2 f1) {
+    const qidx stride = (qidx)gridDim.x * blockDim.x;
     qidx n = blockIdx.x * (qidx)blockDim.x + threadIdx.x;
     if (n >= numIts) return;
     qidx i = insert_bits<NB>(n, ins) | mask;
-    int p = parity64(i & tmask);
     double2 x = ld_amp(a + i);
-    if (MODE == 1) {
-        st_amp(a + i, make_double2(neg_if(x.x, p), neg_if(x.y, p)));
-    } else {
-        st_amp(a + i, cmul(p ? f1 : f0, x));
+    for (;;) {
+        const qidx nn = n + stride;
+        const bool more = nn < numIts;
+        qidx j = 0;
+        double2 xn;
+        if (more) {
+            j = insert_bits<NB>(nn, ins) | mask;
+            xn = ld_amp(a + j);
+        }
+        const int p = parity64(i & tmask);
+        if (MODE == 1) st_amp(a + i, make_double2(neg_if(x.x, p), neg_if(x.y, p)));
+        else st_amp(a + i, cmul(p ? f1 : f0, x));
+        if (!more) break;
+        n = nn; i = j; x = xn;
     }
 }
 
@@ -298,6 +375,14 @@ double2 d2(qg_cplx c) { return make_double2(c.re, c.im); }
 
 #define QG_LAUNCH_PLAIN(KERNEL, NBV, ...) \
     KERNEL<NBV><<<qg_blocks(numIts), QG_THREADS, 0, st>>>(__VA_ARGS__)
+
+// One resident wave of 256-thread blocks (8 per SM), or fewer when there is less work:
+// the grid-stride kernels below then stream their groups with loads in flight.
+unsigned persistent_blocks(qidx items) {
+    qidx full = (qidx)qg_num_sms() * 8;
+    qidx need = (items + QG_THREADS - 1) / QG_THREADS;
+    return (unsigned)(need < full ? need : full);
+}
 
 }  // namespace
 
@@ -340,7 +425,7 @@ int qg_sv_anyCtrlSwap(void* amps, int numQubits, const int* ctrls, const int* ct
     qidx numIts = ((qidx)1 << numQubits) >> p.numFixed;
     qidx flip = ((qidx)1 << targ1) | ((qidx)1 << targ2);
     cudaStream_t st = qg_stream(stream);
-#define L(NBV) QG_LAUNCH_PLAIN(k_swap, NBV, (double2*)amps, numIts, p.ins, p.stateMask, flip)
+#define L(NBV) k_swap<NBV><<<persistent_blocks(numIts), QG_THREADS, 0, st>>>((double2*)amps, numIts, p.ins, p.stateMask, flip)
     QG_DISPATCH_NB(p.numFixed, L)
 #undef L
     qg_note_launch();
@@ -364,11 +449,11 @@ int qg_sv_anyCtrlOneTargDenseMatr(void* amps, int numQubits, const int* ctrls, c
     qidx tbit = (qidx)1 << targ;
     cudaStream_t st = qg_stream(stream);
     if (real) {
-#define L(NBV) k_dense1<NBV, 1><<<qg_blocks(numIts), QG_THREADS, 0, st>>>((double2*)amps, numIts, p.ins, p.stateMask, tbit, M)
+#define L(NBV) k_dense1<NBV, 1><<<persistent_blocks(numIts), QG_THREADS, 0, st>>>((double2*)amps, numIts, p.ins, p.stateMask, tbit, M)
         QG_DISPATCH_NB(p.numFixed, L)
 #undef L
     } else {
-#define L(NBV) k_dense1<NBV, 0><<<qg_blocks(numIts), QG_THREADS, 0, st>>>((double2*)amps, numIts, p.ins, p.stateMask, tbit, M)
+#define L(NBV) k_dense1<NBV, 0><<<persistent_blocks(numIts), QG_THREADS, 0, st>>>((double2*)amps, numIts, p.ins, p.stateMask, tbit, M)
         QG_DISPATCH_NB(p.numFixed, L)
 #undef L
     }
@@ -501,7 +586,7 @@ int qg_sv_anyCtrlOneTargDiagMatr(void* amps, int numQubits, const int* ctrls, co
         QG_TRY(qg_make_plan(numQubits, ctrls, ctrlStates, numCtrls, &targ, &tv, 1, &p));
         qidx numIts = ((qidx)1 << numQubits) >> p.numFixed;
         double2 f = d2(one0 ? elems[1] : elems[0]);
-#define L(NBV) k_diag1<NBV, 1><<<qg_blocks(numIts), QG_THREADS, 0, st>>>((double2*)amps, numIts, p.ins, p.stateMask, 0, f, f)
+#define L(NBV) k_diag1<NBV, 1><<<persistent_blocks(numIts), QG_THREADS, 0, st>>>((double2*)amps, numIts, p.ins, p.stateMask, 0, f, f)
         QG_DISPATCH_NB(p.numFixed, L)
 #undef L
     } else {
@@ -509,7 +594,7 @@ int qg_sv_anyCtrlOneTargDiagMatr(void* amps, int numQubits, const int* ctrls, co
         QG_TRY(qg_make_plan(numQubits, ctrls, ctrlStates, numCtrls, nullptr, nullptr, 0, &p));
         qidx numIts = ((qidx)1 << numQubits) >> p.numFixed;
         qidx tbit = (qidx)1 << targ;
-#define L(NBV) k_diag1<NBV, 0><<<qg_blocks(numIts), QG_THREADS, 0, st>>>((double2*)amps, numIts, p.ins, p.stateMask, tbit, d2(elems[0]), d2(elems[1]))
+#define L(NBV) k_diag1<NBV, 0><<<persistent_blocks(numIts), QG_THREADS, 0, st>>>((double2*)amps, numIts, p.ins, p.stateMask, tbit, d2(elems[0]), d2(elems[1]))
         QG_DISPATCH_NB(p.numFixed, L)
 #undef L
     }
@@ -616,10 +701,10 @@ int qg_sv_anyCtrlPauliTensorOrGadget(void* amps, int numQubits, const int* ctrls
     if (f0.x == 0.0 && f0.y == 0.0 && unit1) mode = 3;
     else if (f0.y == 0.0 && f1.y == 0.0) mode = 1;
     else if (f0.y == 0.0 && f1.x == 0.0) mode = 2;
-#define L0(NBV) k_pauli<NBV, 0><<<qg_blocks(numIts), QG_THREADS, 0, st>>>((double2*)amps, numIts, p.ins, p.stateMask, maskXY, maskYZ, f0, f1)
-#define L1(NBV) k_pauli<NBV, 1><<<qg_blocks(numIts), QG_THREADS, 0, st>>>((double2*)amps, numIts, p.ins, p.stateMask, maskXY, maskYZ, f0, f1)
-#define L2(NBV) k_pauli<NBV, 2><<<qg_blocks(numIts), QG_THREADS, 0, st>>>((double2*)amps, numIts, p.ins, p.stateMask, maskXY, maskYZ, f0, f1)
-#define L3(NBV) k_pauli<NBV, 3><<<qg_blocks(numIts), QG_THREADS, 0, st>>>((double2*)amps, numIts, p.ins, p.stateMask, maskXY, maskYZ, f0, f1)
+#define L0(NBV) k_pauli<NBV, 0><<<persistent_blocks(numIts), QG_THREADS, 0, st>>>((double2*)amps, numIts, p.ins, p.stateMask, maskXY, maskYZ, f0, f1)
+#define L1(NBV) k_pauli<NBV, 1><<<persistent_blocks(numIts), QG_THREADS, 0, st>>>((double2*)amps, numIts, p.ins, p.stateMask, maskXY, maskYZ, f0, f1)
+#define L2(NBV) k_pauli<NBV, 2><<<persistent_blocks(numIts), QG_THREADS, 0, st>>>((double2*)amps, numIts, p.ins, p.stateMask, maskXY, maskYZ, f0, f1)
+#define L3(NBV) k_pauli<NBV, 3><<<persistent_blocks(numIts), QG_THREADS, 0, st>>>((double2*)amps, numIts, p.ins, p.stateMask, maskXY, maskYZ, f0, f1)
     switch (mode) {
         case 0: QG_DISPATCH_NB(p.numFixed, L0) break;
         case 1: QG_DISPATCH_NB(p.numFixed, L1) break;
@@ -649,11 +734,11 @@ int qg_sv_anyCtrlAnyTargZOrPhaseGadget(void* amps, int numQubits, const int* ctr
     cudaStream_t st = qg_stream(stream);
     bool ztensor = fac0.re == 1.0 && fac0.im == 0.0 && fac1.re == -1.0 && fac1.im == 0.0;
     if (ztensor) {
-#define L(NBV) k_zphase<NBV, 1><<<qg_blocks(numIts), QG_THREADS, 0, st>>>((double2*)amps, numIts, p.ins, p.stateMask, tmask, d2(fac0), d2(fac1))
+#define L(NBV) k_zphase<NBV, 1><<<persistent_blocks(numIts), QG_THREADS, 0, st>>>((double2*)amps, numIts, p.ins, p.stateMask, tmask, d2(fac0), d2(fac1))
         QG_DISPATCH_NB(p.numFixed, L)
 #undef L
     } else {
-#define L(NBV) k_zphase<NBV, 0><<<qg_blocks(numIts), QG_THREADS, 0, st>>>((double2*)amps, numIts, p.ins, p.stateMask, tmask, d2(fac0), d2(fac1))
+#define L(NBV) k_zphase<NBV, 0><<<persistent_blocks(numIts), QG_THREADS, 0, st>>>((double2*)amps, numIts, p.ins, p.stateMask, tmask, d2(fac0), d2(fac1))
         QG_DISPATCH_NB(p.numFixed, L)
 #undef L
     }

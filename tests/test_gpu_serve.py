@@ -1,0 +1,71 @@
+"""The continuous-batching server on the GPU: served results (FP32 fused, small
+registers in shared memory, large ones on streams) against the FP64 oracle;
+each request's result is the same alone and in a mix of other requests; the
+queue drains when the HBM budget cannot hold every request at once."""
+import numpy as np
+import pytest
+
+import qcircuits as qc
+
+pytestmark = pytest.mark.gpu
+
+
+def _requests(sizes, seed):
+    from quest_gb300.serve import hea_request
+    rng = np.random.default_rng(seed)
+    out = []
+    for n in sizes:
+        depth = int(rng.integers(3, 9))
+        out.append((n, hea_request(n, depth, rng)))
+    return out
+
+
+def test_served_results_match_the_fp64_oracle(env):
+    from quest_gb300.serve import Server, circuit_of, text_of
+    reqs = _requests([5, 8, 11, 13, 14, 15, 16, 18], 1)
+    server = Server(1 << 30)
+    try:
+        got = server.run_all([(circuit_of(n, ops), codes) for n, (ops, codes) in reqs])
+    finally:
+        server.close()
+    for (n, (ops, codes)), vals in zip(reqs, got):
+        zero = np.zeros(1 << n, dtype=np.complex128)
+        zero[0] = 1
+        _, want, _ = qc.oracle().run(text_of(ops, codes), n, 0, zero)
+        assert np.max(np.abs(vals - want)) < 2e-5, n
+
+
+def test_result_is_the_same_alone_and_in_the_mix(env):
+    from quest_gb300.serve import Server, circuit_of
+    probe = _requests([12, 17], 7)
+    others = _requests([6, 9, 10, 12, 13, 14, 15, 16, 17, 19, 8, 11, 14, 18], 8)
+    alone = []
+    for n, (ops, codes) in probe:
+        s = Server(1 << 30)
+        try:
+            alone.append(s.run_all([(circuit_of(n, ops), codes)])[0])
+        finally:
+            s.close()
+    mix = [(circuit_of(n, ops), codes) for n, (ops, codes) in others]
+    mix.insert(3, (circuit_of(probe[0][0], probe[0][1][0]), probe[0][1][1]))
+    mix.insert(9, (circuit_of(probe[1][0], probe[1][1][0]), probe[1][1][1]))
+    s = Server(1 << 30)
+    try:
+        got = s.run_all(mix)
+    finally:
+        s.close()
+    assert np.max(np.abs(got[3] - alone[0])) <= 1e-12
+    assert np.max(np.abs(got[9] - alone[1])) <= 1e-12
+
+
+def test_queue_drains_under_a_tight_memory_budget(env):
+    from quest_gb300.serve import Server, circuit_of
+    reqs = _requests([18, 19, 18, 19, 18, 19], 3)
+    # room for about one 19-qubit register (4 MiB state + circuit) at a time
+    s = Server(12 << 20)
+    try:
+        got = s.run_all([(circuit_of(n, ops), codes) for n, (ops, codes) in reqs])
+        assert s.stats()["hbm_in_use"] == 0
+    finally:
+        s.close()
+    assert len(got) == 6 and all(np.all(np.isfinite(v)) for v in got)
