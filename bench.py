@@ -527,6 +527,9 @@ def run_precision(args, world, rank, local, dist):
 
 # ------------------------------------------------------------------ serving form
 
+def log(msg):
+    print(f"[bench {time.strftime('%H:%M:%S')}] {msg}", file=sys.stderr, flush=True)
+
 def run_serve(args, world, rank, local, dist):
     """Poisson stream of hardware-efficient-ansatz requests (8-26 qubits, depth 10-100,
     16 Pauli expectations each).  Served: FP32 fused blocks through the continuous-
@@ -570,8 +573,10 @@ def run_serve(args, world, rank, local, dist):
         for (n, depth, ops, codes), ta in zip(reqs, arrivals):
             while time.perf_counter() - t0 < ta:
                 time.sleep(1e-4)
+            t1 = time.perf_counter()
             vals.append(plain_one(n, ops, codes))
             lat.append(time.perf_counter() - t0 - ta)
+            log(f"plain  n={n:2d} depth={depth:3d} gates={len(ops):5d} {1e3 * (time.perf_counter() - t1):9.1f} ms")
         return time.perf_counter() - t0, lat, vals
 
     def run_served(arrivals):
@@ -580,15 +585,21 @@ def run_serve(args, world, rank, local, dist):
         t0 = time.perf_counter()
         nxt, futs, live, lat, vals = 0, {}, {}, [None] * len(reqs), [None] * len(reqs)
         done = 0
+        last_progress = time.perf_counter()
         while done < len(reqs):
             now = time.perf_counter() - t0
+            if time.perf_counter() - last_progress > args.stall_s:
+                raise RuntimeError(f"served path made no progress for {args.stall_s} s: {server.stats()}, "
+                                   f"{len(futs)} circuits being fused, {len(live)} in the server, {done} done")
             while nxt < len(reqs) and arrivals[nxt] <= now:
                 n, depth, ops, codes = reqs[nxt]
                 futs[nxt] = pool.submit(circuit_of, n, ops)
                 nxt += 1
+            progressed = False
             for i in [i for i, f in futs.items() if f.done()]:
                 live[server.submit(futs.pop(i).result(), reqs[i][3])] = i
-            server.poll()
+                progressed = True
+            progressed |= server.poll() > 0
             for rid in list(live):
                 ok, v = server.result(rid)
                 if ok:
@@ -597,8 +608,12 @@ def run_serve(args, world, rank, local, dist):
                     vals[i] = v
                     server.release(rid)
                     done += 1
+                    last_progress = time.perf_counter()
+                    log(f"served n={reqs[i][0]:2d} depth={reqs[i][1]:3d} latency {1e3 * lat[i]:9.1f} ms")
             if not futs and not live and nxt < len(reqs):
                 time.sleep(max(0.0, min(1e-3, arrivals[nxt] - (time.perf_counter() - t0))))
+            elif not progressed:
+                time.sleep(5e-5)   # leaves the interpreter lock to the fusing threads
         makespan = time.perf_counter() - t0
         pool.shutdown()
         server.close()
@@ -613,15 +628,20 @@ def run_serve(args, world, rank, local, dist):
 
     zero = [0.0] * len(reqs)
     # saturation: every request queued at t = 0
+    log("phase: plain, saturation")
     ms_plain, lat_p0, vals_plain = run_plain(zero)
+    log(f"phase: served, saturation (plain took {ms_plain:.1f} s)")
     ms_served, lat_s0, vals_served = run_served(zero)
+    log(f"served took {ms_served:.1f} s")
     err = max(float(np.max(np.abs(a - b))) for a, b in zip(vals_plain, vals_served))
     cps_plain = len(reqs) / ms_plain
     cps_served = len(reqs) / ms_served
     # Poisson arrivals at `load` x the plain path's capacity, the same stream for both
     lam = args.load * cps_plain
     arrivals = list(np.cumsum(np.random.default_rng(11).exponential(1.0 / lam, len(reqs))))
+    log(f"phase: Poisson at {lam:.2f}/s, plain")
     _, lat_p, _ = run_plain(arrivals)
+    log("phase: Poisson, served")
     _, lat_s, _ = run_served(arrivals)
     pct = lambda xs, q: float(np.percentile(np.array(xs) * 1e3, q))
     line = {"metric": "serving: circuits/s and p50/p99 latency, served FP32 fused batched vs plain per-gate FP64",
@@ -662,6 +682,7 @@ def main():
     ap.add_argument("--hbm-budget-gib", type=int, default=64)
     ap.add_argument("--fuse-threads", type=int, default=8)
     ap.add_argument("--load", type=float, default=0.8, help="Poisson rate as a fraction of the plain path's capacity")
+    ap.add_argument("--stall-s", type=float, default=120.0, help="serve: abort if no request finishes for this long")
     ap.add_argument("--acc-qubits", type=int, default=28, help="precision form: qubits of the accuracy check")
     ap.add_argument("--fused-impl", default="tc", choices=["tc", "simt"])
     args = ap.parse_args()

@@ -213,6 +213,10 @@ int qg_circuit_create(qg_circuit** out, int numQubits);
 int qg_circuit_destroy(qg_circuit* circuit);
 /* appends a dense unitary on 1..5 qubits; matr row-major 2^k x 2^k, index bit i <-> targs[i] */
 int qg_circuit_add_matrix(qg_circuit* circuit, const int* targs, int numTargs, const qg_cplx* matr);
+/* appends numGates 1- or 2-qubit unitaries at once: gate g acts on numTargs[g] qubits
+ * targs[2g], targs[2g+1] with the row-major matrix in the first 4^numTargs[g] entries of
+ * matrs[16g .. 16g+15] */
+int qg_circuit_add_matrices(qg_circuit* circuit, int numGates, const int* numTargs, const int* targs, const qg_cplx* matrs);
 /* greedy fusion into blocks of at most maxFusedQubits (1..5) qubits; matrices upload at the first apply */
 int qg_circuit_fuse(qg_circuit* circuit, int maxFusedQubits);
 int qg_circuit_get_num_gates(const qg_circuit* circuit, int* out);

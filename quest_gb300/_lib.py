@@ -99,6 +99,7 @@ ABI = {
     "qg_circuit_create": [ctypes.POINTER(vp), I],
     "qg_circuit_destroy": [vp],
     "qg_circuit_add_matrix": [vp, c_int_p, I, c_cplx_p],
+    "qg_circuit_add_matrices": [vp, I, c_int_p, c_int_p, c_cplx_p],
     "qg_circuit_fuse": [vp, I],
     "qg_circuit_get_num_gates": [vp, c_int_p],
     "qg_circuit_get_num_blocks": [vp, c_int_p],

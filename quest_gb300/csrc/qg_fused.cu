@@ -34,38 +34,81 @@ bool qg_tc_supported(int numQubits);
 
 namespace {
 
-// y = G x on the space of `qs` (sorted); G acts on gate qubits `gq` (a subset of qs)
+bool is_diagonal(const QgGate& g) {
+    size_t GD = (size_t)1 << g.targs.size();
+    for (size_t r = 0; r < GD; r++)
+        for (size_t c = 0; c < GD; c++)
+            if (r != c && g.m[r * GD + c] != cd(0, 0)) return false;
+    return true;
+}
+
+// M <- G M on the space of `qs` (sorted); G acts on its targets, a subset of qs
 void apply_gate_to_columns(std::vector<cd>& M, const std::vector<int>& qs, const QgGate& g) {
-    int m = (int)qs.size();
-    size_t D = (size_t)1 << m;
-    int gk = (int)g.targs.size();
-    size_t GD = (size_t)1 << gk;
-    std::vector<int> pos(gk);
-    for (int i = 0; i < gk; i++) pos[i] = (int)(std::find(qs.begin(), qs.end(), g.targs[i]) - qs.begin());
-    size_t gmask = 0;
-    for (int i = 0; i < gk; i++) gmask |= (size_t)1 << pos[i];
-    std::vector<cd> in(GD), out(GD);
-    // rows of M are indexed by output basis states; apply G to every column
-    for (size_t col = 0; col < D; col++) {
-        for (size_t base = 0; base < D; base++) {
-            if (base & gmask) continue;
-            for (size_t j = 0; j < GD; j++) {
-                size_t r = base;
-                for (int i = 0; i < gk; i++) if ((j >> i) & 1) r |= (size_t)1 << pos[i];
-                in[j] = M[r * D + col];
-            }
+    const int m = (int)qs.size();
+    const size_t D = (size_t)1 << m;
+    const int gk = (int)g.targs.size();
+    const size_t GD = (size_t)1 << gk;
+    size_t gbit[5], gmask = 0;
+    for (int i = 0; i < gk; i++) {
+        gbit[i] = (size_t)1 << (std::find(qs.begin(), qs.end(), g.targs[i]) - qs.begin());
+        gmask |= gbit[i];
+    }
+    size_t offs[32];
+    for (size_t j = 0; j < GD; j++) {
+        size_t o = 0;
+        for (int i = 0; i < gk; i++) if ((j >> i) & 1) o |= gbit[i];
+        offs[j] = o;
+    }
+    if (is_diagonal(g)) {
+        // a diagonal gate scales whole rows of M
+        for (size_t r = 0; r < D; r++) {
+            size_t j = 0;
+            for (int i = 0; i < gk; i++) if (r & gbit[i]) j |= (size_t)1 << i;
+            cd d = g.m[j * GD + j];
+            if (d == cd(1, 0)) continue;
+            cd* row = &M[r * D];
+            for (size_t c = 0; c < D; c++) row[c] *= d;
+        }
+        return;
+    }
+    cd in[32];
+    for (size_t base = 0; base < D; base++) {
+        if (base & gmask) continue;
+        for (size_t col = 0; col < D; col++) {
+            for (size_t j = 0; j < GD; j++) in[j] = M[(base | offs[j]) * D + col];
             for (size_t r2 = 0; r2 < GD; r2++) {
                 cd acc = 0;
-                for (size_t j = 0; j < GD; j++) acc += g.m[r2 * GD + j] * in[j];
-                out[r2] = acc;
-            }
-            for (size_t j = 0; j < GD; j++) {
-                size_t r = base;
-                for (int i = 0; i < gk; i++) if ((j >> i) & 1) r |= (size_t)1 << pos[i];
-                M[r * D + col] = out[j];
+                const cd* grow = &g.m[r2 * GD];
+                for (size_t j = 0; j < GD; j++) acc += grow[j] * in[j];
+                M[(base | offs[r2]) * D + col] = acc;
             }
         }
     }
+}
+
+// Runs of one-qubit gates on the same qubit collapse into one 2x2 gate (their product),
+// so the block fuser sees fewer, denser gates.
+std::vector<QgGate> merge_single_qubit_runs(const std::vector<QgGate>& gates, int numQubits) {
+    std::vector<QgGate> out;
+    std::vector<int> pending(numQubits, -1);   // index in `out` of an open 1q gate per qubit
+    for (const QgGate& g : gates) {
+        if (g.targs.size() == 1) {
+            int q = g.targs[0];
+            if (pending[q] >= 0) {
+                QgGate& p = out[pending[q]];
+                cd a = g.m[0], b = g.m[1], c = g.m[2], d = g.m[3];
+                cd e = p.m[0], f = p.m[1], h = p.m[2], k = p.m[3];
+                p.m = {a * e + b * h, a * f + b * k, c * e + d * h, c * f + d * k};   // g * p
+            } else {
+                pending[q] = (int)out.size();
+                out.push_back(g);
+            }
+            continue;
+        }
+        for (int q : g.targs) pending[q] = -1;
+        out.push_back(g);
+    }
+    return out;
 }
 
 // re-express M (over qs) on the larger sorted set qs2 (M tensor identity)
@@ -124,56 +167,113 @@ void emit(std::vector<QgBlock>& out, OpenBlock& b) {
 
 }  // namespace
 
-// Greedy fusion: open blocks have pairwise disjoint qubits (so they commute).
-// A gate joins the single open block it overlaps if the union still fits in k
-// qubits, merges the blocks it overlaps when they fit together, joins a block
-// with room when it overlaps none, and otherwise closes what it overlaps.
-static void fuse_gates(const std::vector<QgGate>& gates, int k, std::vector<QgBlock>& out) {
+// Greedy fusion.  Open blocks have pairwise disjoint qubits (so they commute).  A
+// gate joins the single open block it overlaps if the union still fits in k qubits,
+// merges the blocks it overlaps when they fit together, joins the nearest block
+// with room when it overlaps none, and otherwise closes what it overlaps and starts
+// a new block.  Diagonal gates (CZ, controlled phases, RZ ...) that would force a
+// closure are held back instead: a diagonal gate commutes with every diagonal gate
+// and with every gate on other qubits, so it may wait until the first non-diagonal
+// gate on one of its qubits, which places it first.  Every reordering swaps
+// commuting gates, so the product of the emitted blocks equals the circuit.
+namespace {
+
+struct Fuser {
+    int k;
     std::vector<OpenBlock> open;
+    std::vector<QgBlock>& out;
     int order = 0;
-    for (const QgGate& g : gates) {
+
+    std::vector<int> hits(const QgGate& g) const {
         std::vector<int> hit;
         for (int i = 0; i < (int)open.size(); i++)
             for (int q : g.targs)
                 if (std::find(open[i].qs.begin(), open[i].qs.end(), q) != open[i].qs.end()) { hit.push_back(i); break; }
+        return hit;
+    }
+
+    // places g without closing any block; false if that is impossible
+    bool try_place(const QgGate& g) {
+        std::vector<int> hit = hits(g);
         std::vector<int> uni = g.targs;
         for (int i : hit)
             for (int q : open[i].qs)
                 if (std::find(uni.begin(), uni.end(), q) == uni.end()) uni.push_back(q);
-        if (!hit.empty() && (int)uni.size() <= k) {
+        if (!hit.empty()) {
+            if ((int)uni.size() > k) return false;
             // merge every hit block into the first, then absorb the gate
             OpenBlock& b0 = open[hit[0]];
             for (size_t h = 1; h < hit.size(); h++) {
-                OpenBlock& bh = open[hit[h]];
                 QgGate as;
-                as.targs = bh.qs;
-                as.m = bh.m;
+                as.targs = open[hit[h]].qs;
+                as.m = open[hit[h]].m;
                 absorb(b0, as);
             }
             absorb(b0, g);
             for (int h = (int)hit.size() - 1; h >= 1; h--) open.erase(open.begin() + hit[h]);
-            continue;
+            return true;
         }
-        if (hit.empty()) {
-            int best = -1;
-            for (int i = 0; i < (int)open.size(); i++)
-                if ((int)(open[i].qs.size() + g.targs.size()) <= k && (best < 0 || open[i].qs.size() > open[best].qs.size())) best = i;
-            if (best >= 0) {
-                absorb(open[best], g);
-                continue;
+        // join the open block with room whose qubits lie nearest (contiguous windows keep
+        // later nearest-neighbour gates inside one block); ties go to the larger block
+        int best = -1, bestDist = 1 << 30;
+        for (int i = 0; i < (int)open.size(); i++) {
+            if ((int)(open[i].qs.size() + g.targs.size()) > k) continue;
+            int dist = 1 << 30;
+            for (int a : open[i].qs)
+                for (int b : g.targs) dist = std::min(dist, std::abs(a - b));
+            if (best < 0 || dist < bestDist || (dist == bestDist && open[i].qs.size() > open[best].qs.size())) {
+                best = i;
+                bestDist = dist;
             }
-            open.push_back(block_from(g, order++));
-            continue;
         }
-        // overlapping blocks that cannot merge: close them (in creation order), start anew
+        if (best >= 0) absorb(open[best], g);
+        else open.push_back(block_from(g, order++));
+        return true;
+    }
+
+    // places g, closing the blocks it overlaps (in creation order) if it must
+    void place(const QgGate& g) {
+        if (try_place(g)) return;
+        std::vector<int> hit = hits(g);
         std::sort(hit.begin(), hit.end(), [&](int a, int b) { return open[a].order < open[b].order; });
         for (int i : hit) emit(out, open[i]);
         std::sort(hit.begin(), hit.end());
         for (int h = (int)hit.size() - 1; h >= 0; h--) open.erase(open.begin() + hit[h]);
         open.push_back(block_from(g, order++));
     }
-    std::sort(open.begin(), open.end(), [](const OpenBlock& a, const OpenBlock& b) { return a.order < b.order; });
-    for (auto& b : open) emit(out, b);
+};
+
+bool shares_qubit(const QgGate& a, const QgGate& b) {
+    for (int q : a.targs)
+        if (std::find(b.targs.begin(), b.targs.end(), q) != b.targs.end()) return true;
+    return false;
+}
+
+}  // namespace
+
+static void fuse_gates(const std::vector<QgGate>& gatesIn, int numQubits, int k, std::vector<QgBlock>& out) {
+    const std::vector<QgGate> gates = merge_single_qubit_runs(gatesIn, numQubits);
+    Fuser f{k, {}, out};
+    std::vector<QgGate> pending;   // diagonal gates held back
+    for (const QgGate& g : gates) {
+        const bool diag = is_diagonal(g);
+        if (!diag) {
+            for (size_t i = 0; i < pending.size();) {
+                if (shares_qubit(pending[i], g)) {
+                    f.place(pending[i]);
+                    pending.erase(pending.begin() + i);
+                } else {
+                    i++;
+                }
+            }
+            f.place(g);
+            continue;
+        }
+        if (!f.try_place(g)) pending.push_back(g);
+    }
+    for (const QgGate& p : pending) f.place(p);
+    std::sort(f.open.begin(), f.open.end(), [](const OpenBlock& a, const OpenBlock& b) { return a.order < b.order; });
+    for (auto& b : f.open) emit(out, b);
 }
 
 // ============================================================== FP32 kernels
@@ -414,13 +514,23 @@ int qg_circuit_add_matrix(qg_circuit* c, const int* targs, int numTargs, const q
     return QG_OK;
 }
 
+int qg_circuit_add_matrices(qg_circuit* c, int numGates, const int* numTargs, const int* targs, const qg_cplx* matrs) {
+    if (!c || numGates < 0 || (numGates > 0 && (!numTargs || !targs || !matrs))) return qg_fail(QG_ERR_ARG, "bad gate list");
+    for (int g = 0; g < numGates; g++) {
+        int k = numTargs[g];
+        if (k < 1 || k > 2) return qg_fail(QG_ERR_ARG, "gate %d: the bulk call takes 1- and 2-qubit gates", g);
+        QG_TRY(qg_circuit_add_matrix(c, targs + 2 * g, k, matrs + 16 * (size_t)g));
+    }
+    return QG_OK;
+}
+
 int qg_circuit_fuse(qg_circuit* c, int maxFusedQubits) {
     if (!c) return qg_fail(QG_ERR_ARG, "null circuit");
     if (maxFusedQubits < 1 || maxFusedQubits > 5) return qg_fail(QG_ERR_ARG, "fusion width %d outside [1, 5]", maxFusedQubits);
     for (auto& g : c->gates)
         if ((int)g.targs.size() > maxFusedQubits) return qg_fail(QG_ERR_ARG, "a gate is wider than the fusion width");
     c->blocks.clear();
-    fuse_gates(c->gates, maxFusedQubits, c->blocks);
+    fuse_gates(c->gates, c->numQubits, maxFusedQubits, c->blocks);
     c->fusedK = maxFusedQubits;
     free_owned(c);
     return QG_OK;

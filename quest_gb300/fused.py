@@ -39,6 +39,16 @@ class Circuit:
         check(lib().qg_circuit_add_matrix(self.h, _lib.ints(targs), len(targs), _cplx(matrix)))
         return self
 
+    def add_many(self, num_targs, targs, mats):
+        """Appends many 1-/2-qubit gates in one call: num_targs (G,), targs (G, 2),
+        mats (G, 16) complex with each gate's row-major matrix in its first 4^k entries."""
+        num_targs = np.ascontiguousarray(num_targs, dtype=np.int32)
+        targs = np.ascontiguousarray(targs, dtype=np.int32)
+        mats = np.ascontiguousarray(mats, dtype=np.complex128)
+        check(lib().qg_circuit_add_matrices(self.h, len(num_targs), num_targs.ctypes.data_as(_lib.c_int_p),
+                                            targs.ctypes.data_as(_lib.c_int_p), mats.ctypes.data_as(_lib.c_cplx_p)))
+        return self
+
     def fuse(self, k=5):
         check(lib().qg_circuit_fuse(self.h, k))
         return self

@@ -39,16 +39,21 @@ def hea_request(nq, depth, rng, num_strings=16):
 
 
 def circuit_of(nq, ops, k=5):
-    """The fused FP32 circuit of an op list."""
-    c = Circuit(nq)
-    for op in ops:
-        if op[0] == "RY":
-            c.add([op[1]], ry(op[2]))
-        elif op[0] == "RZ":
-            c.add([op[1]], rz(op[2]))
-        else:
-            c.add([op[1], op[2]], CZ)
-    return c.fuse(k)
+    """The fused FP32 circuit of an op list (one library call for the whole gate list)."""
+    g = len(ops)
+    kind = np.array([0 if o[0] == "RY" else 1 if o[0] == "RZ" else 2 for o in ops], dtype=np.int32)
+    ang = np.array([o[2] if o[0] != "CZ" else 0.0 for o in ops], dtype=np.float64)
+    q1 = np.array([o[1] for o in ops], dtype=np.int32)
+    q2 = np.array([o[2] if o[0] == "CZ" else 0 for o in ops], dtype=np.int32)
+    mats = np.zeros((g, 16), dtype=np.complex128)
+    c, s = np.cos(ang / 2), np.sin(ang / 2)
+    isy, isz, iscz = kind == 0, kind == 1, kind == 2
+    mats[isy, 0], mats[isy, 1], mats[isy, 2], mats[isy, 3] = c[isy], -s[isy], s[isy], c[isy]
+    mats[isz, 0], mats[isz, 3] = np.exp(-0.5j * ang[isz]), np.exp(0.5j * ang[isz])
+    mats[iscz, 0], mats[iscz, 5], mats[iscz, 10], mats[iscz, 15] = 1, 1, 1, -1
+    num_targs = np.where(iscz, 2, 1).astype(np.int32)
+    targs = np.stack([q1, q2], axis=1)
+    return Circuit(nq).add_many(num_targs, targs, mats).fuse(k)
 
 
 def text_of(ops, codes):

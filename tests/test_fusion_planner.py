@@ -66,3 +66,36 @@ def test_fusion_rejects_wide_gate(built_lib):
     c.add([0, 1, 2], qc.haar_unitary(8, np.random.default_rng(0)))
     with pytest.raises(BackendError):
         c.fuse(2)
+
+
+def test_diagonal_gates_held_back_keep_the_circuit(built_lib):
+    """Diagonal gates (RZ, CZ ladder, controlled phases) that the fuser defers past
+    commuting gates still give the circuit's exact product."""
+    from quest_gb300.fused import Circuit
+    rng = np.random.default_rng(99)
+    n = 7
+    cz = np.diag([1, 1, 1, -1]).astype(np.complex128)
+    gates = []
+    for _ in range(4):
+        for t in range(n):
+            th = rng.uniform(0, 2 * np.pi)
+            gates.append(([t], np.array([[np.cos(th / 2), -np.sin(th / 2)], [np.sin(th / 2), np.cos(th / 2)]])))
+        for t in range(n):
+            gates.append(([t], np.diag(np.exp(1j * rng.uniform(0, 6.3, 2)))))
+        for t in range(n - 1):
+            gates.append(([t, t + 1], cz))
+        a, b = [int(v) for v in rng.choice(n, 2, replace=False)]
+        gates.append(([a, b], np.diag(np.exp(1j * rng.uniform(0, 6.3, 4)))))
+    c = Circuit(n)
+    for t, m in gates:
+        c.add(t, m)
+    c.fuse(5)
+    expect = np.eye(1 << n, dtype=np.complex128)
+    for t, m in gates:
+        expect = full_operator(n, t, m) @ expect
+    got = np.eye(1 << n, dtype=np.complex128)
+    for i in range(c.num_blocks):
+        t, m = c.block(i)
+        got = full_operator(n, t, m) @ got
+    assert np.max(np.abs(got - expect)) < 1e-12
+    assert c.num_blocks <= len(gates) / 6
