@@ -418,21 +418,13 @@ def brickwork_gates(nq, depth, seed):
     return gates
 
 
-def run_precision(args, world, rank, local, dist):
-    """FP32 statevector, brickwork circuit fused into 5-qubit blocks applied as 3xTF32
-    tensor-core GEMM tiles.  Accuracy against the FP64 per-gate path (which is pinned
-    to the FP64 oracle) at `--acc-qubits`; throughput at `--qubits`."""
+def precision_accuracy(na, depth, impl):
+    """Fidelity, max-abs amplitude error and Pauli-expectation error of the fused FP32
+    path against the FP64 per-gate path on the same seeded state and circuit."""
     import ctypes as C
-    from quest_gb300 import _lib, api
+    from quest_gb300 import api
     from quest_gb300.api import Q, comp_matr1
-    from quest_gb300.fused import Circuit, StateVector32, IMPL_TC, IMPL_SIMT
-    L = _lib.lib()
-    _lib.check(L.qg_init(local))
-    api.init_env()
-    nq, na, depth = args.qubits, args.acc_qubits, args.depth
-    impl = IMPL_SIMT if args.fused_impl == "simt" else IMPL_TC
-
-    # ---- accuracy at na qubits
+    from quest_gb300.fused import Circuit, StateVector32
     gates = brickwork_gates(na, depth, seed=0x5155455354 + 4)
     psi0 = random_state(na, seed=0x5155455354 + 4)
     q = Q.createQureg(na)
@@ -462,7 +454,30 @@ def run_precision(args, world, rank, local, dist):
     fid = float(abs(np.vdot(psi32, psi64)) ** 2 / (np.vdot(psi32, psi32).real * np.vdot(psi64, psi64).real))
     maxabs = float(np.max(np.abs(psi32 - psi64)))
     experr = float(np.max(np.abs(np.array(e32) - np.array(list(e64)))))
-    del psi0, psi64, psi32
+    return fid, maxabs, experr
+
+
+def run_precision(args, world, rank, local, dist):
+    """FP32 statevector, brickwork circuit fused into 5-qubit blocks applied as 3xTF32
+    tensor-core GEMM tiles.  Accuracy against the FP64 per-gate path (which is pinned
+    to the FP64 oracle) at `--acc-qubits`; throughput at `--qubits`."""
+    import ctypes as C
+    from quest_gb300 import _lib, api
+    from quest_gb300.api import Q, comp_matr1
+    from quest_gb300.fused import Circuit, StateVector32, IMPL_TC, IMPL_SIMT
+    L = _lib.lib()
+    _lib.check(L.qg_init(local))
+    api.init_env()
+    nq, na, depth = args.qubits, args.acc_qubits, args.depth
+    impl = IMPL_SIMT if args.fused_impl == "simt" else IMPL_TC
+
+    # ---- accuracy at na qubits (0: skipped)
+    fid = maxabs = experr = None
+    if na > 0:
+        fid, maxabs, experr = precision_accuracy(na, depth, impl)
+    accuracy = {"qubits": na, "fidelity": fid, "one_minus_fidelity": None if fid is None else 1 - fid,
+                "max_abs_amp_err": maxabs, "max_pauli_expec_err": experr,
+                "reference": "FP64 per-gate GPU path (parity-pinned to the oracle)"}
 
     # ---- throughput at nq qubits
     gates = brickwork_gates(nq, depth, seed=0x5155455354 + 4)
@@ -517,8 +532,7 @@ def run_precision(args, world, rank, local, dist):
                          "achieved": round(eff / world, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(eff / world / peak, 4), "traffic": None,
                          "tensor_tflops": round(tensor_flops * args.steps / t / 1e12, 1)},
-            "accuracy": {"qubits": na, "fidelity": fid, "one_minus_fidelity": 1 - fid, "max_abs_amp_err": maxabs,
-                         "max_pauli_expec_err": experr, "reference": "FP64 per-gate GPU path (parity-pinned to the oracle)"},
+            "accuracy": accuracy,
             "gpu_launches": int(launches1.value - launches0.value), "tc_error_flag": flag.value,
             "final_total_prob": norm, "clocks": clocks.summary()}
     if rank == 0:
@@ -683,7 +697,7 @@ def main():
     ap.add_argument("--fuse-threads", type=int, default=8)
     ap.add_argument("--load", type=float, default=0.8, help="Poisson rate as a fraction of the plain path's capacity")
     ap.add_argument("--stall-s", type=float, default=120.0, help="serve: abort if no request finishes for this long")
-    ap.add_argument("--acc-qubits", type=int, default=28, help="precision form: qubits of the accuracy check")
+    ap.add_argument("--acc-qubits", type=int, default=28, help="precision form: qubits of the accuracy check (0 skips it)")
     ap.add_argument("--fused-impl", default="tc", choices=["tc", "simt"])
     args = ap.parse_args()
     world, rank, local, dist = dist_setup()
