@@ -448,19 +448,22 @@ def precision_accuracy(na, depth, impl):
     s = StateVector32(na)
     s.set(psi0)
     circ.apply(s, impl=impl)
+    norm_drift = s.total_prob() - 1.0
+    s.normalise(1.0)        # the circuit is unitary and psi0 has norm 1
     e32 = s.expec_paulis(codes)
     psi32 = s.get().astype(np.complex128)
     s.free()
     fid = float(abs(np.vdot(psi32, psi64)) ** 2 / (np.vdot(psi32, psi32).real * np.vdot(psi64, psi64).real))
     maxabs = float(np.max(np.abs(psi32 - psi64)))
     experr = float(np.max(np.abs(np.array(e32) - np.array(list(e64)))))
-    return fid, maxabs, experr
+    return fid, maxabs, experr, norm_drift
 
 
 def run_precision(args, world, rank, local, dist):
     """FP32 statevector, brickwork circuit fused into 5-qubit blocks applied as 3xTF32
-    tensor-core GEMM tiles.  Accuracy against the FP64 per-gate path (which is pinned
-    to the FP64 oracle) at `--acc-qubits`; throughput at `--qubits`."""
+    tensor-core GEMM tiles, then an FP64-summed renormalisation (the circuit is unitary).
+    Accuracy against the FP64 per-gate path (which is pinned to the FP64 oracle) at
+    `--acc-qubits`; throughput at `--qubits`."""
     import ctypes as C
     from quest_gb300 import _lib, api
     from quest_gb300.api import Q, comp_matr1
@@ -472,11 +475,12 @@ def run_precision(args, world, rank, local, dist):
     impl = IMPL_SIMT if args.fused_impl == "simt" else IMPL_TC
 
     # ---- accuracy at na qubits (0: skipped)
-    fid = maxabs = experr = None
+    fid = maxabs = experr = drift = None
     if na > 0:
-        fid, maxabs, experr = precision_accuracy(na, depth, impl)
+        fid, maxabs, experr, drift = precision_accuracy(na, depth, impl)
     accuracy = {"qubits": na, "fidelity": fid, "one_minus_fidelity": None if fid is None else 1 - fid,
                 "max_abs_amp_err": maxabs, "max_pauli_expec_err": experr,
+                "norm_drift_before_normalise": drift,
                 "reference": "FP64 per-gate GPU path (parity-pinned to the oracle)"}
 
     # ---- throughput at nq qubits
@@ -490,6 +494,7 @@ def run_precision(args, world, rank, local, dist):
     s.init_zero()
     for _ in range(args.warmup):
         circ.apply(s, impl=impl)
+        s.normalise(1.0)
     L.qg_sync()
     ev0, ev1 = C.c_void_p(), C.c_void_p()
     L.qg_event_create(C.byref(ev0))
@@ -501,6 +506,7 @@ def run_precision(args, world, rank, local, dist):
         L.qg_event_record(ev0, None)
         for _ in range(args.steps):
             circ.apply(s, impl=impl)
+            s.normalise(1.0)
         L.qg_event_record(ev1, None)
         L.qg_sync()
         barrier(dist)
@@ -514,7 +520,8 @@ def run_precision(args, world, rank, local, dist):
     L.qg_tc_get_error_flag(C.byref(flag))
     s.free()
     pass_bytes = 2 * 8 * (1 << nq)
-    eff = world * args.steps * nblocks * pass_bytes / t / 1e9
+    norm_bytes = 3 * 8 * (1 << nq)     # FP64-summed norm (read) + rescale (read + write)
+    eff = world * args.steps * (nblocks * pass_bytes + norm_bytes) / t / 1e9
     per_pass_ms = t / (args.steps * nblocks) * 1e3
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
     peak = peaks.get("hbm_gbs", 6800.0)

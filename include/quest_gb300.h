@@ -233,6 +233,9 @@ int qg_sv_convert_f64_to_f32(void* dst32, const void* src64, int numQubits, void
 int qg_sv_convert_f32_to_f64(void* dst64, const void* src32, int numQubits, void* stream);
 /* FP64-accumulated reductions of an FP32 statevector */
 int qg_sv32_calcTotalProb(const void* amps32, int numQubits, double* out, void* stream);
+/* scales the state so that its FP64-summed total probability is targetProb (> 0); stays on
+   `stream` (no host round trip).  Removes the norm drift of FP32 products after a unitary circuit. */
+int qg_sv32_normalise(void* amps32, int numQubits, double targetProb, void* stream);
 int qg_sv32_calcExpecPauliStrBatch(const void* amps32, int numQubits, const int64_t* masksXY, const int64_t* masksYZ,
                                    const int* numsY, int numStrings, qg_cplx* out, void* stream);
 
@@ -252,7 +255,9 @@ int qg_server_submit(qg_server* server, qg_circuit* circuit, const int64_t* mask
                      const int* numsY, int numStrings, int64_t* id);
 /* retires finished requests, admits queued ones in arrival order as slots and memory free up, launches their work */
 int qg_server_poll(qg_server* server, int* numDone);
-/* *done = 1 once finished; values = the request's expectation values */
+/* *done = 1 once finished; values = the request's expectation values.  When every gate of
+   the circuit is unitary (max|U^dagger U - I| <= 1e-10) they are <P>/<psi|psi>, with the norm
+   of the final FP32 state summed in FP64; otherwise <psi|P|psi> unnormalised. */
 int qg_server_result(qg_server* server, int64_t id, double* values, int* done);
 int qg_server_release(qg_server* server, int64_t id);
 int qg_server_stats(qg_server* server, int64_t* queued, int64_t* inFlight, int64_t* hbmInUse, int64_t* finished);

@@ -111,6 +111,7 @@ ABI = {
     "qg_sv_convert_f64_to_f32": [vp, vp, I, vp],
     "qg_sv_convert_f32_to_f64": [vp, vp, I, vp],
     "qg_sv32_calcTotalProb": [vp, I, c_dbl_p, vp],
+    "qg_sv32_normalise": [vp, I, D, vp],
     "qg_sv32_calcExpecPauliStrBatch": [vp, I, c_i64_p, c_i64_p, c_int_p, I, c_cplx_p, vp],
     "qg_server_create": [ctypes.POINTER(vp), I64, I, I],
     "qg_server_destroy": [vp],

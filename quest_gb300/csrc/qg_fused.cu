@@ -336,6 +336,19 @@ __global__ void __launch_bounds__(RED_THREADS) k32_sum_norm(const float2* __rest
     block_reduce_and_finish<1>(v, out);
 }
 
+// a_i *= sqrt(target / sum), the sum read from device memory (written by k32_sum_norm)
+__global__ void k32_scale_to_norm(float2* __restrict__ a, qidx n, const double* __restrict__ sum, double target) {
+    const double s = *sum;
+    const float f = s > 0 ? (float)sqrt(target / s) : 1.0f;
+    qidx stride = (qidx)gridDim.x * blockDim.x;
+    for (qidx i = blockIdx.x * (qidx)blockDim.x + threadIdx.x; i < n; i += stride) {
+        float2 x = ld32(a + i);
+        x.x *= f;
+        x.y *= f;
+        a[i] = x;
+    }
+}
+
 // batched Pauli expectation (FP64 accumulation), the reference's per-n term
 template <int NS>
 __global__ void __launch_bounds__(RED_THREADS) k32_expec_pauli_batch(const float2* __restrict__ a, qidx n,
@@ -499,6 +512,17 @@ int qg_circuit_destroy(qg_circuit* c) {
     return QG_OK;
 }
 
+// max |(U^dagger U - I)_ij| <= 1e-10, in FP64
+static bool is_unitary(const cd* u, size_t D) {
+    for (size_t i = 0; i < D; i++)
+        for (size_t j = 0; j < D; j++) {
+            cd s = 0;
+            for (size_t r = 0; r < D; r++) s += std::conj(u[r * D + i]) * u[r * D + j];
+            if (std::abs(s - (i == j ? cd(1) : cd(0))) > 1e-10) return false;
+        }
+    return true;
+}
+
 int qg_circuit_add_matrix(qg_circuit* c, const int* targs, int numTargs, const qg_cplx* matr) {
     if (!c || !matr) return qg_fail(QG_ERR_ARG, "null circuit or matrix");
     if (numTargs < 1 || numTargs > 5) return qg_fail(QG_ERR_ARG, "a circuit gate acts on 1..5 qubits, not %d", numTargs);
@@ -508,6 +532,7 @@ int qg_circuit_add_matrix(qg_circuit* c, const int* targs, int numTargs, const q
     size_t D = (size_t)1 << numTargs;
     g.m.resize(D * D);
     for (size_t i = 0; i < D * D; i++) g.m[i] = cd(matr[i].re, matr[i].im);
+    if (c->allUnitary && !is_unitary(g.m.data(), D)) c->allUnitary = false;
     c->gates.push_back(std::move(g));
     c->blocks.clear();
     free_owned(c);
@@ -622,6 +647,22 @@ int qg_sv32_calcTotalProb(const void* amps, int numQubits, double* out, void* st
     cudaStream_t st = qg_stream(stream);
     k32_sum_norm<<<grid, RED_THREADS, 0, st>>>((const float2*)amps, n, r);
     return red_fetch(r, 1, out, st);
+}
+
+int qg_sv32_normalise(void* amps, int numQubits, double targetProb, void* stream) {
+    QG_TRY(check32(amps, numQubits));
+    if (!(targetProb > 0)) return qg_fail(QG_ERR_ARG, "target probability must be positive");
+    qidx n = (qidx)1 << numQubits;
+    int grid = red_grid(n);
+    RedOut r;
+    QG_TRY(red_setup(grid, 1, &r));
+    cudaStream_t st = qg_stream(stream);
+    k32_sum_norm<<<grid, RED_THREADS, 0, st>>>((const float2*)amps, n, r);
+    qg_note_launch();
+    QG_TRY(qg_check_launch("k32_sum_norm"));
+    k32_scale_to_norm<<<qg_blocks(n), QG_THREADS, 0, st>>>((float2*)amps, n, r.result, targetProb);
+    qg_note_launch();
+    return qg_check_launch("k32_scale_to_norm");
 }
 
 int qg_sv32_calcExpecPauliStrBatch(const void* amps, int numQubits, const int64_t* masksXY, const int64_t* masksYZ,

@@ -31,6 +31,8 @@
 #include <vector>
 
 #define SERVE_MAX_STRINGS 16
+// per result slot: (re, im) per string, then <psi|psi> and a zero
+#define SERVE_RESULT_DOUBLES (2 * SERVE_MAX_STRINGS + 2)
 #define SERVE_SMALL_MAX_QUBITS 14
 #define SERVE_SMALL_THREADS 256
 #define SERVE_STREAMS 16
@@ -48,7 +50,7 @@ struct SmallJob {
     int pad;
     qidx xy[SERVE_MAX_STRINGS];
     qidx yz[SERVE_MAX_STRINGS];
-    double* out;               // 2 * numStrings doubles (before the i^numY factor)
+    double* out;               // SERVE_RESULT_DOUBLES: (re, im) per string before the i^numY factor, then the norm
     float2* stateOut;          // optional copy of the final state (nullptr: none)
 };
 
@@ -108,8 +110,23 @@ __global__ void __launch_bounds__(SERVE_SMALL_THREADS) k_serve_small(const Small
     __syncthreads();
     if (J.stateOut)
         for (int i = threadIdx.x; i < N; i += blockDim.x) J.stateOut[i] = st[i];
-    // expectation values: sum_i sign(j & yz) conj(a_i) a_j, j = i ^ xy, in FP64
+    // <psi|psi> then the expectation values sum_i sign(j & yz) conj(a_i) a_j, j = i ^ xy, in FP64
     __shared__ double red[SERVE_SMALL_THREADS / 32][2];
+    {
+        double nrm = 0;
+        for (int i = threadIdx.x; i < N; i += blockDim.x) nrm += (double)st[i].x * st[i].x + (double)st[i].y * st[i].y;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) nrm += __shfl_down_sync(0xffffffffu, nrm, o);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5][0] = nrm;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double a = 0;
+            for (int w = 0; w < SERVE_SMALL_THREADS / 32; w++) a += red[w][0];
+            J.out[2 * SERVE_MAX_STRINGS] = a;
+            J.out[2 * SERVE_MAX_STRINGS + 1] = 0;
+        }
+        __syncthreads();
+    }
     for (int s = 0; s < J.numStrings; s++) {
         double re = 0, im = 0;
         for (int i = threadIdx.x; i < N; i += blockDim.x) {
@@ -145,12 +162,13 @@ struct ExpecMasks {
 
 __global__ void __launch_bounds__(RED_THREADS) k_serve_expec(const float2* __restrict__ a, qidx n, ExpecMasks m,
                                                             int numStrings, RedOut out) {
-    double v[2 * SERVE_MAX_STRINGS];
+    double v[SERVE_RESULT_DOUBLES];
 #pragma unroll
-    for (int k = 0; k < 2 * SERVE_MAX_STRINGS; k++) v[k] = 0.0;
+    for (int k = 0; k < SERVE_RESULT_DOUBLES; k++) v[k] = 0.0;
     qidx stride = (qidx)gridDim.x * RED_THREADS;
     for (qidx i = blockIdx.x * (qidx)RED_THREADS + threadIdx.x; i < n; i += stride) {
         float2 ai = __ldg(a + i);
+        v[2 * SERVE_MAX_STRINGS] += (double)ai.x * ai.x + (double)ai.y * ai.y;
 #pragma unroll
         for (int s = 0; s < SERVE_MAX_STRINGS; s++) {
             if (s < numStrings) {
@@ -162,7 +180,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_serve_expec(const float2* __res
             }
         }
     }
-    block_reduce_and_finish<2 * SERVE_MAX_STRINGS>(v, out);
+    block_reduce_and_finish<SERVE_RESULT_DOUBLES>(v, out);
 }
 
 // ============================================================== host: the server
@@ -181,6 +199,7 @@ struct Request {
     int stream = -1;         // large requests: index into the stream pool
     cudaEvent_t done = nullptr;
     bool small = false;
+    bool unitary = true;     // every gate of the circuit is unitary: results are normalised
     bool finished = false;
     std::vector<double> values;
 };
@@ -263,7 +282,7 @@ void release_transient_copy(qg_circuit* c) {
 }
 
 size_t state_bytes(const Request& r) {
-    return r.small ? 0 : round_up((size_t)8 << r.nq, 256) + red_scratch_bytes(red_grid((qidx)1 << r.nq), 2 * SERVE_MAX_STRINGS);
+    return r.small ? 0 : round_up((size_t)8 << r.nq, 256) + red_scratch_bytes(red_grid((qidx)1 << r.nq), SERVE_RESULT_DOUBLES);
 }
 
 int launch_large(qg_server* s, Request& r) {
@@ -279,7 +298,7 @@ int launch_large(qg_server* s, Request& r) {
     int grid = red_grid(n);
     RedOut ro;
     ro.ticket = (unsigned int*)scratch;
-    ro.result = s->devResults + (size_t)r.slot * 2 * SERVE_MAX_STRINGS;
+    ro.result = s->devResults + (size_t)r.slot * SERVE_RESULT_DOUBLES;
     ro.partials = (double*)(scratch + 256);
     QG_CUDA(cudaMemsetAsync(scratch, 0, 256, st));
     ExpecMasks m;
@@ -290,8 +309,8 @@ int launch_large(qg_server* s, Request& r) {
     k_serve_expec<<<grid, RED_THREADS, 0, st>>>(amps, n, m, r.numStrings, ro);
     qg_note_launch();
     QG_TRY(qg_check_launch("k_serve_expec"));
-    QG_CUDA(cudaMemcpyAsync(s->hostResults + (size_t)r.slot * 2 * SERVE_MAX_STRINGS, ro.result,
-                            sizeof(double) * 2 * SERVE_MAX_STRINGS, cudaMemcpyDeviceToHost, st));
+    QG_CUDA(cudaMemcpyAsync(s->hostResults + (size_t)r.slot * SERVE_RESULT_DOUBLES, ro.result,
+                            sizeof(double) * SERVE_RESULT_DOUBLES, cudaMemcpyDeviceToHost, st));
     QG_CUDA(cudaEventCreateWithFlags(&r.done, cudaEventDisableTiming));
     QG_CUDA(cudaEventRecord(r.done, st));
     return QG_OK;
@@ -318,7 +337,7 @@ int launch_small_batch(qg_server* s) {
             j.xy[k] = k < r.numStrings ? r.xy[k] : 0;
             j.yz[k] = k < r.numStrings ? r.yz[k] : 0;
         }
-        j.out = s->devResults + (size_t)r.slot * 2 * SERVE_MAX_STRINGS;
+        j.out = s->devResults + (size_t)r.slot * SERVE_RESULT_DOUBLES;
         j.stateOut = nullptr;
         release_transient_copy(r.circ);
     }
@@ -342,9 +361,9 @@ int launch_small_batch(qg_server* s) {
     }
     for (int64_t id : ids) {
         Request& r = s->reqs[id];
-        QG_CUDA(cudaMemcpyAsync(s->hostResults + (size_t)r.slot * 2 * SERVE_MAX_STRINGS,
-                                s->devResults + (size_t)r.slot * 2 * SERVE_MAX_STRINGS,
-                                sizeof(double) * 2 * SERVE_MAX_STRINGS, cudaMemcpyDeviceToHost, s->smallStream));
+        QG_CUDA(cudaMemcpyAsync(s->hostResults + (size_t)r.slot * SERVE_RESULT_DOUBLES,
+                                s->devResults + (size_t)r.slot * SERVE_RESULT_DOUBLES,
+                                sizeof(double) * SERVE_RESULT_DOUBLES, cudaMemcpyDeviceToHost, s->smallStream));
     }
     QG_CUDA(cudaFreeAsync(b.devJobs, s->smallStream));
     QG_CUDA(cudaEventCreateWithFlags(&b.done, cudaEventDisableTiming));
@@ -354,12 +373,15 @@ int launch_small_batch(qg_server* s) {
 }
 
 void finish(qg_server* s, Request& r) {
-    const double* h = s->hostResults + (size_t)r.slot * 2 * SERVE_MAX_STRINGS;
+    const double* h = s->hostResults + (size_t)r.slot * SERVE_RESULT_DOUBLES;
     r.values.resize(r.numStrings);
+    // A unitary circuit keeps the norm of |0>, so values are divided by the FP64 norm of
+    // the final FP32 state: this removes the drift of the FP32 products to first order.
+    double scale = r.unitary ? 1.0 / h[2 * SERVE_MAX_STRINGS] : 1.0;
     for (int k = 0; k < r.numStrings; k++) {
         double re = h[2 * k], im = h[2 * k + 1];
         times_power_of_i(&re, &im, r.ny[k]);
-        r.values[k] = re;
+        r.values[k] = re * scale;
     }
     r.finished = true;
     s->freeSlots.push_back(r.slot);
@@ -383,8 +405,8 @@ int qg_server_create(qg_server** out, int64_t hbmBudgetBytes, int maxInFlight, i
         return qg_check_cuda(e, "cudaMalloc(server arena)");
     }
     s->freeList[0] = s->arenaBytes;
-    QG_CUDA(cudaMalloc(&s->devResults, sizeof(double) * 2 * SERVE_MAX_STRINGS * maxInFlight));
-    QG_CUDA(cudaMallocHost(&s->hostResults, sizeof(double) * 2 * SERVE_MAX_STRINGS * maxInFlight));
+    QG_CUDA(cudaMalloc(&s->devResults, sizeof(double) * SERVE_RESULT_DOUBLES * maxInFlight));
+    QG_CUDA(cudaMallocHost(&s->hostResults, sizeof(double) * SERVE_RESULT_DOUBLES * maxInFlight));
     for (int i = maxInFlight - 1; i >= 0; i--) s->freeSlots.push_back(i);
     for (int i = 0; i < SERVE_STREAMS; i++) QG_CUDA(cudaStreamCreateWithFlags(&s->streams[i], cudaStreamNonBlocking));
     QG_CUDA(cudaStreamCreateWithFlags(&s->smallStream, cudaStreamNonBlocking));
@@ -423,6 +445,7 @@ int qg_server_submit(qg_server* s, qg_circuit* c, const int64_t* masksXY, const 
     r.id = s->nextId++;
     r.circ = c;
     r.numStrings = numStrings;
+    r.unitary = c->allUnitary;
     for (int k = 0; k < numStrings; k++) { r.xy[k] = masksXY[k]; r.yz[k] = masksYZ[k]; r.ny[k] = numsY[k]; }
     r.arenaBytes = need;
     s->reqs[r.id] = r;

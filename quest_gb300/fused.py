@@ -117,6 +117,10 @@ class StateVector32:
         check(lib().qg_sv32_calcTotalProb(self.ptr, self.num_qubits, ctypes.byref(v), None))
         return v.value
 
+    def normalise(self, target=1.0):
+        """Rescales the state to total probability `target` (FP64-summed norm)."""
+        check(lib().qg_sv32_normalise(self.ptr, self.num_qubits, float(target), None))
+
     def expec_paulis(self, codes_list):
         """Expectation values of Pauli strings given as per-qubit codes (0=I,1=X,2=Y,3=Z)."""
         n = len(codes_list)

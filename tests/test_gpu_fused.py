@@ -110,3 +110,21 @@ def test_fp32_reductions_accumulate_in_fp64(env):
         assert np.max(np.abs(got - want)) < 1e-12
     finally:
         s.free()
+
+
+@pytest.mark.gpu
+def test_normalise_rescales_to_the_target_probability(env):
+    from quest_gb300.fused import StateVector32
+    n = 18
+    amps = (qc.random_statevector(n, 9) * 0.93).astype(np.complex64)
+    s = StateVector32(n)
+    try:
+        s.set(amps)
+        s.normalise(0.5)
+        got = s.get().astype(np.complex128)
+        a64 = amps.astype(np.complex128)
+        want = a64 * np.sqrt(0.5 / np.vdot(a64, a64).real)
+        assert np.max(np.abs(got - want)) <= 4 * np.finfo(np.float32).eps * np.max(np.abs(want))
+        assert abs(s.total_prob() - 0.5) < 1e-6
+    finally:
+        s.free()

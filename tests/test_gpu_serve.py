@@ -69,3 +69,32 @@ def test_queue_drains_under_a_tight_memory_budget(env):
     finally:
         s.close()
     assert len(got) == 6 and all(np.all(np.isfinite(v)) for v in got)
+
+
+@pytest.mark.parametrize("n", [4, 16])
+def test_values_are_normalised_only_for_unitary_circuits(env, n):
+    """<P> / <psi|psi> when every gate is unitary; <psi|P|psi> as computed otherwise."""
+    from quest_gb300.fused import Circuit
+    from quest_gb300.serve import Server
+    h = np.array([[1, 1], [1, -1]]) / np.sqrt(2)
+    damp = np.diag([1.0, 0.5])          # not unitary: shrinks the norm
+    codes = [[3] + [0] * (n - 1), [1] * n, [0] * n]
+    for unitary in (True, False):
+        c = Circuit(n)
+        for q in range(n):
+            c.add([q], h)
+        if not unitary:
+            c.add([0], damp)
+        c.fuse(5)
+        psi = np.ones(1 << n) / np.sqrt(1 << n)
+        if not unitary:
+            psi = psi * np.where(np.arange(1 << n) & 1, 0.5, 1.0)
+        sign = np.where(np.arange(1 << n) & 1, -1.0, 1.0)
+        z0, xall, ident = np.vdot(psi, sign * psi).real, np.vdot(psi, psi[::-1]).real, np.vdot(psi, psi).real
+        server = Server(1 << 30)
+        try:
+            got = server.run_all([(c, codes)])[0]
+        finally:
+            server.close()
+        want = np.array([z0, xall, ident]) / (ident if unitary else 1.0)
+        assert np.max(np.abs(got - want)) < 1e-6, (unitary, got, want)
