@@ -231,6 +231,15 @@ def run_gb300(args, world, rank, local, dist):
     os.environ.setdefault("CUDA_DEVICE_ORDER", "PCI_BUS_ID")
     _lib.check(L.qg_init(local if dev_count.value > local else 0))
     api.init_env()
+    _lib.check(L.qg_set_fp64_products(0 if args.fp64_products == "fixed" else 1))
+    # the library's launch-shape autotuner, on a 26-qubit scratch register, before any timing
+    tune_ms = (C.c_double * 8)()
+    tune_n = C.c_int(0)
+    _lib.check(L.qg_autotune_fp64(min(26, args.qubits), tune_ms, 8, C.byref(tune_n)))
+    tppt, tthr = C.c_int(), C.c_int()
+    _lib.check(L.qg_get_kernel_shape(0, C.byref(tppt), C.byref(tthr)))
+    tuning = {"dense1_fx_shape": [tppt.value, tthr.value],
+              "candidates_ms": [round(tune_ms[i], 4) for i in range(tune_n.value)]}
 
     nq = args.qubits
     gates = make_circuit(nq, args.depth, seed=0x5155455354 + 2)
@@ -335,7 +344,9 @@ def run_gb300(args, world, rank, local, dist):
     fma_rate = C.c_double(0)
     _lib.check(L.qg_measure_fp64_fma_rate(C.byref(fma_rate)))
     fp64_ceiling_gbs = fma_rate.value / 16 * 64 / 1e9
-    roofline = {"bound": "hbm", "kernel": "k_dense1 (applyCompMatr1, general complex 2x2, FP64)",
+    kname = ("k_dense1_fx (applyCompMatr1, general complex 2x2, FP64 storage, fixed-point products)"
+             if args.fp64_products == "fixed" else "k_dense1 (applyCompMatr1, general complex 2x2, FP64)")
+    roofline = {"bound": "hbm", "kernel": kname,
                 "achieved": round(achieved, 1), "peak": peak, "peak_source": peak_src, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": args.traffic,
                 "launches_timed": len(dense_ms), "avg_launch_ms": round(avg_dense * 1e3, 4),
@@ -354,11 +365,15 @@ def run_gb300(args, world, rank, local, dist):
         "metric": "30q gate GB/s vs HBM peak (FP64 statevector, depth-20 Haar 1q + 15 CPhase/layer + QFT)",
         "value": round(value, 2), "unit": "GB/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(t_dev / args.steps * 1e3, 3), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Gaussian state, seeded Haar gates)",
+        "vs_baseline": None,
+        "dtype": "f64" if args.fp64_products == "fp64" else
+                 "f64 (storage and all other ops; general 2x2 products in 60-bit block-floating fixed point)",
+        "data": "synthetic (seeded Gaussian state, seeded Haar gates)",
         "config": {"workload": f"{nq}-qubit FP64 statevector (16 GiB at 30 qubits), depth {args.depth} Haar 1q "
                                f"+ 15 CPhase per layer, then full QFT", "qubits": nq, "depth": args.depth,
                    "gates_per_step": step_gates, "algorithmic_bytes_per_step": step_bytes,
-                   "l2": "state (16 GiB) larger than L2; no flush", "parallelism": f"replicas x{world}"},
+                   "l2": "state (16 GiB) larger than L2; no flush", "parallelism": f"replicas x{world}",
+                   "fp64_products": args.fp64_products, "autotune": tuning},
         "e2e": {"value": round(e2e_value, 2), "unit": "GB/s", "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
         "gpu_launches": int(launches1.value - launches0.value),
         "roofline": roofline,
@@ -704,6 +719,8 @@ def main():
     ap.add_argument("--fuse-threads", type=int, default=8)
     ap.add_argument("--load", type=float, default=0.8, help="Poisson rate as a fraction of the plain path's capacity")
     ap.add_argument("--stall-s", type=float, default=120.0, help="serve: abort if no request finishes for this long")
+    ap.add_argument("--fp64-products", default="fixed", choices=["fixed", "fp64"],
+                    help="plain: general complex 2x2 products in block-floating fixed point (default) or IEEE FP64")
     ap.add_argument("--acc-qubits", type=int, default=28, help="precision form: qubits of the accuracy check (0 skips it)")
     ap.add_argument("--fused-impl", default="tc", choices=["tc", "simt"])
     args = ap.parse_args()

@@ -71,6 +71,35 @@ int qg_event_elapsed_ms(void* start, void* stop, float* ms); /* waits for `stop`
 /* FP64 fused multiply-adds per second this GPU sustains (a short probe kernel);
  * the issue rate that bounds the general complex FP64 gates */
 int qg_measure_fp64_fma_rate(double* fmaPerSecond);
+/* How general complex FP64 gates form their products (no counterpart in the reference,
+ * whose GPU kernels use FP64 FMAs):
+ *   0 (default) block-floating 60-bit fixed point on the integer pipes: each amplitude
+ *     pair shares one exponent; per output the error is below 2^-54 of (largest |amp| in
+ *     the pair) x (largest |matrix entry|), the order of IEEE FP64's own bound; pairs
+ *     holding Inf/NaN or with results outside the normal range are evaluated in FP64;
+ *   1 IEEE FP64 fused multiply-adds throughout.
+ * Applies to one-target dense matrices (applyCompMatr1, Hadamard, rotations and their
+ * controlled forms) and one-target diagonals (phase gates, controlled phases);
+ * process-wide. */
+int qg_set_fp64_products(int mode);
+int qg_get_fp64_products(int* mode);
+
+/* ------------------------------------------------------------------ launch-shape autotuner
+ * (no counterpart in the reference, whose launch sizes are fixed formulas,
+ * gpu_subroutines.cpp getNumBlocks)  Kernel 0 = the one-target dense kernel with
+ * fixed-point products.  A shape is (pairs per thread per iteration, threads per
+ * block) from {(1,256), (1,128), (2,256), (2,128)}; default (1,256). */
+#define QG_TUNE_KERNEL_DENSE1 0
+int qg_set_kernel_shape(int kernel, int pairsPerThread, int threadsPerBlock);
+int qg_get_kernel_shape(int kernel, int* pairsPerThread, int* threadsPerBlock);
+/* times every candidate on a scratch register of numQubits (16 B x 2^numQubits of
+ * device memory for the duration of the call) and keeps the fastest; msOut receives
+ * milliseconds per launch for each candidate in the order above */
+int qg_autotune_fp64(int numQubits, double* msOut, int maxOut, int* numOut);
+/* text file: "qg-tune 1", then "<device name> <kernel> <ppt> <threads>" per line;
+ * load applies only the lines for the current device's name */
+int qg_tune_save(const char* path);
+int qg_tune_load(const char* path, int* numApplied);
 
 /* ------------------------------------------------------------------ initialisation
  * replaces gpu_statevec_initUniformState_sub / initDebugState_sub

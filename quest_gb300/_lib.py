@@ -112,6 +112,13 @@ ABI = {
     "qg_sv_convert_f32_to_f64": [vp, vp, I, vp],
     "qg_sv32_calcTotalProb": [vp, I, c_dbl_p, vp],
     "qg_sv32_normalise": [vp, I, D, vp],
+    "qg_set_fp64_products": [I],
+    "qg_get_fp64_products": [c_int_p],
+    "qg_set_kernel_shape": [I, I, I],
+    "qg_get_kernel_shape": [I, c_int_p, c_int_p],
+    "qg_autotune_fp64": [I, c_dbl_p, I, c_int_p],
+    "qg_tune_save": [ctypes.c_char_p],
+    "qg_tune_load": [ctypes.c_char_p, c_int_p],
     "qg_sv32_calcExpecPauliStrBatch": [vp, I, c_i64_p, c_i64_p, c_int_p, I, c_cplx_p, vp],
     "qg_server_create": [ctypes.POINTER(vp), I64, I, I],
     "qg_server_destroy": [vp],

@@ -30,6 +30,18 @@ int qg_check_launch(const char* what);
 void qg_note_launch(int n = 1);
 int qg_num_sms();
 
+// How general complex FP64 gate products are evaluated (qg_set_fp64_products)
+#define QG_FP64_PRODUCTS_FIXED 0   // block-floating 60-bit fixed point on the integer pipes
+#define QG_FP64_PRODUCTS_FP64 1    // IEEE FP64 fused multiply-adds
+int qg_fp64_products_mode();
+
+// Launch shapes chosen by the autotuner (qg_tune.cu): pairs per thread per loop
+// iteration and threads per block, per tunable kernel
+struct QgShape { int ppt; int threads; };
+#define QG_TUNE_DENSE1 0
+#define QG_TUNE_NUM 1
+QgShape qg_tuned_shape(int kernel);
+
 #define QG_CUDA(call)                                                      \
     do {                                                                   \
         cudaError_t _e = (call);                                           \

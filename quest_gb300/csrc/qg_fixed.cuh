@@ -3,24 +3,29 @@
 // GB300 issues about 2 FP64 FMAs per clock per SM, so a general complex 2x2 gate on
 // an FP64 statevector (16 real products per amplitude pair) is bound by the FP64 pipe
 // at roughly a third of HBM bandwidth.  The integer multiply-add pipe is many times
-// wider.  This header applies a real 4x4 operator (the real form of a complex 2x2
-// matrix) to the four doubles of an amplitude pair in 64-bit fixed point:
+// wider.  This header applies a real N x N operator (N = 4: the real form of a complex
+// 2x2 matrix on an amplitude pair; N = 2: a complex scalar on one amplitude) to N
+// doubles in 64-bit fixed point:
 //
-//  * the pair shares one scale: e = the largest biased exponent among its four doubles;
+//  * the input shares one scale: e = the largest biased exponent among its N doubles;
 //    each value becomes x = v * 2^(1082 - e), |x| < 2^60 (denormals are exact: they
 //    enter with exponent 1 and no implicit bit);
 //  * the operator's coefficients share one scale E (|c| < 2^E): m = c * 2^(60 - E);
 //  * x and m split into balanced 32-bit limbs, x = xh*2^32 + xl with xl in
 //    [-2^31, 2^31); each output is R = sum(xh*mh) + (sum(xh*ml + xl*mh) >> 32), the
 //    top 64 bits of the exact 128-bit sum of products minus the dropped xl*ml terms;
-//  * R converts back to a double rounded to nearest (ties away): value = R * 2^(e+E-1078).
+//  * R converts back to a double rounded to nearest: value = R * 2^(e+E-1078).
+//    apply_op does that with integer instructions only (ties away from zero);
+//    apply_op_cvt, which the GPU kernels use, lets the hardware int64 -> double
+//    conversion round (ties to even) and adds the scale to the exponent field.
 //
 // Error per output: at most 2 units of R plus the input truncation, i.e. below
-// 2^-54 of (largest |v| in the pair) * (largest |c|).  IEEE FP64 evaluation of the same
-// 4-term sums has a bound of the same order.  A pair holding Inf or NaN, or whose result
-// would leave the normal double range, returns false and the caller uses FP64.
+// 2^-54 of (largest |v| in the input) * (largest |c|).  IEEE FP64 evaluation of the same
+// 4-term sums has a bound of the same order.  An input holding Inf or NaN, or whose
+// result could leave the normal double range, returns false and the caller uses FP64.
 #pragma once
 #include <stdint.h>
+#include <cmath>
 
 #if defined(__CUDACC__)
 #define QG_HD __host__ __device__ __forceinline__
@@ -30,13 +35,17 @@
 
 namespace qgfx {
 
-// one real operator coefficient row-set: out[r] = sum_j C[r][j] * in[j], in the limb form
-struct Op4 {
-    int32_t h[4][4];    // high limbs, |h| <= 2^28 + 1
-    int32_t l[4][4];    // low limbs in [-2^31, 2^31)
+// a real N x N operator, out[r] = sum_j C[r][j] * in[j], in the limb form (N = 2: a
+// complex scalar acting on one amplitude; N = 4: a complex 2x2 acting on a pair)
+template <int N>
+struct OpN {
+    int32_t h[N][N];    // high limbs, |h| <= 2^28 + 1
+    int32_t l[N][N];    // low limbs in [-2^31, 2^31)
     int32_t expo;       // E: every |C[r][j]| < 2^E
     int32_t pad;
 };
+typedef OpN<4> Op4;
+typedef OpN<2> Op2;
 
 QG_HD uint64_t f64_bits(double v) {
 #if defined(__CUDA_ARCH__)
@@ -99,27 +108,31 @@ QG_HD double from_fixed(int64_t R, int ebase, bool& ok) {
     return bits_f64((sgn << 63) | ((uint64_t)(uint32_t)be << 52) | (q & 0xFFFFFFFFFFFFFull));
 }
 
-// out[r] = sum_j C[r][j] * in[j]; false (outputs undefined) if FP64 must be used
-QG_HD bool apply_op4(const Op4& C, const double in[4], double out[4]) {
-    uint64_t u[4];
+// out[r] = sum_j C[r][j] * in[j]; false (outputs undefined) if FP64 must be used.
+// Bounds: |x| < 2^60 and |m| <= 2^60 give |xh*ml|, |xl*mh| < 2^59 + 2^31, so the
+// 2N middle terms sum below 2^63 for N <= 4.
+template <int N>
+QG_HD bool apply_op(const OpN<N>& C, const double in[N], double out[N]) {
+    static_assert(N >= 1 && N <= 4, "operator size");
+    uint64_t u[N];
     int e = 1;
 #pragma unroll
-    for (int j = 0; j < 4; j++) {
+    for (int j = 0; j < N; j++) {
         u[j] = f64_bits(in[j]);
         const int ej = eff_exponent(u[j]);
         e = ej > e ? ej : e;
     }
-    if (e == 2047) return false;          // Inf or NaN in the pair
-    int32_t xh[4], xl[4];
+    if (e == 2047) return false;          // Inf or NaN in the input
+    int32_t xh[N], xl[N];
 #pragma unroll
-    for (int j = 0; j < 4; j++) to_limbs(u[j], e, xh[j], xl[j]);
+    for (int j = 0; j < N; j++) to_limbs(u[j], e, xh[j], xl[j]);
     bool ok = true;
     const int ebase = e + C.expo + 8;
 #pragma unroll
-    for (int r = 0; r < 4; r++) {
+    for (int r = 0; r < N; r++) {
         int64_t hh = 0, mid = 0;
 #pragma unroll
-        for (int j = 0; j < 4; j++) {
+        for (int j = 0; j < N; j++) {
             hh += (int64_t)xh[j] * C.h[r][j];
             mid += (int64_t)xh[j] * C.l[r][j];
             mid += (int64_t)xl[j] * C.h[r][j];
@@ -127,6 +140,171 @@ QG_HD bool apply_op4(const Op4& C, const double in[4], double out[4]) {
         out[r] = from_fixed(hh + (mid >> 32), ebase, ok);
     }
     return ok;
+}
+
+QG_HD bool apply_op4(const Op4& C, const double in[4], double out[4]) { return apply_op<4>(C, in, out); }
+
+// The same arithmetic with the output step done by the hardware int64 -> double
+// conversion (round to nearest) and the scale applied by an integer add to the
+// exponent field: out_r = double(R) * 2^t, t = e + E - 1078.  On GB300 that conversion
+// runs on the FP64 unit, which the integer arithmetic leaves idle, and replaces
+// about 30 integer ALU instructions per output.  Falls back (returns false) for
+// Inf/NaN and when some output could leave the normal range (scale checked once
+// per input: double(R) lies in [1, 2^58] or is 0).
+QG_HD double i64_to_double(int64_t v) {
+#if defined(__CUDA_ARCH__)
+    return __ll2double_rn((long long)v);
+#else
+    return (double)v;
+#endif
+}
+
+template <int N>
+QG_HD bool apply_op_cvt(const OpN<N>& C, const double in[N], double out[N]) {
+    static_assert(N >= 1 && N <= 4, "operator size");
+    uint64_t u[N];
+    int e = 1;
+#pragma unroll
+    for (int j = 0; j < N; j++) {
+        u[j] = f64_bits(in[j]);
+        const int ej = eff_exponent(u[j]);
+        e = ej > e ? ej : e;
+    }
+    const int t = e + C.expo - 1078;
+    if (1023 + t < 1 || 1082 + t > 2046 || e == 2047) {
+        uint64_t any = 0;
+#pragma unroll
+        for (int j = 0; j < N; j++) any |= u[j] << 1;     // ignores the signs of zeros
+        if (any) return false;
+#pragma unroll
+        for (int r = 0; r < N; r++) out[r] = 0.0;       // all zero: the common case in sparse states
+        return true;
+    }
+    int32_t xh[N], xl[N];
+#pragma unroll
+    for (int j = 0; j < N; j++) to_limbs(u[j], e, xh[j], xl[j]);
+    const uint32_t down = (uint32_t)t << 20;           // adds t to the exponent field
+#pragma unroll
+    for (int r = 0; r < N; r++) {
+        int64_t hh = 0, mid = 0;
+#pragma unroll
+        for (int j = 0; j < N; j++) {
+            hh += (int64_t)xh[j] * C.h[r][j];
+            mid += (int64_t)xh[j] * C.l[r][j];
+            mid += (int64_t)xl[j] * C.h[r][j];
+        }
+        const uint64_t d = f64_bits(i64_to_double(hh + (mid >> 32)));
+        const uint32_t dh = (uint32_t)(d >> 32);
+        out[r] = bits_f64(dh ? ((uint64_t)(dh + down) << 32 | (uint32_t)d) : 0ull);
+    }
+    return true;
+}
+
+// x = v * 2^(1082 - e) for a normal v whose exponent is within 31 of e (d = e - e_v),
+// from its two 32-bit words with 32-bit funnel shifts, split into balanced limbs
+QG_HD void to_limbs_near(uint32_t hi, uint32_t lo, int d, int32_t& xh, int32_t& xl) {
+    const uint32_t mh = (hi & 0xFFFFFu) | 0x100000u;            // 21 high mantissa bits with the implicit 1
+    const uint32_t ah = (mh << 7) | (lo >> 25);                  // (mantissa << 7): 60 bits
+    const uint32_t al = lo << 7;
+    const uint32_t yl = d ? (al >> d) | (ah << (32 - d)) : al;   // >> d, d in [0, 31]
+    const uint32_t yh = ah >> d;
+    const uint32_t s = (uint32_t)((int32_t)hi >> 31);            // 0 or all ones
+    const uint64_t y = ((uint64_t)(yh ^ s) << 32 | (yl ^ s)) - (uint64_t)(int64_t)(int32_t)s;   // +-y
+    const uint32_t x0 = (uint32_t)y;
+    xl = (int32_t)x0;
+    xh = (int32_t)(uint32_t)(y >> 32) + (int32_t)(x0 >> 31);
+}
+
+// apply_op_cvt for the usual input: every value normal and within 2^31 of the largest
+// (no zeros, denormals, Inf/NaN or wide spreads), output scale in range.  Returns false
+// (outputs untouched) otherwise; the caller then uses apply_op_cvt.
+template <int N>
+QG_HD bool apply_op_near(const OpN<N>& C, const double in[N], double out[N]) {
+    uint32_t hi[N], lo[N];
+    int ex[N];
+    int e = 0, emin = 4096;
+#pragma unroll
+    for (int j = 0; j < N; j++) {
+        const uint64_t u = f64_bits(in[j]);
+        hi[j] = (uint32_t)(u >> 32);
+        lo[j] = (uint32_t)u;
+        ex[j] = (int)((hi[j] >> 20) & 0x7FFu);
+        e = ex[j] > e ? ex[j] : e;
+        emin = ex[j] < emin ? ex[j] : emin;
+    }
+    const int t = e + C.expo - 1078;
+    if (emin < 1 || e > 2046 || e - emin > 31 || 1023 + t < 1 || 1082 + t > 2046) return false;
+    int32_t xh[N], xl[N];
+#pragma unroll
+    for (int j = 0; j < N; j++) to_limbs_near(hi[j], lo[j], e - ex[j], xh[j], xl[j]);
+    const uint32_t down = (uint32_t)t << 20;
+#pragma unroll
+    for (int r = 0; r < N; r++) {
+        int64_t hh = 0, mid = 0;
+#pragma unroll
+        for (int j = 0; j < N; j++) {
+            hh += (int64_t)xh[j] * C.h[r][j];
+            mid += (int64_t)xh[j] * C.l[r][j];
+            mid += (int64_t)xl[j] * C.h[r][j];
+        }
+        const uint64_t d = f64_bits(i64_to_double(hh + (mid >> 32)));
+        const uint32_t dh = (uint32_t)(d >> 32);
+        out[r] = bits_f64(dh ? ((uint64_t)(dh + down) << 32 | (uint32_t)d) : 0ull);
+    }
+    return true;
+}
+
+// the fast form when it applies, else the general one; false: use FP64
+template <int N>
+QG_HD bool apply_op_best(const OpN<N>& C, const double in[N], double out[N]) {
+    return apply_op_near<N>(C, in, out) || apply_op_cvt<N>(C, in, out);
+}
+
+// Host: the limb form of a real N x N operator C (row-major).  Returns false when a
+// coefficient is not finite (the caller then keeps FP64).
+template <int N>
+inline bool make_op(const double* C, OpN<N>& op) {
+    int E = -100000;
+    for (int i = 0; i < N * N; i++) {
+        if (!(C[i] - C[i] == 0.0)) return false;   // Inf or NaN
+        if (C[i] != 0.0) {
+            int ex;
+            std::frexp(C[i], &ex);                   // |C| < 2^ex
+            E = ex > E ? ex : E;
+        }
+    }
+    if (E == -100000) E = 0;                         // the zero operator
+    op.expo = E;
+    op.pad = 0;
+    for (int r = 0; r < N; r++)
+        for (int j = 0; j < N; j++) {
+            const int64_t m = (int64_t)std::llround(std::ldexp(C[N * r + j], 60 - E));
+            const uint32_t lo = (uint32_t)m;
+            op.l[r][j] = (int32_t)lo;
+            op.h[r][j] = (int32_t)((m - (int64_t)(int32_t)lo) >> 32);
+        }
+    return true;
+}
+
+inline bool make_op4(const double C[16], Op4& op) { return make_op<4>(C, op); }
+
+// Host: multiplication by the complex scalar f = (re, im) on (a.re, a.im)
+inline bool make_scalar_op(double re, double im, Op2& op) {
+    const double C[4] = {re, -im, im, re};
+    return make_op<2>(C, op);
+}
+
+// Host: the real form of out = U * (a0, a1) for a complex 2x2 U given as
+// {re00, im00, re01, im01, re10, im10, re11, im11}; in/out order (a0.re, a0.im, a1.re, a1.im)
+inline void real_form_2x2(const double u[8], double C[16]) {
+    for (int r = 0; r < 2; r++)
+        for (int j = 0; j < 2; j++) {
+            const double re = u[2 * (2 * r + j)], im = u[2 * (2 * r + j) + 1];
+            C[4 * (2 * r) + 2 * j] = re;           // out_r.re += re * a_j.re
+            C[4 * (2 * r) + 2 * j + 1] = -im;      //           - im * a_j.im
+            C[4 * (2 * r + 1) + 2 * j] = im;       // out_r.im += im * a_j.re
+            C[4 * (2 * r + 1) + 2 * j + 1] = re;   //           + re * a_j.im
+        }
 }
 
 }  // namespace qgfx

@@ -14,6 +14,7 @@
 namespace {
 thread_local std::string g_last_error;
 std::atomic<long long> g_launches{0};
+std::atomic<int> g_fp64_products{QG_FP64_PRODUCTS_FIXED};
 
 struct DeviceCache {
     void* scratch = nullptr;
@@ -69,6 +70,7 @@ int qg_check_launch(const char* what) {
 }
 
 void qg_note_launch(int n) { g_launches += n; }
+int qg_fp64_products_mode() { return g_fp64_products.load(); }
 
 int qg_num_sms() {
     DeviceCache& c = cache_for_current();
@@ -303,6 +305,19 @@ int qg_event_elapsed_ms(void* start, void* stop, float* ms) {
 
 int qg_get_launch_count(int64_t* out) {
     *out = (int64_t)g_launches.load();
+    return QG_OK;
+}
+
+int qg_set_fp64_products(int mode) {
+    if (mode != QG_FP64_PRODUCTS_FIXED && mode != QG_FP64_PRODUCTS_FP64)
+        return qg_fail(QG_ERR_ARG, "FP64 product mode %d is neither 0 (fixed point) nor 1 (FP64)", mode);
+    g_fp64_products = mode;
+    return QG_OK;
+}
+
+int qg_get_fp64_products(int* mode) {
+    if (!mode) return qg_fail(QG_ERR_ARG, "null argument");
+    *mode = g_fp64_products.load();
     return QG_OK;
 }
 

@@ -14,12 +14,15 @@
 // Reference algorithms: quest/src/cpu/cpu_subroutines.cpp (index maps and
 // arithmetic of each cpu_statevec_* routine) and quest/src/gpu/gpu_kernels.cuh.
 #include "qg_common.cuh"
+#include "qg_fixed.cuh"
 
 #include <cmath>
 #include <complex>
 #include <algorithm>
 #include <cstring>
 #include <vector>
+#include <map>
+#include <mutex>
 
 // ============================================================== initialisation
 
@@ -106,6 +109,57 @@ __global__ void k_dense1(double2* __restrict__ a, qidx numIts, Ins ins, qidx mas
         st_amp(a + (i0 | tbit), o1);
         if (!more) break;
         n = nn; i0 = j0; x = xn; y = yn;
+    }
+}
+
+// General complex 2x2 through the integer pipes: each pair is evaluated in
+// block-floating 60-bit fixed point (qg_fixed.cuh); a pair holding Inf/NaN or with a
+// result outside the normal double range is evaluated in FP64 instead.  Each thread
+// takes PPT pairs per iteration (independent work for the integer pipes) and loads
+// the next iteration's pairs before computing the current ones.
+template <int NB, int PPT, int THREADS>
+__global__ void __launch_bounds__(THREADS) k_dense1_fx(double2* __restrict__ a, qidx numIts, Ins ins, qidx mask,
+                                                      qidx tbit, qgfx::Op4 C, Mat1 M) {
+    const qidx stride = (qidx)gridDim.x * THREADS;
+    qidx n = blockIdx.x * (qidx)THREADS + threadIdx.x;
+    if (n >= numIts) return;
+    qidx i0[PPT];
+    double2 x[PPT], y[PPT];
+#pragma unroll
+    for (int k = 0; k < PPT; k++) {
+        const qidx m = n + k * stride;
+        i0[k] = m < numIts ? (insert_bits<NB>(m, ins) | mask) : ~(qidx)0;
+        if (m < numIts) { x[k] = ld_amp(a + i0[k]); y[k] = ld_amp(a + (i0[k] | tbit)); }
+    }
+    for (;;) {
+        const qidx nn = n + PPT * stride;
+        qidx j0[PPT];
+        double2 xn[PPT], yn[PPT];
+#pragma unroll
+        for (int k = 0; k < PPT; k++) {
+            const qidx m = nn + k * stride;
+            j0[k] = m < numIts ? (insert_bits<NB>(m, ins) | mask) : ~(qidx)0;
+            if (m < numIts) { xn[k] = ld_amp(a + j0[k]); yn[k] = ld_amp(a + (j0[k] | tbit)); }
+        }
+#pragma unroll
+        for (int k = 0; k < PPT; k++) {
+            if (i0[k] == ~(qidx)0) continue;
+            const double in[4] = {x[k].x, x[k].y, y[k].x, y[k].y};
+            double out[4];
+            double2 o0, o1;
+            if (qgfx::apply_op_best<4>(C, in, out)) {
+                o0 = make_double2(out[0], out[1]);
+                o1 = make_double2(out[2], out[3]);
+            } else {
+                dense1_pair<0>(M, x[k], y[k], o0, o1);
+            }
+            st_amp(a + i0[k], o0);
+            st_amp(a + (i0[k] | tbit), o1);
+        }
+        if (nn >= numIts) break;
+        n = nn;
+#pragma unroll
+        for (int k = 0; k < PPT; k++) { i0[k] = j0[k]; x[k] = xn[k]; y[k] = yn[k]; }
     }
 }
 
@@ -204,6 +258,40 @@ __global__ void k_diag1(double2* __restrict__ a, qidx numIts, Ins ins, qidx mask
         }
         double2 f = (MODE == 1) ? d0 : ((i & tbit) ? d1 : d0);
         st_amp(a + i, cmul(f, x));
+        if (!more) break;
+        n = nn; i = j; x = xn;
+    }
+}
+
+// k_diag1 through the integer pipes: each amplitude times its factor in block-floating
+// fixed point (qg_fixed.cuh); amplitudes holding Inf/NaN or with a result outside the
+// normal range take the FP64 product instead.
+template <int NB, int MODE>
+__global__ void __launch_bounds__(QG_THREADS) k_diag1_fx(double2* __restrict__ a, qidx numIts, Ins ins, qidx mask, qidx tbit,
+                                                        double2 d0, double2 d1, qgfx::Op2 F0, qgfx::Op2 F1) {
+    const qidx stride = (qidx)gridDim.x * blockDim.x;
+    qidx n = blockIdx.x * (qidx)blockDim.x + threadIdx.x;
+    if (n >= numIts) return;
+    qidx i = insert_bits<NB>(n, ins) | mask;
+    double2 x = ld_amp(a + i);
+    for (;;) {
+        const qidx nn = n + stride;
+        const bool more = nn < numIts;
+        qidx j = 0;
+        double2 xn;
+        if (more) {
+            j = insert_bits<NB>(nn, ins) | mask;
+            xn = ld_amp(a + j);
+        }
+        const bool second = (MODE == 0) && (i & tbit);
+        const double in[2] = {x.x, x.y};
+        double out[2];
+        double2 o;
+        if (qgfx::apply_op_best<2>(second ? F1 : F0, in, out))
+            o = make_double2(out[0], out[1]);
+        else
+            o = cmul(second ? d1 : d0, x);
+        st_amp(a + i, o);
         if (!more) break;
         n = nn; i = j; x = xn;
     }
@@ -384,6 +472,57 @@ unsigned persistent_blocks(qidx items) {
     return (unsigned)(need < full ? need : full);
 }
 
+// a persistent grid of as many QG_THREADS-blocks as stay resident on every SM
+// (the fixed-point kernels hold more registers than the FP64 ones)
+template <typename Kernel>
+unsigned resident_blocks(Kernel k, qidx items, int threads = QG_THREADS) {
+    static std::mutex mu;
+    static std::map<const void*, int> perSm;
+    int b = 0;
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        auto it = perSm.find((const void*)k);
+        if (it == perSm.end()) {
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k, threads, 0) != cudaSuccess || b < 1) b = 1;
+            perSm[(const void*)k] = b;
+        } else {
+            b = it->second;
+        }
+    }
+    qidx full = (qidx)qg_num_sms() * b;
+    qidx need = (items + threads - 1) / threads;
+    return (unsigned)(need < full ? need : full);
+}
+
+// k_dense1_fx with a launch shape (pairs per thread per iteration, threads per block)
+template <int PPT, int THREADS>
+int launch_dense1_fx_shape(const QubitPlan& p, qidx numIts, double2* amps, qidx tbit, const qgfx::Op4& C, const Mat1& M,
+                           cudaStream_t st) {
+    const qidx groups = (numIts + PPT - 1) / PPT;
+#define L(NBV) k_dense1_fx<NBV, PPT, THREADS><<<resident_blocks(k_dense1_fx<NBV, PPT, THREADS>, groups, THREADS), THREADS, 0, st>>>(amps, numIts, p.ins, p.stateMask, tbit, C, M)
+    QG_DISPATCH_NB(p.numFixed, L)
+#undef L
+    return QG_OK;
+}
+
+int launch_dense1_fx(QgShape shape, const QubitPlan& p, qidx numIts, double2* amps, qidx tbit, const qgfx::Op4& C,
+                     const Mat1& M, cudaStream_t st) {
+    switch (shape.ppt * 1000 + shape.threads) {
+        case 1128: return launch_dense1_fx_shape<1, 128>(p, numIts, amps, tbit, C, M, st);
+        case 2128: return launch_dense1_fx_shape<2, 128>(p, numIts, amps, tbit, C, M, st);
+        case 2256: return launch_dense1_fx_shape<2, 256>(p, numIts, amps, tbit, C, M, st);
+        default: return launch_dense1_fx_shape<1, 256>(p, numIts, amps, tbit, C, M, st);
+    }
+}
+
+// the limb form of a complex 2x2 (row-major) for k_dense1_fx; false: keep FP64
+bool make_fx(const qg_cplx* matr, qgfx::Op4& C) {
+    double u[8], R[16];
+    for (int i = 0; i < 4; i++) { u[2 * i] = matr[i].re; u[2 * i + 1] = matr[i].im; }
+    qgfx::real_form_2x2(u, R);
+    return qgfx::make_op4(R, C);
+}
+
 }  // namespace
 
 extern "C" {
@@ -440,6 +579,7 @@ int qg_sv_anyCtrlOneTargDenseMatr(void* amps, int numQubits, const int* ctrls, c
     QubitPlan p;
     QG_TRY(qg_make_plan(numQubits, ctrls, ctrlStates, numCtrls, &targ, &tv, 1, &p));
     Mat1 M;
+    qgfx::Op4 C;
     bool real = true;
     for (int i = 0; i < 4; i++) {
         M.m[i] = d2(matr[i]);
@@ -448,7 +588,9 @@ int qg_sv_anyCtrlOneTargDenseMatr(void* amps, int numQubits, const int* ctrls, c
     qidx numIts = ((qidx)1 << numQubits) >> p.numFixed;
     qidx tbit = (qidx)1 << targ;
     cudaStream_t st = qg_stream(stream);
-    if (real) {
+    if (qg_fp64_products_mode() == QG_FP64_PRODUCTS_FIXED && make_fx(matr, C)) {
+        QG_TRY(launch_dense1_fx(qg_tuned_shape(QG_TUNE_DENSE1), p, numIts, (double2*)amps, tbit, C, M, st));
+    } else if (real) {
 #define L(NBV) k_dense1<NBV, 1><<<persistent_blocks(numIts), QG_THREADS, 0, st>>>((double2*)amps, numIts, p.ins, p.stateMask, tbit, M)
         QG_DISPATCH_NB(p.numFixed, L)
 #undef L
@@ -586,17 +728,32 @@ int qg_sv_anyCtrlOneTargDiagMatr(void* amps, int numQubits, const int* ctrls, co
         QG_TRY(qg_make_plan(numQubits, ctrls, ctrlStates, numCtrls, &targ, &tv, 1, &p));
         qidx numIts = ((qidx)1 << numQubits) >> p.numFixed;
         double2 f = d2(one0 ? elems[1] : elems[0]);
-#define L(NBV) k_diag1<NBV, 1><<<persistent_blocks(numIts), QG_THREADS, 0, st>>>((double2*)amps, numIts, p.ins, p.stateMask, 0, f, f)
-        QG_DISPATCH_NB(p.numFixed, L)
+        qgfx::Op2 F;
+        if (qg_fp64_products_mode() == QG_FP64_PRODUCTS_FIXED && qgfx::make_scalar_op(f.x, f.y, F)) {
+#define L(NBV) k_diag1_fx<NBV, 1><<<resident_blocks(k_diag1_fx<NBV, 1>, numIts), QG_THREADS, 0, st>>>((double2*)amps, numIts, p.ins, p.stateMask, 0, f, f, F, F)
+            QG_DISPATCH_NB(p.numFixed, L)
 #undef L
+        } else {
+#define L(NBV) k_diag1<NBV, 1><<<persistent_blocks(numIts), QG_THREADS, 0, st>>>((double2*)amps, numIts, p.ins, p.stateMask, 0, f, f)
+            QG_DISPATCH_NB(p.numFixed, L)
+#undef L
+        }
     } else {
         QubitPlan p;
         QG_TRY(qg_make_plan(numQubits, ctrls, ctrlStates, numCtrls, nullptr, nullptr, 0, &p));
         qidx numIts = ((qidx)1 << numQubits) >> p.numFixed;
         qidx tbit = (qidx)1 << targ;
-#define L(NBV) k_diag1<NBV, 0><<<persistent_blocks(numIts), QG_THREADS, 0, st>>>((double2*)amps, numIts, p.ins, p.stateMask, tbit, d2(elems[0]), d2(elems[1]))
-        QG_DISPATCH_NB(p.numFixed, L)
+        qgfx::Op2 F0, F1;
+        if (qg_fp64_products_mode() == QG_FP64_PRODUCTS_FIXED && qgfx::make_scalar_op(elems[0].re, elems[0].im, F0) &&
+            qgfx::make_scalar_op(elems[1].re, elems[1].im, F1)) {
+#define L(NBV) k_diag1_fx<NBV, 0><<<resident_blocks(k_diag1_fx<NBV, 0>, numIts), QG_THREADS, 0, st>>>((double2*)amps, numIts, p.ins, p.stateMask, tbit, d2(elems[0]), d2(elems[1]), F0, F1)
+            QG_DISPATCH_NB(p.numFixed, L)
 #undef L
+        } else {
+#define L(NBV) k_diag1<NBV, 0><<<persistent_blocks(numIts), QG_THREADS, 0, st>>>((double2*)amps, numIts, p.ins, p.stateMask, tbit, d2(elems[0]), d2(elems[1]))
+            QG_DISPATCH_NB(p.numFixed, L)
+#undef L
+        }
     }
     qg_note_launch();
     return qg_check_launch("diag1");
