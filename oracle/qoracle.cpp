@@ -238,6 +238,89 @@ extern "C" void orc_sv_diagK(double* amps, int nq, const int* ctrls, const int* 
     }
 }
 
+/* cpu_statevec_allTargDiagMatr_sub: cpu_subroutines.cpp:713-738
+ * (a_n *= d_n, or d_n^p with std::pow(qcomp,qcomp) when an exponent is given) */
+extern "C" void orc_sv_allTargDiag(double* amps, int nq, const double* elems, const double* exponent) {
+    const cplx* d = C(elems);
+    cplx* a = C(amps);
+    cplx ex = exponent ? cplx(exponent[0], exponent[1]) : cplx(1, 0);
+    bool hasPower = exponent && ex != cplx(1, 0);
+    idx numIts = pow2(nq);
+    #pragma omp parallel for NT
+    for (idx n = 0; n < numIts; n++) {
+        cplx e = d[n];
+        if (hasPower) e = std::pow(e, ex);
+        a[n] *= e;
+    }
+}
+
+/* cpu_densmatr_allTargDiagMatr_sub: cpu_subroutines.cpp:740-784
+ * (rho[r][c] *= d_r^p, and unless multiplyOnly also *= conj(d_c^p); flat n = c*dim + r) */
+extern "C" void orc_dm_allTargDiag(double* amps, int nKet, const double* elems, const double* exponent, int multiplyOnly) {
+    const cplx* d = C(elems);
+    cplx* a = C(amps);
+    cplx ex = exponent ? cplx(exponent[0], exponent[1]) : cplx(1, 0);
+    bool hasPower = exponent && ex != cplx(1, 0);
+    idx dim = pow2(nKet), numIts = dim * dim;
+    #pragma omp parallel for NT
+    for (idx n = 0; n < numIts; n++) {
+        cplx fac = d[n % dim];
+        if (hasPower) fac = std::pow(fac, ex);
+        if (!multiplyOnly) {
+            cplx term = d[n / dim];
+            if (hasPower) term = std::pow(term, ex);
+            fac *= std::conj(term);
+        }
+        a[n] *= fac;
+    }
+}
+
+/* the diagonal element raised as the expectation routines do: cpu_subroutines.cpp:2194-2200 */
+static cplx expecElem(cplx e, cplx ex, bool hasPower, bool useRealPow) {
+    if (hasPower && !useRealPow) return std::pow(e, ex);
+    if (hasPower && useRealPow) return cplx(std::pow(std::real(e), std::real(ex)), 0);
+    return e;
+}
+
+/* cpu_statevec_calcExpecFullStateDiagMatr_sub: cpu_subroutines.cpp:2175-2212
+ * (sum_n d_n^p |a_n|^2; hasPower iff the exponent differs from 1, accelerator.cpp:1020-1021) */
+extern "C" void orc_sv_expecAllTargDiag(double* out, const double* amps, int nq, const double* elems, const double* exponent, int useRealPow) {
+    const cplx* d = C(elems);
+    const cplx* a = C(amps);
+    cplx ex = exponent ? cplx(exponent[0], exponent[1]) : cplx(1, 0);
+    bool hasPower = ex != cplx(1, 0);
+    bool realPow = useRealPow && hasPower;
+    double re = 0, im = 0;
+    idx numIts = pow2(nq);
+    #pragma omp parallel for reduction(+:re,im) NT
+    for (idx n = 0; n < numIts; n++) {
+        cplx t = expecElem(d[n], ex, hasPower, realPow) * std::norm(a[n]);
+        re += std::real(t);
+        im += std::imag(t);
+    }
+    out[0] = re;
+    out[1] = im;
+}
+
+/* cpu_densmatr_calcExpecFullStateDiagMatr_sub: cpu_subroutines.cpp:2215-2258 (sum_r d_r^p rho[r][r]) */
+extern "C" void orc_dm_expecAllTargDiag(double* out, const double* amps, int nKet, const double* elems, const double* exponent, int useRealPow) {
+    const cplx* d = C(elems);
+    const cplx* a = C(amps);
+    cplx ex = exponent ? cplx(exponent[0], exponent[1]) : cplx(1, 0);
+    bool hasPower = ex != cplx(1, 0);
+    bool realPow = useRealPow && hasPower;
+    double re = 0, im = 0;
+    idx dim = pow2(nKet);
+    #pragma omp parallel for reduction(+:re,im) NT
+    for (idx n = 0; n < dim; n++) {
+        cplx t = expecElem(d[n], ex, hasPower, realPow) * a[n * (dim + 1)];
+        re += std::real(t);
+        im += std::imag(t);
+    }
+    out[0] = re;
+    out[1] = im;
+}
+
 /* cpu_statevector_anyCtrlPauliTensorOrGadget_subA + applyPauliUponAmpPair:
  * cpu_subroutines.cpp:802-906 */
 extern "C" void orc_sv_pauliTensorOrGadget(double* amps, int nq, const int* ctrls, const int* states, int nc,
@@ -820,6 +903,24 @@ bool Runner::run(const std::string& text) {
         } else if (op == "DKP") {        /* applyMultiStateControlledDiagMatrPower: operations.cpp:468-500 */
             int k; is >> k; auto t = rdInts(is, k); auto d = rdDbl(is, 2 << k); auto ex = rdDbl(is, 2);
             diag({}, {}, t, d, ex.data());
+        } else if (op == "FSD") {        /* (apply|multiply)FullStateDiagMatr[Power]: operations.cpp:537-576 */
+            int mult, hasPow; is >> mult >> hasPow;
+            vector<double> ex = hasPow ? rdDbl(is, 2) : vector<double>{1.0, 0.0};
+            auto d = rdDbl(is, 2 * (size_t)pow2(n));
+            if (isDM) orc_dm_allTargDiag(amps, n, d.data(), ex.data(), mult);
+            else orc_sv_allTargDiag(amps, n, d.data(), ex.data());
+        } else if (op == "EXPFSD") {     /* calcExpec[NonHermitian]FullStateDiagMatr[Power]: calculations.cpp:85-215 */
+            int kind; is >> kind;        /* 0: Hermitian, 1: Hermitian power (real p), 2: non-Hermitian, 3: non-Hermitian power */
+            vector<double> ex = {1.0, 0.0};
+            if (kind == 1) { double p; is >> p; ex = {p, 0.0}; }
+            if (kind == 3) ex = rdDbl(is, 2);
+            auto d = rdDbl(is, 2 * (size_t)pow2(n));
+            double v[2];
+            int useRealPow = kind == 1;
+            if (isDM) orc_dm_expecAllTargDiag(v, amps, n, d.data(), ex.data(), useRealPow);
+            else orc_sv_expecAllTargDiag(v, amps, n, d.data(), ex.data(), useRealPow);
+            results.push_back(v[0]);
+            if (kind >= 2) results.push_back(v[1]);
         } else if (op == "PSTR") {
             std::string s; is >> s; pauliStr({}, {}, parsePauli(s));
         } else if (op == "CPSTR") {

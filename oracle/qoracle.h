@@ -48,6 +48,11 @@ void orc_dm_dephasing2(double* amps, int nKet, int q1, int q2, double prob);
 void orc_dm_damping1(double* amps, int nKet, int qubit, double prob);
 void orc_dm_pauliChannel1(double* amps, int nKet, int qubit, double pX, double pY, double pZ);
 void orc_dm_projector(double* amps, int nKet, const int* qubits, const int* outcomes, int n, double prob);
+/* FullStateDiagMatr: elems are 2^n complex; exponent NULL = no power */
+void orc_sv_allTargDiag(double* amps, int nq, const double* elems, const double* exponent);
+void orc_dm_allTargDiag(double* amps, int nKet, const double* elems, const double* exponent, int multiplyOnly);
+void orc_sv_expecAllTargDiag(double* out2, const double* amps, int nq, const double* elems, const double* exponent, int useRealPow);
+void orc_dm_expecAllTargDiag(double* out2, const double* amps, int nKet, const double* elems, const double* exponent, int useRealPow);
 
 double orc_sv_totalProb(const double* amps, int nq);
 double orc_dm_totalProb(const double* amps, int nKet);

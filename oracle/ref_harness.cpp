@@ -133,6 +133,36 @@ extern "C" int ref_run_circuit(const char* text, int numQubits, int isDensMatr, 
         else if (op == "PROBQ") { int a, o; is >> a >> o; res.push_back(calcProbOfQubitOutcome(q, a, o)); }
         else if (op == "PROBMQ") { int k; is >> k; auto a = rdInts(is, k); auto o = rdInts(is, k); res.push_back(calcProbOfMultiQubitOutcome(q, a.data(), o.data(), k)); }
         else if (op == "EXPEC") { std::string s; is >> s; res.push_back(calcExpecPauliStr(q, pauliOf(s))); }
+        else if (op == "FSD") {
+            int mult, hasPow; is >> mult >> hasPow;
+            vector<double> e = hasPow ? rdDbl(is, 2) : vector<double>{1.0, 0.0};
+            qindex dim = (qindex)1 << numQubits;
+            FullStateDiagMatr m = createFullStateDiagMatr(numQubits);
+            auto d = rdDbl(is, 2 * (size_t)dim);
+            setFullStateDiagMatr(m, 0, toC(d).data(), dim);
+            qcomp ex(e[0], e[1]);
+            if (mult && hasPow) multiplyFullStateDiagMatrPower(q, m, ex);
+            else if (mult) multiplyFullStateDiagMatr(q, m);
+            else if (hasPow) applyFullStateDiagMatrPower(q, m, ex);
+            else applyFullStateDiagMatr(q, m);
+            destroyFullStateDiagMatr(m);
+        }
+        else if (op == "EXPFSD") {
+            int kind; is >> kind;
+            double p = 1;
+            vector<double> e = {1.0, 0.0};
+            if (kind == 1) is >> p;
+            if (kind == 3) e = rdDbl(is, 2);
+            qindex dim = (qindex)1 << numQubits;
+            FullStateDiagMatr m = createFullStateDiagMatr(numQubits);
+            auto d = rdDbl(is, 2 * (size_t)dim);
+            setFullStateDiagMatr(m, 0, toC(d).data(), dim);
+            if (kind == 0) res.push_back(calcExpecFullStateDiagMatr(q, m));
+            if (kind == 1) res.push_back(calcExpecFullStateDiagMatrPower(q, m, p));
+            if (kind == 2) { qcomp v = calcExpecNonHermitianFullStateDiagMatr(q, m); res.push_back(std::real(v)); res.push_back(std::imag(v)); }
+            if (kind == 3) { qcomp v = calcExpecNonHermitianFullStateDiagMatrPower(q, m, qcomp(e[0], e[1])); res.push_back(std::real(v)); res.push_back(std::imag(v)); }
+            destroyFullStateDiagMatr(m);
+        }
         else { g_err = "unknown op " + op; rc = -1; break; }
     }
     std::memcpy(amps, q.cpuAmps, sizeof(qcomp) * q.numAmps);

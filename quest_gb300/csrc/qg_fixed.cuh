@@ -204,9 +204,15 @@ QG_HD bool apply_op_cvt(const OpN<N>& C, const double in[N], double out[N]) {
 // from its two 32-bit words with 32-bit funnel shifts, split into balanced limbs
 QG_HD void to_limbs_near(uint32_t hi, uint32_t lo, int d, int32_t& xh, int32_t& xl) {
     const uint32_t mh = (hi & 0xFFFFFu) | 0x100000u;            // 21 high mantissa bits with the implicit 1
-    const uint32_t ah = (mh << 7) | (lo >> 25);                  // (mantissa << 7): 60 bits
+#if defined(__CUDA_ARCH__)
+    const uint32_t ah = __funnelshift_l(lo, mh, 7);              // (mantissa << 7): 60 bits
     const uint32_t al = lo << 7;
-    const uint32_t yl = d ? (al >> d) | (ah << (32 - d)) : al;   // >> d, d in [0, 31]
+    const uint32_t yl = __funnelshift_r(al, ah, d);              // >> d, d in [0, 31]
+#else
+    const uint32_t ah = (mh << 7) | (lo >> 25);
+    const uint32_t al = lo << 7;
+    const uint32_t yl = d ? (al >> d) | (ah << (32 - d)) : al;
+#endif
     const uint32_t yh = ah >> d;
     const uint32_t s = (uint32_t)((int32_t)hi >> 31);            // 0 or all ones
     const uint64_t y = ((uint64_t)(yh ^ s) << 32 | (yl ^ s)) - (uint64_t)(int64_t)(int32_t)s;   // +-y

@@ -117,49 +117,65 @@ __global__ void k_dense1(double2* __restrict__ a, qidx numIts, Ins ins, qidx mas
 // result outside the normal double range is evaluated in FP64 instead.  Each thread
 // takes PPT pairs per iteration (independent work for the integer pipes) and loads
 // the next iteration's pairs before computing the current ones.
+__device__ __forceinline__ void dense1_fx_pair(const qgfx::Op4& C, const Mat1& M, double2 x, double2 y, double2& o0,
+                                               double2& o1) {
+    const double in[4] = {x.x, x.y, y.x, y.y};
+    double out[4];
+    if (qgfx::apply_op_best<4>(C, in, out)) {
+        o0 = make_double2(out[0], out[1]);
+        o1 = make_double2(out[2], out[3]);
+    } else {
+        dense1_pair<0>(M, x, y, o0, o1);
+    }
+}
+
 template <int NB, int PPT, int THREADS>
 __global__ void __launch_bounds__(THREADS) k_dense1_fx(double2* __restrict__ a, qidx numIts, Ins ins, qidx mask,
                                                       qidx tbit, qgfx::Op4 C, Mat1 M) {
     const qidx stride = (qidx)gridDim.x * THREADS;
-    qidx n = blockIdx.x * (qidx)THREADS + threadIdx.x;
-    if (n >= numIts) return;
-    qidx i0[PPT];
-    double2 x[PPT], y[PPT];
-#pragma unroll
-    for (int k = 0; k < PPT; k++) {
-        const qidx m = n + k * stride;
-        i0[k] = m < numIts ? (insert_bits<NB>(m, ins) | mask) : ~(qidx)0;
-        if (m < numIts) { x[k] = ld_amp(a + i0[k]); y[k] = ld_amp(a + (i0[k] | tbit)); }
-    }
-    for (;;) {
-        const qidx nn = n + PPT * stride;
-        qidx j0[PPT];
-        double2 xn[PPT], yn[PPT];
+    const qidx span = PPT * stride;
+    const qidx tid = blockIdx.x * (qidx)THREADS + threadIdx.x;
+    const qidx groups = numIts / span;      // rounds in which all PPT pairs of every thread exist
+    if (groups > 0) {
+        qidx i0[PPT];
+        double2 x[PPT], y[PPT];
 #pragma unroll
         for (int k = 0; k < PPT; k++) {
-            const qidx m = nn + k * stride;
-            j0[k] = m < numIts ? (insert_bits<NB>(m, ins) | mask) : ~(qidx)0;
-            if (m < numIts) { xn[k] = ld_amp(a + j0[k]); yn[k] = ld_amp(a + (j0[k] | tbit)); }
+            i0[k] = insert_bits<NB>(tid + k * stride, ins) | mask;
+            x[k] = ld_amp(a + i0[k]);
+            y[k] = ld_amp(a + (i0[k] | tbit));
         }
+        for (qidx g = 1;; g++) {
+            const bool more = g < groups;
+            qidx j0[PPT];
+            double2 xn[PPT], yn[PPT];
+            if (more) {
 #pragma unroll
-        for (int k = 0; k < PPT; k++) {
-            if (i0[k] == ~(qidx)0) continue;
-            const double in[4] = {x[k].x, x[k].y, y[k].x, y[k].y};
-            double out[4];
-            double2 o0, o1;
-            if (qgfx::apply_op_best<4>(C, in, out)) {
-                o0 = make_double2(out[0], out[1]);
-                o1 = make_double2(out[2], out[3]);
-            } else {
-                dense1_pair<0>(M, x[k], y[k], o0, o1);
+                for (int k = 0; k < PPT; k++) {
+                    j0[k] = insert_bits<NB>(g * span + tid + k * stride, ins) | mask;
+                    xn[k] = ld_amp(a + j0[k]);
+                    yn[k] = ld_amp(a + (j0[k] | tbit));
+                }
             }
-            st_amp(a + i0[k], o0);
-            st_amp(a + (i0[k] | tbit), o1);
-        }
-        if (nn >= numIts) break;
-        n = nn;
 #pragma unroll
-        for (int k = 0; k < PPT; k++) { i0[k] = j0[k]; x[k] = xn[k]; y[k] = yn[k]; }
+            for (int k = 0; k < PPT; k++) {
+                double2 o0, o1;
+                dense1_fx_pair(C, M, x[k], y[k], o0, o1);
+                st_amp(a + i0[k], o0);
+                st_amp(a + (i0[k] | tbit), o1);
+            }
+            if (!more) break;
+#pragma unroll
+            for (int k = 0; k < PPT; k++) { i0[k] = j0[k]; x[k] = xn[k]; y[k] = yn[k]; }
+        }
+    }
+    // the remaining pairs, one at a time
+    for (qidx n = groups * span + tid; n < numIts; n += stride) {
+        const qidx i = insert_bits<NB>(n, ins) | mask;
+        double2 o0, o1;
+        dense1_fx_pair(C, M, ld_amp(a + i), ld_amp(a + (i | tbit)), o0, o1);
+        st_amp(a + i, o0);
+        st_amp(a + (i | tbit), o1);
     }
 }
 

@@ -238,3 +238,74 @@ def config1_circuit(nq, layers, seed, num_expec=16):
     for _ in range(num_expec):
         L.append(f"EXPEC {pauli_text([int(v) for v in rng.integers(0, 4, size=nq)])}")
     return "\n".join(L) + "\n"
+
+
+def isometry_kraus(rng):
+    """Four 4x4 Kraus operators: the 4x4 blocks of a random 16x4 isometry (QR of a
+    complex Gaussian matrix), so sum_i K_i^dagger K_i = I."""
+    g = rng.standard_normal((16, 4)) + 1j * rng.standard_normal((16, 4))
+    q, r = np.linalg.qr(g)
+    q = q * (np.diag(r) / np.abs(np.diag(r)))
+    return [q[4 * i:4 * i + 4, :] for i in range(4)]
+
+
+def config3_circuit(nq, layers, seed, num_expec=16):
+    """The density-matrix method: `layers` x (random 1-qubit Haar unitaries on every
+    qubit on even layers, random 2-qubit Haar unitaries on disjoint random pairs on odd
+    layers; each layer followed by mixDepolarising(p=0.01) on every qubit and one
+    random 2-qubit 4-operator CPTP mixKrausMap), then calcPurity and `num_expec`
+    Pauli expectations with I/X/Y/Z uniform per qubit."""
+    rng = np.random.default_rng(seed)
+    L = []
+    for layer in range(layers):
+        if layer % 2 == 0:
+            for t in range(nq):
+                L.append(f"U1 {t} {mat_tokens(haar_unitary(2, rng))}")
+        else:
+            perm = [int(v) for v in rng.permutation(nq)]
+            for i in range(0, nq - 1, 2):
+                L.append(f"U2 {perm[i]} {perm[i + 1]} {mat_tokens(haar_unitary(4, rng))}")
+        for t in range(nq):
+            L.append(f"DEPOL {t} {fmt(0.01)}")
+        a, b = (int(v) for v in rng.choice(nq, size=2, replace=False))
+        L.append(f"KRAUS 2 {a} {b} 4 " + " ".join(mat_tokens(o) for o in isometry_kraus(rng)))
+    L.append("PURITY")
+    for _ in range(num_expec):
+        L.append(f"EXPEC {pauli_text([int(v) for v in rng.integers(0, 4, size=nq)])}")
+    return "\n".join(L) + "\n"
+
+
+def fullstate_diag_circuit(nq, is_dm, seed):
+    """FullStateDiagMatr on a register prepared by a few gates: apply (unit-modulus
+    elements), apply with a real power, multiply (general elements), multiply with a
+    complex power, then the four expectation forms (Hermitian, Hermitian with a real
+    power of positive elements, non-Hermitian, non-Hermitian with a complex power)."""
+    rng = np.random.default_rng(seed)
+    dim = 1 << nq
+
+    def elems(kind):
+        if kind == "phase":
+            return np.exp(1j * rng.uniform(0, 2 * np.pi, dim))
+        if kind == "real+":
+            return rng.uniform(0.2, 2.0, dim).astype(np.complex128)
+        if kind == "real":
+            return rng.uniform(-2.0, 2.0, dim).astype(np.complex128)
+        return (rng.uniform(0.3, 1.5, dim) * np.exp(1j * rng.uniform(0, 2 * np.pi, dim)))
+
+    L = [f"H {t}" for t in range(nq)]
+    L.append(f"U1 0 {mat_tokens(haar_unitary(2, rng))}")
+    if nq > 1:
+        L.append(f"U2 0 {nq - 1} {mat_tokens(haar_unitary(4, rng))}")
+    L.append(f"FSD 0 0 {mat_tokens(elems('phase'))}")
+    L.append(f"FSD 0 1 {fmt(rng.uniform(-2, 2))} 0.0 {mat_tokens(elems('phase'))}")
+    L.append("TOTALPROB")
+    L.append(f"EXPFSD 0 {mat_tokens(elems('real'))}")
+    L.append(f"EXPFSD 1 {fmt(rng.uniform(0.5, 2.5))} {mat_tokens(elems('real+'))}")
+    L.append(f"EXPFSD 2 {mat_tokens(elems('general'))}")
+    L.append(f"EXPFSD 3 {fmt(rng.uniform(-1, 2))} {fmt(rng.uniform(-1, 1))} {mat_tokens(elems('general'))}")
+    L.append(f"EXPEC {pauli_text([int(v) for v in rng.integers(0, 4, size=nq)])}")
+    # multiplying leaves a density matrix non-Hermitian: only the total probability after
+    L.append(f"FSD 1 0 {mat_tokens(elems('general'))}")
+    L.append(f"FSD 1 1 {fmt(rng.uniform(0.5, 1.5))} {fmt(rng.uniform(-0.5, 0.5))} {mat_tokens(elems('general'))}")
+    L.append("TOTALPROB")
+    return "\n".join(L) + "\n"

@@ -50,6 +50,18 @@ def test_every_op_vs_oracle(env, nq, is_dm, seed):
     assert o1.tolist() == o2.tolist()
 
 
+@pytest.mark.parametrize("nq,layers", [(4, 6), (7, 4)])
+def test_config3_shape_vs_oracle(env, nq, layers):
+    """The density-matrix method's circuit shape (Haar layers, depolarising on every
+    qubit, a 2-qubit Kraus map per layer, purity, 16 Pauli expectations) at small size."""
+    text = qc.config3_circuit(nq, layers, 33 + nq)
+    amps = qc.random_density_matrix(nq, 33 + nq)
+    a1, r1, _ = qc.oracle().run(text, nq, 1, amps)
+    a2, r2, _ = run_gpu(env, text, nq, 1, amps)
+    assert np.max(np.abs(a1 - a2)) <= TOL
+    assert r1.size == 17 and np.max(np.abs(r1 - r2)) <= TOL
+
+
 def test_config1_shape_vs_oracle(env):
     """The plain method's circuit shape at 14 qubits, 4 layers."""
     nq = 14
