@@ -199,6 +199,23 @@ int qg_dm_calcProbOfMultiQubitOutcome(const void* amps, int numKetQubits, const 
  * deterministic (no atomics on the probabilities). outProbs: HOST array of 2^num */
 int qg_sv_calcProbsOfAllMultiQubitOutcomes(double* outProbs, const void* amps, int numQubits, const int* qubits, int num,
                                            void* stream);
+/* ------------------------------------------------------------------ all-target diagonals (FullStateDiagMatr)
+ * elems: DEVICE array of 2^n complex (n ket qubits for a density matrix), 16-byte aligned.
+ * With hasPower the elements are raised to `exponent` (complex pow, exp(w log z)). */
+/* gpu_statevec_allTargDiagMatr_sub (gpu_subroutines.hpp:76; gpu_thrust.cuh:729-742): a_i *= d_i^p */
+int qg_sv_allTargDiagMatr(void* amps, int numQubits, const void* elems, qg_cplx exponent, int hasPower, void* stream);
+/* gpu_densmatr_allTargDiagMatr_sub (gpu_subroutines.hpp:78; gpu_kernels.cuh:556-588):
+ * rho[r][c] *= d_r^p, and unless multiplyOnly also *= conj(d_c^p) */
+int qg_dm_allTargDiagMatr(void* amps, int numKetQubits, const void* elems, qg_cplx exponent, int hasPower, int multiplyOnly,
+                          void* stream);
+/* gpu_statevec_calcExpecFullStateDiagMatr_sub (gpu_subroutines.hpp:176; gpu_thrust.cuh:977-988):
+ * sum_i f(d_i) |a_i|^2 with f = d^p (complex pow) or, with useRealPow, re(d)^re(p) */
+int qg_sv_calcExpecFullStateDiagMatr(const void* amps, int numQubits, const void* elems, qg_cplx exponent, int hasPower,
+                                     int useRealPow, qg_cplx* out, void* stream);
+/* gpu_densmatr_calcExpecFullStateDiagMatr_sub (gpu_subroutines.hpp:177; gpu_thrust.cuh:991-1008): sum_r f(d_r) rho[r][r] */
+int qg_dm_calcExpecFullStateDiagMatr(const void* amps, int numKetQubits, const void* elems, qg_cplx exponent, int hasPower,
+                                     int useRealPow, qg_cplx* out, void* stream);
+
 /* gpu_statevec_calcExpecAnyTargZ_sub (gpu_subroutines.hpp:169; gpu_thrust.cuh:888-900) */
 int qg_sv_calcExpecAnyTargZ(const void* amps, int numQubits, const int* targs, int numTargs, double* out, void* stream);
 /* gpu_densmatr_calcExpecAnyTargZ_sub (gpu_subroutines.hpp:170; gpu_thrust.cuh:903-915) */
@@ -255,6 +272,26 @@ int qg_circuit_get_block(const qg_circuit* circuit, int i, int* targs, int* numT
 /* impl: 0 automatic (tensor cores for 5-qubit blocks on >= 12 qubits), 1 SIMT FP32, 2 tensor cores */
 int qg_sv32_apply_circuit(qg_circuit* circuit, void* amps32, int numQubits, int impl, void* stream);
 int qg_tc_get_error_flag(int* out);    /* 1 if a tensor-core kernel's bounded wait ran out */
+
+/* Fusion autotuner (no counterpart in the reference): times the circuit fused at each
+ * width k from its widest gate to 5 with the SIMT kernel, and at k = 5 with the
+ * tensor-core kernel (>= 12 qubits), on a scratch FP32 register of the circuit's size
+ * (8 B x 2^n for the duration of the call).  Leaves the circuit fused at the fastest
+ * width, with that kernel used by applies that pass impl = 0; a later qg_circuit_fuse
+ * clears the preference.  Candidate i (in the order tried, at most maxOut reported) is
+ * (candK[i], candImpl[i]) and took msOut[i] ms per circuit; any output may be NULL. */
+int qg_circuit_autotune(qg_circuit* circuit, int* bestK, int* bestImpl, int* candK, int* candImpl, double* msOut,
+                        int maxOut, int* numOut);
+
+/* CUDA graph of one application of a fused circuit to one FP32 register (no
+ * counterpart in the reference).  The graph holds the register's address and the
+ * circuit's device copy: it stays valid while both live and the circuit is not
+ * re-fused.  Launching it replays every block kernel with one host call. */
+typedef struct qg_graph qg_graph;
+int qg_circuit_graph_create(qg_circuit* circuit, void* amps32, int numQubits, int impl, qg_graph** out);
+int qg_graph_launch(qg_graph* graph, void* stream);
+int qg_graph_get_num_kernels(const qg_graph* graph, int* out);
+int qg_graph_destroy(qg_graph* graph);
 
 int qg_sv32_initUniformState(void* amps32, int numQubits, qg_cplxf amp, void* stream);
 int qg_sv32_initClassicalState(void* amps32, int numQubits, int64_t index, void* stream);

@@ -83,6 +83,23 @@ typedef struct {
     qcomp_t* gpuElems;
 } DiagMatr;
 
+/* quest/include/matrices.h:195-230 */
+typedef struct {
+    int numQubits;
+    qindex numElems;
+    int isGpuAccelerated;
+    int isMultithreaded;
+    int isDistributed;
+    qindex numElemsPerNode;
+    int* isApproxUnitary;
+    int* isApproxHermitian;
+    int* isApproxNonZero;
+    int* isStrictlyNonNegative;
+    int* wasGpuSynced;
+    qcomp_t* cpuElems;
+    qcomp_t* gpuElems;
+} FullStateDiagMatr;
+
 /* quest/include/channels.h:74-101 */
 typedef struct {
     int numQubits;
@@ -224,6 +241,20 @@ qreal calcProbOfMultiQubitOutcome(Qureg qureg, int* qubits, int* outcomes, int n
 void  calcProbsOfAllMultiQubitOutcomes(qreal* outcomeProbs, Qureg qureg, int* qubits, int numQubits);    /* :265 */
 qreal calcTotalProb(Qureg qureg);                                                                        /* :278 */
 qreal calcPurity(Qureg qureg);                                                                           /* :293 */
+
+/* FullStateDiagMatr: matrices.h:755-923, operations.h:970-990, calculations.h:170-318 */
+FullStateDiagMatr createFullStateDiagMatr(int numQubits);
+void destroyFullStateDiagMatr(FullStateDiagMatr matr);
+void setFullStateDiagMatr(FullStateDiagMatr out, qindex startInd, const qcomp_t* in, qindex numElems);
+void syncFullStateDiagMatr(FullStateDiagMatr matr);
+void multiplyFullStateDiagMatr(Qureg qureg, FullStateDiagMatr matrix);
+void multiplyFullStateDiagMatrPower(Qureg qureg, FullStateDiagMatr matrix, qcomp_t exponent);
+void applyFullStateDiagMatr(Qureg qureg, FullStateDiagMatr matrix);
+void applyFullStateDiagMatrPower(Qureg qureg, FullStateDiagMatr matrix, qcomp_t exponent);
+qreal calcExpecFullStateDiagMatr(Qureg qureg, FullStateDiagMatr matrix);
+qreal calcExpecFullStateDiagMatrPower(Qureg qureg, FullStateDiagMatr matrix, qreal exponent);
+qcomp_t calcExpecNonHermitianFullStateDiagMatr(Qureg qureg, FullStateDiagMatr matrix);
+qcomp_t calcExpecNonHermitianFullStateDiagMatrPower(Qureg qureg, FullStateDiagMatr matrix, qcomp_t exponent);
 
 #ifdef __cplusplus
 }

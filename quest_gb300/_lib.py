@@ -106,12 +106,21 @@ ABI = {
     "qg_circuit_get_block": [vp, I, c_int_p, c_int_p, c_cplx_p],
     "qg_sv32_apply_circuit": [vp, vp, I, I, vp],
     "qg_tc_get_error_flag": [c_int_p],
+    "qg_circuit_autotune": [vp, c_int_p, c_int_p, c_int_p, c_int_p, c_dbl_p, I, c_int_p],
+    "qg_circuit_graph_create": [vp, vp, I, I, ctypes.POINTER(vp)],
+    "qg_graph_launch": [vp, vp],
+    "qg_graph_get_num_kernels": [vp, c_int_p],
+    "qg_graph_destroy": [vp],
     "qg_sv32_initUniformState": [vp, I, qg_cplxf, vp],
     "qg_sv32_initClassicalState": [vp, I, I64, vp],
     "qg_sv_convert_f64_to_f32": [vp, vp, I, vp],
     "qg_sv_convert_f32_to_f64": [vp, vp, I, vp],
     "qg_sv32_calcTotalProb": [vp, I, c_dbl_p, vp],
     "qg_sv32_normalise": [vp, I, D, vp],
+    "qg_sv_allTargDiagMatr": [vp, I, vp, qg_cplx, I, vp],
+    "qg_dm_allTargDiagMatr": [vp, I, vp, qg_cplx, I, I, vp],
+    "qg_sv_calcExpecFullStateDiagMatr": [vp, I, vp, qg_cplx, I, I, c_cplx_p, vp],
+    "qg_dm_calcExpecFullStateDiagMatr": [vp, I, vp, qg_cplx, I, I, c_cplx_p, vp],
     "qg_set_fp64_products": [I],
     "qg_get_fp64_products": [c_int_p],
     "qg_set_kernel_shape": [I, I, I],

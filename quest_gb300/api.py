@@ -60,6 +60,13 @@ class DiagMatr(ctypes.Structure):
                 ("cpuElems", _CP), ("gpuElems", _CP)]
 
 
+class FullStateDiagMatr(ctypes.Structure):
+    _fields_ = [("numQubits", ctypes.c_int), ("numElems", qindex), ("isGpuAccelerated", ctypes.c_int),
+                ("isMultithreaded", ctypes.c_int), ("isDistributed", ctypes.c_int), ("numElemsPerNode", qindex),
+                ("isApproxUnitary", _IP), ("isApproxHermitian", _IP), ("isApproxNonZero", _IP),
+                ("isStrictlyNonNegative", _IP), ("wasGpuSynced", _IP), ("cpuElems", _CP), ("gpuElems", _CP)]
+
+
 class SuperOp(ctypes.Structure):
     _fields_ = [("numQubits", ctypes.c_int), ("numRows", qindex), ("cpuElems", ctypes.POINTER(_CP)),
                 ("cpuElemsFlat", _CP), ("gpuElemsFlat", _CP), ("wasGpuSynced", _IP)]
@@ -180,6 +187,18 @@ _PROTOS = {
     "calcProbsOfAllMultiQubitOutcomes": (V, [ctypes.POINTER(D), Qureg, _IP, I]),
     "calcTotalProb": (D, [Qureg]),
     "calcPurity": (D, [Qureg]),
+    "createFullStateDiagMatr": (FullStateDiagMatr, [I]),
+    "destroyFullStateDiagMatr": (V, [FullStateDiagMatr]),
+    "setFullStateDiagMatr": (V, [FullStateDiagMatr, qindex, ctypes.c_void_p, qindex]),
+    "syncFullStateDiagMatr": (V, [FullStateDiagMatr]),
+    "multiplyFullStateDiagMatr": (V, [Qureg, FullStateDiagMatr]),
+    "multiplyFullStateDiagMatrPower": (V, [Qureg, FullStateDiagMatr, qg_cplx]),
+    "applyFullStateDiagMatr": (V, [Qureg, FullStateDiagMatr]),
+    "applyFullStateDiagMatrPower": (V, [Qureg, FullStateDiagMatr, qg_cplx]),
+    "calcExpecFullStateDiagMatr": (D, [Qureg, FullStateDiagMatr]),
+    "calcExpecFullStateDiagMatrPower": (D, [Qureg, FullStateDiagMatr, D]),
+    "calcExpecNonHermitianFullStateDiagMatr": (qg_cplx, [Qureg, FullStateDiagMatr]),
+    "calcExpecNonHermitianFullStateDiagMatrPower": (qg_cplx, [Qureg, FullStateDiagMatr, qg_cplx]),
 }
 
 
@@ -323,3 +342,14 @@ def get_amps(qureg):
 def seeds(*values):
     arr = (ctypes.c_uint * len(values))(*values)
     Q.setSeeds(arr, len(values))
+
+
+def full_state_diag(elems):
+    """A FullStateDiagMatr holding `elems` (2^n complex); destroy it with Q.destroyFullStateDiagMatr."""
+    e = np.ascontiguousarray(np.asarray(elems, dtype=np.complex128).reshape(-1))
+    n = int(e.size).bit_length() - 1
+    if e.size != 1 << n:
+        raise ValueError("a FullStateDiagMatr holds 2^n elements")
+    m = Q.createFullStateDiagMatr(n)
+    Q.setFullStateDiagMatr(m, 0, e.ctypes.data, e.size)
+    return m

@@ -9,8 +9,9 @@ import ctypes
 
 import numpy as np
 
-from .api import (Q, comp_matr, comp_matr1, comp_matr2, diag_matr, diag_matr1, diag_matr2, ints, kraus_map,
-                  pauli_str, seeds)
+from ._lib import qg_cplx
+from .api import (Q, comp_matr, comp_matr1, comp_matr2, diag_matr, diag_matr1, diag_matr2, full_state_diag, ints,
+                  kraus_map, pauli_str, seeds)
 
 
 def _f(tokens, k):
@@ -77,6 +78,32 @@ def run_text(text, qureg):
             Q.applyDiagMatr1(qureg, int(a[0]), diag_matr1(_cvals(a[1:5])))
         elif op == "D2":
             Q.applyDiagMatr2(qureg, int(a[0]), int(a[1]), diag_matr2(_cvals(a[2:10])))
+        elif op == "FSD":
+            mult, has_pow = int(a[0]), int(a[1])
+            ex = (float(a[2]), float(a[3])) if has_pow else None
+            m = full_state_diag(_cvals(a[4 if has_pow else 2:]))
+            try:
+                if ex is None:
+                    (Q.multiplyFullStateDiagMatr if mult else Q.applyFullStateDiagMatr)(qureg, m)
+                else:
+                    (Q.multiplyFullStateDiagMatrPower if mult else Q.applyFullStateDiagMatrPower)(qureg, m, qg_cplx(*ex))
+            finally:
+                Q.destroyFullStateDiagMatr(m)
+        elif op == "EXPFSD":
+            kind = int(a[0])
+            skip = {0: 1, 1: 2, 2: 1, 3: 3}[kind]
+            m = full_state_diag(_cvals(a[skip:]))
+            try:
+                if kind == 0:
+                    results.append(Q.calcExpecFullStateDiagMatr(qureg, m))
+                elif kind == 1:
+                    results.append(Q.calcExpecFullStateDiagMatrPower(qureg, m, float(a[1])))
+                else:
+                    v = (Q.calcExpecNonHermitianFullStateDiagMatr(qureg, m) if kind == 2 else
+                         Q.calcExpecNonHermitianFullStateDiagMatrPower(qureg, m, qg_cplx(float(a[1]), float(a[2]))))
+                    results += [v.re, v.im]
+            finally:
+                Q.destroyFullStateDiagMatr(m)
         elif op in ("DK", "CDK", "DKP"):
             if op == "CDK":
                 nc = int(a[0]); c = a[1:1 + nc]; s = a[1 + nc:1 + 2 * nc]; a = a[1 + 2 * nc:]
@@ -89,7 +116,6 @@ def run_text(text, qureg):
                     Q.applyMultiStateControlledDiagMatr(qureg, ints(c), ints(s), nc, ints(t), k, d)
                 else:
                     ex = a[1 + k + (2 << k):]
-                    from ._lib import qg_cplx
                     Q.applyDiagMatrPower(qureg, ints(t), k, d, qg_cplx(float(ex[0]), float(ex[1])))
             finally:
                 Q.destroyDiagMatr(d)

@@ -40,6 +40,7 @@ struct qg_circuit {
     bool uploaded = false;      // block matrices are copied to the device at the first apply
     bool ownsDevice = false;    // the device copy was allocated here (else it lives in a caller's arena)
     bool allUnitary = true;     // every gate satisfies max|U^dagger U - I| <= 1e-10
+    int preferredImpl = 0;      // set by qg_circuit_autotune: the kernel an automatic apply uses
 };
 
 // bytes of the device copy of the fused blocks (descriptors, FP32 matrices, tensor-core operands)

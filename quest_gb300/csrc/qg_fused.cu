@@ -31,6 +31,7 @@ size_t qg_tc_operand_floats();
 void qg_tc_build_operands(const std::complex<double>* m32x32, float* out);
 int qg_tc_apply_block(float2* amps, int numQubits, const int* targs, const float* devOperands, cudaStream_t st);
 bool qg_tc_supported(int numQubits);
+int qg_tc_prepare();
 
 namespace {
 
@@ -557,6 +558,7 @@ int qg_circuit_fuse(qg_circuit* c, int maxFusedQubits) {
     c->blocks.clear();
     fuse_gates(c->gates, c->numQubits, maxFusedQubits, c->blocks);
     c->fusedK = maxFusedQubits;
+    c->preferredImpl = 0;
     free_owned(c);
     return QG_OK;
 }
@@ -591,6 +593,7 @@ int qg_sv32_apply_circuit(qg_circuit* c, void* amps, int numQubits, int impl, vo
     if (numQubits != c->numQubits) return qg_fail(QG_ERR_ARG, "circuit has %d qubits, state has %d", c->numQubits, numQubits);
     if (c->blocks.empty() && !c->gates.empty()) return qg_fail(QG_ERR_ARG, "circuit was not fused (qg_circuit_fuse)");
     cudaStream_t st = qg_stream(stream);
+    if (impl == 0 && c->preferredImpl != 0) impl = c->preferredImpl;
     for (const QgBlock& b : c->blocks) {
         bool tc = b.targs.size() == 5 && (impl == 2 || (impl == 0 && qg_tc_supported(numQubits)));
         if (tc) {
@@ -599,6 +602,128 @@ int qg_sv32_apply_circuit(qg_circuit* c, void* amps, int numQubits, int impl, vo
             QG_TRY(launch_fused_simt((float2*)amps, numQubits, b.targs, c->devF32 + b.off32, st));
         }
     }
+    return QG_OK;
+}
+
+// ---------------------------------------------------------------- CUDA graphs of a circuit
+
+struct qg_graph {
+    cudaGraphExec_t exec = nullptr;
+    int numKernels = 0;
+};
+
+int qg_circuit_graph_create(qg_circuit* c, void* amps, int numQubits, int impl, qg_graph** out) {
+    QG_TRY(check32(amps, numQubits));
+    if (!c || !out) return qg_fail(QG_ERR_ARG, "null argument");
+    if (numQubits != c->numQubits) return qg_fail(QG_ERR_ARG, "circuit has %d qubits, state has %d", c->numQubits, numQubits);
+    if (c->blocks.empty() && !c->gates.empty()) return qg_fail(QG_ERR_ARG, "circuit was not fused (qg_circuit_fuse)");
+    // everything that allocates or synchronises happens before the capture
+    if (!c->uploaded) QG_TRY(qg_circuit_upload(c, nullptr));
+    if (numQubits >= 12) QG_TRY(qg_tc_prepare());
+    cudaStream_t s = nullptr;
+    QG_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    int64_t before = 0, after = 0;
+    qg_get_launch_count(&before);
+    cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) {
+        cudaStreamDestroy(s);
+        return qg_check_cuda(e, "cudaStreamBeginCapture");
+    }
+    int rc = qg_sv32_apply_circuit(c, amps, numQubits, impl, s);
+    cudaGraph_t graph = nullptr;
+    e = cudaStreamEndCapture(s, &graph);
+    qg_get_launch_count(&after);
+    qg_note_launch(-(int)(after - before));        // captured, not launched
+    cudaStreamDestroy(s);
+    if (rc != QG_OK || e != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc != QG_OK ? rc : qg_check_cuda(e, "cudaStreamEndCapture");
+    }
+    cudaGraphExec_t exec = nullptr;
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return qg_check_cuda(e, "cudaGraphInstantiate");
+    qg_graph* g = new qg_graph;
+    g->exec = exec;
+    g->numKernels = (int)(after - before);
+    *out = g;
+    return QG_OK;
+}
+
+int qg_graph_launch(qg_graph* g, void* stream) {
+    if (!g) return qg_fail(QG_ERR_ARG, "null graph");
+    QG_CUDA(cudaGraphLaunch(g->exec, qg_stream(stream)));
+    qg_note_launch(g->numKernels);
+    return QG_OK;
+}
+
+int qg_graph_get_num_kernels(const qg_graph* g, int* out) {
+    if (!g || !out) return qg_fail(QG_ERR_ARG, "null argument");
+    *out = g->numKernels;
+    return QG_OK;
+}
+
+int qg_graph_destroy(qg_graph* g) {
+    if (!g) return QG_OK;
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    delete g;
+    return QG_OK;
+}
+
+// ---------------------------------------------------------------- fusion autotuner
+
+// Times the circuit fused at every width k in [widest gate, 5] with the SIMT kernel,
+// and at k = 5 with the tensor-core kernel (12 qubits and up), on a scratch register
+// of the circuit's size; leaves the circuit fused at the fastest width with that
+// kernel preferred by automatic applies.  Candidate i (in the order tried) is
+// (candK[i], candImpl[i]) and took msOut[i] milliseconds per circuit.
+int qg_circuit_autotune(qg_circuit* c, int* bestK, int* bestImpl, int* candK, int* candImpl, double* msOut, int maxOut,
+                        int* numOut) {
+    if (!c) return qg_fail(QG_ERR_ARG, "null circuit");
+    const int nq = c->numQubits;
+    if (nq < 5) return qg_fail(QG_ERR_ARG, "autotuning needs at least 5 qubits");
+    int widest = 1;
+    for (const auto& g : c->gates) widest = std::max(widest, (int)g.targs.size());
+    void* amps = nullptr;
+    QG_TRY(qg_alloc(&amps, (int64_t)8 << nq));
+    void* ev0 = nullptr;
+    void* ev1 = nullptr;
+    int rc = QG_OK, n = 0, kBest = 5, iBest = 1;
+    double tBest = 1e300;
+    if ((rc = qg_event_create(&ev0)) == QG_OK) rc = qg_event_create(&ev1);
+    for (int k = std::max(3, widest); k <= 5 && rc == QG_OK; k++) {
+        for (int impl = 1; impl <= 2 && rc == QG_OK; impl++) {
+            if (impl == 2 && (k != 5 || nq < 12)) continue;
+            if ((rc = qg_circuit_fuse(c, k)) != QG_OK) break;
+            if ((rc = qg_circuit_upload(c, nullptr)) != QG_OK) break;
+            if ((rc = qg_sv32_initClassicalState(amps, nq, 0, nullptr)) != QG_OK) break;
+            if ((rc = qg_sv32_apply_circuit(c, amps, nq, impl, nullptr)) != QG_OK) break;    // warm-up
+            const int reps = 2;
+            if ((rc = qg_event_record(ev0, nullptr)) != QG_OK) break;
+            for (int r = 0; r < reps && rc == QG_OK; r++) rc = qg_sv32_apply_circuit(c, amps, nq, impl, nullptr);
+            if (rc == QG_OK) rc = qg_event_record(ev1, nullptr);
+            float ms = 0;
+            if (rc == QG_OK) rc = qg_event_elapsed_ms(ev0, ev1, &ms);
+            if (rc != QG_OK) break;
+            const double per = ms / reps;
+            if (n < maxOut) {
+                if (msOut) msOut[n] = per;
+                if (candK) candK[n] = k;
+                if (candImpl) candImpl[n] = impl;
+            }
+            n++;
+            if (per < tBest) { tBest = per; kBest = k; iBest = impl; }
+        }
+    }
+    if (ev0) qg_event_destroy(ev0);
+    if (ev1) qg_event_destroy(ev1);
+    qg_free(amps);
+    if (rc != QG_OK) return rc;
+    QG_TRY(qg_circuit_fuse(c, kBest));
+    c->preferredImpl = iBest;
+    if (bestK) *bestK = kBest;
+    if (bestImpl) *bestImpl = iBest;
+    if (numOut) *numOut = n;
     return QG_OK;
 }
 

@@ -23,6 +23,8 @@
 // TMEM and returns.
 #include "qg_common.cuh"
 
+#include <mutex>
+
 #include <cmath>
 #include <complex>
 #include <cstring>
@@ -296,12 +298,27 @@ int* g_tc_error = nullptr;
 
 bool qg_tc_supported(int numQubits) { return numQubits >= 12; }
 
-int qg_tc_apply_block(float2* amps, int numQubits, const int* targs, const float* devOperands, cudaStream_t st) {
-    if (numQubits < 12) return qg_fail(QG_ERR_ARG, "the tensor-core block kernel needs at least 12 qubits (one 128-group tile)");
+// one-time set-up (the error flag's memory, the kernel's shared-memory limit); done
+// before the first launch and before any stream capture of one
+int qg_tc_prepare() {
+    static std::mutex mu;
+    static bool attr = false;
+    std::lock_guard<std::mutex> lock(mu);
     if (!g_tc_error) {
         QG_CUDA(cudaMalloc(&g_tc_error, sizeof(int)));
         QG_CUDA(cudaMemset(g_tc_error, 0, sizeof(int)));
     }
+    if (!attr) {
+        const size_t smem = 2 * TC_A_BYTES + 2 * TC_B_BYTES + 64 + 1024;
+        QG_CUDA(cudaFuncSetAttribute(k32_fused_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        attr = true;
+    }
+    return QG_OK;
+}
+
+int qg_tc_apply_block(float2* amps, int numQubits, const int* targs, const float* devOperands, cudaStream_t st) {
+    if (numQubits < 12) return qg_fail(QG_ERR_ARG, "the tensor-core block kernel needs at least 12 qubits (one 128-group tile)");
+    if (!g_tc_error) QG_TRY(qg_tc_prepare());
     int zeros[5] = {0, 0, 0, 0, 0};
     QubitPlan p;
     QG_TRY(qg_make_plan(numQubits, nullptr, nullptr, 0, targs, zeros, 5, &p));
@@ -317,11 +334,6 @@ int qg_tc_apply_block(float2* amps, int numQubits, const int* targs, const float
     a.ops = devOperands;
     a.errorFlag = g_tc_error;
     size_t smem = 2 * TC_A_BYTES + 2 * TC_B_BYTES + 64 + 1024;
-    static bool attr = false;
-    if (!attr) {
-        QG_CUDA(cudaFuncSetAttribute(k32_fused_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        attr = true;
-    }
     int sms = qg_num_sms();
     qidx grid = std::min<qidx>(a.numTiles, (qidx)sms * 2);
     k32_fused_tc<<<(unsigned)grid, TC_THREADS, smem, st>>>(a);

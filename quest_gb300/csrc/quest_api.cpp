@@ -878,6 +878,181 @@ qreal calcPurity(Qureg q) {
     return q.isDensityMatrix ? v : v * v;
 }
 
+// ---------------------------------------------------------------- FullStateDiagMatr
+// createFullStateDiagMatr / setFullStateDiagMatr / syncFullStateDiagMatr: matrices.cpp;
+// the GPU copy is made at creation and refreshed by every set or sync.
+
+FullStateDiagMatr createFullStateDiagMatr(int k) {
+    const char* func = "createFullStateDiagMatr";
+    FullStateDiagMatr m;
+    std::memset(&m, 0, sizeof(m));
+    if (!check(k >= 1 && k <= 33, func, "Invalid number of qubits for a FullStateDiagMatr.")) return m;
+    m.numQubits = k;
+    m.numElems = (qindex)1 << k;
+    m.numElemsPerNode = m.numElems;
+    m.isGpuAccelerated = 1;
+    int** flags[] = {&m.isApproxUnitary, &m.isApproxHermitian, &m.isApproxNonZero, &m.isStrictlyNonNegative, &m.wasGpuSynced};
+    for (auto f : flags) { *f = (int*)std::malloc(sizeof(int)); **f = -1; }
+    *m.wasGpuSynced = 0;
+    m.cpuElems = (qcomp_t*)std::calloc((size_t)m.numElems, sizeof(qcomp_t));
+    void* g = nullptr;
+    if (!backend(qg_alloc(&g, (int64_t)sizeof(qcomp_t) * m.numElems), func)) return m;
+    m.gpuElems = (qcomp_t*)g;
+    backend(qg_copy_h2d(m.gpuElems, m.cpuElems, (int64_t)sizeof(qcomp_t) * m.numElems, nullptr), func);
+    return m;
+}
+
+void destroyFullStateDiagMatr(FullStateDiagMatr m) {
+    int* flags[] = {m.isApproxUnitary, m.isApproxHermitian, m.isApproxNonZero, m.isStrictlyNonNegative, m.wasGpuSynced};
+    for (auto f : flags) std::free(f);
+    std::free(m.cpuElems);
+    if (m.gpuElems) qg_free(m.gpuElems);
+}
+
+void syncFullStateDiagMatr(FullStateDiagMatr m) {
+    const char* func = "syncFullStateDiagMatr";
+    if (!check(m.cpuElems && m.gpuElems, func, "The FullStateDiagMatr was not created.")) return;
+    backend(qg_copy_h2d(m.gpuElems, m.cpuElems, (int64_t)sizeof(qcomp_t) * m.numElems, nullptr), func);
+    *m.wasGpuSynced = 1;
+    *m.isApproxUnitary = *m.isApproxHermitian = *m.isApproxNonZero = *m.isStrictlyNonNegative = -1;
+}
+
+void setFullStateDiagMatr(FullStateDiagMatr m, qindex start, const qcomp_t* in, qindex num) {
+    const char* func = "setFullStateDiagMatr";
+    if (!check(m.cpuElems && m.gpuElems, func, "The FullStateDiagMatr was not created.")) return;
+    if (!check(start >= 0 && num >= 0 && start + num <= m.numElems, func,
+               "The start index and number of elements exceed the matrix's elements.")) return;
+    std::memcpy(m.cpuElems + start, in, sizeof(qcomp_t) * (size_t)num);
+    backend(qg_copy_h2d(m.gpuElems + start, in, (int64_t)sizeof(qcomp_t) * num, nullptr), func);
+    *m.wasGpuSynced = 1;
+    *m.isApproxUnitary = *m.isApproxHermitian = *m.isApproxNonZero = *m.isStrictlyNonNegative = -1;
+}
+
+namespace {
+
+// validate_matrixFields + validate_matrixAndQuregAreCompatible (validation.cpp)
+bool fsdCompatible(const Qureg& q, const FullStateDiagMatr& m, const char* func) {
+    if (!checkQureg(q, func)) return false;
+    if (!check(m.cpuElems && m.gpuElems, func, "The FullStateDiagMatr was not created.")) return false;
+    return check(m.numQubits == q.numQubits, func,
+                 "The FullStateDiagMatr has a different number of qubits than the Qureg.");
+}
+
+// every |d_i|^2 within epsilon of 1 (the diagonal of a unitary)
+bool fsdUnitary(const FullStateDiagMatr& m, const char* func) {
+    if (*m.isApproxUnitary == -1) {
+        int ok = 1;
+        for (qindex i = 0; i < m.numElems && ok; i++) ok = std::abs(std::norm(C(m.cpuElems[i])) - 1) <= g_eps;
+        *m.isApproxUnitary = ok;
+    }
+    return check(*m.isApproxUnitary == 1, func, "The given matrix was not (approximately) unitary.");
+}
+
+bool fsdHermitian(const FullStateDiagMatr& m, const char* func) {
+    if (*m.isApproxHermitian == -1) {
+        int ok = 1;
+        for (qindex i = 0; i < m.numElems && ok; i++) ok = std::abs(m.cpuElems[i].im) <= g_eps;
+        *m.isApproxHermitian = ok;
+    }
+    return check(*m.isApproxHermitian == 1, func, "The given matrix was not (approximately) Hermitian.");
+}
+
+// validate_matrixExpIsNonDiverging: a (near) zero element under a negative power
+bool fsdNonDiverging(const FullStateDiagMatr& m, cd p, const char* func) {
+    if (p.real() >= 0) return true;
+    for (qindex i = 0; i < m.numElems; i++)
+        if (std::abs(C(m.cpuElems[i])) <= g_eps)
+            return fail(func, "The given exponent is negative and the matrix has a (near) zero element, "
+                              "so the matrix power diverges.");
+    return true;
+}
+
+void fsdApply(Qureg q, FullStateDiagMatr m, cd p, bool multiplyOnly, const char* func) {
+    const bool hasPower = p != cd(1, 0);
+    qg_cplx ex = {p.real(), p.imag()};
+    if (q.isDensityMatrix)
+        backend(qg_dm_allTargDiagMatr(q.gpuAmps, q.numQubits, m.gpuElems, ex, hasPower, multiplyOnly, g_stream), func);
+    else
+        backend(qg_sv_allTargDiagMatr(q.gpuAmps, q.numQubits, m.gpuElems, ex, hasPower, g_stream), func);
+}
+
+// accelerator.cpp:1010-1030: no power (and so no real-power) when the exponent is 1
+cd fsdExpec(Qureg q, FullStateDiagMatr m, cd p, bool useRealPow, const char* func) {
+    const bool hasPower = p != cd(1, 0);
+    qg_cplx ex = {p.real(), p.imag()}, out = {0, 0};
+    if (q.isDensityMatrix)
+        backend(qg_dm_calcExpecFullStateDiagMatr(q.gpuAmps, q.numQubits, m.gpuElems, ex, hasPower, useRealPow && hasPower, &out, g_stream), func);
+    else
+        backend(qg_sv_calcExpecFullStateDiagMatr(q.gpuAmps, q.numQubits, m.gpuElems, ex, hasPower, useRealPow && hasPower, &out, g_stream), func);
+    return cd(out.re, out.im);
+}
+
+}  // namespace
+
+// operations.cpp:537-576
+void multiplyFullStateDiagMatr(Qureg q, FullStateDiagMatr m) {
+    const char* func = "multiplyFullStateDiagMatr";
+    if (!fsdCompatible(q, m, func)) return;
+    fsdApply(q, m, cd(1, 0), true, func);
+}
+
+void multiplyFullStateDiagMatrPower(Qureg q, FullStateDiagMatr m, qcomp_t e) {
+    const char* func = "multiplyFullStateDiagMatrPower";
+    if (!fsdCompatible(q, m, func) || !fsdNonDiverging(m, C(e), func)) return;
+    fsdApply(q, m, C(e), true, func);
+}
+
+void applyFullStateDiagMatr(Qureg q, FullStateDiagMatr m) {
+    const char* func = "applyFullStateDiagMatr";
+    if (!fsdCompatible(q, m, func) || !fsdUnitary(m, func)) return;
+    fsdApply(q, m, cd(1, 0), false, func);
+}
+
+void applyFullStateDiagMatrPower(Qureg q, FullStateDiagMatr m, qcomp_t e) {
+    const char* func = "applyFullStateDiagMatrPower";
+    if (!fsdCompatible(q, m, func) || !fsdUnitary(m, func)) return;
+    if (!check(std::abs(e.im) <= g_eps, func, "The exponent of a unitary matrix must be real so that the result stays unitary."))
+        return;
+    if (!fsdNonDiverging(m, C(e), func)) return;
+    fsdApply(q, m, C(e), false, func);
+}
+
+// calculations.cpp:85-215
+qcomp_t calcExpecNonHermitianFullStateDiagMatr(Qureg q, FullStateDiagMatr m) {
+    const char* func = "calcExpecNonHermitianFullStateDiagMatr";
+    if (!fsdCompatible(q, m, func)) return qcomp_t{0, 0};
+    return Q(fsdExpec(q, m, cd(1, 0), false, func));
+}
+
+qcomp_t calcExpecNonHermitianFullStateDiagMatrPower(Qureg q, FullStateDiagMatr m, qcomp_t e) {
+    const char* func = "calcExpecNonHermitianFullStateDiagMatrPower";
+    if (!fsdCompatible(q, m, func) || !fsdNonDiverging(m, C(e), func)) return qcomp_t{0, 0};
+    return Q(fsdExpec(q, m, C(e), false, func));
+}
+
+qreal calcExpecFullStateDiagMatr(Qureg q, FullStateDiagMatr m) {
+    const char* func = "calcExpecFullStateDiagMatr";
+    if (!fsdCompatible(q, m, func) || !fsdHermitian(m, func)) return 0;
+    cd v = fsdExpec(q, m, cd(1, 0), false, func);
+    if (q.isDensityMatrix && !check(std::abs(v.imag()) <= REDUCTION_EPS_FACTOR * g_eps, func,
+                                    "The calculated expectation value was not approximately real.")) return 0;
+    return v.real();
+}
+
+qreal calcExpecFullStateDiagMatrPower(Qureg q, FullStateDiagMatr m, qreal p) {
+    const char* func = "calcExpecFullStateDiagMatrPower";
+    if (!fsdCompatible(q, m, func) || !fsdHermitian(m, func) || !fsdNonDiverging(m, cd(p, 0), func)) return 0;
+    // validate_matrixExpIsHermitian: a non-integer power of a negative element is not real
+    if (p != std::floor(p))
+        for (qindex i = 0; i < m.numElems; i++)
+            if (!check(m.cpuElems[i].re >= -g_eps, func,
+                       "The matrix has a negative element, so a non-integer power of it is not Hermitian.")) return 0;
+    cd v = fsdExpec(q, m, cd(p, 0), true, func);
+    if (q.isDensityMatrix && !check(std::abs(v.imag()) <= REDUCTION_EPS_FACTOR * g_eps, func,
+                                    "The calculated expectation value was not approximately real.")) return 0;
+    return v.real();
+}
+
 qreal calcProbOfMultiQubitOutcome(Qureg q, int* qs, int* os, int n) {
     const char* func = "calcProbOfMultiQubitOutcome";
     if (!checkQureg(q, func) || !checkQubits(q, qs, n, func, "target qubits")) return 0;

@@ -77,6 +77,46 @@ class Circuit:
     def apply(self, state, impl=IMPL_AUTO, stream=None):
         check(lib().qg_sv32_apply_circuit(self.h, state.ptr, state.num_qubits, impl, stream))
 
+    def autotune(self):
+        """Fuses at the fastest width with the fastest kernel (timed on this GPU);
+        returns (k, impl, {(k, impl): ms per circuit})."""
+        k, impl, n = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        ck, ci, ms = (ctypes.c_int * 8)(), (ctypes.c_int * 8)(), (ctypes.c_double * 8)()
+        check(lib().qg_circuit_autotune(self.h, ctypes.byref(k), ctypes.byref(impl), ck, ci, ms, 8, ctypes.byref(n)))
+        return k.value, impl.value, {(ck[i], ci[i]): ms[i] for i in range(min(n.value, 8))}
+
+    def graph(self, state, impl=IMPL_AUTO):
+        """A CUDA graph of one application of this circuit to `state`."""
+        return Graph(self, state, impl)
+
+
+class Graph:
+    def __init__(self, circuit, state, impl=IMPL_AUTO):
+        h = ctypes.c_void_p()
+        check(lib().qg_circuit_graph_create(circuit.h, state.ptr, state.num_qubits, impl, ctypes.byref(h)))
+        self.h = h
+        self._keep = (circuit, state)
+
+    @property
+    def num_kernels(self):
+        n = ctypes.c_int()
+        check(lib().qg_graph_get_num_kernels(self.h, ctypes.byref(n)))
+        return n.value
+
+    def launch(self, stream=None):
+        check(lib().qg_graph_launch(self.h, stream))
+
+    def close(self):
+        if self.h is not None and self.h.value:
+            lib().qg_graph_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
 
 class StateVector32:
     """An FP32 (complex64) statevector in device memory."""

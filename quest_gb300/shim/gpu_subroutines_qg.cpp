@@ -115,8 +115,12 @@ void gpu_statevec_anyCtrlAnyTargDiagMatr_sub(Qureg q, vector<int> c, vector<int>
 }
 INSTANTIATE_EXPONENTIABLE_CONJUGABLE_FUNC_OPTIMISED_FOR_NUM_CTRLS_AND_TARGS(void, gpu_statevec_anyCtrlAnyTargDiagMatr_sub, (Qureg, vector<int>, vector<int>, vector<int>, DiagMatr, qcomp))
 
-template <bool HasPower> void gpu_statevec_allTargDiagMatr_sub(Qureg, FullStateDiagMatr, qcomp) { unsupported(__func__); }
-template <bool HasPower, bool MultiplyOnly> void gpu_densmatr_allTargDiagMatr_sub(Qureg, FullStateDiagMatr, qcomp) { unsupported(__func__); }
+template <bool HasPower> void gpu_statevec_allTargDiagMatr_sub(Qureg q, FullStateDiagMatr m, qcomp e) {
+    ok(qg_sv_allTargDiagMatr(q.gpuAmps, nq(q), m.gpuElems, C(e), HasPower, nullptr), __func__);
+}
+template <bool HasPower, bool MultiplyOnly> void gpu_densmatr_allTargDiagMatr_sub(Qureg q, FullStateDiagMatr m, qcomp e) {
+    ok(qg_dm_allTargDiagMatr(q.gpuAmps, q.numQubits, m.gpuElems, C(e), HasPower, MultiplyOnly, nullptr), __func__);
+}
 template void gpu_statevec_allTargDiagMatr_sub<true>(Qureg, FullStateDiagMatr, qcomp);
 template void gpu_statevec_allTargDiagMatr_sub<false>(Qureg, FullStateDiagMatr, qcomp);
 template void gpu_densmatr_allTargDiagMatr_sub<true, true>(Qureg, FullStateDiagMatr, qcomp);
@@ -244,8 +248,16 @@ qcomp gpu_densmatr_calcExpecPauliStr_sub(Qureg q, vector<int> x, vector<int> y, 
     ok(qg_dm_calcExpecPauliStr(q.gpuAmps, q.numQubits, P(x), (int)x.size(), P(y), (int)y.size(), P(z), (int)z.size(), &v, nullptr), __func__);
     return qcomp(v.re, v.im);
 }
-template <bool HasPower, bool UseRealPow> qcomp gpu_statevec_calcExpecFullStateDiagMatr_sub(Qureg, FullStateDiagMatr, qcomp) { unsupported(__func__); }
-template <bool HasPower, bool UseRealPow> qcomp gpu_densmatr_calcExpecFullStateDiagMatr_sub(Qureg, FullStateDiagMatr, qcomp) { unsupported(__func__); }
+template <bool HasPower, bool UseRealPow> qcomp gpu_statevec_calcExpecFullStateDiagMatr_sub(Qureg q, FullStateDiagMatr m, qcomp e) {
+    qg_cplx v{0, 0};
+    ok(qg_sv_calcExpecFullStateDiagMatr(q.gpuAmps, nq(q), m.gpuElems, C(e), HasPower, UseRealPow, &v, nullptr), __func__);
+    return qcomp(v.re, v.im);
+}
+template <bool HasPower, bool UseRealPow> qcomp gpu_densmatr_calcExpecFullStateDiagMatr_sub(Qureg q, FullStateDiagMatr m, qcomp e) {
+    qg_cplx v{0, 0};
+    ok(qg_dm_calcExpecFullStateDiagMatr(q.gpuAmps, q.numQubits, m.gpuElems, C(e), HasPower, UseRealPow, &v, nullptr), __func__);
+    return qcomp(v.re, v.im);
+}
 template qcomp gpu_statevec_calcExpecFullStateDiagMatr_sub<true, true>(Qureg, FullStateDiagMatr, qcomp);
 template qcomp gpu_statevec_calcExpecFullStateDiagMatr_sub<true, false>(Qureg, FullStateDiagMatr, qcomp);
 template qcomp gpu_statevec_calcExpecFullStateDiagMatr_sub<false, true>(Qureg, FullStateDiagMatr, qcomp);

@@ -5,7 +5,7 @@ own sources by `make -C oracle ref REF=<QuEST sources>`).
 Each fixture stores the circuit text, the input amplitudes, and the reference's
 output amplitudes, reduction results and sampled measurement outcomes.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [case names]
 """
 import os
 import sys
@@ -29,6 +29,8 @@ CASES = [
     ("dm5_every", 5, 1, "every", 24),
     ("sv12_config1", 12, 0, "config1", 31),
     ("dm6_config3", 6, 1, "config3", 41),
+    ("sv5_fullstate_diag", 5, 0, "fsd", 51),
+    ("dm3_fullstate_diag", 3, 1, "fsd", 52),
 ]
 
 
@@ -82,6 +84,8 @@ def make_case(name, nq, is_dm, kind, seed):
         text = qc.every_op_circuit(nq, is_dm, seed)
     elif kind == "config1":
         text = qc.config1_circuit(nq, 3, seed)
+    elif kind == "fsd":
+        text = qc.fullstate_diag_circuit(nq, is_dm, seed)
     else:
         text = config3_circuit(nq, 3, seed)
     amps = qc.random_density_matrix(nq, seed) if is_dm else qc.random_statevector(nq, seed)
@@ -92,7 +96,10 @@ def main():
     ref = qc.reference()
     if ref is None:
         sys.exit("the reference library is not built: make -C oracle ref REF=<QuEST sources>")
+    only = set(sys.argv[1:])          # optional: names of the cases to (re)generate
     for name, nq, is_dm, kind, seed in CASES:
+        if only and name not in only:
+            continue
         text, amps = make_case(name, nq, is_dm, kind, seed)
         out, res, outs = ref.run(text, nq, is_dm, amps)
         np.savez_compressed(os.path.join(HERE, name + ".npz"), text=np.array(text), nq=nq, is_dm=is_dm,

@@ -128,3 +128,54 @@ def test_normalise_rescales_to_the_target_probability(env):
         assert abs(s.total_prob() - 0.5) < 1e-6
     finally:
         s.free()
+
+
+@pytest.mark.parametrize("impl", [1, 2])
+def test_graph_replays_the_circuit(env, impl):
+    """A CUDA graph of the block kernels gives the same bits as applying the circuit."""
+    from quest_gb300.fused import Circuit, StateVector32
+    n = 14
+    rng = np.random.default_rng(21)
+    gates = brickwork(n, 6, rng)
+    amps = qc.random_statevector(n, 21)
+    c = Circuit(n)
+    for t, m in gates:
+        c.add(t, m)
+    c.fuse(5)
+    direct, replay = StateVector32(n), StateVector32(n)
+    try:
+        direct.set(amps)
+        c.apply(direct, impl=impl)
+        c.apply(direct, impl=impl)
+        replay.set(amps)
+        g = c.graph(replay, impl=impl)
+        assert g.num_kernels == c.num_blocks
+        g.launch()
+        g.launch()
+        g.close()
+        assert np.array_equal(direct.get().view(np.float32), replay.get().view(np.float32))
+    finally:
+        direct.free()
+        replay.free()
+
+
+def test_autotune_fuses_at_the_fastest_candidate(env):
+    from quest_gb300.fused import Circuit, StateVector32
+    n = 16
+    rng = np.random.default_rng(22)
+    gates = brickwork(n, 8, rng)
+    amps = qc.random_statevector(n, 22)
+    c = Circuit(n)
+    for t, m in gates:
+        c.add(t, m)
+    k, impl, ms = c.autotune()
+    assert (k, impl) == min(ms, key=ms.get)
+    assert set(ms) == {(3, 1), (4, 1), (5, 1), (5, 2)}
+    s = StateVector32(n)
+    try:
+        s.set(amps)
+        c.apply(s)                       # automatic: the tuned kernel
+        got = s.get().astype(np.complex128)
+    finally:
+        s.free()
+    assert fidelity(got, run_oracle(n, amps, gates)) >= 1 - 1e-6

@@ -274,3 +274,44 @@ def test_abi_rejects_bad_arguments(env):
         assert L.qg_sv_anyCtrlOneTargDenseMatr(None, 3, None, None, 0, 0, m, None) == -2
     finally:
         env.Q.destroyQureg(q)
+
+
+@pytest.mark.parametrize("nq,is_dm,seed", [(1, 0, 61), (5, 0, 62), (12, 0, 63), (1, 1, 64), (4, 1, 65), (6, 1, 66)])
+def test_fullstate_diag_vs_oracle(env, nq, is_dm, seed):
+    """FullStateDiagMatr: apply / multiply with and without powers, and the four
+    expectation forms, on statevectors and density matrices."""
+    text = qc.fullstate_diag_circuit(nq, is_dm, seed)
+    amps = qc.random_density_matrix(nq, seed) if is_dm else qc.random_statevector(nq, seed)
+    a1, r1, _ = qc.oracle().run(text, nq, is_dm, amps)
+    a2, r2, _ = run_gpu(env, text, nq, is_dm, amps)
+    assert np.max(np.abs(a1 - a2)) <= TOL
+    assert r1.size == r2.size and np.max(np.abs(r1 - r2)) <= TOL
+
+
+def test_fullstate_diag_validation(env):
+    """The reference's checks: apply needs a unitary diagonal, the Hermitian expectation a
+    real one, and a negative power of a zero element diverges."""
+    from quest_gb300.api import QuESTError, full_state_diag
+    from quest_gb300._lib import qg_cplx
+    Q = env.Q
+    q = Q.createQureg(3)
+    try:
+        bad = full_state_diag(np.full(8, 0.5 + 0j))
+        with pytest.raises(QuESTError):
+            Q.applyFullStateDiagMatr(q, bad)
+        Q.multiplyFullStateDiagMatr(q, bad)            # non-unitary is fine for multiply
+        Q.destroyFullStateDiagMatr(bad)
+        cplx = full_state_diag(np.full(8, 1j))
+        with pytest.raises(QuESTError):
+            Q.calcExpecFullStateDiagMatr(q, cplx)
+        Q.destroyFullStateDiagMatr(cplx)
+        zero = full_state_diag(np.zeros(8, dtype=complex))
+        with pytest.raises(QuESTError):
+            Q.multiplyFullStateDiagMatrPower(q, zero, qg_cplx(-1.0, 0.0))
+        Q.destroyFullStateDiagMatr(zero)
+        wrong = full_state_diag(np.ones(16, dtype=complex))
+        with pytest.raises(QuESTError):
+            Q.applyFullStateDiagMatr(q, wrong)
+        Q.destroyFullStateDiagMatr(wrong)
+    finally:
+        Q.destroyQureg(q)
