@@ -231,6 +231,11 @@ int qg_dm_calcExpecPauliStr(const void* amps, int numKetQubits, const int* targs
  * Strings are given as (maskXY, maskYZ, numY) triples; out[s] is string s's value. */
 int qg_sv_calcExpecPauliStrBatch(const void* amps, int numQubits, const int64_t* masksXY, const int64_t* masksYZ,
                                  const int* numsY, int numStrings, qg_cplx* out, void* stream);
+/* the density-matrix form (no one-pass counterpart in the reference, which runs one
+ * gpu_densmatr_calcExpecPauliStr_sub per string, gpu_subroutines.hpp:174): masks on the
+ * ket qubits; up to 16 strings per pass over the 2^N columns */
+int qg_dm_calcExpecPauliStrBatch(const void* amps, int numKetQubits, const int64_t* masksXY, const int64_t* masksYZ,
+                                 const int* numsY, int numStrings, qg_cplx* out, void* stream);
 
 /* The same batched Pauli expectation values, for callers that cannot allocate
  * device or pinned memory during the call (their HBM is reserved up front by

@@ -95,6 +95,7 @@ ABI = {
     "qg_sv_calcExpecPauliStr": [vp, I, c_int_p, I, c_int_p, I, c_int_p, I, c_cplx_p, vp],
     "qg_dm_calcExpecPauliStr": [vp, I, c_int_p, I, c_int_p, I, c_int_p, I, c_cplx_p, vp],
     "qg_sv_calcExpecPauliStrBatch": [vp, I, c_i64_p, c_i64_p, c_int_p, I, c_cplx_p, vp],
+    "qg_dm_calcExpecPauliStrBatch": [vp, I, c_i64_p, c_i64_p, c_int_p, I, c_cplx_p, vp],
     "qg_sv_calcExpecPauliStrBatch_noalloc": [vp, I, c_i64_p, c_i64_p, c_int_p, I, c_cplx_p, vp],
     "qg_circuit_create": [ctypes.POINTER(vp), I],
     "qg_circuit_destroy": [vp],

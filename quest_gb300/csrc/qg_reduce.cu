@@ -145,6 +145,37 @@ __global__ void __launch_bounds__(RED_THREADS) k_expec_pauli_batch(const double2
     block_reduce_and_finish<2 * NS>(v, out);
 }
 
+// Density-matrix form of the batch: per column n and string s the element
+// rho[n ^ maskXY_s][n] with its sign; NS strings per pass over the 2^N columns.
+template <int NS>
+__global__ void __launch_bounds__(RED_THREADS) k_dm_expec_pauli_batch(const double2* __restrict__ a, qidx dim,
+                                                                     const qidx* __restrict__ mXY, const qidx* __restrict__ mYZ,
+                                                                     int numStrings, RedOut out) {
+    double v[2 * NS];
+#pragma unroll
+    for (int k = 0; k < 2 * NS; k++) v[k] = 0.0;
+    __shared__ qidx sXY[NS], sYZ[NS];
+    if (threadIdx.x < NS) {
+        sXY[threadIdx.x] = threadIdx.x < numStrings ? mXY[threadIdx.x] : 0;
+        sYZ[threadIdx.x] = threadIdx.x < numStrings ? mYZ[threadIdx.x] : 0;
+    }
+    __syncthreads();
+    qidx stride = (qidx)gridDim.x * RED_THREADS;
+    for (qidx n = blockIdx.x * (qidx)RED_THREADS + threadIdx.x; n < dim; n += stride) {
+#pragma unroll
+        for (int s = 0; s < NS; s++) {
+            if (s < numStrings) {
+                qidx i = n ^ sXY[s];
+                double2 x = __ldg(a + i + n * dim);
+                double sg = parity64(i & sYZ[s]) ? -1.0 : 1.0;
+                v[2 * s] += sg * x.x;
+                v[2 * s + 1] += sg * x.y;
+            }
+        }
+    }
+    block_reduce_and_finish<2 * NS>(v, out);
+}
+
 // histogram of all outcomes of `num` qubits, one bin per blockIdx.y (deterministic)
 template <int NB>
 __global__ void __launch_bounds__(RED_THREADS) k_probs_all(const double2* __restrict__ a, qidx numIts, Ins ins,
@@ -387,10 +418,36 @@ int qg_dm_calcExpecPauliStr(const void* amps, int nKet, const int* x, int nx, co
     return QG_OK;
 }
 
+}  // extern "C"
+
+namespace {
+int expec_pauli_batch(const void* amps, int numQubits, bool dm, const int64_t* masksXY, const int64_t* masksYZ,
+                      const int* numsY, int numStrings, qg_cplx* out, void* stream);
+}  // namespace
+
+extern "C" {
+
 int qg_sv_calcExpecPauliStrBatch(const void* amps, int numQubits, const int64_t* masksXY, const int64_t* masksYZ,
                                  const int* numsY, int numStrings, qg_cplx* out, void* stream) {
     QG_TRY(qg_check_amps(amps, numQubits));
+    return expec_pauli_batch(amps, numQubits, false, masksXY, masksYZ, numsY, numStrings, out, stream);
+}
+
+int qg_dm_calcExpecPauliStrBatch(const void* amps, int numKetQubits, const int64_t* masksXY, const int64_t* masksYZ,
+                                 const int* numsY, int numStrings, qg_cplx* out, void* stream) {
+    QG_TRY(check_dm_amps(amps, numKetQubits));
+    return expec_pauli_batch(amps, numKetQubits, true, masksXY, masksYZ, numsY, numStrings, out, stream);
+}
+
+}  // extern "C"
+
+namespace {
+
+// up to 16 strings per pass; numQubits = the ket qubits of a density matrix
+int expec_pauli_batch(const void* amps, int numQubits, bool dm, const int64_t* masksXY, const int64_t* masksYZ,
+                      const int* numsY, int numStrings, qg_cplx* out, void* stream) {
     if (numStrings < 0) return qg_fail(QG_ERR_ARG, "negative string count");
+    if (numStrings > 0 && (!masksXY || !masksYZ || !numsY || !out)) return qg_fail(QG_ERR_ARG, "null argument");
     qidx lim = ((qidx)1 << numQubits) - 1;
     for (int s = 0; s < numStrings; s++)
         if ((masksXY[s] & ~lim) || (masksYZ[s] & ~lim)) return qg_fail(QG_ERR_ARG, "Pauli string %d targets a qubit beyond %d", s, numQubits);
@@ -408,12 +465,16 @@ int qg_sv_calcExpecPauliStrBatch(const void* amps, int numQubits, const int64_t*
         char* base = (char*)s;
         r.ticket = (unsigned int*)base;
         r.result = (double*)(base + 256);
-        qidx* dm = (qidx*)(base + 256 + 8 * 2 * NS);
+        qidx* dmask = (qidx*)(base + 256 + 8 * 2 * NS);
         r.partials = (double*)(base + 256 + 8 * 2 * NS + 8 * 2 * NS);
         std::vector<qidx> hm(2 * NS, 0);
         for (int k = 0; k < cnt; k++) { hm[k] = masksXY[s0 + k]; hm[NS + k] = masksYZ[s0 + k]; }
-        QG_CUDA(cudaMemcpyAsync(dm, hm.data(), 8 * 2 * NS, cudaMemcpyHostToDevice, st));
-        k_expec_pauli_batch<NS><<<grid, RED_THREADS, 0, st>>>((const double2*)amps, n, dm, dm + NS, cnt, r);
+        QG_CUDA(cudaMemcpyAsync(dmask, hm.data(), 8 * 2 * NS, cudaMemcpyHostToDevice, st));
+        if (dm)
+            k_dm_expec_pauli_batch<NS><<<grid, RED_THREADS, 0, st>>>((const double2*)amps, n, dmask, dmask + NS, cnt, r);
+        else
+            k_expec_pauli_batch<NS><<<grid, RED_THREADS, 0, st>>>((const double2*)amps, n, dmask, dmask + NS, cnt, r);
+        qg_note_launch();
         double v[2 * NS];
         QG_TRY(red_fetch(r, 2 * NS, v, st));
         for (int k = 0; k < cnt; k++) {
@@ -426,4 +487,5 @@ int qg_sv_calcExpecPauliStrBatch(const void* amps, int numQubits, const int64_t*
     return QG_OK;
 }
 
-}  // extern "C"
+}  // namespace
+

@@ -1098,10 +1098,6 @@ qreal calcExpecPauliStr(Qureg q, PauliStr str) {
 void calcExpecPauliStrs(qreal* out, Qureg q, const PauliStr* strs, int num) {
     const char* func = "calcExpecPauliStrs";
     if (!checkQureg(q, func)) return;
-    if (q.isDensityMatrix) {
-        for (int s = 0; s < num; s++) out[s] = calcExpecPauliStr(q, strs[s]);
-        return;
-    }
     vector<int64_t> mxy(num), myz(num);
     vector<int> ny(num);
     for (int s = 0; s < num; s++) {
@@ -1117,8 +1113,14 @@ void calcExpecPauliStrs(qreal* out, Qureg q, const PauliStr* strs, int num) {
         ny[s] = numY(codes);
     }
     vector<qcomp_t> v(num);
-    if (!backend(qg_sv_calcExpecPauliStrBatch(q.gpuAmps, q.numQubits, mxy.data(), myz.data(), ny.data(), num, v.data(), g_stream), func)) return;
-    for (int s = 0; s < num; s++) out[s] = v[s].re;
+    int rc = q.isDensityMatrix
+                 ? qg_dm_calcExpecPauliStrBatch(q.gpuAmps, q.numQubits, mxy.data(), myz.data(), ny.data(), num, v.data(), g_stream)
+                 : qg_sv_calcExpecPauliStrBatch(q.gpuAmps, q.numQubits, mxy.data(), myz.data(), ny.data(), num, v.data(), g_stream);
+    if (!backend(rc, func)) return;
+    for (int s = 0; s < num; s++) {
+        if (!check(std::abs(v[s].im) <= REDUCTION_EPS_FACTOR * g_eps, func, "The expectation value was not approximately real.")) return;
+        out[s] = v[s].re;
+    }
 }
 
 }  // extern "C"

@@ -315,3 +315,25 @@ def test_fullstate_diag_validation(env):
         Q.destroyFullStateDiagMatr(wrong)
     finally:
         Q.destroyQureg(q)
+
+
+@pytest.mark.parametrize("nq,is_dm", [(9, 0), (5, 1), (7, 1)])
+def test_pauli_batch_matches_oracle(env, nq, is_dm):
+    """calcExpecPauliStrs (one pass per 16 strings, statevector and density matrix)
+    against the oracle's one-string-at-a-time expectations; 40 strings cross a pass
+    boundary."""
+    import ctypes
+    rng = np.random.default_rng(70 + nq + is_dm)
+    codes = [[int(v) for v in rng.integers(0, 4, nq)] for _ in range(40)]
+    amps = qc.random_density_matrix(nq, 70 + nq) if is_dm else qc.random_statevector(nq, 70 + nq)
+    _, want, _ = qc.oracle().run("".join(f"EXPEC {qc.pauli_text(c)}\n" for c in codes), nq, is_dm, amps)
+    Q = env.Q
+    q = Q.createDensityQureg(nq) if is_dm else Q.createQureg(nq)
+    try:
+        env.set_amps(q, amps)
+        strs = (env.PauliStr * len(codes))(*[env.pauli_str(c) for c in codes])
+        got = (ctypes.c_double * len(codes))()
+        Q.calcExpecPauliStrs(got, q, strs, len(codes))
+    finally:
+        Q.destroyQureg(q)
+    assert np.max(np.abs(np.array(list(got)) - want)) <= TOL
