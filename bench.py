@@ -487,7 +487,7 @@ def run_precision(args, world, rank, local, dist):
     _lib.check(L.qg_init(local))
     api.init_env()
     nq, na, depth = args.qubits, args.acc_qubits, args.depth
-    impl = {"simt": IMPL_SIMT, "tc": IMPL_TC, "tc2": 3}[args.fused_impl]
+    impl = {"simt": IMPL_SIMT, "tc": IMPL_TC}[args.fused_impl]
 
     # ---- accuracy at na qubits (0: skipped)
     fid = maxabs = experr = drift = None
@@ -550,7 +550,7 @@ def run_precision(args, world, rank, local, dist):
                                    f"<=5-qubit blocks", "qubits": nq, "depth": depth, "gates": len(gates),
                        "blocks": nblocks, "impl": args.fused_impl},
             "circuits_per_s": round(world * args.steps / t, 3), "ms_per_block_pass": round(per_pass_ms, 3),
-            "roofline": {"bound": "hbm", "kernel": {IMPL_TC: "k32_fused_tc", 3: "k32_fused_tc2"}.get(impl, "k32_fused"),
+            "roofline": {"bound": "hbm", "kernel": "k32_fused_tc" if impl == IMPL_TC else "k32_fused",
                          "achieved": round(eff / world, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(eff / world / peak, 4), "traffic": None,
                          "tensor_tflops": round(tensor_flops * args.steps / t / 1e12, 1)},
@@ -722,7 +722,7 @@ def main():
     ap.add_argument("--fp64-products", default="fixed", choices=["fixed", "fp64"],
                     help="plain: general complex 2x2 products in block-floating fixed point (default) or IEEE FP64")
     ap.add_argument("--acc-qubits", type=int, default=28, help="precision form: qubits of the accuracy check (0 skips it)")
-    ap.add_argument("--fused-impl", default="tc", choices=["tc", "tc2", "simt"])
+    ap.add_argument("--fused-impl", default="tc", choices=["tc", "simt"])
     args = ap.parse_args()
     world, rank, local, dist = dist_setup()
     if args.config == "serve":

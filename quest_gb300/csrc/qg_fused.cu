@@ -29,8 +29,7 @@
 // tensor-core operand builder, defined in qg_fused_tc.cu
 size_t qg_tc_operand_floats();
 void qg_tc_build_operands(const std::complex<double>* m32x32, float* out);
-int qg_tc_apply_block(float2* amps, int numQubits, const int* targs, const float* devOperands, cudaStream_t st,
-                      bool pipelined);
+int qg_tc_apply_block(float2* amps, int numQubits, const int* targs, const float* devOperands, cudaStream_t st);
 bool qg_tc_supported(int numQubits);
 int qg_tc_prepare();
 
@@ -596,9 +595,9 @@ int qg_sv32_apply_circuit(qg_circuit* c, void* amps, int numQubits, int impl, vo
     cudaStream_t st = qg_stream(stream);
     if (impl == 0 && c->preferredImpl != 0) impl = c->preferredImpl;
     for (const QgBlock& b : c->blocks) {
-        bool tc = b.targs.size() == 5 && (impl >= 2 || (impl == 0 && qg_tc_supported(numQubits)));
+        bool tc = b.targs.size() == 5 && (impl == 2 || (impl == 0 && qg_tc_supported(numQubits)));
         if (tc) {
-            QG_TRY(qg_tc_apply_block((float2*)amps, numQubits, b.targs.data(), c->devTC + b.offTC, st, impl == 3));
+            QG_TRY(qg_tc_apply_block((float2*)amps, numQubits, b.targs.data(), c->devTC + b.offTC, st));
         } else {
             QG_TRY(launch_fused_simt((float2*)amps, numQubits, b.targs, c->devF32 + b.off32, st));
         }

@@ -138,6 +138,18 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
     return ok != 0;
 }
 
+// bounded wait on an mbarrier phase; false if it ran out.  The clock is read once
+// per 256 polls, not per poll.
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = globaltimer_ns();
+    for (;;) {
+        for (int i = 0; i < 256; i++)
+            if (mbar_try_wait(bar, parity)) return true;
+        if (globaltimer_ns() - t0 > TC_WAIT_NS) return false;
+    }
+}
+
 #define TMEM_LD16(taddr, r)                                                                              \
     asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];" \
                  : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),    \
@@ -252,12 +264,7 @@ __global__ void __launch_bounds__(TC_THREADS, 2) k32_fused_tc(TcArgs args) {
         }
 
         // ---- every thread waits for the MMAs (bounded by %globaltimer)
-        {
-            const uint64_t t0 = globaltimer_ns();
-            while (!mbar_try_wait(barAddr, phase)) {
-                if (globaltimer_ns() - t0 > TC_WAIT_NS) { *abortFlag = 1; break; }
-            }
-        }
+        if (!mbar_wait_bounded(barAddr, phase)) *abortFlag = 1;
         phase ^= 1;
         __syncthreads();
         if (*abortFlag) {
@@ -290,189 +297,6 @@ __global__ void __launch_bounds__(TC_THREADS, 2) k32_fused_tc(TcArgs args) {
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(TC_TMEM_COLS));
 }
 
-// ---------------------------------------------------------------- pipelined kernel
-//
-// One CTA of 256 threads per SM.  Thread (row g = tid & 127, half h = tid >> 7) owns
-// group g's matrix indices j in [16h, 16h+16) of every tile: it copies those 16
-// amplitudes from global memory into a 3-stage shared-memory ring with cp.async
-// (8 bytes each, straight from global to shared), later splits them into the TF32
-// hi/lo operand rows, and finally stores its group's outputs k in [16h, 16h+16).
-// Every thread touches only its own ring slots, so a thread's own cp.async wait is
-// the only synchronisation the ring needs.  Two TMEM accumulator sets (2 x 128
-// columns) let tile k's MMAs run while tile k-1's results are read out and stored;
-// the single A operand buffer is reused once tile k-1's MMAs have completed.
-
-#define TC2_THREADS 256
-#define TC2_STAGES 3
-#define TC2_RAW_BYTES (TC_M * 32 * 8)      // one tile of raw amplitudes, [j][group] float2: 32 KiB
-#define TC2_TMEM_COLS 256                  // two accumulator sets of (64 large + 64 small) columns
-#define TC2_SMEM (2 * TC_A_BYTES + 2 * TC_B_BYTES + TC2_STAGES * TC2_RAW_BYTES + 64 + 1024)
-
-__device__ __forceinline__ void cp_async8(uint32_t dst, const void* src) {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" :: "r"(dst), "l"(src) : "memory");
-}
-
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-
-// bounded wait on an mbarrier phase; false if it ran out
-__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
-    const uint64_t t0 = globaltimer_ns();
-    while (!mbar_try_wait(bar, parity))
-        if (globaltimer_ns() - t0 > TC_WAIT_NS) return false;
-    return true;
-}
-
-__global__ void __launch_bounds__(TC2_THREADS, 1) k32_fused_tc2(TcArgs args) {
-    extern __shared__ __align__(1024) unsigned char smem_raw[];
-    unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    float* sAh = (float*)smem;
-    float* sAl = (float*)(smem + TC_A_BYTES);
-    float* sBh = (float*)(smem + 2 * TC_A_BYTES);
-    float2* sRaw = (float2*)(smem + 2 * TC_A_BYTES + 2 * TC_B_BYTES);
-    uint64_t* bar = (uint64_t*)(smem + 2 * TC_A_BYTES + 2 * TC_B_BYTES + TC2_STAGES * TC2_RAW_BYTES);
-    uint32_t* tmemSlot = (uint32_t*)(bar + 2);
-    volatile int* abortFlag = (volatile int*)(tmemSlot + 1);
-
-    const int tid = threadIdx.x, warp = tid >> 5;
-    const int row = tid & (TC_M - 1), half = tid >> 7;
-    const qidx numTiles = args.numTiles;
-    const qidx grid = gridDim.x;
-    qidx myTiles = 0;
-    if ((qidx)blockIdx.x < numTiles) myTiles = (numTiles - 1 - blockIdx.x) / grid + 1;
-    if (myTiles == 0) return;
-
-    {   // stage Bh, Bl once (already in the tile layout)
-        const float4* src = (const float4*)args.ops;
-        float4* dst = (float4*)sBh;
-        for (int i = tid; i < (2 * TC_B_BYTES) / 16; i += TC2_THREADS) dst[i] = __ldg(src + i);
-    }
-    if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_addr(bar)), "r"(1));
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_addr(bar + 1)), "r"(1));
-        asm volatile("fence.mbarrier_init.release.cluster;");
-        *abortFlag = 0;
-    }
-    if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" :: "r"(smem_addr(tmemSlot)), "r"(TC2_TMEM_COLS));
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
-    }
-    asm volatile("fence.proxy.async.shared::cta;");
-    asm volatile("tcgen05.fence::before_thread_sync;");
-    __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;");
-    const uint32_t tmem = *tmemSlot;
-    const uint32_t idesc = make_idesc();
-    const uint32_t aH = smem_addr(sAh), aL = smem_addr(sAl), bH = smem_addr(sBh), bL = bH + TC_B_BYTES;
-    const uint32_t raw0 = smem_addr(sRaw);
-
-    // this thread's 16 amplitudes of tile number t (t-th tile of this CTA) into ring stage t % STAGES
-    auto issue_loads = [&](qidx t) {
-        if (t < myTiles) {
-            const qidx tile = blockIdx.x + t * grid;
-            const qidx base = insert_bits<5>(tile * TC_M + row, args.ins);
-            const uint32_t st = raw0 + (uint32_t)(t % TC2_STAGES) * TC2_RAW_BYTES;
-#pragma unroll
-            for (int i = 0; i < 16; i++) {
-                const int j = 16 * half + i;
-                cp_async8(st + (uint32_t)(j * TC_M + row) * 8, args.amps + base + args.off[j]);
-            }
-        }
-        cp_async_commit();     // one group per tile number, empty past the end
-    };
-
-    // tile number t's outputs of this thread, from TMEM set t & 1
-    auto epilogue = [&](qidx t) {
-        const qidx tile = blockIdx.x + t * grid;
-        const qidx base = insert_bits<5>(tile * TC_M + row, args.ins);
-        const uint32_t taddr = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(t & 1) * 128 + 32 * half;
-#pragma unroll
-        for (int c = 0; c < 2; c++) {
-            uint32_t big[16], small[16];
-            TMEM_LD16(taddr + 16 * c, big);
-            TMEM_LD16(taddr + TC_N + 16 * c, small);
-            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-            for (int k = 0; k < 8; k++) {
-                const float re = __uint_as_float(small[2 * k]) + __uint_as_float(big[2 * k]);
-                const float im = __uint_as_float(small[2 * k + 1]) + __uint_as_float(big[2 * k + 1]);
-                __stcs(args.amps + base + args.off[16 * half + 8 * c + k], make_float2(re, im));
-            }
-        }
-    };
-
-#pragma unroll 1
-    for (int s = 0; s < TC2_STAGES - 1; s++) issue_loads(s);
-
-    bool aborted = false;
-    for (qidx t = 0; t < myTiles; t++) {
-        issue_loads(t + TC2_STAGES - 1);
-        asm volatile("cp.async.wait_group %0;" :: "n"(TC2_STAGES - 1) : "memory");   // tile t has landed
-        // the A buffers are free once tile t-1's MMAs have completed
-        if (t > 0 && !mbar_wait_bounded(smem_addr(bar + ((t - 1) & 1)), (uint32_t)(((t - 1) >> 1) & 1))) *abortFlag = 1;
-
-        // ---- split this thread's 16 amplitudes into TF32 hi/lo operand rows (kk = 2j + c)
-        const float2* raw = sRaw + (size_t)(t % TC2_STAGES) * (TC2_RAW_BYTES / 8);
-#pragma unroll
-        for (int q = 0; q < 8; q++) {
-            const int j = 16 * half + 2 * q;
-            const float2 x0 = raw[j * TC_M + row], x1 = raw[(j + 1) * TC_M + row];
-            float4 h, l;
-            h.x = tf32_hi(x0.x); l.x = tf32_hi(x0.x - h.x);
-            h.y = tf32_hi(x0.y); l.y = tf32_hi(x0.y - h.y);
-            h.z = tf32_hi(x1.x); l.z = tf32_hi(x1.x - h.z);
-            h.w = tf32_hi(x1.y); l.w = tf32_hi(x1.y - h.w);
-            const unsigned o = core_offset(row, 2 * j, TC_M);
-            *(float4*)((unsigned char*)sAh + o) = h;
-            *(float4*)((unsigned char*)sAl + o) = l;
-        }
-        asm volatile("fence.proxy.async.shared::cta;");
-        asm volatile("tcgen05.fence::before_thread_sync;");
-        __syncthreads();
-        asm volatile("tcgen05.fence::after_thread_sync;");
-        if (*abortFlag) { aborted = true; break; }
-
-        // ---- one thread issues tile t's 24 MMAs into TMEM set t & 1 and commits them
-        if (tid == 0) {
-            const uint32_t lboA = (TC_M / 8) * 128, lboB = (TC_N / 8) * 128, sbo = 128;
-            const uint32_t dset = tmem + (uint32_t)(t & 1) * 128;
-            for (int part = 0; part < 3; part++) {
-                const uint32_t a = (part == 0) ? aL : aH;
-                const uint32_t b = (part == 1) ? bL : bH;
-                const uint32_t d = (part == 2) ? dset : dset + TC_N;
-                uint32_t acc = (part == 1) ? 1u : 0u;
-#pragma unroll
-                for (int s = 0; s < TC_K / 8; s++) {
-                    mma_tf32(d, make_desc(a + s * 2 * lboA, lboA, sbo), make_desc(b + s * 2 * lboB, lboB, sbo), idesc, acc);
-                    acc = 1;
-                }
-            }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
-                         :: "r"(smem_addr(bar + (t & 1))) : "memory");
-        }
-
-        // ---- while they run: tile t-1's results (its MMAs completed above)
-        if (t > 0) {
-            asm volatile("tcgen05.fence::after_thread_sync;");
-            epilogue(t - 1);
-            asm volatile("tcgen05.fence::before_thread_sync;");
-        }
-    }
-    if (!aborted) {
-        const qidx last = myTiles - 1;
-        if (!mbar_wait_bounded(smem_addr(bar + (last & 1)), (uint32_t)((last >> 1) & 1))) *abortFlag = 1;
-        __syncthreads();
-        if (!*abortFlag) {
-            asm volatile("tcgen05.fence::after_thread_sync;");
-            epilogue(last);
-        }
-    }
-    if (*abortFlag && tid == 0) atomicExch(args.errorFlag, 1);
-    asm volatile("cp.async.wait_all;" ::: "memory");
-    asm volatile("tcgen05.fence::before_thread_sync;");
-    __syncthreads();
-    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(TC2_TMEM_COLS));
-}
-
 // ---------------------------------------------------------------- host: launch
 
 namespace {
@@ -494,14 +318,12 @@ int qg_tc_prepare() {
     if (!attr) {
         const size_t smem = 2 * TC_A_BYTES + 2 * TC_B_BYTES + 64 + 1024;
         QG_CUDA(cudaFuncSetAttribute(k32_fused_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        QG_CUDA(cudaFuncSetAttribute(k32_fused_tc2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC2_SMEM));
         attr = true;
     }
     return QG_OK;
 }
 
-int qg_tc_apply_block(float2* amps, int numQubits, const int* targs, const float* devOperands, cudaStream_t st,
-                      bool pipelined) {
+int qg_tc_apply_block(float2* amps, int numQubits, const int* targs, const float* devOperands, cudaStream_t st) {
     if (numQubits < 12) return qg_fail(QG_ERR_ARG, "the tensor-core block kernel needs at least 12 qubits (one 128-group tile)");
     if (!g_tc_error) QG_TRY(qg_tc_prepare());
     int zeros[5] = {0, 0, 0, 0, 0};
@@ -519,12 +341,6 @@ int qg_tc_apply_block(float2* amps, int numQubits, const int* targs, const float
     a.ops = devOperands;
     a.errorFlag = g_tc_error;
     int sms = qg_num_sms();
-    if (pipelined) {
-        qidx grid = std::min<qidx>(a.numTiles, (qidx)sms);
-        k32_fused_tc2<<<(unsigned)grid, TC2_THREADS, TC2_SMEM, st>>>(a);
-        qg_note_launch();
-        return qg_check_launch("k32_fused_tc2");
-    }
     size_t smem = 2 * TC_A_BYTES + 2 * TC_B_BYTES + 64 + 1024;
     qidx grid = std::min<qidx>(a.numTiles, (qidx)sms * 2);
     k32_fused_tc<<<(unsigned)grid, TC_THREADS, smem, st>>>(a);

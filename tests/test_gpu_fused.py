@@ -58,7 +58,7 @@ def fidelity(a, b):
 
 
 @pytest.mark.parametrize("n,depth", [(12, 6), (15, 8), (18, 10)])
-@pytest.mark.parametrize("impl", [1, 2, 3])
+@pytest.mark.parametrize("impl", [1, 2])
 def test_fused_brickwork_vs_fp64_oracle(env, n, depth, impl):
     rng = np.random.default_rng(n * 10 + depth)
     gates = brickwork(n, depth, rng)
@@ -88,12 +88,9 @@ def test_single_5qubit_block_every_layout(env, targs):
     scale = np.max(np.abs(ref))
     simt, _ = run_fused(env, n, amps, [(targs, u)], 5, 1)
     tc, _ = run_fused(env, n, amps, [(targs, u)], 5, 2)
-    tc2, _ = run_fused(env, n, amps, [(targs, u)], 5, 3)
     assert np.max(np.abs(simt - ref)) <= 2e-6 * scale
     assert np.max(np.abs(tc - ref)) <= 2e-6 * scale
     assert np.max(np.abs(tc - simt)) <= 2e-6 * scale
-    # the pipelined kernel does the same arithmetic as the single-buffered one
-    assert np.array_equal(tc.view(np.float64), tc2.view(np.float64))
 
 
 def test_fp32_reductions_accumulate_in_fp64(env):
@@ -133,7 +130,7 @@ def test_normalise_rescales_to_the_target_probability(env):
         s.free()
 
 
-@pytest.mark.parametrize("impl", [1, 2, 3])
+@pytest.mark.parametrize("impl", [1, 2])
 def test_graph_replays_the_circuit(env, impl):
     """A CUDA graph of the block kernels gives the same bits as applying the circuit."""
     from quest_gb300.fused import Circuit, StateVector32
