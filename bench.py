@@ -344,11 +344,19 @@ def run_gb300(args, world, rank, local, dist):
     fma_rate = C.c_double(0)
     _lib.check(L.qg_measure_fp64_fma_rate(C.byref(fma_rate)))
     fp64_ceiling_gbs = fma_rate.value / 16 * 64 / 1e9
+    # DRAM bytes per dense launch: given on the command line, else scaled from the ncu
+    # capture of the same kernel at 28 qubits (dram__bytes_read.sum + dram__bytes_write.sum
+    # = 8.530e9 B for 2^27 pairs: 63.55 B per pair; the FP64-FMA kernel's capture: 8.53e9 B too)
+    if args.traffic is not None:
+        traffic, traffic_src = args.traffic, "command line"
+    else:
+        traffic = round(63.55 * (1 << (nq - 1)))
+        traffic_src = "ncu capture at 28 qubits (63.55 B per amplitude pair) scaled to this size"
     kname = ("k_dense1_fx (applyCompMatr1, general complex 2x2, FP64 storage, fixed-point products)"
              if args.fp64_products == "fixed" else "k_dense1 (applyCompMatr1, general complex 2x2, FP64)")
     roofline = {"bound": "hbm", "kernel": kname,
                 "achieved": round(achieved, 1), "peak": peak, "peak_source": peak_src, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "traffic": args.traffic,
+                "frac": round(achieved / peak, 4), "traffic": traffic, "traffic_source": traffic_src,
                 "launches_timed": len(dense_ms), "avg_launch_ms": round(avg_dense * 1e3, 4),
                 "fp64_fma_per_s": round(fma_rate.value, -8), "fp64_ceiling_gbs": round(fp64_ceiling_gbs, 1),
                 "fp64_ceiling_frac": round(achieved / fp64_ceiling_gbs, 4)}
