@@ -236,9 +236,12 @@ def run_gb300(args, world, rank, local, dist):
     tune_ms = (C.c_double * 8)()
     tune_n = C.c_int(0)
     _lib.check(L.qg_autotune_fp64(min(26, args.qubits), tune_ms, 8, C.byref(tune_n)))
-    tppt, tthr = C.c_int(), C.c_int()
-    _lib.check(L.qg_get_kernel_shape(0, C.byref(tppt), C.byref(tthr)))
-    tuning = {"dense1_fx_shape": [tppt.value, tthr.value],
+    shapes = []
+    for kern in (0, 1):
+        tppt, tthr = C.c_int(), C.c_int()
+        _lib.check(L.qg_get_kernel_shape(kern, C.byref(tppt), C.byref(tthr)))
+        shapes.append([tppt.value, tthr.value])
+    tuning = {"dense1_fx_shape": shapes[0], "diag1_fx_shape": shapes[1],
               "candidates_ms": [round(tune_ms[i], 4) for i in range(tune_n.value)]}
 
     nq = args.qubits

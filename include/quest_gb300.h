@@ -86,15 +86,18 @@ int qg_get_fp64_products(int* mode);
 
 /* ------------------------------------------------------------------ launch-shape autotuner
  * (no counterpart in the reference, whose launch sizes are fixed formulas,
- * gpu_subroutines.cpp getNumBlocks)  Kernel 0 = the one-target dense kernel with
- * fixed-point products.  A shape is (pairs per thread per iteration, threads per
- * block) from {(1,256), (1,128), (2,256), (2,128)}; default (1,256). */
+ * gpu_subroutines.cpp getNumBlocks)  Kernel 0 = the one-target dense kernel, 1 = the
+ * one-target diagonal kernel, both with fixed-point products.  A shape is (items per
+ * thread per iteration, threads per block) from {(1,256), (1,128), (2,256), (2,128)};
+ * default (1,256). */
 #define QG_TUNE_KERNEL_DENSE1 0
+#define QG_TUNE_KERNEL_DIAG1 1
 int qg_set_kernel_shape(int kernel, int pairsPerThread, int threadsPerBlock);
 int qg_get_kernel_shape(int kernel, int* pairsPerThread, int* threadsPerBlock);
-/* times every candidate on a scratch register of numQubits (16 B x 2^numQubits of
- * device memory for the duration of the call) and keeps the fastest; msOut receives
- * milliseconds per launch for each candidate in the order above */
+/* times every candidate of every tunable kernel on a scratch register of numQubits
+ * (16 B x 2^numQubits of device memory for the duration of the call) and keeps the
+ * fastest per kernel; msOut[kernel * 4 + candidate] receives milliseconds per launch,
+ * candidates in the order above */
 int qg_autotune_fp64(int numQubits, double* msOut, int maxOut, int* numOut);
 /* text file: "qg-tune 1", then "<device name> <kernel> <ppt> <threads>" per line;
  * load applies only the lines for the current device's name */

@@ -8,13 +8,13 @@
 // doubles in 64-bit fixed point:
 //
 //  * the input shares one scale: e = the largest biased exponent among its N doubles;
-//    each value becomes x = v * 2^(1082 - e), |x| < 2^60 (denormals are exact: they
-//    enter with exponent 1 and no implicit bit);
+//    each value becomes x = v * 2^(S + 1075 - e), |x| < 2^(53+S) with S = 7 (N <= 4) or
+//    6 (N = 8) (denormals are exact: they enter with exponent 1 and no implicit bit);
 //  * the operator's coefficients share one scale E (|c| < 2^E): m = c * 2^(60 - E);
 //  * x and m split into balanced 32-bit limbs, x = xh*2^32 + xl with xl in
 //    [-2^31, 2^31); each output is R = sum(xh*mh) + (sum(xh*ml + xl*mh) >> 32), the
 //    top 64 bits of the exact 128-bit sum of products minus the dropped xl*ml terms;
-//  * R converts back to a double rounded to nearest: value = R * 2^(e+E-1078).
+//  * R converts back to a double rounded to nearest: value = R * 2^(e+E-1071-S).
 //    apply_op does that with integer instructions only (ties away from zero);
 //    apply_op_cvt, which the GPU kernels use, lets the hardware int64 -> double
 //    conversion round (ties to even) and adds the scale to the exponent field.
@@ -81,12 +81,21 @@ QG_HD int eff_exponent(uint64_t u) {
     return ei + (ei == 0);
 }
 
-// v (bits u) at the pair scale e: x = v * 2^(1082 - e), split into balanced limbs
-QG_HD void to_limbs(uint64_t u, int e, int32_t& xh, int32_t& xl) {
+// The input scale leaves headroom for the 2N middle products of one output:
+// |x| < 2^(53+S) with S = 7 for N <= 4 (x < 2^60) and S = 6 for N = 8 (x < 2^59), so
+// 2N terms of at most 2^(52+S) (xh*ml) or 2^59 (xl*mh) stay below 2^63.
+template <int N>
+struct FxShift {
+    static_assert(N >= 1 && N <= 8, "operator size");
+    static constexpr int S = (N <= 4) ? 7 : 6;
+};
+
+// v (bits u) at the pair scale e: x = v * 2^(S + 1075 - e), split into balanced limbs
+QG_HD void to_limbs(uint64_t u, int e, int32_t& xh, int32_t& xl, int S = 7) {
     const int ei = (int)((u >> 52) & 0x7FF);
     const uint64_t mant = (u & 0xFFFFFFFFFFFFFull) | (ei ? (1ull << 52) : 0ull);
     const int d = e - (ei + (ei == 0));
-    const uint64_t x = d < 64 ? (mant << 7) >> d : 0ull;
+    const uint64_t x = d < 64 ? (mant << S) >> d : 0ull;
     const int64_t sx = (u >> 63) ? -(int64_t)x : (int64_t)x;
     const uint32_t lo = (uint32_t)sx;
     xl = (int32_t)lo;
@@ -113,7 +122,7 @@ QG_HD double from_fixed(int64_t R, int ebase, bool& ok) {
 // 2N middle terms sum below 2^63 for N <= 4.
 template <int N>
 QG_HD bool apply_op(const OpN<N>& C, const double in[N], double out[N]) {
-    static_assert(N >= 1 && N <= 4, "operator size");
+    constexpr int S = FxShift<N>::S;
     uint64_t u[N];
     int e = 1;
 #pragma unroll
@@ -125,9 +134,9 @@ QG_HD bool apply_op(const OpN<N>& C, const double in[N], double out[N]) {
     if (e == 2047) return false;          // Inf or NaN in the input
     int32_t xh[N], xl[N];
 #pragma unroll
-    for (int j = 0; j < N; j++) to_limbs(u[j], e, xh[j], xl[j]);
+    for (int j = 0; j < N; j++) to_limbs(u[j], e, xh[j], xl[j], S);
     bool ok = true;
-    const int ebase = e + C.expo + 8;
+    const int ebase = e + C.expo + 8 + (7 - S);
 #pragma unroll
     for (int r = 0; r < N; r++) {
         int64_t hh = 0, mid = 0;
@@ -146,7 +155,7 @@ QG_HD bool apply_op4(const Op4& C, const double in[4], double out[4]) { return a
 
 // The same arithmetic with the output step done by the hardware int64 -> double
 // conversion (round to nearest) and the scale applied by an integer add to the
-// exponent field: out_r = double(R) * 2^t, t = e + E - 1078.  On GB300 that conversion
+// exponent field: out_r = double(R) * 2^t, t = e + E - 1071 - S.  On GB300 that conversion
 // runs on the FP64 unit, which the integer arithmetic leaves idle, and replaces
 // about 30 integer ALU instructions per output.  Falls back (returns false) for
 // Inf/NaN and when some output could leave the normal range (scale checked once
@@ -161,7 +170,7 @@ QG_HD double i64_to_double(int64_t v) {
 
 template <int N>
 QG_HD bool apply_op_cvt(const OpN<N>& C, const double in[N], double out[N]) {
-    static_assert(N >= 1 && N <= 4, "operator size");
+    constexpr int S = FxShift<N>::S;
     uint64_t u[N];
     int e = 1;
 #pragma unroll
@@ -170,7 +179,7 @@ QG_HD bool apply_op_cvt(const OpN<N>& C, const double in[N], double out[N]) {
         const int ej = eff_exponent(u[j]);
         e = ej > e ? ej : e;
     }
-    const int t = e + C.expo - 1078;
+    const int t = e + C.expo - 1078 + (7 - S);
     if (1023 + t < 1 || 1082 + t > 2046 || e == 2047) {
         uint64_t any = 0;
 #pragma unroll
@@ -182,7 +191,7 @@ QG_HD bool apply_op_cvt(const OpN<N>& C, const double in[N], double out[N]) {
     }
     int32_t xh[N], xl[N];
 #pragma unroll
-    for (int j = 0; j < N; j++) to_limbs(u[j], e, xh[j], xl[j]);
+    for (int j = 0; j < N; j++) to_limbs(u[j], e, xh[j], xl[j], S);
     const uint32_t down = (uint32_t)t << 20;           // adds t to the exponent field
 #pragma unroll
     for (int r = 0; r < N; r++) {
@@ -200,17 +209,18 @@ QG_HD bool apply_op_cvt(const OpN<N>& C, const double in[N], double out[N]) {
     return true;
 }
 
-// x = v * 2^(1082 - e) for a normal v whose exponent is within 31 of e (d = e - e_v),
+// x = v * 2^(S + 1075 - e) for a normal v whose exponent is within 31 of e (d = e - e_v),
 // from its two 32-bit words with 32-bit funnel shifts, split into balanced limbs
+template <int S>
 QG_HD void to_limbs_near(uint32_t hi, uint32_t lo, int d, int32_t& xh, int32_t& xl) {
     const uint32_t mh = (hi & 0xFFFFFu) | 0x100000u;            // 21 high mantissa bits with the implicit 1
 #if defined(__CUDA_ARCH__)
-    const uint32_t ah = __funnelshift_l(lo, mh, 7);              // (mantissa << 7): 60 bits
-    const uint32_t al = lo << 7;
+    const uint32_t ah = __funnelshift_l(lo, mh, S);              // (mantissa << S): 53 + S bits
+    const uint32_t al = lo << S;
     const uint32_t yl = __funnelshift_r(al, ah, d);              // >> d, d in [0, 31]
 #else
-    const uint32_t ah = (mh << 7) | (lo >> 25);
-    const uint32_t al = lo << 7;
+    const uint32_t ah = (mh << S) | (lo >> (32 - S));
+    const uint32_t al = lo << S;
     const uint32_t yl = d ? (al >> d) | (ah << (32 - d)) : al;
 #endif
     const uint32_t yh = ah >> d;
@@ -238,11 +248,12 @@ QG_HD bool apply_op_near(const OpN<N>& C, const double in[N], double out[N]) {
         e = ex[j] > e ? ex[j] : e;
         emin = ex[j] < emin ? ex[j] : emin;
     }
-    const int t = e + C.expo - 1078;
+    constexpr int S = FxShift<N>::S;
+    const int t = e + C.expo - 1078 + (7 - S);
     if (emin < 1 || e > 2046 || e - emin > 31 || 1023 + t < 1 || 1082 + t > 2046) return false;
     int32_t xh[N], xl[N];
 #pragma unroll
-    for (int j = 0; j < N; j++) to_limbs_near(hi[j], lo[j], e - ex[j], xh[j], xl[j]);
+    for (int j = 0; j < N; j++) to_limbs_near<S>(hi[j], lo[j], e - ex[j], xh[j], xl[j]);
     const uint32_t down = (uint32_t)t << 20;
 #pragma unroll
     for (int r = 0; r < N; r++) {
@@ -298,6 +309,20 @@ inline bool make_op4(const double C[16], Op4& op) { return make_op<4>(C, op); }
 inline bool make_scalar_op(double re, double im, Op2& op) {
     const double C[4] = {re, -im, im, re};
     return make_op<2>(C, op);
+}
+
+// Host: the real form (2D x 2D, row-major) of a complex D x D matrix u (row-major,
+// interleaved re/im); in/out order (a0.re, a0.im, a1.re, a1.im, ...)
+inline void real_form(const double* u, int D, double* C) {
+    const int W = 2 * D;
+    for (int r = 0; r < D; r++)
+        for (int j = 0; j < D; j++) {
+            const double re = u[2 * (D * r + j)], im = u[2 * (D * r + j) + 1];
+            C[W * (2 * r) + 2 * j] = re;
+            C[W * (2 * r) + 2 * j + 1] = -im;
+            C[W * (2 * r + 1) + 2 * j] = im;
+            C[W * (2 * r + 1) + 2 * j + 1] = re;
+        }
 }
 
 // Host: the real form of out = U * (a0, a1) for a complex 2x2 U given as

@@ -201,6 +201,36 @@ __global__ void k_dense2(double2* __restrict__ a, qidx numIts, Ins ins, qidx mas
     }
 }
 
+// k_dense2 through the integer pipes: the real 8x8 form of the matrix on each group
+// of four amplitudes in block-floating fixed point (qg_fixed.cuh); groups holding
+// Inf/NaN or with results outside the normal range take the FP64 products.
+template <int NB>
+__global__ void __launch_bounds__(QG_THREADS) k_dense2_fx(double2* __restrict__ a, qidx numIts, Ins ins, qidx mask,
+                                                         qidx b1, qidx b2, qgfx::OpN<8> C, Mat2 M) {
+    const qidx stride = (qidx)gridDim.x * blockDim.x;
+    for (qidx n = blockIdx.x * (qidx)blockDim.x + threadIdx.x; n < numIts; n += stride) {
+        const qidx i00 = insert_bits<NB>(n, ins) | mask;
+        const qidx idx[4] = {i00, i00 | b1, i00 | b2, i00 | b1 | b2};
+        double2 v[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) v[j] = ld_amp(a + idx[j]);
+        const double in[8] = {v[0].x, v[0].y, v[1].x, v[1].y, v[2].x, v[2].y, v[3].x, v[3].y};
+        double out[8];
+        if (qgfx::apply_op_best<8>(C, in, out)) {
+#pragma unroll
+            for (int r = 0; r < 4; r++) st_amp(a + idx[r], make_double2(out[2 * r], out[2 * r + 1]));
+        } else {
+#pragma unroll
+            for (int r = 0; r < 4; r++) {
+                double2 acc = cmul(M.m[4 * r], v[0]);
+#pragma unroll
+                for (int j = 1; j < 4; j++) acc = cfma(M.m[4 * r + j], v[j], acc);
+                st_amp(a + idx[r], acc);
+            }
+        }
+    }
+}
+
 // ============================================================== few-target dense (3..5 targets)
 // Each thread caches its 2^K amplitudes in registers; the matrix (already
 // conjugated if requested) sits in parameter space.
@@ -282,34 +312,56 @@ __global__ void k_diag1(double2* __restrict__ a, qidx numIts, Ins ins, qidx mask
 // k_diag1 through the integer pipes: each amplitude times its factor in block-floating
 // fixed point (qg_fixed.cuh); amplitudes holding Inf/NaN or with a result outside the
 // normal range take the FP64 product instead.
-template <int NB, int MODE>
-__global__ void __launch_bounds__(QG_THREADS) k_diag1_fx(double2* __restrict__ a, qidx numIts, Ins ins, qidx mask, qidx tbit,
-                                                        double2 d0, double2 d1, qgfx::Op2 F0, qgfx::Op2 F1) {
-    const qidx stride = (qidx)gridDim.x * blockDim.x;
-    qidx n = blockIdx.x * (qidx)blockDim.x + threadIdx.x;
-    if (n >= numIts) return;
-    qidx i = insert_bits<NB>(n, ins) | mask;
-    double2 x = ld_amp(a + i);
-    for (;;) {
-        const qidx nn = n + stride;
-        const bool more = nn < numIts;
-        qidx j = 0;
-        double2 xn;
-        if (more) {
-            j = insert_bits<NB>(nn, ins) | mask;
-            xn = ld_amp(a + j);
+__device__ __forceinline__ double2 diag1_fx_amp(const qgfx::Op2& F, double2 f, double2 x) {
+    const double in[2] = {x.x, x.y};
+    double out[2];
+    if (qgfx::apply_op_best<2>(F, in, out)) return make_double2(out[0], out[1]);
+    return cmul(f, x);
+}
+
+// MODE 1: every visited amplitude times F0 (the target bit is part of the fixed mask);
+// MODE 0: F0 or F1 by the target bit.  PPT amplitudes per thread per round, the
+// next round's loads issued before this round's products.
+template <int NB, int MODE, int PPT, int THREADS>
+__global__ void __launch_bounds__(THREADS) k_diag1_fx(double2* __restrict__ a, qidx numIts, Ins ins, qidx mask, qidx tbit,
+                                                     double2 d0, double2 d1, qgfx::Op2 F0, qgfx::Op2 F1) {
+    const qidx stride = (qidx)gridDim.x * THREADS;
+    const qidx span = PPT * stride;
+    const qidx tid = blockIdx.x * (qidx)THREADS + threadIdx.x;
+    const qidx groups = numIts / span;
+    if (groups > 0) {
+        qidx i[PPT];
+        double2 x[PPT];
+#pragma unroll
+        for (int k = 0; k < PPT; k++) {
+            i[k] = insert_bits<NB>(tid + k * stride, ins) | mask;
+            x[k] = ld_amp(a + i[k]);
         }
-        const bool second = (MODE == 0) && (i & tbit);
-        const double in[2] = {x.x, x.y};
-        double out[2];
-        double2 o;
-        if (qgfx::apply_op_best<2>(second ? F1 : F0, in, out))
-            o = make_double2(out[0], out[1]);
-        else
-            o = cmul(second ? d1 : d0, x);
-        st_amp(a + i, o);
-        if (!more) break;
-        n = nn; i = j; x = xn;
+        for (qidx g = 1;; g++) {
+            const bool more = g < groups;
+            qidx j[PPT];
+            double2 xn[PPT];
+            if (more) {
+#pragma unroll
+                for (int k = 0; k < PPT; k++) {
+                    j[k] = insert_bits<NB>(g * span + tid + k * stride, ins) | mask;
+                    xn[k] = ld_amp(a + j[k]);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < PPT; k++) {
+                const bool second = (MODE == 0) && (i[k] & tbit);
+                st_amp(a + i[k], diag1_fx_amp(second ? F1 : F0, second ? d1 : d0, x[k]));
+            }
+            if (!more) break;
+#pragma unroll
+            for (int k = 0; k < PPT; k++) { i[k] = j[k]; x[k] = xn[k]; }
+        }
+    }
+    for (qidx n = groups * span + tid; n < numIts; n += stride) {
+        const qidx ii = insert_bits<NB>(n, ins) | mask;
+        const bool second = (MODE == 0) && (ii & tbit);
+        st_amp(a + ii, diag1_fx_amp(second ? F1 : F0, second ? d1 : d0, ld_amp(a + ii)));
     }
 }
 
@@ -531,6 +583,27 @@ int launch_dense1_fx(QgShape shape, const QubitPlan& p, qidx numIts, double2* am
     }
 }
 
+template <int MODE, int PPT, int THREADS>
+int launch_diag1_fx_shape(const QubitPlan& p, qidx numIts, double2* amps, qidx tbit, double2 d0, double2 d1,
+                          const qgfx::Op2& F0, const qgfx::Op2& F1, cudaStream_t st) {
+    const qidx groups = (numIts + PPT - 1) / PPT;
+#define L(NBV) k_diag1_fx<NBV, MODE, PPT, THREADS><<<resident_blocks(k_diag1_fx<NBV, MODE, PPT, THREADS>, groups, THREADS), THREADS, 0, st>>>(amps, numIts, p.ins, p.stateMask, tbit, d0, d1, F0, F1)
+    QG_DISPATCH_NB(p.numFixed, L)
+#undef L
+    return QG_OK;
+}
+
+template <int MODE>
+int launch_diag1_fx(QgShape shape, const QubitPlan& p, qidx numIts, double2* amps, qidx tbit, double2 d0, double2 d1,
+                    const qgfx::Op2& F0, const qgfx::Op2& F1, cudaStream_t st) {
+    switch (shape.ppt * 1000 + shape.threads) {
+        case 1128: return launch_diag1_fx_shape<MODE, 1, 128>(p, numIts, amps, tbit, d0, d1, F0, F1, st);
+        case 2128: return launch_diag1_fx_shape<MODE, 2, 128>(p, numIts, amps, tbit, d0, d1, F0, F1, st);
+        case 2256: return launch_diag1_fx_shape<MODE, 2, 256>(p, numIts, amps, tbit, d0, d1, F0, F1, st);
+        default: return launch_diag1_fx_shape<MODE, 1, 256>(p, numIts, amps, tbit, d0, d1, F0, F1, st);
+    }
+}
+
 // the limb form of a complex 2x2 (row-major) for k_dense1_fx; false: keep FP64
 bool make_fx(const qg_cplx* matr, qgfx::Op4& C) {
     double u[8], R[16];
@@ -631,9 +704,19 @@ int qg_sv_anyCtrlTwoTargDenseMatr(void* amps, int numQubits, const int* ctrls, c
     qidx numIts = ((qidx)1 << numQubits) >> p.numFixed;
     qidx b1 = (qidx)1 << targ1, b2 = (qidx)1 << targ2;
     cudaStream_t st = qg_stream(stream);
-#define L(NBV) QG_LAUNCH_PLAIN(k_dense2, NBV, (double2*)amps, numIts, p.ins, p.stateMask, b1, b2, M)
-    QG_DISPATCH_NB(p.numFixed, L)
+    double u[32], R[64];
+    for (int i = 0; i < 16; i++) { u[2 * i] = matr[i].re; u[2 * i + 1] = matr[i].im; }
+    qgfx::real_form(u, 4, R);
+    qgfx::OpN<8> C;
+    if (qg_fp64_products_mode() == QG_FP64_PRODUCTS_FIXED && qgfx::make_op<8>(R, C)) {
+#define L(NBV) k_dense2_fx<NBV><<<resident_blocks(k_dense2_fx<NBV>, numIts), QG_THREADS, 0, st>>>((double2*)amps, numIts, p.ins, p.stateMask, b1, b2, C, M)
+        QG_DISPATCH_NB(p.numFixed, L)
 #undef L
+    } else {
+#define L(NBV) QG_LAUNCH_PLAIN(k_dense2, NBV, (double2*)amps, numIts, p.ins, p.stateMask, b1, b2, M)
+        QG_DISPATCH_NB(p.numFixed, L)
+#undef L
+    }
     qg_note_launch();
     return qg_check_launch("dense2");
 }
@@ -746,9 +829,7 @@ int qg_sv_anyCtrlOneTargDiagMatr(void* amps, int numQubits, const int* ctrls, co
         double2 f = d2(one0 ? elems[1] : elems[0]);
         qgfx::Op2 F;
         if (qg_fp64_products_mode() == QG_FP64_PRODUCTS_FIXED && qgfx::make_scalar_op(f.x, f.y, F)) {
-#define L(NBV) k_diag1_fx<NBV, 1><<<resident_blocks(k_diag1_fx<NBV, 1>, numIts), QG_THREADS, 0, st>>>((double2*)amps, numIts, p.ins, p.stateMask, 0, f, f, F, F)
-            QG_DISPATCH_NB(p.numFixed, L)
-#undef L
+            QG_TRY(launch_diag1_fx<1>(qg_tuned_shape(QG_TUNE_DIAG1), p, numIts, (double2*)amps, 0, f, f, F, F, st));
         } else {
 #define L(NBV) k_diag1<NBV, 1><<<persistent_blocks(numIts), QG_THREADS, 0, st>>>((double2*)amps, numIts, p.ins, p.stateMask, 0, f, f)
             QG_DISPATCH_NB(p.numFixed, L)
@@ -762,9 +843,8 @@ int qg_sv_anyCtrlOneTargDiagMatr(void* amps, int numQubits, const int* ctrls, co
         qgfx::Op2 F0, F1;
         if (qg_fp64_products_mode() == QG_FP64_PRODUCTS_FIXED && qgfx::make_scalar_op(elems[0].re, elems[0].im, F0) &&
             qgfx::make_scalar_op(elems[1].re, elems[1].im, F1)) {
-#define L(NBV) k_diag1_fx<NBV, 0><<<resident_blocks(k_diag1_fx<NBV, 0>, numIts), QG_THREADS, 0, st>>>((double2*)amps, numIts, p.ins, p.stateMask, tbit, d2(elems[0]), d2(elems[1]), F0, F1)
-            QG_DISPATCH_NB(p.numFixed, L)
-#undef L
+            QG_TRY(launch_diag1_fx<0>(qg_tuned_shape(QG_TUNE_DIAG1), p, numIts, (double2*)amps, tbit, d2(elems[0]),
+                                      d2(elems[1]), F0, F1, st));
         } else {
 #define L(NBV) k_diag1<NBV, 0><<<persistent_blocks(numIts), QG_THREADS, 0, st>>>((double2*)amps, numIts, p.ins, p.stateMask, tbit, d2(elems[0]), d2(elems[1]))
             QG_DISPATCH_NB(p.numFixed, L)

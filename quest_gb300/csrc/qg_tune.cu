@@ -6,7 +6,9 @@
 // file keyed by the device name, so a deployment tunes once per GPU model.
 #include "qg_common.cuh"
 
+#include <algorithm>
 #include <atomic>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -15,9 +17,9 @@ namespace {
 
 struct Candidate { int ppt, threads; };
 const Candidate kCandidates[] = {{1, 256}, {1, 128}, {2, 256}, {2, 128}};
-const char* kKernelNames[QG_TUNE_NUM] = {"dense1_fx"};
+const char* kKernelNames[QG_TUNE_NUM] = {"dense1_fx", "diag1_fx"};
 
-std::atomic<int> g_shape[QG_TUNE_NUM] = {{1 * 1000 + 256}};
+std::atomic<int> g_shape[QG_TUNE_NUM] = {{1 * 1000 + 256}, {1 * 1000 + 256}};
 
 bool is_candidate(int ppt, int threads) {
     for (const auto& c : kCandidates)
@@ -60,10 +62,12 @@ int qg_get_kernel_shape(int kernel, int* ppt, int* threads) {
     return QG_OK;
 }
 
-// Times every candidate shape of the one-target dense kernel (fixed-point products)
-// on a scratch register of numQubits (16 B x 2^numQubits of device memory, freed
-// before returning), keeps the fastest and reports per-candidate milliseconds per
-// launch in msOut (up to maxOut entries, in candidate order) when given.
+// Times every candidate shape of the tunable kernels on a scratch register of
+// numQubits (16 B x 2^numQubits of device memory, freed before returning): the
+// one-target dense kernel (fixed-point products) on a fixed unitary, and the
+// one-target diagonal kernel on a controlled phase.  Keeps the fastest shape per kernel
+// and reports milliseconds per launch in msOut, kernel-major: msOut[k * 4 + c] for
+// candidate c (up to maxOut entries).
 int qg_autotune_fp64(int numQubits, double* msOut, int maxOut, int* numOut) {
     if (numQubits < 10 || numQubits > 32) return qg_fail(QG_ERR_ARG, "tune on 10..32 qubits, not %d", numQubits);
     const int64_t bytes = (int64_t)16 << numQubits;
@@ -71,36 +75,46 @@ int qg_autotune_fp64(int numQubits, double* msOut, int maxOut, int* numOut) {
     QG_TRY(qg_alloc(&amps, bytes));
     int rc = QG_OK;
     const qg_cplx amp = {1.0 / std::sqrt((double)((int64_t)1 << numQubits)), 0.0};
-    // a fixed non-trivial unitary: phase * rotation
+    // a fixed non-trivial unitary (phase * rotation) and a phase
     const double c = std::cos(0.37), s = std::sin(0.37), pc = std::cos(0.11), ps = std::sin(0.11);
     const qg_cplx m[4] = {{c * pc, c * ps}, {-s * pc, -s * ps}, {s * pc, s * ps}, {c * pc, c * ps}};
+    const qg_cplx phase[2] = {{1.0, 0.0}, {std::cos(0.23), std::sin(0.23)}};
     void* ev0 = nullptr;
     void* ev1 = nullptr;
-    const int saved = g_shape[QG_TUNE_DENSE1].load();
-    int best = saved;
-    double bestMs = 1e30;
+    int saved[QG_TUNE_NUM], best[QG_TUNE_NUM];
+    for (int k = 0; k < QG_TUNE_NUM; k++) saved[k] = best[k] = g_shape[k].load();
     int n = 0;
-    if ((rc = qg_event_create(&ev0)) != QG_OK || (rc = qg_event_create(&ev1)) != QG_OK) goto done;
-    if ((rc = qg_sv_initUniformState(amps, numQubits, amp, nullptr)) != QG_OK) goto done;
-    for (const auto& cand : kCandidates) {
-        g_shape[QG_TUNE_DENSE1] = cand.ppt * 1000 + cand.threads;
-        const int reps = 6;
-        for (int w = 0; w < 2 && rc == QG_OK; w++)
-            rc = qg_sv_anyCtrlOneTargDenseMatr(amps, numQubits, nullptr, nullptr, 0, w % numQubits, m, nullptr);
-        if (rc == QG_OK) rc = qg_event_record(ev0, nullptr);
-        for (int r = 0; r < reps && rc == QG_OK; r++)
-            rc = qg_sv_anyCtrlOneTargDenseMatr(amps, numQubits, nullptr, nullptr, 0, (r * 7) % numQubits, m, nullptr);
-        if (rc == QG_OK) rc = qg_event_record(ev1, nullptr);
-        float ms = 0;
-        if (rc == QG_OK) rc = qg_event_elapsed_ms(ev0, ev1, &ms);
-        if (rc != QG_OK) break;
-        const double per = ms / reps;
-        if (msOut && n < maxOut) msOut[n] = per;
-        n++;
-        if (per < bestMs) { bestMs = per; best = cand.ppt * 1000 + cand.threads; }
+    if ((rc = qg_event_create(&ev0)) == QG_OK) rc = qg_event_create(&ev1);
+    if (rc == QG_OK) rc = qg_sv_initUniformState(amps, numQubits, amp, nullptr);
+    for (int kern = 0; kern < QG_TUNE_NUM && rc == QG_OK; kern++) {
+        double bestMs = 1e30;
+        int ci = 0;
+        for (const auto& cand : kCandidates) {
+            g_shape[kern] = cand.ppt * 1000 + cand.threads;
+            auto run = [&](int r) {
+                const int t = (r * 7) % (numQubits - 2) + 2;
+                if (kern == QG_TUNE_DENSE1)
+                    return qg_sv_anyCtrlOneTargDenseMatr(amps, numQubits, nullptr, nullptr, 0, t, m, nullptr);
+                const int ctrl = (t + 3) % numQubits == t ? 0 : (t + 3) % numQubits;
+                return qg_sv_anyCtrlOneTargDiagMatr(amps, numQubits, &ctrl, nullptr, 1, t, phase, nullptr);
+            };
+            const int reps = 6;
+            for (int w = 0; w < 2 && rc == QG_OK; w++) rc = run(w);
+            if (rc == QG_OK) rc = qg_event_record(ev0, nullptr);
+            for (int r = 0; r < reps && rc == QG_OK; r++) rc = run(r);
+            if (rc == QG_OK) rc = qg_event_record(ev1, nullptr);
+            float ms = 0;
+            if (rc == QG_OK) rc = qg_event_elapsed_ms(ev0, ev1, &ms);
+            if (rc != QG_OK) break;
+            const double per = ms / reps;
+            const int slot = kern * 4 + ci;
+            if (msOut && slot < maxOut) msOut[slot] = per;
+            n = std::max(n, slot + 1);
+            if (per < bestMs) { bestMs = per; best[kern] = cand.ppt * 1000 + cand.threads; }
+            ci++;
+        }
     }
-done:
-    g_shape[QG_TUNE_DENSE1] = rc == QG_OK ? best : saved;
+    for (int k = 0; k < QG_TUNE_NUM; k++) g_shape[k] = rc == QG_OK ? best[k] : saved[k];
     if (numOut) *numOut = n;
     if (ev0) qg_event_destroy(ev0);
     if (ev1) qg_event_destroy(ev1);

@@ -172,6 +172,46 @@ static void run_all() {
             worstRatio = std::fmax(worstRatio, (double)(err / bound));
         }
     }
+    // 8x8 real operators (complex 4x4: two-qubit gates) on four amplitudes
+    for (int t = 0; t < 50000; t++) {
+        std::complex<double> m[16];
+        for (auto& v : m) v = std::complex<double>(nd(g), nd(g));
+        for (int c = 0; c < 4; c++) {           // Gram-Schmidt on the columns: a Haar-like unitary
+            for (int p = 0; p < c; p++) {
+                std::complex<double> dot = 0;
+                for (int r = 0; r < 4; r++) dot += std::conj(m[4 * r + p]) * m[4 * r + c];
+                for (int r = 0; r < 4; r++) m[4 * r + c] -= dot * m[4 * r + p];
+            }
+            double nrm = 0;
+            for (int r = 0; r < 4; r++) nrm += std::norm(m[4 * r + c]);
+            for (int r = 0; r < 4; r++) m[4 * r + c] /= std::sqrt(nrm);
+        }
+        if (t & 1)
+            for (auto& v : m) v *= std::ldexp(1.0, (int)(g() % 12) - 6);   // non-unitary scales too
+        double u16[32], C8[64], in8[8], out8[8];
+        for (int i = 0; i < 16; i++) { u16[2 * i] = m[i].real(); u16[2 * i + 1] = m[i].imag(); }
+        qgfx::real_form(u16, 4, C8);
+        qgfx::OpN<8> op;
+        if (!qgfx::make_op<8>(C8, op)) { failures++; continue; }
+        const int s0 = scale(g);
+        for (int j = 0; j < 8; j++) in8[j] = std::ldexp(nd(g), s0 - (int)(g() % 4) * spread(g) / 8);
+        bool ok = variant == 2 ? qgfx::apply_op_best<8>(op, in8, out8)
+                  : variant ? qgfx::apply_op_cvt<8>(op, in8, out8) : qgfx::apply_op<8>(op, in8, out8);
+        if (!ok) { failures++; std::printf("8x8 fell back\n"); continue; }
+        ld maxIn = 0, maxC = 0;
+        for (int j = 0; j < 8; j++) maxIn = std::fmax(maxIn, std::fabs((ld)in8[j]));
+        for (int i = 0; i < 64; i++) maxC = std::fmax(maxC, std::fabs((ld)C8[i]));
+        for (int r = 0; r < 8; r++) {
+            ld ref = 0;
+            for (int j = 0; j < 8; j++) ref += (ld)C8[8 * r + j] * (ld)in8[j];
+            // the 8-term bound: one more input bit dropped, twice the terms
+            ld bound = std::ldexp((ld)3.0, -53) * maxIn * maxC + std::ldexp(std::fabs(ref), -53) + 1e-320L;
+            ld err = std::fabs((ld)out8[r] - ref);
+            numChecked++;
+            if (err > bound) { failures++; if (failures < 10) std::printf("8x8 out of bound %Lg %Lg\n", err, bound); }
+            worstRatio = std::fmax(worstRatio, (double)(err / bound));
+        }
+    }
     std::printf("%s variant=%d checked=%ld fallback=%ld worst_err_over_bound=%.3f fp64_fma_worst_over_bound=%.3f failures=%d\n",
                 failures ? "FAIL" : "OK", variant, numChecked, numFallback, worstRatio, worstRatioF64, failures);
 }

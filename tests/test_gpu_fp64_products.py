@@ -1,4 +1,4 @@
-"""General complex one-target gates on FP64 states in both product modes
+"""General complex one- and two-target gates on FP64 states in both product modes
 (qg_set_fp64_products): block-floating fixed point on the integer pipes (the
 default) and IEEE FP64.  Both must meet the FP64 bar against the oracle (max-abs
 <= 1e-12); the fixed-point path must hand pairs with Inf/NaN or results outside the
@@ -27,6 +27,9 @@ def _haar_circuit(nq, layers, seed):
             lines.append(f"U1 {t} {qc.mat_tokens(qc.haar_unitary(2, rng))}")
         c1, c2, t = (int(v) for v in rng.choice(nq, 3, replace=False))
         lines.append(f"CU1 2 {c1} {c2} 1 0 {t} {qc.mat_tokens(qc.haar_unitary(2, rng))}")
+        a, b = (int(v) for v in rng.choice(nq, 2, replace=False))
+        lines.append(f"U2 {a} {b} {qc.mat_tokens(qc.haar_unitary(4, rng))}")
+        lines.append(f"CU2 1 {c1} 1 {t} {c2} {qc.mat_tokens(qc.haar_unitary(4, rng))}")
     lines.append("TOTALPROB")
     return "\n".join(lines) + "\n"
 
@@ -102,14 +105,18 @@ def test_every_launch_shape_gives_the_same_bits(env):
     amps = qc.random_statevector(nq, 9)
     want, _, _ = qc.oracle().run(text, nq, 0, amps)
     outs = []
+    text += "".join(f"CPS {c} {t} {0.1 + 0.3 * c}\n" for c, t in [(0, 5), (3, 9), (12, 2)])
+    want, _, _ = qc.oracle().run(text, nq, 0, amps)
     try:
         for ppt, thr in [(1, 256), (1, 128), (2, 256), (2, 128)]:
             assert L.qg_set_kernel_shape(0, ppt, thr) == 0
+            assert L.qg_set_kernel_shape(1, ppt, thr) == 0
             out, _ = _run(env, text, nq, amps)
             assert np.max(np.abs(out - want)) <= TOL
             outs.append(out)
     finally:
         L.qg_set_kernel_shape(0, 1, 256)
+        L.qg_set_kernel_shape(1, 1, 256)
     for o in outs[1:]:
         assert np.array_equal(o.view(np.float64), outs[0].view(np.float64))
 
@@ -122,11 +129,13 @@ def test_autotune_picks_the_fastest_candidate(env):
     n = ctypes.c_int()
     try:
         assert L.qg_autotune_fp64(22, ms, 8, ctypes.byref(n)) == 0
-        assert n.value == 4 and all(ms[i] > 0 for i in range(4))
-        ppt, thr = ctypes.c_int(), ctypes.c_int()
-        assert L.qg_get_kernel_shape(0, ctypes.byref(ppt), ctypes.byref(thr)) == 0
+        assert n.value == 8 and all(ms[i] > 0 for i in range(8))
         cands = [(1, 256), (1, 128), (2, 256), (2, 128)]
-        best = min(range(4), key=lambda i: ms[i])
-        assert (ppt.value, thr.value) == cands[best]
+        for kernel in (0, 1):
+            ppt, thr = ctypes.c_int(), ctypes.c_int()
+            assert L.qg_get_kernel_shape(kernel, ctypes.byref(ppt), ctypes.byref(thr)) == 0
+            best = min(range(4), key=lambda i: ms[4 * kernel + i])
+            assert (ppt.value, thr.value) == cands[best]
     finally:
         L.qg_set_kernel_shape(0, 1, 256)
+        L.qg_set_kernel_shape(1, 1, 256)
