@@ -8,20 +8,22 @@
 // doubles in 64-bit fixed point:
 //
 //  * the input shares one scale: e = the largest biased exponent among its N doubles;
-//    each value becomes x = v * 2^(S + 1075 - e), |x| < 2^(53+S) with S = 7 (N <= 4) or
-//    6 (N = 8) (denormals are exact: they enter with exponent 1 and no implicit bit);
-//  * the operator's coefficients share one scale E (|c| < 2^E): m = c * 2^(60 - E);
+//    each value becomes x = v * 2^(S + 1075 - e), |x| < 2^(53+S) with S from 7 (N <= 4)
+//    down to 4 (N = 32) (denormals are exact: they enter with exponent 1 and no implicit bit);
+//  * the operator's coefficients share one scale E (|c| < 2^E): m = c * 2^(Q - E);
 //  * x and m split into balanced 32-bit limbs, x = xh*2^32 + xl with xl in
 //    [-2^31, 2^31); each output is R = sum(xh*mh) + (sum(xh*ml + xl*mh) >> 32), the
 //    top 64 bits of the exact 128-bit sum of products minus the dropped xl*ml terms;
-//  * R converts back to a double rounded to nearest: value = R * 2^(e+E-1071-S).
+//  * R converts back to a double rounded to nearest: value = R * 2^(e+E-S-Q-1011).
 //    apply_op does that with integer instructions only (ties away from zero);
 //    apply_op_cvt, which the GPU kernels use, lets the hardware int64 -> double
 //    conversion round (ties to even) and adds the scale to the exponent field.
 //
-// Error per output: at most 2 units of R plus the input truncation, i.e. below
-// 2^-54 of (largest |v| in the input) * (largest |c|).  IEEE FP64 evaluation of the same
-// 4-term sums has a bound of the same order.  An input holding Inf or NaN, or whose
+// Error per output, relative to (largest |v| in the input) x (largest |c|): N input
+// truncations of 2^-(52+S), N coefficient roundings of 2^-Q, and N/4 + 1 units of R
+// (2^(13-S-Q) each) for the dropped low x low products; plus half an ulp of the result.
+// That is below 2^-54 for N = 4 and 2^-48.8 for N = 32, the order of IEEE FP64's own
+// bound for the same N-term sums (tests/fx_check.cpp checks it on random operators).  An input holding Inf or NaN, or whose
 // result could leave the normal double range, returns false and the caller uses FP64.
 #pragma once
 #include <stdint.h>
@@ -81,13 +83,18 @@ QG_HD int eff_exponent(uint64_t u) {
     return ei + (ei == 0);
 }
 
-// The input scale leaves headroom for the 2N middle products of one output:
-// |x| < 2^(53+S) with S = 7 for N <= 4 (x < 2^60) and S = 6 for N = 8 (x < 2^59), so
-// 2N terms of at most 2^(52+S) (xh*ml) or 2^59 (xl*mh) stay below 2^63.
+// Scales that leave headroom for the 2N middle products of one output: inputs
+// |x| < 2^(53+S), coefficients |m| <= 2^Q, so |xh*ml| <= 2^(S+52) and
+// |xl*mh| <= 2^(Q-1) (+2^31) and N of each stay below 2^63:
+//   N <= 4: S = 7, Q = 60;  N = 8: S = 6, Q = 60;  N = 16: S = 5, Q = 59;  N = 32: S = 4, Q = 58.
+// |R| <= N * 2^(S+Q-11) = 2^RL, and value = R * 2^(e + E - S - Q - 1011).
 template <int N>
 struct FxShift {
-    static_assert(N >= 1 && N <= 8, "operator size");
-    static constexpr int S = (N <= 4) ? 7 : 6;
+    static_assert(N >= 1 && N <= 32, "operator size");
+    static constexpr int S = (N <= 4) ? 7 : (N <= 8) ? 6 : (N <= 16) ? 5 : 4;
+    static constexpr int Q = (N <= 8) ? 60 : (N <= 16) ? 59 : 58;
+    static constexpr int RL = (N <= 2 ? 1 : N <= 4 ? 2 : N <= 8 ? 3 : N <= 16 ? 4 : 5) + S + Q - 11;
+    static constexpr int TOFF = S + Q + 1011;     // value = R * 2^(e + E - TOFF)
 };
 
 // v (bits u) at the pair scale e: x = v * 2^(S + 1075 - e), split into balanced limbs
@@ -136,7 +143,7 @@ QG_HD bool apply_op(const OpN<N>& C, const double in[N], double out[N]) {
 #pragma unroll
     for (int j = 0; j < N; j++) to_limbs(u[j], e, xh[j], xl[j], S);
     bool ok = true;
-    const int ebase = e + C.expo + 8 + (7 - S);
+    const int ebase = e + C.expo + 1086 - FxShift<N>::TOFF;
 #pragma unroll
     for (int r = 0; r < N; r++) {
         int64_t hh = 0, mid = 0;
@@ -155,7 +162,7 @@ QG_HD bool apply_op4(const Op4& C, const double in[4], double out[4]) { return a
 
 // The same arithmetic with the output step done by the hardware int64 -> double
 // conversion (round to nearest) and the scale applied by an integer add to the
-// exponent field: out_r = double(R) * 2^t, t = e + E - 1071 - S.  On GB300 that conversion
+// exponent field: out_r = double(R) * 2^t, t = e + E - S - Q - 1011.  On GB300 that conversion
 // runs on the FP64 unit, which the integer arithmetic leaves idle, and replaces
 // about 30 integer ALU instructions per output.  Falls back (returns false) for
 // Inf/NaN and when some output could leave the normal range (scale checked once
@@ -179,8 +186,8 @@ QG_HD bool apply_op_cvt(const OpN<N>& C, const double in[N], double out[N]) {
         const int ej = eff_exponent(u[j]);
         e = ej > e ? ej : e;
     }
-    const int t = e + C.expo - 1078 + (7 - S);
-    if (1023 + t < 1 || 1082 + t > 2046 || e == 2047) {
+    const int t = e + C.expo - FxShift<N>::TOFF;
+    if (1023 + t < 1 || 1023 + FxShift<N>::RL + t > 2046 || e == 2047) {
         uint64_t any = 0;
 #pragma unroll
         for (int j = 0; j < N; j++) any |= u[j] << 1;     // ignores the signs of zeros
@@ -249,8 +256,8 @@ QG_HD bool apply_op_near(const OpN<N>& C, const double in[N], double out[N]) {
         emin = ex[j] < emin ? ex[j] : emin;
     }
     constexpr int S = FxShift<N>::S;
-    const int t = e + C.expo - 1078 + (7 - S);
-    if (emin < 1 || e > 2046 || e - emin > 31 || 1023 + t < 1 || 1082 + t > 2046) return false;
+    const int t = e + C.expo - FxShift<N>::TOFF;
+    if (emin < 1 || e > 2046 || e - emin > 31 || 1023 + t < 1 || 1023 + FxShift<N>::RL + t > 2046) return false;
     int32_t xh[N], xl[N];
 #pragma unroll
     for (int j = 0; j < N; j++) to_limbs_near<S>(hi[j], lo[j], e - ex[j], xh[j], xl[j]);
@@ -269,6 +276,67 @@ QG_HD bool apply_op_near(const OpN<N>& C, const double in[N], double out[N]) {
         out[r] = bits_f64(dh ? ((uint64_t)(dh + down) << 32 | (uint32_t)d) : 0ull);
     }
     return true;
+}
+
+// The same arithmetic split in two, for callers that store each output as it is
+// formed (wide operators, whose N outputs would not fit in registers at once):
+// fx_prepare puts the N inputs at their common scale as limbs (false: use FP64);
+// fx_row then forms output r.  The results equal apply_op_best's bit for bit.
+template <int N>
+QG_HD bool fx_prepare(const OpN<N>& C, const double in[N], int32_t xh[N], int32_t xl[N], uint32_t& down, bool& zero) {
+    constexpr int S = FxShift<N>::S;
+    // two passes over the inputs (scale, then limbs) so that no per-input state beyond
+    // the inputs themselves stays live: at N = 32 registers are the limit
+    int e = 0, emin = 4096, eg = 1;
+    uint64_t any = 0;
+#pragma unroll
+    for (int j = 0; j < N; j++) {
+        const uint64_t u = f64_bits(in[j]);
+        any |= u << 1;
+        const int ej = (int)((u >> 52) & 0x7FF);
+        e = ej > e ? ej : e;
+        emin = ej < emin ? ej : emin;
+        const int ejg = ej + (ej == 0);
+        eg = ejg > eg ? ejg : eg;
+    }
+    zero = false;
+    const int t = e + C.expo - FxShift<N>::TOFF;
+    if (emin >= 1 && e <= 2046 && e - emin <= 31 && 1023 + t >= 1 && 1023 + FxShift<N>::RL + t <= 2046) {
+#pragma unroll
+        for (int j = 0; j < N; j++) {
+            const uint64_t u = f64_bits(in[j]);
+            const uint32_t hi = (uint32_t)(u >> 32);
+            to_limbs_near<S>(hi, (uint32_t)u, e - (int)((hi >> 20) & 0x7FFu), xh[j], xl[j]);
+        }
+        down = (uint32_t)t << 20;
+        return true;
+    }
+    // the general form: exponents counted with denormals as 1
+    const int tg = eg + C.expo - FxShift<N>::TOFF;
+    if (1023 + tg < 1 || 1023 + FxShift<N>::RL + tg > 2046 || eg == 2047) {
+        if (any) return false;
+        zero = true;                      // all zero: every output is zero
+        return true;
+    }
+#pragma unroll
+    for (int j = 0; j < N; j++) to_limbs(f64_bits(in[j]), eg, xh[j], xl[j], S);
+    down = (uint32_t)tg << 20;
+    return true;
+}
+
+template <int N>
+QG_HD double fx_row(const OpN<N>& C, int r, const int32_t xh[N], const int32_t xl[N], uint32_t down, bool zero) {
+    if (zero) return 0.0;
+    int64_t hh = 0, mid = 0;
+#pragma unroll
+    for (int j = 0; j < N; j++) {
+        hh += (int64_t)xh[j] * C.h[r][j];
+        mid += (int64_t)xh[j] * C.l[r][j];
+        mid += (int64_t)xl[j] * C.h[r][j];
+    }
+    const uint64_t d = f64_bits(i64_to_double(hh + (mid >> 32)));
+    const uint32_t dh = (uint32_t)(d >> 32);
+    return bits_f64(dh ? ((uint64_t)(dh + down) << 32 | (uint32_t)d) : 0ull);
 }
 
 // the fast form when it applies, else the general one; false: use FP64
@@ -295,7 +363,7 @@ inline bool make_op(const double* C, OpN<N>& op) {
     op.pad = 0;
     for (int r = 0; r < N; r++)
         for (int j = 0; j < N; j++) {
-            const int64_t m = (int64_t)std::llround(std::ldexp(C[N * r + j], 60 - E));
+            const int64_t m = (int64_t)std::llround(std::ldexp(C[N * r + j], FxShift<N>::Q - E));
             const uint32_t lo = (uint32_t)m;
             op.l[r][j] = (int32_t)lo;
             op.h[r][j] = (int32_t)((m - (int64_t)(int32_t)lo) >> 32);

@@ -259,6 +259,49 @@ __global__ void __launch_bounds__(128) k_denseK(double2* __restrict__ a, qidx nu
     }
 }
 
+// k_denseK through the integer pipes (K = 3, 4): the real 2^(K+1)-square form of the
+// matrix on each group, inputs put at their common scale once, each output formed and
+// stored in turn (qg_fixed.cuh fx_prepare / fx_row); groups that need FP64 use M.
+template <int K, int NB>
+__global__ void __launch_bounds__(128) k_denseK_fx(double2* __restrict__ a, qidx numIts, Ins ins, qidx mask, MatK<K> M,
+                                                  qgfx::OpN<2 << K> C) {
+    constexpr int D = 1 << K, N = 2 << K;
+    const qidx stride = (qidx)gridDim.x * blockDim.x;
+    for (qidx n = blockIdx.x * (qidx)blockDim.x + threadIdx.x; n < numIts; n += stride) {
+        const qidx base = insert_bits<NB>(n, ins) | mask;
+        double in[N];
+#pragma unroll
+        for (int j = 0; j < D; j++) {
+            const double2 v = ld_amp(a + base + M.off[j]);
+            in[2 * j] = v.x;
+            in[2 * j + 1] = v.y;
+        }
+        int32_t xh[N], xl[N];
+        uint32_t down;
+        bool zero;
+        if (qgfx::fx_prepare<N>(C, in, xh, xl, down, zero)) {
+            // rows one after another at K = 4 (fully unrolled, the schedule runs out of registers)
+#pragma unroll (K <= 3 ? D : 1)
+            for (int r = 0; r < D; r++)
+                st_amp(a + base + M.off[r], make_double2(qgfx::fx_row<N>(C, 2 * r, xh, xl, down, zero),
+                                                         qgfx::fx_row<N>(C, 2 * r + 1, xh, xl, down, zero)));
+        } else {
+            // nothing has been stored: reload the group (keeping the inputs live across the
+            // fixed-point path would not fit in registers at K = 4)
+            double2 v[D];
+#pragma unroll
+            for (int j = 0; j < D; j++) v[j] = a[base + M.off[j]];
+#pragma unroll
+            for (int r = 0; r < D; r++) {
+                double2 acc = cmul(M.m[r * D], v[0]);
+#pragma unroll
+                for (int j = 1; j < D; j++) acc = cfma(M.m[r * D + j], v[j], acc);
+                st_amp(a + base + M.off[r], acc);
+            }
+        }
+    }
+}
+
 // ============================================================== many-target dense (>= 6 targets)
 // One CTA per 2^K block: the block's amplitudes are staged in `cache` (shared
 // memory, or a per-CTA slot of global scratch beyond shared capacity), then each
@@ -735,6 +778,20 @@ int launch_denseK(double2* amps, qidx numIts, const QubitPlan& p, const qg_cplx*
         for (int b = 0; b < K; b++)
             if ((j >> b) & 1) o |= (qidx)1 << targs[b];
         M.off[j] = o;
+    }
+    if constexpr (K <= 4) {
+        if (qg_fp64_products_mode() == QG_FP64_PRODUCTS_FIXED) {
+            std::vector<double> u(2 * D * D), R(4 * D * D);
+            for (int i = 0; i < D * D; i++) { u[2 * i] = M.m[i].x; u[2 * i + 1] = M.m[i].y; }
+            qgfx::real_form(u.data(), D, R.data());
+            qgfx::OpN<2 * D> C;
+            if (qgfx::make_op<2 * D>(R.data(), C)) {
+#define L(NBV) k_denseK_fx<K, NBV><<<resident_blocks(k_denseK_fx<K, NBV>, numIts, 128), 128, 0, st>>>(amps, numIts, p.ins, p.stateMask, M, C)
+                QG_DISPATCH_NB(p.numFixed, L)
+#undef L
+                return QG_OK;
+            }
+        }
     }
     unsigned blocks = (unsigned)((numIts + 127) / 128);
 #define L(NBV) k_denseK<K, NBV><<<blocks, 128, 0, st>>>(amps, numIts, p.ins, p.stateMask, M)

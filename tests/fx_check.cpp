@@ -6,6 +6,7 @@
 #include <cmath>
 #include <random>
 #include <complex>
+#include <vector>
 
 #include "qg_fixed.cuh"
 
@@ -67,6 +68,70 @@ static void haar2(std::mt19937_64& g, double u[8]) {
     b /= n1; d /= n1;
     std::complex<double> m[4] = {a, b, c, d};
     for (int i = 0; i < 4; i++) { u[2 * i] = m[i].real(); u[2 * i + 1] = m[i].imag(); }
+}
+
+// D x D complex (N = 2D real) Haar-like unitaries on random inputs; the error bound
+// grows with the number of terms and the bits given up for headroom
+template <int N>
+static void check_wide(std::mt19937_64& g, int cases) {
+    constexpr int D = N / 2;
+    std::normal_distribution<double> nd;
+    std::uniform_int_distribution<int> scale(-70, 8);
+    for (int t = 0; t < cases; t++) {
+        std::vector<std::complex<double>> m(D * D);
+        for (auto& v : m) v = std::complex<double>(nd(g), nd(g));
+        for (int c = 0; c < D; c++) {
+            for (int p = 0; p < c; p++) {
+                std::complex<double> dot = 0;
+                for (int r = 0; r < D; r++) dot += std::conj(m[D * r + p]) * m[D * r + c];
+                for (int r = 0; r < D; r++) m[D * r + c] -= dot * m[D * r + p];
+            }
+            double nrm = 0;
+            for (int r = 0; r < D; r++) nrm += std::norm(m[D * r + c]);
+            for (int r = 0; r < D; r++) m[D * r + c] /= std::sqrt(nrm);
+        }
+        std::vector<double> u(2 * D * D), C(N * N), in(N), out(N);
+        for (int i = 0; i < D * D; i++) { u[2 * i] = m[i].real(); u[2 * i + 1] = m[i].imag(); }
+        qgfx::real_form(u.data(), D, C.data());
+        qgfx::OpN<N> op;
+        if (!qgfx::make_op<N>(C.data(), op)) { failures++; continue; }
+        const int s0 = scale(g);
+        for (int j = 0; j < N; j++) in[j] = std::ldexp(nd(g), s0 - (int)(g() % 3));
+        bool ok = variant == 2 ? qgfx::apply_op_best<N>(op, in.data(), out.data())
+                  : variant ? qgfx::apply_op_cvt<N>(op, in.data(), out.data()) : qgfx::apply_op<N>(op, in.data(), out.data());
+        if (!ok) { failures++; std::printf("%dx%d fell back\n", N, N); continue; }
+        if (variant == 2) {   // the streaming split gives apply_op_best's bits
+            int32_t xh[N], xl[N];
+            uint32_t down;
+            bool zero;
+            if (!qgfx::fx_prepare<N>(op, in.data(), xh, xl, down, zero)) { failures++; continue; }
+            for (int r = 0; r < N; r++)
+                if (qgfx::f64_bits(qgfx::fx_row<N>(op, r, xh, xl, down, zero)) != qgfx::f64_bits(out[r])) {
+                    failures++;
+                    std::printf("streaming split differs\n");
+                    break;
+                }
+        }
+        ld maxIn = 0, maxC = 0;
+        for (int j = 0; j < N; j++) maxIn = std::fmax(maxIn, std::fabs((ld)in[j]));
+        for (int i = 0; i < N * N; i++) maxC = std::fmax(maxC, std::fabs((ld)C[i]));
+        for (int r = 0; r < N; r++) {
+            ld ref = 0;
+            for (int j = 0; j < N; j++) ref += (ld)C[N * r + j] * (ld)in[j];
+            // N terms, each input truncated at 2^-(52+S) of the largest and each coefficient
+            // rounded at 2^-Q of the largest; the dropped low x low products and the shift
+            // of the middle sum cost N/4 + 1 units of R, one unit being 2^(13-S-Q) of
+            // (largest input) x (largest coefficient); half an ulp for the final rounding
+            constexpr int S = qgfx::FxShift<N>::S, Q = qgfx::FxShift<N>::Q;
+            ld bound = (ld)N * (std::ldexp((ld)1, -(52 + S)) + std::ldexp((ld)1, -Q)) * maxIn * maxC
+                       + (ld)(N / 4 + 1) * std::ldexp((ld)1, 13 - S - Q) * maxIn * maxC
+                       + std::ldexp(std::fabs(ref), -53) + 1e-320L;
+            ld err = std::fabs((ld)out[r] - ref);
+            numChecked++;
+            if (err > bound) { failures++; if (failures < 10) std::printf("%dx%d out of bound %Lg %Lg\n", N, N, err, bound); }
+            worstRatio = std::fmax(worstRatio, (double)(err / bound));
+        }
+    }
 }
 
 static void run_all();
@@ -212,6 +277,10 @@ static void run_all() {
             worstRatio = std::fmax(worstRatio, (double)(err / bound));
         }
     }
+    // 16x16 and 32x32 real operators (three- and four-target matrices, two-qubit
+    // superoperators) on 8 and 16 amplitudes
+    check_wide<16>(g, 20000);
+    check_wide<32>(g, 10000);
     std::printf("%s variant=%d checked=%ld fallback=%ld worst_err_over_bound=%.3f fp64_fma_worst_over_bound=%.3f failures=%d\n",
                 failures ? "FAIL" : "OK", variant, numChecked, numFallback, worstRatio, worstRatioF64, failures);
 }

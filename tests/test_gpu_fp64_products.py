@@ -30,6 +30,10 @@ def _haar_circuit(nq, layers, seed):
         a, b = (int(v) for v in rng.choice(nq, 2, replace=False))
         lines.append(f"U2 {a} {b} {qc.mat_tokens(qc.haar_unitary(4, rng))}")
         lines.append(f"CU2 1 {c1} 1 {t} {c2} {qc.mat_tokens(qc.haar_unitary(4, rng))}")
+        for k in (3, 4):
+            if nq >= k:
+                tk = [int(v) for v in rng.choice(nq, k, replace=False)]
+                lines.append(f"UK {k} {' '.join(map(str, tk))} {qc.mat_tokens(qc.haar_unitary(1 << k, rng))}")
     lines.append("TOTALPROB")
     return "\n".join(lines) + "\n"
 
@@ -59,6 +63,30 @@ def test_both_modes_meet_the_fp64_bar(env, nq, layers, seed):
             assert np.max(np.abs(got[mode][1] - wres)) <= TOL, mode
         # the two modes agree far inside the bar
         assert np.max(np.abs(got[0][0] - got[1][0])) <= 1e-14
+    finally:
+        _set_mode(0)
+
+
+@pytest.mark.parametrize("nq", [3, 5])
+def test_density_matrix_channels_in_both_modes(env, nq):
+    """Kraus maps (superoperators on 2 and 4 Choi targets), depolarising and unitaries
+    on density matrices meet the FP64 bar in both product modes."""
+    text = qc.config3_circuit(nq, 4, 90 + nq)
+    amps = qc.random_density_matrix(nq, 90 + nq)
+    want, wres, _ = qc.oracle().run(text, nq, 1, amps)
+    from quest_gb300.circuit import run_text
+    try:
+        for mode in (0, 1):
+            _set_mode(mode)
+            q = env.Q.createDensityQureg(nq)
+            try:
+                env.set_amps(q, amps)
+                res, _ = run_text(text, q)
+                got = env.get_amps(q)
+            finally:
+                env.Q.destroyQureg(q)
+            assert np.max(np.abs(got - want)) <= TOL, mode
+            assert np.max(np.abs(res - wres)) <= TOL, mode
     finally:
         _set_mode(0)
 
