@@ -37,11 +37,16 @@ AMP_BYTES = 16
 
 # ------------------------------------------------------------------ workload
 
-def haar_2x2(rng):
-    z = (rng.standard_normal((2, 2)) + 1j * rng.standard_normal((2, 2))) / np.sqrt(2)
+def haar(dim, rng):
+    """A Haar-random dim x dim unitary (QR of a complex Gaussian matrix, R's diagonal phase-fixed)."""
+    z = (rng.standard_normal((dim, dim)) + 1j * rng.standard_normal((dim, dim))) / np.sqrt(2)
     q, r = np.linalg.qr(z)
     d = np.diag(r)
     return q * (d / np.abs(d))
+
+
+def haar_2x2(rng):
+    return haar(2, rng)
 
 
 def make_circuit(nq, depth, seed):
@@ -710,6 +715,75 @@ def run_serve(args, world, rank, local, dist):
         print(json.dumps(line), flush=True)
 
 
+def run_gates(args, world, rank, local, dist):
+    """Per-gate-kind timing on one FP64 register: 1- to 4-target dense unitaries, a
+    controlled phase and a swap, in both product modes (fixed point, FP64 FMAs), after
+    the launch-shape autotuner.  ms per launch from CUDA events over `--steps` launches."""
+    import ctypes as C
+    from quest_gb300 import _lib, api
+    from quest_gb300._lib import qg_cplx
+    L = _lib.lib()
+    _lib.check(L.qg_init(local))
+    api.init_env()
+    n = args.qubits if "--qubits" in sys.argv else 28
+    ms_buf, cnt = (C.c_double * 8)(), C.c_int(0)
+    _lib.check(L.qg_autotune_fp64(min(26, n), ms_buf, 8, C.byref(cnt)))
+    p = C.c_void_p()
+    _lib.check(L.qg_alloc(C.byref(p), 16 << n))
+    _lib.check(L.qg_sv_initUniformState(p, n, qg_cplx(1 / np.sqrt(2.0 ** n), 0), None))
+    rng = np.random.default_rng(0x5155455354 + 6)
+    e0, e1 = C.c_void_p(), C.c_void_p()
+    L.qg_event_create(C.byref(e0))
+    L.qg_event_create(C.byref(e1))
+    state_bytes = 16 << n
+    phase = (qg_cplx * 2)(qg_cplx(1, 0), qg_cplx(np.cos(0.3), np.sin(0.3)))
+
+    def timed(fn):
+        for _ in range(max(1, args.warmup)):
+            fn()
+        L.qg_sync()
+        L.qg_event_record(e0, None)
+        for _ in range(args.steps):
+            fn()
+        L.qg_event_record(e1, None)
+        ms = C.c_float()
+        L.qg_event_elapsed_ms(e0, e1, C.byref(ms))
+        return ms.value / args.steps
+
+    rows = []
+    for mode in ("fixed", "fp64"):
+        _lib.check(L.qg_set_fp64_products(0 if mode == "fixed" else 1))
+        for k in (1, 2, 3, 4):
+            D = 1 << k
+            u = haar(D, rng).reshape(-1)
+            m = (qg_cplx * (D * D))(*[qg_cplx(v.real, v.imag) for v in u])
+            t = (C.c_int * k)(*range(3, 3 + k))
+            ms = timed(lambda: _lib.check(L.qg_sv_anyCtrlAnyTargDenseMatr(p, n, None, None, 0, t, k, m, 0, None)))
+            rows.append({"gate": f"dense, {k} target(s)", "products": mode, "ms": round(ms, 4),
+                         "gbs": round(2 * state_bytes / ms / 1e6, 1)})
+        ctrl = C.c_int(2)
+        ms = timed(lambda: _lib.check(L.qg_sv_anyCtrlOneTargDiagMatr(p, n, C.byref(ctrl), None, 1, 7, phase, None)))
+        rows.append({"gate": "controlled phase (quarter of the amplitudes)", "products": mode, "ms": round(ms, 4),
+                     "gbs": round(2 * state_bytes / 4 / ms / 1e6, 1)})
+    _lib.check(L.qg_set_fp64_products(0))
+    ms = timed(lambda: _lib.check(L.qg_sv_anyCtrlSwap(p, n, None, None, 0, 4, 9, None)))
+    rows.append({"gate": "swap (half of the amplitudes)", "products": "none", "ms": round(ms, 4),
+                 "gbs": round(2 * state_bytes / 2 / ms / 1e6, 1)})
+    L.qg_free(p)
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    peak = peaks.get("hbm_gbs", 6800.0)
+    for r in rows:
+        r["frac_of_hbm"] = round(r["gbs"] / peak, 3)
+    line = {"metric": "per-gate GB/s on an FP64 statevector, by gate kind and product mode", "value": rows[0]["gbs"],
+            "unit": "GB/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64 storage", "data": "synthetic (uniform state, seeded Haar gates)",
+            "config": {"workload": f"{n}-qubit FP64 statevector, one gate per launch", "qubits": n,
+                       "l2": "state larger than L2; no flush"},
+            "gates": rows, "hbm_peak_gbs": peak}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -720,9 +794,9 @@ def main():
     ap.add_argument("--depth", type=int, default=20)
     ap.add_argument("--cpu-sample", type=int, default=45, help="gates of the circuit timed on the host CPU")
     ap.add_argument("--traffic", type=float, default=None, help="ncu DRAM bytes per dense launch, if captured")
-    ap.add_argument("--config", default="plain", choices=["plain", "precision", "serve"],
+    ap.add_argument("--config", default="plain", choices=["plain", "precision", "serve", "gates"],
                     help="plain: the 30-qubit FP64 per-gate circuit (default); precision: FP32 fused blocks; "
-                         "serve: request stream, served vs plain")
+                         "serve: request stream, served vs plain; gates: per-gate-kind timing (28 qubits)")
     ap.add_argument("--requests", type=int, default=48)
     ap.add_argument("--min-qubits", type=int, default=8)
     ap.add_argument("--max-qubits", type=int, default=26)
@@ -738,6 +812,8 @@ def main():
     world, rank, local, dist = dist_setup()
     if args.config == "serve":
         run_serve(args, world, rank, local, dist)
+    elif args.config == "gates":
+        run_gates(args, world, rank, local, dist)
     elif args.config == "precision":
         if args.qubits == 30 and "--qubits" not in sys.argv:
             args.qubits = 32
