@@ -154,6 +154,9 @@ class ClockSampler:
 # ------------------------------------------------------------------ distributed plumbing (replicas)
 
 def dist_setup():
+    """Replicas: one process per GPU under torchrun (NCCL), or gloo where no GPU is
+    visible (the replica logic's CPU tests).  No data-path collective: only a barrier
+    around the timed region and the max of the ranks' times."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -161,8 +164,11 @@ def dist_setup():
     if world > 1:
         import torch
         import torch.distributed as td
-        torch.cuda.set_device(local)
-        td.init_process_group("nccl")
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+            td.init_process_group("nccl")
+        else:
+            td.init_process_group("gloo")
         dist = td
     return world, rank, local, dist
 
@@ -176,7 +182,8 @@ def max_over_ranks(dist, value):
     if dist is None:
         return value
     import torch
-    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    device = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=device)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
