@@ -725,7 +725,8 @@ def run_serve(args, world, rank, local, dist):
 def run_gates(args, world, rank, local, dist):
     """Per-gate-kind timing on one FP64 register: 1- to 4-target dense unitaries, a
     controlled phase and a swap, in both product modes (fixed point, FP64 FMAs), after
-    the launch-shape autotuner.  ms per launch from CUDA events over `--steps` launches."""
+    the launch-shape autotuner; then density-matrix channels on a register of half
+    the qubits (the same bytes).  ms per call from CUDA events over `--steps` calls."""
     import ctypes as C
     from quest_gb300 import _lib, api
     from quest_gb300._lib import qg_cplx
@@ -777,6 +778,35 @@ def run_gates(args, world, rank, local, dist):
     rows.append({"gate": "swap (half of the amplitudes)", "products": "none", "ms": round(ms, 4),
                  "gbs": round(2 * state_bytes / 2 / ms / 1e6, 1)})
     L.qg_free(p)
+
+    # density-matrix channels on an N-qubit density matrix (its 2N-qubit Choi vector has
+    # the same bytes as the statevector above); every channel below streams the whole
+    # Choi vector once, a one-qubit unitary twice (ket and bra)
+    from quest_gb300.api import Q, comp_matr1, kraus_map
+    nd = n // 2
+    dm = Q.createDensityQureg(nd)
+    Q.initPlusState(dm)
+    pass_bytes = 2 * state_bytes
+    u1 = comp_matr1(haar(2, rng))
+    k1 = kraus_map([np.sqrt(0.7) * np.eye(2), np.sqrt(0.3) * haar(2, rng)])
+    iso = haar(16, rng)[:, :4]                                    # a 16x4 isometry: four 4x4 Kraus operators
+    k2 = kraus_map([iso[4 * i:4 * i + 4, :] for i in range(4)])
+    dm_gates = [("applyCompMatr1 on the density matrix (2 passes)", 2, lambda: Q.applyCompMatr1(dm, 3, u1)),
+                ("mixDepolarising", 1, lambda: Q.mixDepolarising(dm, 3, 0.01)),
+                ("mixTwoQubitDepolarising", 1, lambda: Q.mixTwoQubitDepolarising(dm, 3, 8, 0.01)),
+                ("mixDephasing (the off-diagonal half)", 0.5, lambda: Q.mixDephasing(dm, 3, 0.05)),
+                ("mixDamping", 1, lambda: Q.mixDamping(dm, 3, 0.05)),
+                ("mixKrausMap, 1 qubit (2-target superoperator)", 1, lambda: Q.mixKrausMap(dm, (C.c_int * 1)(3), 1, k1)),
+                ("mixKrausMap, 2 qubits (4-target superoperator)", 1,
+                 lambda: Q.mixKrausMap(dm, (C.c_int * 2)(3, 8), 2, k2))]
+    for mode in ("fixed", "fp64"):
+        _lib.check(L.qg_set_fp64_products(0 if mode == "fixed" else 1))
+        for name, passes, fn in dm_gates:
+            ms = timed(fn)
+            rows.append({"gate": f"DM {nd}q: {name}", "products": mode, "ms": round(ms, 4),
+                         "gbs": round(passes * pass_bytes / ms / 1e6, 1)})
+    _lib.check(L.qg_set_fp64_products(0))
+    Q.destroyQureg(dm)
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
     peak = peaks.get("hbm_gbs", 6800.0)
     for r in rows:

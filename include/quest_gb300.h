@@ -334,6 +334,10 @@ int qg_server_poll(qg_server* server, int* numDone);
    of the final FP32 state summed in FP64; otherwise <psi|P|psi> unnormalised. */
 int qg_server_result(qg_server* server, int64_t id, double* values, int* done);
 int qg_server_release(qg_server* server, int64_t id);
+/* the client went away: a queued request is dropped at once (its circuit is no longer
+ * needed); one on the GPU is dropped when it completes, its slot and memory returned
+ * then; a finished one is released.  The id is unknown afterwards. */
+int qg_server_cancel(qg_server* server, int64_t id);
 int qg_server_stats(qg_server* server, int64_t* queued, int64_t* inFlight, int64_t* hbmInUse, int64_t* finished);
 
 #ifdef __cplusplus

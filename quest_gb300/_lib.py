@@ -136,6 +136,7 @@ ABI = {
     "qg_server_poll": [vp, c_int_p],
     "qg_server_result": [vp, I64, c_dbl_p, c_int_p],
     "qg_server_release": [vp, I64],
+    "qg_server_cancel": [vp, I64],
     "qg_server_stats": [vp, c_i64_p, c_i64_p, c_i64_p, c_i64_p],
 }
 

@@ -201,6 +201,7 @@ struct Request {
     bool small = false;
     bool unitary = true;     // every gate of the circuit is unitary: results are normalised
     bool finished = false;
+    bool cancelled = false;  // the client went away while it ran: dropped when it completes
     std::vector<double> values;
 };
 
@@ -458,10 +459,16 @@ int qg_server_poll(qg_server* s, int* numDone) {
     if (!s) return qg_fail(QG_ERR_ARG, "null server");
     int done = 0;
     // retire finished work
+    std::vector<int64_t> dropped;    // cancelled requests that completed: nobody reads them
     for (auto it = s->batches.begin(); it != s->batches.end();) {
         cudaError_t q = cudaEventQuery(it->done);
         if (q == cudaSuccess) {
-            for (int64_t id : it->ids) { finish(s, s->reqs[id]); done++; }
+            for (int64_t id : it->ids) {
+                Request& r = s->reqs[id];
+                finish(s, r);
+                if (r.cancelled) dropped.push_back(id);
+                else done++;
+            }
             cudaEventDestroy(it->done);
             it = s->batches.erase(it);
         } else if (q == cudaErrorNotReady) {
@@ -478,11 +485,13 @@ int qg_server_poll(qg_server* s, int* numDone) {
             cudaEventDestroy(r.done);
             r.done = nullptr;
             finish(s, r);
-            done++;
+            if (r.cancelled) dropped.push_back(r.id);
+            else done++;
         } else if (q != cudaErrorNotReady) {
             return qg_check_cuda(q, "cudaEventQuery(request)");
         }
     }
+    for (int64_t id : dropped) s->reqs.erase(id);
     // admit in arrival order while slots and memory allow (a large request that does not
     // fit yet blocks the queue, so admission stays first-come first-served)
     while (!s->queue.empty() && !s->freeSlots.empty()) {
@@ -521,6 +530,25 @@ int qg_server_release(qg_server* s, int64_t id) {
     auto it = s->reqs.find(id);
     if (it == s->reqs.end() || !it->second.finished) return qg_fail(QG_ERR_ARG, "request %lld is not finished", (long long)id);
     s->reqs.erase(it);
+    return QG_OK;
+}
+
+int qg_server_cancel(qg_server* s, int64_t id) {
+    if (!s) return qg_fail(QG_ERR_ARG, "null server");
+    auto it = s->reqs.find(id);
+    if (it == s->reqs.end() || it->second.cancelled) return qg_fail(QG_ERR_ARG, "unknown request %lld", (long long)id);
+    Request& r = it->second;
+    if (r.finished) {                        // done already: same as releasing it
+        s->reqs.erase(it);
+        return QG_OK;
+    }
+    if (r.slot < 0) {                        // still queued: nothing on the GPU
+        for (auto q = s->queue.begin(); q != s->queue.end(); ++q)
+            if (*q == id) { s->queue.erase(q); break; }
+        s->reqs.erase(it);
+        return QG_OK;
+    }
+    r.cancelled = true;                      // in flight: its slot and memory return when it completes
     return QG_OK;
 }
 

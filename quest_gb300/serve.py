@@ -122,6 +122,11 @@ class Server:
         check(lib().qg_server_release(self.h, rid))
         self._circuits.pop(rid, None)
 
+    def cancel(self, rid):
+        """Drops a request whose client went away (queued: at once; running: when it completes)."""
+        check(lib().qg_server_cancel(self.h, rid))
+        self._circuits.pop(rid, None)
+
     def stats(self):
         q, f, m, d = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
         check(lib().qg_server_stats(self.h, ctypes.byref(q), ctypes.byref(f), ctypes.byref(m), ctypes.byref(d)))

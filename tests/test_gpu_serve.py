@@ -98,3 +98,56 @@ def test_values_are_normalised_only_for_unitary_circuits(env, n):
             server.close()
         want = np.array([z0, xall, ident]) / (ident if unitary else 1.0)
         assert np.max(np.abs(got - want)) < 1e-6, (unitary, got, want)
+
+
+def test_cancelled_requests_free_their_memory(env):
+    """A client that goes away: one request cancelled while on the GPU, one while still
+    queued.  The others complete with the right values and nothing stays held."""
+    from quest_gb300.serve import Server, circuit_of, text_of
+    reqs = _requests([9, 18, 18, 12, 18, 10], 5)
+    circs = [circuit_of(n, ops) for n, (ops, codes) in reqs]
+    server = Server(6 << 20)          # room for one 18-qubit request at a time
+    try:
+        ids = [server.submit(c, codes) for c, (n, (ops, codes)) in zip(circs, reqs)]
+        server.poll()                 # admits and launches what fits
+        st = server.stats()
+        assert st["in_flight"] >= 1 and st["queued"] >= 1
+        running, queued = ids[1], ids[4]
+        server.cancel(running)
+        server.cancel(queued)
+        keep = [i for i in ids if i not in (running, queued)]
+        got = {}
+        for _ in range(100000):
+            server.poll()
+            for rid in keep:
+                if rid not in got:
+                    done, vals = server.result(rid)
+                    if done:
+                        got[rid] = vals
+            if len(got) == len(keep):
+                break
+        assert len(got) == len(keep)
+        for k, rid in enumerate(ids):
+            if rid in got:
+                n, (ops, codes) = reqs[k]
+                zero = np.zeros(1 << n, dtype=np.complex128)
+                zero[0] = 1
+                _, want, _ = qc.oracle().run(text_of(ops, codes), n, 0, zero)
+                assert np.max(np.abs(got[rid] - want)) < 2e-5
+                server.release(rid)
+        for _ in range(1000):          # the cancelled request still on the GPU retires too
+            server.poll()
+            if server.stats()["hbm_in_use"] == 0:
+                break
+        st = server.stats()
+        assert st == {**st, "queued": 0, "in_flight": 0, "hbm_in_use": 0}
+        with pytest.raises(Exception):
+            server.result(running)
+    finally:
+        server.close()
+
+
+def test_budget_larger_than_the_gpu_is_refused(env):
+    from quest_gb300.serve import Server
+    with pytest.raises(Exception):
+        Server(1 << 50)               # a petabyte: the allocation fails cleanly
