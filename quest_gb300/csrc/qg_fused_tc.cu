@@ -11,14 +11,14 @@
 // part a TF32 value, and D = Xl*Bh + Xh*Bl + Xh*Bh accumulated in FP32 (the
 // Xl*Bl term is below FP32 rounding).  Bh/Bl are built once per block on the host.
 //
-// Per CTA tile: 128 threads each load one group's 32 amplitudes (coalesced
-// 8-byte loads: consecutive threads own consecutive groups), split them into
-// TF32 hi/lo parts and store both into shared memory in the no-swizzle K-major
-// core-matrix layout (8 rows x 16 bytes per core matrix); one thread issues the
+// Per CTA tile: 256 threads, two per group row, each load 16 of the group's 32
+// amplitudes (coalesced 8-byte loads: consecutive threads own consecutive groups),
+// split them into TF32 hi/lo parts and store both into shared memory in the
+// no-swizzle K-major core-matrix layout (8 rows x 16 bytes per core matrix); one thread issues the
 // 24 MMAs (3 products x 8 K-steps of 8) into two 128-lane x 64-column TMEM
 // accumulators (large term, small terms) and commits them to an mbarrier; every
-// warp then reads its 32 TMEM lanes (tcgen05.ld 32x32b), adds the two
-// accumulators in FP32 and writes its groups' 32 outputs back.
+// warp then reads its 32 TMEM lanes (tcgen05.ld 32x32b) in its half of the columns,
+// adds the two accumulators in FP32 and writes its groups' 16 outputs back.
 // Every wait is bounded: a wait that runs out sets the error flag, frees the
 // TMEM and returns.
 #include "qg_common.cuh"
@@ -32,7 +32,7 @@
 #define TC_M 128              // groups per tile (MMA M)
 #define TC_K 64               // real K (32 complex amplitudes)
 #define TC_N 64               // real N
-#define TC_THREADS 128
+#define TC_THREADS 256           // two threads per group row: each holds 16 of its 32 amplitudes
 #define TC_TMEM_COLS 128          // two 64-column accumulators: the large and the small 3xTF32 terms
 #define TC_WAIT_NS 2000000000ull   // a tile's MMAs take microseconds; 2 s means they never completed
 
@@ -179,6 +179,7 @@ __global__ void __launch_bounds__(TC_THREADS, 2) k32_fused_tc(TcArgs args) {
     volatile int* abortFlag = (volatile int*)(tmemSlot + 1);
 
     const int tid = threadIdx.x, warp = tid >> 5;
+    const int row = tid & (TC_M - 1), half = tid >> 7;   // thread (row g, half h): j in [16h, 16h+16)
 
     // stage Bh, Bl once (already in the tile layout)
     {
@@ -208,23 +209,23 @@ __global__ void __launch_bounds__(TC_THREADS, 2) k32_fused_tc(TcArgs args) {
     // Software pipeline: the next tile's 32 amplitudes per thread are loaded into
     // registers while this tile's MMAs run and its results are written back.
     qidx tile = blockIdx.x;
-    float2 x[32];
+    float2 x[16];
     qidx base = 0;
     if (tile < args.numTiles) {
-        base = insert_bits<5>(tile * TC_M + tid, args.ins);
+        base = insert_bits<5>(tile * TC_M + row, args.ins);
 #pragma unroll
-        for (int j = 0; j < 32; j++) x[j] = __ldcs(args.amps + base + args.off[j]);
+        for (int i = 0; i < 16; i++) x[i] = __ldcs(args.amps + base + args.off[16 * half + i]);
     }
     for (; tile < args.numTiles; tile += gridDim.x) {
         // ---- split into TF32 hi/lo and store in the K-major core layout (kk = 2j + c)
 #pragma unroll
-        for (int q = 0; q < 16; q++) {
+        for (int q = 0; q < 8; q++) {
             float4 h, l;
             h.x = tf32_hi(x[2 * q].x);     l.x = tf32_hi(x[2 * q].x - h.x);
             h.y = tf32_hi(x[2 * q].y);     l.y = tf32_hi(x[2 * q].y - h.y);
             h.z = tf32_hi(x[2 * q + 1].x); l.z = tf32_hi(x[2 * q + 1].x - h.z);
             h.w = tf32_hi(x[2 * q + 1].y); l.w = tf32_hi(x[2 * q + 1].y - h.w);
-            unsigned o = core_offset(tid, 4 * q, TC_M);
+            unsigned o = core_offset(row, 4 * (8 * half + q), TC_M);
             *(float4*)((unsigned char*)sAh + o) = h;
             *(float4*)((unsigned char*)sAl + o) = l;
         }
@@ -258,9 +259,9 @@ __global__ void __launch_bounds__(TC_THREADS, 2) k32_fused_tc(TcArgs args) {
         const qidx cur = base;
         const qidx next = tile + gridDim.x;
         if (next < args.numTiles) {
-            base = insert_bits<5>(next * TC_M + tid, args.ins);
+            base = insert_bits<5>(next * TC_M + row, args.ins);
 #pragma unroll
-            for (int j = 0; j < 32; j++) x[j] = __ldcs(args.amps + base + args.off[j]);
+            for (int i = 0; i < 16; i++) x[i] = __ldcs(args.amps + base + args.off[16 * half + i]);
         }
 
         // ---- every thread waits for the MMAs (bounded by %globaltimer)
@@ -273,11 +274,11 @@ __global__ void __launch_bounds__(TC_THREADS, 2) k32_fused_tc(TcArgs args) {
         }
         asm volatile("tcgen05.fence::after_thread_sync;");
 
-        // ---- epilogue: warp w reads TMEM lanes 32w..32w+31 (its groups), 16 columns of
-        //      each accumulator at a time, and writes 8 amplitudes per chunk
-        const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+        // ---- epilogue: warp w reads TMEM lanes 32(w mod 4).. (its groups) and the 32
+        //      columns of its half (outputs k in [16h, 16h+16)), 16 at a time
+        const uint32_t taddr = tmem + ((uint32_t)((warp & 3) * 32) << 16) + 32 * half;
 #pragma unroll
-        for (int c = 0; c < 4; c++) {
+        for (int c = 0; c < 2; c++) {
             uint32_t big[16], small[16];
             TMEM_LD16(taddr + 16 * c, big);
             TMEM_LD16(taddr + TC_N + 16 * c, small);
@@ -286,7 +287,7 @@ __global__ void __launch_bounds__(TC_THREADS, 2) k32_fused_tc(TcArgs args) {
             for (int k = 0; k < 8; k++) {
                 float re = __uint_as_float(small[2 * k]) + __uint_as_float(big[2 * k]);
                 float im = __uint_as_float(small[2 * k + 1]) + __uint_as_float(big[2 * k + 1]);
-                __stcs(args.amps + cur + args.off[8 * c + k], make_float2(re, im));
+                __stcs(args.amps + cur + args.off[16 * half + 8 * c + k], make_float2(re, im));
             }
         }
         asm volatile("tcgen05.fence::before_thread_sync;");
