@@ -283,7 +283,7 @@ QG_HD bool apply_op_near(const OpN<N>& C, const double in[N], double out[N]) {
 // fx_prepare puts the N inputs at their common scale as limbs (false: use FP64);
 // fx_row then forms output r.  The results equal apply_op_best's bit for bit.
 template <int N>
-QG_HD bool fx_prepare(const OpN<N>& C, const double in[N], int32_t xh[N], int32_t xl[N], uint32_t& down, bool& zero) {
+QG_HD bool fx_prepare_e(int expo, const double in[N], int32_t xh[N], int32_t xl[N], uint32_t& down, bool& zero) {
     constexpr int S = FxShift<N>::S;
     // two passes over the inputs (scale, then limbs) so that no per-input state beyond
     // the inputs themselves stays live: at N = 32 registers are the limit
@@ -300,7 +300,7 @@ QG_HD bool fx_prepare(const OpN<N>& C, const double in[N], int32_t xh[N], int32_
         eg = ejg > eg ? ejg : eg;
     }
     zero = false;
-    const int t = e + C.expo - FxShift<N>::TOFF;
+    const int t = e + expo - FxShift<N>::TOFF;
     if (emin >= 1 && e <= 2046 && e - emin <= 31 && 1023 + t >= 1 && 1023 + FxShift<N>::RL + t <= 2046) {
 #pragma unroll
         for (int j = 0; j < N; j++) {
@@ -312,7 +312,7 @@ QG_HD bool fx_prepare(const OpN<N>& C, const double in[N], int32_t xh[N], int32_
         return true;
     }
     // the general form: exponents counted with denormals as 1
-    const int tg = eg + C.expo - FxShift<N>::TOFF;
+    const int tg = eg + expo - FxShift<N>::TOFF;
     if (1023 + tg < 1 || 1023 + FxShift<N>::RL + tg > 2046 || eg == 2047) {
         if (any) return false;
         zero = true;                      // all zero: every output is zero
@@ -322,6 +322,11 @@ QG_HD bool fx_prepare(const OpN<N>& C, const double in[N], int32_t xh[N], int32_
     for (int j = 0; j < N; j++) to_limbs(f64_bits(in[j]), eg, xh[j], xl[j], S);
     down = (uint32_t)tg << 20;
     return true;
+}
+
+template <int N>
+QG_HD bool fx_prepare(const OpN<N>& C, const double in[N], int32_t xh[N], int32_t xl[N], uint32_t& down, bool& zero) {
+    return fx_prepare_e<N>(C.expo, in, xh, xl, down, zero);
 }
 
 template <int N>
@@ -337,6 +342,113 @@ QG_HD double fx_row(const OpN<N>& C, int r, const int32_t xh[N], const int32_t x
     const uint64_t d = f64_bits(i64_to_double(hh + (mid >> 32)));
     const uint32_t dh = (uint32_t)(d >> 32);
     return bits_f64(dh ? ((uint64_t)(dh + down) << 32 | (uint32_t)d) : 0ull);
+}
+
+// ---------------------------------------------------------------- complex operators, 3 products
+// A complex D x D matrix U = A + iB on D complex inputs X = x + iy, with Gauss's
+// three-product form per term: A(x+y), (A+B)y and (B-A)x give
+//   Re Y = sum A(x+y) - sum (A+B)y,   Im Y = sum A(x+y) + sum (B-A)x,
+// and the first sum is shared by both parts: 3D products per complex output instead
+// of the 4D of the real 2D x 2D form.  The scales are those of OpN<2D>: (x+y) and
+// (A+B), (B-A) carry one more bit, and each sum has D terms instead of 2D, so the
+// middle sums stay below 2^63.
+template <int D>
+struct CopN {
+    int32_t ah[D][D], al[D][D];   // A
+    int32_t ph[D][D], pl[D][D];   // A + B
+    int32_t qh[D][D], ql[D][D];   // B - A
+    int32_t expo;                 // E: |A|, |B| < 2^E  (so |A+B|, |B-A| < 2^(E+1))
+    int32_t pad;
+};
+
+// Host: the limb form of a complex D x D matrix (row-major, interleaved re/im)
+template <int D>
+inline bool make_cop(const double* u, CopN<D>& op) {
+    constexpr int Q = FxShift<2 * D>::Q;
+    int E = -100000;
+    for (int i = 0; i < 2 * D * D; i++) {
+        if (!(u[i] - u[i] == 0.0)) return false;
+        if (u[i] != 0.0) {
+            int ex;
+            std::frexp(u[i], &ex);
+            E = ex > E ? ex : E;
+        }
+    }
+    if (E == -100000) E = 0;
+    op.expo = E;
+    op.pad = 0;
+    auto limbs = [](int64_t m, int32_t& h, int32_t& l) {
+        const uint32_t lo = (uint32_t)m;
+        l = (int32_t)lo;
+        h = (int32_t)((m - (int64_t)(int32_t)lo) >> 32);
+    };
+    for (int r = 0; r < D; r++)
+        for (int j = 0; j < D; j++) {
+            // A and B rounded once to the fixed-point quantum; A + B and B - A formed
+            // exactly from those integers (a sum in double would round at 2^-53)
+            const int64_t a = (int64_t)std::llround(std::ldexp(u[2 * (D * r + j)], Q - E));
+            const int64_t b = (int64_t)std::llround(std::ldexp(u[2 * (D * r + j) + 1], Q - E));
+            limbs(a, op.ah[r][j], op.al[r][j]);
+            limbs(a + b, op.ph[r][j], op.pl[r][j]);
+            limbs(b - a, op.qh[r][j], op.ql[r][j]);
+        }
+    return true;
+}
+
+QG_HD void split_limbs(int64_t v, int32_t& h, int32_t& l) {
+    const uint32_t lo = (uint32_t)v;
+    l = (int32_t)lo;
+    h = (int32_t)(uint32_t)((uint64_t)v >> 32) + (int32_t)(lo >> 31);
+}
+
+// The D complex inputs (2D doubles) at their common scale as limbs of x, y and x + y;
+// false: use FP64.  Same scale rules as fx_prepare<2D>.
+template <int D>
+QG_HD bool cfx_prepare(const CopN<D>& C, const double in[2 * D], int32_t xh[D], int32_t xl[D], int32_t yh[D],
+                       int32_t yl[D], int32_t sh[D], int32_t sl[D], uint32_t& down, bool& zero) {
+    constexpr int N = 2 * D;
+    int32_t h[N], l[N];
+    if (!fx_prepare_e<N>(C.expo, in, h, l, down, zero)) return false;
+#pragma unroll
+    for (int j = 0; j < D; j++) {
+        const int64_t x = ((int64_t)h[2 * j] << 32) + (int64_t)l[2 * j];
+        const int64_t y = ((int64_t)h[2 * j + 1] << 32) + (int64_t)l[2 * j + 1];
+        xh[j] = h[2 * j]; xl[j] = l[2 * j];
+        yh[j] = h[2 * j + 1]; yl[j] = l[2 * j + 1];
+        split_limbs(x + y, sh[j], sl[j]);
+    }
+    return true;
+}
+
+// top 64 bits of sum_j (mh*2^32 + ml) * (vh*2^32 + vl) without the low x low terms
+template <int D>
+QG_HD int64_t limb_dot(const int32_t (&mh)[D][D], const int32_t (&ml)[D][D], int r, const int32_t* vh, const int32_t* vl) {
+    int64_t hh = 0, mid = 0;
+#pragma unroll
+    for (int j = 0; j < D; j++) {
+        hh += (int64_t)vh[j] * mh[r][j];
+        mid += (int64_t)vh[j] * ml[r][j];
+        mid += (int64_t)vl[j] * mh[r][j];
+    }
+    return hh + (mid >> 32);
+}
+
+QG_HD double fx_to_double(int64_t R, uint32_t down) {
+    const uint64_t d = f64_bits(i64_to_double(R));
+    const uint32_t dh = (uint32_t)(d >> 32);
+    return bits_f64(dh ? ((uint64_t)(dh + down) << 32 | (uint32_t)d) : 0ull);
+}
+
+// complex output r: (re, im)
+template <int D>
+QG_HD void cfx_row(const CopN<D>& C, int r, const int32_t* xh, const int32_t* xl, const int32_t* yh, const int32_t* yl,
+                   const int32_t* sh, const int32_t* sl, uint32_t down, bool zero, double& re, double& im) {
+    if (zero) { re = 0.0; im = 0.0; return; }
+    const int64_t t1 = limb_dot<D>(C.ah, C.al, r, sh, sl);
+    const int64_t t2 = limb_dot<D>(C.ph, C.pl, r, yh, yl);
+    const int64_t t3 = limb_dot<D>(C.qh, C.ql, r, xh, xl);
+    re = fx_to_double(t1 - t2, down);
+    im = fx_to_double(t1 + t3, down);
 }
 
 // the fast form when it applies, else the general one; false: use FP64

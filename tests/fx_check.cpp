@@ -134,6 +134,49 @@ static void check_wide(std::mt19937_64& g, int cases) {
     }
 }
 
+// complex D x D operators in the three-product form against long double, and against
+// the real-form (four-product) result
+template <int D>
+static void check_complex(std::mt19937_64& g, int cases) {
+    constexpr int N = 2 * D;
+    std::normal_distribution<double> nd;
+    std::uniform_int_distribution<int> scale(-70, 8);
+    for (int t = 0; t < cases; t++) {
+        std::vector<double> u(2 * D * D), C(N * N), in(N);
+        for (auto& v : u) v = nd(g) * (t & 1 ? 0.3 : 1.0);
+        qgfx::real_form(u.data(), D, C.data());
+        qgfx::CopN<D> op;
+        if (!qgfx::make_cop<D>(u.data(), op)) { failures++; continue; }
+        const int s0 = scale(g);
+        for (int j = 0; j < N; j++) in[j] = std::ldexp(nd(g), s0 - (int)(g() % 3));
+        int32_t xh[D], xl[D], yh[D], yl[D], sh[D], sl[D];
+        uint32_t down;
+        bool zero;
+        if (!qgfx::cfx_prepare<D>(op, in.data(), xh, xl, yh, yl, sh, sl, down, zero)) { failures++; continue; }
+        ld maxIn = 0, maxC = 0;
+        for (int j = 0; j < N; j++) maxIn = std::fmax(maxIn, std::fabs((ld)in[j]));
+        for (int i = 0; i < N * N; i++) maxC = std::fmax(maxC, std::fabs((ld)C[i]));
+        constexpr int S = qgfx::FxShift<N>::S, Q = qgfx::FxShift<N>::Q;
+        for (int r = 0; r < D; r++) {
+            double out[2];
+            qgfx::cfx_row<D>(op, r, xh, xl, yh, yl, sh, sl, down, zero, out[0], out[1]);
+            for (int c = 0; c < 2; c++) {
+                ld ref = 0;
+                for (int j = 0; j < N; j++) ref += (ld)C[N * (2 * r + c)] * 0 + (ld)C[N * (2 * r + c) + j] * (ld)in[j];
+                // as the real form, with twice the coefficient rounding (A + B, B - A) and
+                // two sums' dropped terms per part
+                ld bound = (ld)N * (std::ldexp((ld)1, -(52 + S)) + std::ldexp((ld)2, -Q)) * maxIn * maxC
+                           + (ld)(2 * (D / 4 + 1)) * std::ldexp((ld)1, 13 - S - Q) * maxIn * maxC
+                           + std::ldexp(std::fabs(ref), -53) + 1e-320L;
+                ld err = std::fabs((ld)out[c] - ref);
+                numChecked++;
+                if (err > bound) { failures++; if (failures < 10) std::printf("complex %d out of bound %Lg %Lg\n", D, err, bound); }
+                worstRatio = std::fmax(worstRatio, (double)(err / bound));
+            }
+        }
+    }
+}
+
 static void run_all();
 
 int main() {
@@ -281,6 +324,10 @@ static void run_all() {
     // superoperators) on 8 and 16 amplitudes
     check_wide<16>(g, 20000);
     check_wide<32>(g, 10000);
+    check_complex<2>(g, 20000);
+    check_complex<4>(g, 20000);
+    check_complex<8>(g, 10000);
+    check_complex<16>(g, 5000);
     std::printf("%s variant=%d checked=%ld fallback=%ld worst_err_over_bound=%.3f fp64_fma_worst_over_bound=%.3f failures=%d\n",
                 failures ? "FAIL" : "OK", variant, numChecked, numFallback, worstRatio, worstRatioF64, failures);
 }
