@@ -11,16 +11,13 @@
 // part a TF32 value, and D = Xl*Bh + Xh*Bl + Xh*Bh accumulated in FP32 (the
 // Xl*Bl term is below FP32 rounding).  Bh/Bl are built once per block on the host.
 //
-// Per CTA tile: 256 threads, two per group row, each load 16 of the group's 32
-// amplitudes (coalesced 8-byte loads: consecutive threads own consecutive groups),
-// split them into TF32 hi/lo parts and store both into shared memory in the
-// no-swizzle K-major core-matrix layout (8 rows x 16 bytes per core matrix); one thread issues the
-// 24 MMAs (3 products x 8 K-steps of 8) into two 128-lane x 64-column TMEM
-// accumulators (large term, small terms) and commits them to an mbarrier; every
-// warp then reads its 32 TMEM lanes (tcgen05.ld 32x32b) in its half of the columns,
-// adds the two accumulators in FP32 and writes its groups' 16 outputs back.
-// Every wait is bounded: a wait that runs out sets the error flag, frees the
-// TMEM and returns.
+// Per tile, the producers split the 128 groups' amplitudes into TF32 hi/lo parts and
+// store both into shared memory in the no-swizzle K-major core-matrix layout (8 rows x
+// 16 bytes per core matrix); one thread issues the 24 MMAs (3 products x 8 K-steps of
+// 8) into two 128-lane x 64-column TMEM accumulators (large term, small terms); the
+// epilogue reads its TMEM lane (tcgen05.ld 32x32b), adds the two accumulators in FP32
+// and writes the group's 32 outputs back.  Every wait is bounded: a wait that runs out
+// sets the error flag, waits for the tensor core, frees the TMEM and returns.
 #include "qg_common.cuh"
 
 #include <mutex>
@@ -32,8 +29,6 @@
 #define TC_M 128              // groups per tile (MMA M)
 #define TC_K 64               // real K (32 complex amplitudes)
 #define TC_N 64               // real N
-#define TC_THREADS 256           // two threads per group row: each holds 16 of its 32 amplitudes
-#define TC_TMEM_COLS 128          // two 64-column accumulators: the large and the small 3xTF32 terms
 #define TC_WAIT_NS 2000000000ull   // a tile's MMAs take microseconds; 2 s means they never completed
 
 // shared-memory operand sizes (bytes)
@@ -167,33 +162,70 @@ struct TcArgs {
     int* errorFlag;    // set to 1 if a bounded wait ran out
 };
 
-__global__ void __launch_bounds__(TC_THREADS, 2) k32_fused_tc(TcArgs args) {
+// ---------------------------------------------------------------- kernel
+//
+// One persistent CTA per SM with three roles that hand tiles to one another through
+// mbarriers, so that loads, tensor-core work and stores of different tiles overlap:
+// * producers: TPR threads per group row load the row's 32 amplitudes, split them into
+//   TF32 hi/lo parts and write them into one of two A operand buffers.  Each holds
+//   NBUF tiles of loads in registers: NBUF - 1 tiles are in flight while one is split;
+// * one MMA warp (one elected thread): the 24 MMAs of a tile into one of two TMEM
+//   accumulator sets, committed to that buffer's "MMA done" barrier;
+// * 4 epilogue warps: one thread per group row (TMEM lane) reads the two accumulators,
+//   adds them and stores the row's 32 outputs.
+// Barriers per buffer s: aFull[s] (one arrival per producer), mmaDone[s] (the commit;
+// it also frees A[s]), tmemEmpty[s] (128 epilogue arrivals).  Tile i of a CTA uses
+// buffer i & 1 for the (i >> 1)-th time, which gives every wait's phase parity.
+#define WS_EPILOGUE 128
+#define TC_TPR 4       // producer threads per group row
+#define TC_NBUF 3      // register buffers per producer (tiles of loads in flight + 1)
+#define WS_TMEM_COLS 256
+#define WS_SMEM_BYTES (4 * TC_A_BYTES + 2 * TC_B_BYTES + 128 + 1024)
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(bar) : "memory");
+}
+
+// TPR producer threads per group row, each holding 32 / TPR amplitudes of it; NBUF
+// register buffers per producer, so NBUF - 1 tiles of loads are in flight while one
+// tile is split (the loop is unrolled NBUF times so buffers are never copied).
+template <int TPR, int NBUF>
+struct WsShape {
+    static constexpr int PRODUCERS = 128 * TPR;
+    static constexpr int AMPS = 32 / TPR;
+    static constexpr int MMA_WARP = PRODUCERS / 32;
+    static constexpr int THREADS = PRODUCERS + 32 + WS_EPILOGUE;
+};
+
+template <int TPR, int NBUF>
+__global__ void __launch_bounds__(WsShape<TPR, NBUF>::THREADS, 1) k32_fused_tc(TcArgs args) {
+    using S = WsShape<TPR, NBUF>;
+    constexpr int AMPS = S::AMPS;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    float* sAh = (float*)smem;
-    float* sAl = (float*)(smem + TC_A_BYTES);
-    float* sBh = (float*)(smem + 2 * TC_A_BYTES);
-    float* sBl = (float*)(smem + 2 * TC_A_BYTES + TC_B_BYTES);
-    uint64_t* bar = (uint64_t*)(smem + 2 * TC_A_BYTES + 2 * TC_B_BYTES);
-    uint32_t* tmemSlot = (uint32_t*)(bar + 1);
+    // A[s] = hi part then lo part (TC_A_BYTES each), s = 0, 1; then Bh, Bl
+    float* sB = (float*)(smem + 4 * TC_A_BYTES);
+    uint64_t* bars = (uint64_t*)(smem + 4 * TC_A_BYTES + 2 * TC_B_BYTES);   // aFull[2], mmaDone[2], tmemEmpty[2]
+    uint32_t* tmemSlot = (uint32_t*)(bars + 6);
     volatile int* abortFlag = (volatile int*)(tmemSlot + 1);
 
-    const int tid = threadIdx.x, warp = tid >> 5;
-    const int row = tid & (TC_M - 1), half = tid >> 7;   // thread (row g, half h): j in [16h, 16h+16)
-
-    // stage Bh, Bl once (already in the tile layout)
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     {
         const float4* src = (const float4*)args.ops;
-        float4* dst = (float4*)sBh;   // sBh and sBl are contiguous
-        for (int i = tid; i < (2 * TC_B_BYTES) / 16; i += TC_THREADS) dst[i] = __ldg(src + i);
+        float4* dst = (float4*)sB;
+        for (int i = tid; i < (2 * TC_B_BYTES) / 16; i += S::THREADS) dst[i] = __ldg(src + i);
     }
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_addr(bar)), "r"(1));
+        for (int s = 0; s < 2; s++) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_addr(bars + s)), "r"(S::PRODUCERS));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_addr(bars + 2 + s)), "r"(1));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_addr(bars + 4 + s)), "r"(WS_EPILOGUE));
+        }
         asm volatile("fence.mbarrier_init.release.cluster;");
         *abortFlag = 0;
     }
-    if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" :: "r"(smem_addr(tmemSlot)), "r"(TC_TMEM_COLS));
+    if (warp == S::MMA_WARP) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" :: "r"(smem_addr(tmemSlot)), "r"(WS_TMEM_COLS));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     asm volatile("fence.proxy.async.shared::cta;");
@@ -201,101 +233,127 @@ __global__ void __launch_bounds__(TC_THREADS, 2) k32_fused_tc(TcArgs args) {
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t tmem = *tmemSlot;
-    const uint32_t idesc = make_idesc();
-    const uint32_t aH = smem_addr(sAh), aL = smem_addr(sAl), bH = smem_addr(sBh), bL = smem_addr(sBl);
-    const uint32_t barAddr = smem_addr(bar);
-    uint32_t phase = 0;
+    const qidx first = blockIdx.x, step = gridDim.x;
+    const qidx nLocal = args.numTiles > first ? (args.numTiles - first + step - 1) / step : 0;
+    const uint32_t aFull = smem_addr(bars), mmaDone = smem_addr(bars + 2), tmemEmpty = smem_addr(bars + 4);
 
-    // Software pipeline: the next tile's 32 amplitudes per thread are loaded into
-    // registers while this tile's MMAs run and its results are written back.
-    qidx tile = blockIdx.x;
-    float2 x[16];
-    qidx base = 0;
-    if (tile < args.numTiles) {
-        base = insert_bits<5>(tile * TC_M + row, args.ins);
+    if (warp < S::MMA_WARP) {
+        // ---------------- producers: thread (row, part) holds amplitudes [AMPS*part, AMPS*part + AMPS) of its row
+        const int row = tid & (TC_M - 1), part = tid >> 7;
+        const qidx* off = args.off + AMPS * part;
+        float2 x[NBUF][AMPS];
+        auto load = [&](float2 (&dst)[AMPS], qidx i) {
+            const qidx base = insert_bits<5>((first + i * step) * TC_M + row, args.ins);
 #pragma unroll
-        for (int i = 0; i < 16; i++) x[i] = __ldcs(args.amps + base + args.off[16 * half + i]);
-    }
-    for (; tile < args.numTiles; tile += gridDim.x) {
-        // ---- split into TF32 hi/lo and store in the K-major core layout (kk = 2j + c)
+            for (int k = 0; k < AMPS; k++) dst[k] = __ldcs(args.amps + base + off[k]);
+        };
 #pragma unroll
-        for (int q = 0; q < 8; q++) {
-            float4 h, l;
-            h.x = tf32_hi(x[2 * q].x);     l.x = tf32_hi(x[2 * q].x - h.x);
-            h.y = tf32_hi(x[2 * q].y);     l.y = tf32_hi(x[2 * q].y - h.y);
-            h.z = tf32_hi(x[2 * q + 1].x); l.z = tf32_hi(x[2 * q + 1].x - h.z);
-            h.w = tf32_hi(x[2 * q + 1].y); l.w = tf32_hi(x[2 * q + 1].y - h.w);
-            unsigned o = core_offset(row, 4 * (8 * half + q), TC_M);
-            *(float4*)((unsigned char*)sAh + o) = h;
-            *(float4*)((unsigned char*)sAl + o) = l;
+        for (int b = 0; b < NBUF - 1; b++)
+            if (b < nLocal) load(x[b], b);
+        bool stop = false;
+        for (qidx i0 = 0; i0 < nLocal && !stop; i0 += NBUF) {
+#pragma unroll
+            for (int b = 0; b < NBUF; b++) {
+                const qidx i = i0 + b;
+                if (i >= nLocal) break;
+                if (i + NBUF - 1 < nLocal) load(x[(b + NBUF - 1) % NBUF], i + NBUF - 1);
+                const int s = (int)(i & 1);
+                const uint32_t u = (uint32_t)(i >> 1);
+                if (u >= 1 && !mbar_wait_bounded(mmaDone + 8 * s, (u - 1) & 1)) *abortFlag = 1;
+                if (*abortFlag) { stop = true; break; }
+                unsigned char* sAh = smem + (2 * s) * TC_A_BYTES;
+                unsigned char* sAl = sAh + TC_A_BYTES;
+#pragma unroll
+                for (int q = 0; q < AMPS / 2; q++) {
+                    const float2 p0 = x[b][2 * q], p1 = x[b][2 * q + 1];
+                    float4 h, l;
+                    h.x = tf32_hi(p0.x); l.x = tf32_hi(p0.x - h.x);
+                    h.y = tf32_hi(p0.y); l.y = tf32_hi(p0.y - h.y);
+                    h.z = tf32_hi(p1.x); l.z = tf32_hi(p1.x - h.z);
+                    h.w = tf32_hi(p1.y); l.w = tf32_hi(p1.y - h.w);
+                    const unsigned o = core_offset(row, 4 * ((AMPS / 2) * part + q), TC_M);
+                    *(float4*)(sAh + o) = h;
+                    *(float4*)(sAl + o) = l;
+                }
+                asm volatile("fence.proxy.async.shared::cta;");
+                mbar_arrive(aFull + 8 * s);
+            }
         }
-        asm volatile("fence.proxy.async.shared::cta;");
-        asm volatile("tcgen05.fence::before_thread_sync;");
-        __syncthreads();
-        asm volatile("tcgen05.fence::after_thread_sync;");
-
-        // ---- one thread issues the 24 MMAs (8 K-steps per product) and commits them:
-        //      columns 64..127 accumulate the small terms Al*Bh + Ah*Bl, columns 0..63 the
-        //      large term Ah*Bh; the epilogue adds the two in FP32
-        if (tid == 0) {
+    } else if (warp == S::MMA_WARP) {
+        // ---------------- MMA issue (one thread)
+        if (lane == 0) {
+            const uint32_t idesc = make_idesc();
             const uint32_t lboA = (TC_M / 8) * 128, lboB = (TC_N / 8) * 128, sbo = 128;
-            for (int part = 0; part < 3; part++) {
-                uint32_t a = (part == 0) ? aL : aH;
-                uint32_t b = (part == 1) ? bL : bH;
-                uint32_t d = (part == 2) ? tmem : tmem + TC_N;
-                uint32_t acc = (part == 1) ? 1u : 0u;
+            const uint32_t bH = smem_addr(sB), bL = bH + TC_B_BYTES;
+            qidx issued = 0;
+            for (qidx i = 0; i < nLocal; i++) {
+                const int s = (int)(i & 1);
+                const uint32_t u = (uint32_t)(i >> 1);
+                if (!mbar_wait_bounded(aFull + 8 * s, u & 1)) *abortFlag = 1;
+                if (!*abortFlag && u >= 1 && !mbar_wait_bounded(tmemEmpty + 8 * s, (u - 1) & 1)) *abortFlag = 1;
+                if (*abortFlag) break;
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                const uint32_t aH = smem_addr(smem + (2 * s) * TC_A_BYTES), aL = aH + TC_A_BYTES;
+                const uint32_t dBase = tmem + (uint32_t)s * 128;
+                for (int prod = 0; prod < 3; prod++) {
+                    const uint32_t a = (prod == 0) ? aL : aH;
+                    const uint32_t b = (prod == 1) ? bL : bH;
+                    const uint32_t d = (prod == 2) ? dBase : dBase + TC_N;
+                    uint32_t acc = (prod == 1) ? 1u : 0u;
 #pragma unroll
-                for (int s = 0; s < TC_K / 8; s++) {
-                    uint64_t ad = make_desc(a + s * 2 * lboA, lboA, sbo);
-                    uint64_t bd = make_desc(b + s * 2 * lboB, lboB, sbo);
-                    mma_tf32(d, ad, bd, idesc, acc);
-                    acc = 1;
+                    for (int k = 0; k < TC_K / 8; k++) {
+                        mma_tf32(d, make_desc(a + k * 2 * lboA, lboA, sbo), make_desc(b + k * 2 * lboB, lboB, sbo), idesc, acc);
+                        acc = 1;
+                    }
+                }
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" :: "r"(mmaDone + 8 * s) : "memory");
+                issued = i + 1;
+            }
+            // no MMA may still be running when the accumulators are freed
+            if (issued > 0) {
+                const qidx l = issued - 1;
+                if (!mbar_wait_bounded(mmaDone + 8 * (int)(l & 1), (uint32_t)(l >> 1) & 1)) *abortFlag = 1;
+            }
+        }
+        __syncwarp();
+    } else {
+        // ---------------- epilogue: TMEM lane quarter = warp % 4
+        const int quarter = warp & 3;
+        const int row = 32 * quarter + lane;
+        for (qidx i = 0; i < nLocal; i++) {
+            const int s = (int)(i & 1);
+            const uint32_t u = (uint32_t)(i >> 1);
+            // the warp leaves together: it runs warp-collective TMEM loads
+            const bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(mmaDone + 8 * s, u & 1));
+            if (!ok && lane == 0) *abortFlag = 1;
+            if (!ok || __shfl_sync(0xffffffffu, lane == 0 ? *abortFlag : 0, 0)) break;
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            const qidx base = insert_bits<5>((first + i * step) * TC_M + row, args.ins);
+            const uint32_t taddr = tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)s * 128;
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+                uint32_t big[16], small[16];
+                TMEM_LD16(taddr + 16 * c, big);
+                TMEM_LD16(taddr + TC_N + 16 * c, small);
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                if (c == 3) {
+                    asm volatile("tcgen05.fence::before_thread_sync;");
+                    mbar_arrive(tmemEmpty + 8 * s);
+                }
+#pragma unroll
+                for (int k = 0; k < 8; k++) {
+                    const float re = __uint_as_float(small[2 * k]) + __uint_as_float(big[2 * k]);
+                    const float im = __uint_as_float(small[2 * k + 1]) + __uint_as_float(big[2 * k + 1]);
+                    __stcs(args.amps + base + args.off[8 * c + k], make_float2(re, im));
                 }
             }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" :: "r"(barAddr) : "memory");
         }
-
-        // ---- while the MMAs run: load the next tile (registers only; shared memory is busy)
-        const qidx cur = base;
-        const qidx next = tile + gridDim.x;
-        if (next < args.numTiles) {
-            base = insert_bits<5>(next * TC_M + row, args.ins);
-#pragma unroll
-            for (int i = 0; i < 16; i++) x[i] = __ldcs(args.amps + base + args.off[16 * half + i]);
-        }
-
-        // ---- every thread waits for the MMAs (bounded by %globaltimer)
-        if (!mbar_wait_bounded(barAddr, phase)) *abortFlag = 1;
-        phase ^= 1;
-        __syncthreads();
-        if (*abortFlag) {
-            if (tid == 0) atomicExch(args.errorFlag, 1);
-            break;
-        }
-        asm volatile("tcgen05.fence::after_thread_sync;");
-
-        // ---- epilogue: warp w reads TMEM lanes 32(w mod 4).. (its groups) and the 32
-        //      columns of its half (outputs k in [16h, 16h+16)), 16 at a time
-        const uint32_t taddr = tmem + ((uint32_t)((warp & 3) * 32) << 16) + 32 * half;
-#pragma unroll
-        for (int c = 0; c < 2; c++) {
-            uint32_t big[16], small[16];
-            TMEM_LD16(taddr + 16 * c, big);
-            TMEM_LD16(taddr + TC_N + 16 * c, small);
-            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-            for (int k = 0; k < 8; k++) {
-                float re = __uint_as_float(small[2 * k]) + __uint_as_float(big[2 * k]);
-                float im = __uint_as_float(small[2 * k + 1]) + __uint_as_float(big[2 * k + 1]);
-                __stcs(args.amps + cur + args.off[16 * half + 8 * c + k], make_float2(re, im));
-            }
-        }
-        asm volatile("tcgen05.fence::before_thread_sync;");
-        __syncthreads();   // TMEM and the A buffers may now be overwritten
-        asm volatile("tcgen05.fence::after_thread_sync;");
     }
+    asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
-    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(TC_TMEM_COLS));
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    if (tid == 0 && *abortFlag) atomicExch(args.errorFlag, 1);
+    if (warp == S::MMA_WARP) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(WS_TMEM_COLS));
 }
 
 // ---------------------------------------------------------------- host: launch
@@ -317,8 +375,7 @@ int qg_tc_prepare() {
         QG_CUDA(cudaMemset(g_tc_error, 0, sizeof(int)));
     }
     if (!attr) {
-        const size_t smem = 2 * TC_A_BYTES + 2 * TC_B_BYTES + 64 + 1024;
-        QG_CUDA(cudaFuncSetAttribute(k32_fused_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        QG_CUDA(cudaFuncSetAttribute(k32_fused_tc<TC_TPR, TC_NBUF>, cudaFuncAttributeMaxDynamicSharedMemorySize, WS_SMEM_BYTES));
         attr = true;
     }
     return QG_OK;
@@ -341,10 +398,8 @@ int qg_tc_apply_block(float2* amps, int numQubits, const int* targs, const float
     }
     a.ops = devOperands;
     a.errorFlag = g_tc_error;
-    int sms = qg_num_sms();
-    size_t smem = 2 * TC_A_BYTES + 2 * TC_B_BYTES + 64 + 1024;
-    qidx grid = std::min<qidx>(a.numTiles, (qidx)sms * 2);
-    k32_fused_tc<<<(unsigned)grid, TC_THREADS, smem, st>>>(a);
+    const unsigned grid = (unsigned)std::min<qidx>(a.numTiles, (qidx)qg_num_sms());
+    k32_fused_tc<TC_TPR, TC_NBUF><<<grid, WsShape<TC_TPR, TC_NBUF>::THREADS, WS_SMEM_BYTES, st>>>(a);
     qg_note_launch();
     return qg_check_launch("k32_fused_tc");
 }
