@@ -160,6 +160,17 @@ struct TcArgs {
     qidx off[32];      // amplitude offset of matrix index j within a group
     const float* ops;  // Bh, Bl (global)
     int* errorFlag;    // set to 1 if a bounded wait ran out
+    // Staged mode, for blocks whose lowest target is below 5 (a warp's 32 groups are
+    // then not 32 adjacent amplitudes).  A tile's 4096 amplitudes are numbered in
+    // address order by a 12-bit local index L: bit p of L sits at amplitude bit P[p],
+    // P = the five targets and the seven lowest other bits, ascending.
+    int stage;
+    qidx lbit[12];     // 2^P[p]
+    int lrow[7];       // L bit holding bit i of the group row
+    int lj[5];         // L bit holding bit b of the matrix index j
+    qidx kp[16];       // producer element k: amplitude offset of the L bits above the producer index = k
+    qidx ke[32];       // epilogue element k: amplitude offset of L bits 7..11 = k
+    int sj[32];        // stage_slot of the L bits of matrix index j (the slot map is linear over XOR)
 };
 
 // ---------------------------------------------------------------- kernel
@@ -177,14 +188,42 @@ struct TcArgs {
 // it also frees A[s]), tmemEmpty[s] (128 epilogue arrivals).  Tile i of a CTA uses
 // buffer i & 1 for the (i >> 1)-th time, which gives every wait's phase parity.
 #define WS_EPILOGUE 128
-#define TC_TPR 4       // producer threads per group row
-#define TC_NBUF 3      // register buffers per producer (tiles of loads in flight + 1)
+// launch shapes: producer threads per group row and register buffers per producer
+// (tiles of loads in flight + 1), for the direct and the staged mode
+#define TC_TPR 2
+#define TC_NBUF 3
+#define TC_TPR_STAGED 4
+#define TC_NBUF_STAGED 2
 #define WS_TMEM_COLS 256
-#define WS_SMEM_BYTES (4 * TC_A_BYTES + 2 * TC_B_BYTES + 128 + 1024)
+#define WS_STAGE_BYTES (TC_M * 32 * 8)     // one tile of amplitudes (32 KiB)
+// shared memory: A[2] (hi, lo), Bh, Bl, the staging buffers the mode uses, barriers.
+// Shared memory and L1 share one array per SM, and L1 holds the loads in flight, so a
+// launch asks only for what its mode uses.
+#define WS_SMEM_BYTES(nstage) (4 * TC_A_BYTES + 2 * TC_B_BYTES + (nstage) * WS_STAGE_BYTES + 128 + 1024)
 
 __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(bar) : "memory");
 }
+
+// named barrier over `count` threads (a multiple of 32)
+__device__ __forceinline__ void named_sync(int id, int count) {
+    asm volatile("bar.sync %0, %1;" :: "r"(id), "r"(count) : "memory");
+}
+
+// named barrier that also ORs a flag over the `count` threads: every thread gets the
+// same answer, so a group that must leave a loop leaves it together
+__device__ __forceinline__ bool named_sync_or(int id, int count, bool flag) {
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\tbar.red.or.pred q, %2, %3, p;\n\tselp.u32 %0, 1, 0, q;\n\t}\n"
+        : "=r"(r) : "r"((uint32_t)flag), "r"(id), "r"(count) : "memory");
+    return r != 0;
+}
+
+// staging-buffer slot of local index e: the low five bits are XORed with the next
+// five, so that both address-order and group-row-order accesses of a warp spread
+// over the banks
+__device__ __forceinline__ int stage_slot(int e) { return e ^ ((e >> 5) & 31); }
 
 // TPR producer threads per group row, each holding 32 / TPR amplitudes of it; NBUF
 // register buffers per producer, so NBUF - 1 tiles of loads are in flight while one
@@ -192,20 +231,26 @@ __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
 template <int TPR, int NBUF>
 struct WsShape {
     static constexpr int PRODUCERS = 128 * TPR;
+    static constexpr int PBITS = TPR == 1 ? 7 : TPR == 2 ? 8 : 9;   // log2(PRODUCERS)
     static constexpr int AMPS = 32 / TPR;
     static constexpr int MMA_WARP = PRODUCERS / 32;
     static constexpr int THREADS = PRODUCERS + 32 + WS_EPILOGUE;
 };
 
-template <int TPR, int NBUF>
+// STAGED: the producers load in address order through a staging buffer; STAGED_OUT:
+// the epilogue stores in address order through a second one.
+template <int TPR, int NBUF, bool STAGED, bool STAGED_OUT>
 __global__ void __launch_bounds__(WsShape<TPR, NBUF>::THREADS, 1) k32_fused_tc(TcArgs args) {
     using S = WsShape<TPR, NBUF>;
     constexpr int AMPS = S::AMPS;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    // A[s] = hi part then lo part (TC_A_BYTES each), s = 0, 1; then Bh, Bl
+    // A[s] = hi part then lo part (TC_A_BYTES each), s = 0, 1; Bh, Bl; the producers'
+    // and the epilogue's staging buffers; barriers
     float* sB = (float*)(smem + 4 * TC_A_BYTES);
-    uint64_t* bars = (uint64_t*)(smem + 4 * TC_A_BYTES + 2 * TC_B_BYTES);   // aFull[2], mmaDone[2], tmemEmpty[2]
+    float2* sStageP = (float2*)(smem + 4 * TC_A_BYTES + 2 * TC_B_BYTES);
+    float2* sStageE = (float2*)(smem + 4 * TC_A_BYTES + 2 * TC_B_BYTES + (STAGED ? WS_STAGE_BYTES : 0));
+    uint64_t* bars = (uint64_t*)(smem + 4 * TC_A_BYTES + 2 * TC_B_BYTES + ((int)STAGED + (int)STAGED_OUT) * WS_STAGE_BYTES);   // aFull[2], mmaDone[2], tmemEmpty[2]
     uint32_t* tmemSlot = (uint32_t*)(bars + 6);
     volatile int* abortFlag = (volatile int*)(tmemSlot + 1);
 
@@ -238,14 +283,31 @@ __global__ void __launch_bounds__(WsShape<TPR, NBUF>::THREADS, 1) k32_fused_tc(T
     const uint32_t aFull = smem_addr(bars), mmaDone = smem_addr(bars + 2), tmemEmpty = smem_addr(bars + 4);
 
     if (warp < S::MMA_WARP) {
-        // ---------------- producers: thread (row, part) holds amplitudes [AMPS*part, AMPS*part + AMPS) of its row
+        // ---------------- producers.  Direct mode: thread (row, part) loads amplitudes
+        // [AMPS*part, AMPS*part + AMPS) of its row.  Staged mode: it loads the tile's
+        // elements L = tid + PRODUCERS * k (address order) into the staging buffer, then
+        // reads its row's amplitudes back from there.
         const int row = tid & (TC_M - 1), part = tid >> 7;
-        const qidx* off = args.off + AMPS * part;
+        qidx tOff = 0;
+        int sRow = 0, sTid = 0;
+        if constexpr (STAGED) {
+            int eRow = 0;
+#pragma unroll
+            for (int p = 0; p < S::PBITS; p++) tOff += ((tid >> p) & 1) ? args.lbit[p] : 0;
+#pragma unroll
+            for (int i = 0; i < 7; i++) eRow |= ((row >> i) & 1) << args.lrow[i];
+            sRow = stage_slot(eRow);
+            sTid = stage_slot(tid);
+        } else {
+            tOff = insert_bits<5>(row, args.ins);
+        }
+        const float2* src = args.amps + tOff;
+        const qidx* off = STAGED ? args.kp : args.off + AMPS * part;
         float2 x[NBUF][AMPS];
         auto load = [&](float2 (&dst)[AMPS], qidx i) {
-            const qidx base = insert_bits<5>((first + i * step) * TC_M + row, args.ins);
+            const float2* p = src + insert_bits<5>((first + i * step) * TC_M, args.ins);
 #pragma unroll
-            for (int k = 0; k < AMPS; k++) dst[k] = __ldcs(args.amps + base + off[k]);
+            for (int k = 0; k < AMPS; k++) dst[k] = __ldcs(p + off[k]);
         };
 #pragma unroll
         for (int b = 0; b < NBUF - 1; b++)
@@ -259,13 +321,32 @@ __global__ void __launch_bounds__(WsShape<TPR, NBUF>::THREADS, 1) k32_fused_tc(T
                 if (i + NBUF - 1 < nLocal) load(x[(b + NBUF - 1) % NBUF], i + NBUF - 1);
                 const int s = (int)(i & 1);
                 const uint32_t u = (uint32_t)(i >> 1);
-                if (u >= 1 && !mbar_wait_bounded(mmaDone + 8 * s, (u - 1) & 1)) *abortFlag = 1;
-                if (*abortFlag) { stop = true; break; }
+                bool bad = u >= 1 && !mbar_wait_bounded(mmaDone + 8 * s, (u - 1) & 1);
+                if (bad) *abortFlag = 1;
+                if constexpr (STAGED) {
+                    // all producers have finished reading the previous tile's staging
+                    if (named_sync_or(1, S::PRODUCERS, bad || *abortFlag)) { stop = true; break; }
+                    // slot(tid + PRODUCERS k) = slot(tid) ^ slot(PRODUCERS k), the second a constant
+#pragma unroll
+                    for (int k = 0; k < AMPS; k++) sStageP[sTid ^ stage_slot(S::PRODUCERS * k)] = x[b][k];
+                    named_sync(1, S::PRODUCERS);
+                } else if (*abortFlag) {
+                    stop = true;
+                    break;
+                }
                 unsigned char* sAh = smem + (2 * s) * TC_A_BYTES;
                 unsigned char* sAl = sAh + TC_A_BYTES;
 #pragma unroll
                 for (int q = 0; q < AMPS / 2; q++) {
-                    const float2 p0 = x[b][2 * q], p1 = x[b][2 * q + 1];
+                    float2 p0, p1;
+                    if constexpr (STAGED) {
+                        const int* sj = args.sj + AMPS * part + 2 * q;
+                        p0 = sStageP[sRow ^ sj[0]];
+                        p1 = sStageP[sRow ^ sj[1]];
+                    } else {
+                        p0 = x[b][2 * q];
+                        p1 = x[b][2 * q + 1];
+                    }
                     float4 h, l;
                     h.x = tf32_hi(p0.x); l.x = tf32_hi(p0.x - h.x);
                     h.y = tf32_hi(p0.y); l.y = tf32_hi(p0.y - h.y);
@@ -317,18 +398,43 @@ __global__ void __launch_bounds__(WsShape<TPR, NBUF>::THREADS, 1) k32_fused_tc(T
         }
         __syncwarp();
     } else {
-        // ---------------- epilogue: TMEM lane quarter = warp % 4
+        // ---------------- epilogue: TMEM lane quarter = warp % 4, one group row per
+        // thread.  Direct mode stores the row's 32 outputs; staged mode writes them into
+        // the staging buffer and stores the tile's elements L = row + 128 k in address order.
         const int quarter = warp & 3;
         const int row = 32 * quarter + lane;
+        qidx eOff = 0;
+        int sRow = 0;
+        if constexpr (STAGED_OUT) {
+            int eRow = 0;
+#pragma unroll
+            for (int p = 0; p < 7; p++) eOff += ((row >> p) & 1) ? args.lbit[p] : 0;
+#pragma unroll
+            for (int i = 0; i < 7; i++) eRow |= ((row >> i) & 1) << args.lrow[i];
+            sRow = stage_slot(eRow);
+        } else {
+            eOff = insert_bits<5>(row, args.ins);
+        }
+        float2* dstRow = args.amps + eOff;
+        const int sOut = stage_slot(row);
         for (qidx i = 0; i < nLocal; i++) {
             const int s = (int)(i & 1);
             const uint32_t u = (uint32_t)(i >> 1);
-            // the warp leaves together: it runs warp-collective TMEM loads
-            const bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(mmaDone + 8 * s, u & 1));
-            if (!ok && lane == 0) *abortFlag = 1;
-            if (!ok || __shfl_sync(0xffffffffu, lane == 0 ? *abortFlag : 0, 0)) break;
+            const bool waited = mbar_wait_bounded(mmaDone + 8 * s, u & 1);
+            if constexpr (STAGED_OUT) {
+                // the whole epilogue leaves together (named barriers below); this barrier
+                // also orders the previous tile's staging reads before this tile's writes
+                const bool bad = named_sync_or(2, WS_EPILOGUE, !waited || *abortFlag);
+                if (!waited) *abortFlag = 1;
+                if (bad) break;
+            } else {
+                // the warp leaves together: it runs warp-collective TMEM loads
+                const bool ok = __all_sync(0xffffffffu, waited);
+                if (!ok && lane == 0) *abortFlag = 1;
+                if (!ok || __shfl_sync(0xffffffffu, lane == 0 ? *abortFlag : 0, 0)) break;
+            }
             asm volatile("tcgen05.fence::after_thread_sync;");
-            const qidx base = insert_bits<5>((first + i * step) * TC_M + row, args.ins);
+            float2* dst = dstRow + insert_bits<5>((first + i * step) * TC_M, args.ins);
             const uint32_t taddr = tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)s * 128;
 #pragma unroll
             for (int c = 0; c < 4; c++) {
@@ -344,8 +450,17 @@ __global__ void __launch_bounds__(WsShape<TPR, NBUF>::THREADS, 1) k32_fused_tc(T
                 for (int k = 0; k < 8; k++) {
                     const float re = __uint_as_float(small[2 * k]) + __uint_as_float(big[2 * k]);
                     const float im = __uint_as_float(small[2 * k + 1]) + __uint_as_float(big[2 * k + 1]);
-                    __stcs(args.amps + base + args.off[8 * c + k], make_float2(re, im));
+                    if constexpr (STAGED_OUT)
+                        sStageE[sRow ^ args.sj[8 * c + k]] = make_float2(re, im);
+                    else
+                        __stcs(dst + args.off[8 * c + k], make_float2(re, im));
                 }
+            }
+            if constexpr (STAGED_OUT) {
+                named_sync(2, WS_EPILOGUE);
+                // slot(row + 128 k) = slot(row) ^ slot(128 k)
+#pragma unroll 8
+                for (int k = 0; k < 32; k++) __stcs(dst + args.ke[k], sStageE[sOut ^ stage_slot(WS_EPILOGUE * k)]);
             }
         }
     }
@@ -364,6 +479,17 @@ int* g_tc_error = nullptr;
 
 bool qg_tc_supported(int numQubits) { return numQubits >= 12; }
 
+namespace {
+// the host form of insert_bits: a zero opened at each listed position
+qidx insert_bits_host(qidx n, const Ins& ins) {
+    for (int i = 0; i < ins.num; i++) {
+        const qidx lo = n & ins.low[i];
+        n = ((n ^ lo) << 1) | lo;
+    }
+    return n;
+}
+}  // namespace
+
 // one-time set-up (the error flag's memory, the kernel's shared-memory limit); done
 // before the first launch and before any stream capture of one
 int qg_tc_prepare() {
@@ -375,7 +501,9 @@ int qg_tc_prepare() {
         QG_CUDA(cudaMemset(g_tc_error, 0, sizeof(int)));
     }
     if (!attr) {
-        QG_CUDA(cudaFuncSetAttribute(k32_fused_tc<TC_TPR, TC_NBUF>, cudaFuncAttributeMaxDynamicSharedMemorySize, WS_SMEM_BYTES));
+        QG_CUDA(cudaFuncSetAttribute(k32_fused_tc<TC_TPR, TC_NBUF, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, WS_SMEM_BYTES(0)));
+        QG_CUDA(cudaFuncSetAttribute(k32_fused_tc<TC_TPR_STAGED, TC_NBUF_STAGED, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, WS_SMEM_BYTES(1)));
+        QG_CUDA(cudaFuncSetAttribute(k32_fused_tc<TC_TPR_STAGED, TC_NBUF_STAGED, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, WS_SMEM_BYTES(2)));
         attr = true;
     }
     return QG_OK;
@@ -398,8 +526,63 @@ int qg_tc_apply_block(float2* amps, int numQubits, const int* targs, const float
     }
     a.ops = devOperands;
     a.errorFlag = g_tc_error;
+    // Row-by-row access makes one warp instruction touch `lines` distinct 128-byte lines
+    // (32 groups, one amplitude each).  Measured on GB300 at 30 qubits: 32 lines run
+    // fastest fully staged (5.3 ms against 8.9 ms row by row), 16 lines with staged loads
+    // only (4.7 against 5.1), 8 or fewer row by row (2.8-3.9 against 3.4-5.4 staged).
+    int lines = 0;
+    {
+        qidx seen[32];
+        for (int r = 0; r < 32; r++) {
+            const qidx line = insert_bits_host(r, p.ins) >> 4;   // 16 FP32 amplitudes per line
+            bool dup = false;
+            for (int q = 0; q < lines; q++) dup |= seen[q] == line;
+            if (!dup) seen[lines++] = line;
+        }
+    }
+    a.stage = lines >= 32 ? 2 : lines >= 16 ? 1 : 0;
+    {
+        // local bit positions: the targets and the seven lowest other bits, ascending
+        int pos[12], n = 0, rows = 0;
+        for (int q = 0; q < numQubits && n < 12; q++) {
+            bool isTarg = false;
+            for (int b = 0; b < 5; b++) isTarg |= targs[b] == q;
+            if (isTarg || rows < 7) {
+                if (!isTarg) rows++;
+                pos[n++] = q;
+            }
+        }
+        int r = 0;
+        for (int pb = 0; pb < 12; pb++) {
+            a.lbit[pb] = (qidx)1 << pos[pb];
+            int jb = -1;
+            for (int b = 0; b < 5; b++) if (targs[b] == pos[pb]) jb = b;
+            if (jb >= 0) a.lj[jb] = pb;
+            else a.lrow[r++] = pb;
+        }
+        constexpr int PB = WsShape<TC_TPR_STAGED, TC_NBUF_STAGED>::PBITS;
+        for (int k = 0; k < (1 << (12 - PB)); k++) {
+            a.kp[k] = 0;
+            for (int c = 0; c < 12 - PB; c++) if ((k >> c) & 1) a.kp[k] += a.lbit[PB + c];
+        }
+        for (int k = 0; k < 32; k++) {
+            a.ke[k] = 0;
+            int ej = 0;
+            for (int c = 0; c < 5; c++) {
+                if ((k >> c) & 1) a.ke[k] += a.lbit[7 + c];
+                if ((k >> c) & 1) ej |= 1 << a.lj[c];
+            }
+            a.sj[k] = ej ^ ((ej >> 5) & 31);
+        }
+    }
     const unsigned grid = (unsigned)std::min<qidx>(a.numTiles, (qidx)qg_num_sms());
-    k32_fused_tc<TC_TPR, TC_NBUF><<<grid, WsShape<TC_TPR, TC_NBUF>::THREADS, WS_SMEM_BYTES, st>>>(a);
+    using SS = WsShape<TC_TPR_STAGED, TC_NBUF_STAGED>;
+    if (a.stage == 2)
+        k32_fused_tc<TC_TPR_STAGED, TC_NBUF_STAGED, true, true><<<grid, SS::THREADS, WS_SMEM_BYTES(2), st>>>(a);
+    else if (a.stage == 1)
+        k32_fused_tc<TC_TPR_STAGED, TC_NBUF_STAGED, true, false><<<grid, SS::THREADS, WS_SMEM_BYTES(1), st>>>(a);
+    else
+        k32_fused_tc<TC_TPR, TC_NBUF, false, false><<<grid, WsShape<TC_TPR, TC_NBUF>::THREADS, WS_SMEM_BYTES(0), st>>>(a);
     qg_note_launch();
     return qg_check_launch("k32_fused_tc");
 }

@@ -77,10 +77,15 @@ def test_fused_brickwork_vs_fp64_oracle(env, n, depth, impl):
     assert flag.value == 0
 
 
-@pytest.mark.parametrize("targs", [[0, 1, 2, 3, 4], [7, 8, 9, 10, 11], [11, 0, 6, 3, 9], [2, 5, 6, 10, 13],
-                                   [13, 12, 1, 0, 7]])
-def test_single_5qubit_block_every_layout(env, targs):
-    n = 14
+# The tensor-core kernel picks its mode from how many 128-byte lines one warp instruction
+# would touch row by row: 32 lines (e.g. targets 0-4, or 0-3 and any) load and store in
+# address order through shared memory, 16 lines (e.g. 1-5) load that way only, and the
+# rest go row by row.  These layouts cover all three.
+@pytest.mark.parametrize("n,targs", [(14, [0, 1, 2, 3, 4]), (14, [7, 8, 9, 10, 11]), (14, [11, 0, 6, 3, 9]),
+                                     (14, [2, 5, 6, 10, 13]), (14, [13, 12, 1, 0, 7]), (14, [1, 2, 3, 4, 5]),
+                                     (14, [4, 5, 6, 7, 8]), (14, [5, 6, 7, 8, 9]), (12, [0, 1, 2, 3, 11]),
+                                     (12, [11, 10, 9, 8, 7])])
+def test_single_5qubit_block_every_layout(env, n, targs):
     rng = np.random.default_rng(sum(targs))
     u = qc.haar_unitary(32, rng)
     amps = qc.random_statevector(n, 3)
@@ -179,3 +184,21 @@ def test_autotune_fuses_at_the_fastest_candidate(env):
     finally:
         s.free()
     assert fidelity(got, run_oracle(n, amps, gates)) >= 1 - 1e-6
+
+
+# 1024 tiles of 128 groups: every CTA runs several tiles, so both operand buffers and
+# both accumulator sets are reused (the barrier phases of later tiles)
+@pytest.mark.parametrize("targs", [[0, 1, 2, 3, 4], [1, 2, 3, 4, 5], [3, 9, 0, 15, 21], [5, 6, 7, 8, 9],
+                                   [17, 18, 19, 20, 21]])
+def test_single_block_many_tiles_per_cta(env, targs):
+    n = 22
+    rng = np.random.default_rng(7 + sum(targs))
+    u = qc.haar_unitary(32, rng)
+    amps = qc.random_statevector(n, 11)
+    ref = run_oracle(n, amps, [(targs, u)])
+    tc, _ = run_fused(env, n, amps, [(targs, u)], 5, 2)
+    assert np.max(np.abs(tc - ref)) <= 2e-6 * np.max(np.abs(ref))
+    from quest_gb300 import _lib
+    flag = ctypes.c_int(0)
+    _lib.lib().qg_tc_get_error_flag(ctypes.byref(flag))
+    assert flag.value == 0
