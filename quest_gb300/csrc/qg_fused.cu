@@ -326,27 +326,75 @@ __global__ void __launch_bounds__(128) k32_fused(float2* __restrict__ a, qidx nu
     }
 }
 
-// sum |a_i|^2 in FP64 over an FP32 vector
-__global__ void __launch_bounds__(RED_THREADS) k32_sum_norm(const float2* __restrict__ a, qidx n, RedOut out) {
-    double v[1] = {0.0};
-    qidx stride = (qidx)gridDim.x * RED_THREADS;
-    for (qidx i = blockIdx.x * (qidx)RED_THREADS + threadIdx.x; i < n; i += stride) {
-        float2 x = ld32(a + i);
-        v[0] += (double)x.x * x.x + (double)x.y * x.y;
+// sum |a_i|^2 in FP64 over an FP32 vector (n even): two amplitudes per 16-byte load,
+// four loads in flight per thread, four independent FP64 accumulators.  Each square
+// is exact in FP64; the FP64 adds (two per amplitude) bound the kernel near 2.5 TB/s
+// on GB300.
+__device__ __forceinline__ double sq4(float4 x) {
+    return fma((double)x.x, (double)x.x, fma((double)x.y, (double)x.y, fma((double)x.z, (double)x.z, (double)x.w * x.w)));
+}
+
+__global__ void __launch_bounds__(RED_THREADS) k32_sum_norm(const float2* __restrict__ a, qidx n, bool vec16, RedOut out) {
+    const qidx stride = (qidx)gridDim.x * RED_THREADS;
+    qidx i = blockIdx.x * (qidx)RED_THREADS + threadIdx.x;
+    if (!vec16) {   // a pointer that is 8- but not 16-byte aligned: one amplitude per load
+        double v[1] = {0.0};
+        for (; i < n; i += stride) {
+            const float2 x = __ldcs(a + i);
+            v[0] += (double)x.x * x.x + (double)x.y * x.y;
+        }
+        block_reduce_and_finish<1>(v, out);
+        return;
     }
+    const float4* a4 = (const float4*)a;
+    const qidx n4 = n >> 1;
+    double v0 = 0.0, v1 = 0.0, v2 = 0.0, v3 = 0.0;
+    for (; i + 3 * stride < n4; i += 4 * stride) {
+        const float4 x0 = __ldcs(a4 + i), x1 = __ldcs(a4 + i + stride);
+        const float4 x2 = __ldcs(a4 + i + 2 * stride), x3 = __ldcs(a4 + i + 3 * stride);
+        v0 += sq4(x0);
+        v1 += sq4(x1);
+        v2 += sq4(x2);
+        v3 += sq4(x3);
+    }
+    for (; i < n4; i += stride) v0 += sq4(__ldcs(a4 + i));
+    double v[1] = {(v0 + v1) + (v2 + v3)};
     block_reduce_and_finish<1>(v, out);
 }
 
-// a_i *= sqrt(target / sum), the sum read from device memory (written by k32_sum_norm)
-__global__ void k32_scale_to_norm(float2* __restrict__ a, qidx n, const double* __restrict__ sum, double target) {
-    const double s = *sum;
-    const float f = s > 0 ? (float)sqrt(target / s) : 1.0f;
-    qidx stride = (qidx)gridDim.x * blockDim.x;
-    for (qidx i = blockIdx.x * (qidx)blockDim.x + threadIdx.x; i < n; i += stride) {
-        float2 x = ld32(a + i);
-        x.x *= f;
-        x.y *= f;
-        a[i] = x;
+// a_i *= sqrt(target / sum), the sum read from device memory (written by k32_sum_norm);
+// the factor is computed once per block, and each thread moves 16-byte pairs
+__global__ void __launch_bounds__(256) k32_scale_to_norm(float2* __restrict__ a, qidx n, bool vec16, const double* __restrict__ sum, double target) {
+    __shared__ float sf;
+    if (threadIdx.x == 0) {
+        const double s = *sum;
+        sf = s > 0 ? (float)sqrt(target / s) : 1.0f;
+    }
+    __syncthreads();
+    const float f = sf;
+    const qidx stride = (qidx)gridDim.x * blockDim.x;
+    qidx i = blockIdx.x * (qidx)blockDim.x + threadIdx.x;
+    if (!vec16) {
+        for (; i < n; i += stride) {
+            float2 x = __ldcs(a + i);
+            x.x *= f; x.y *= f;
+            __stcs(a + i, x);
+        }
+        return;
+    }
+    float4* a4 = (float4*)a;
+    const qidx n4 = n >> 1;
+    for (; i + stride < n4; i += 2 * stride) {
+        float4 x0 = __ldcs(a4 + i), x1 = __ldcs(a4 + i + stride);
+        x0.x *= f; x0.y *= f; x0.z *= f; x0.w *= f;
+        x1.x *= f; x1.y *= f; x1.z *= f; x1.w *= f;
+        __stcs(a4 + i, x0);
+        __stcs(a4 + i + stride, x1);
+    }
+    for (; i < n4; i += stride) {
+        float4 x = __ldcs(a4 + i);
+        x.x *= f; x.y *= f; x.z *= f; x.w *= f;
+        __stcs(a4 + i, x);
     }
 }
 
@@ -770,7 +818,7 @@ int qg_sv32_calcTotalProb(const void* amps, int numQubits, double* out, void* st
     RedOut r;
     QG_TRY(red_setup(grid, 1, &r));
     cudaStream_t st = qg_stream(stream);
-    k32_sum_norm<<<grid, RED_THREADS, 0, st>>>((const float2*)amps, n, r);
+    k32_sum_norm<<<grid, RED_THREADS, 0, st>>>((const float2*)amps, n, ((uintptr_t)amps & 15) == 0, r);
     return red_fetch(r, 1, out, st);
 }
 
@@ -782,10 +830,12 @@ int qg_sv32_normalise(void* amps, int numQubits, double targetProb, void* stream
     RedOut r;
     QG_TRY(red_setup(grid, 1, &r));
     cudaStream_t st = qg_stream(stream);
-    k32_sum_norm<<<grid, RED_THREADS, 0, st>>>((const float2*)amps, n, r);
+    const bool vec16 = ((uintptr_t)amps & 15) == 0;
+    k32_sum_norm<<<grid, RED_THREADS, 0, st>>>((const float2*)amps, n, vec16, r);
     qg_note_launch();
     QG_TRY(qg_check_launch("k32_sum_norm"));
-    k32_scale_to_norm<<<qg_blocks(n), QG_THREADS, 0, st>>>((float2*)amps, n, r.result, targetProb);
+    const unsigned sgrid = (unsigned)std::min<qidx>(qg_blocks(n / 2, 256), (qidx)qg_num_sms() * 8);
+    k32_scale_to_norm<<<sgrid, 256, 0, st>>>((float2*)amps, n, vec16, r.result, targetProb);
     qg_note_launch();
     return qg_check_launch("k32_scale_to_norm");
 }

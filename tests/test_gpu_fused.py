@@ -135,6 +135,34 @@ def test_normalise_rescales_to_the_target_probability(env):
         s.free()
 
 
+def test_fp32_norm_and_rescale_on_an_8_byte_aligned_pointer(env):
+    # the norm and rescale kernels move 16-byte amplitude pairs when the pointer allows
+    # it; a pointer that is only 8-byte aligned takes their one-amplitude path
+    from quest_gb300 import _lib
+    lib = _lib.lib()
+    n = 15
+    amps = (qc.random_statevector(n, 21) * 1.7).astype(np.complex64)
+    a64 = amps.astype(np.complex128)
+    want_sum = np.vdot(a64, a64).real
+    base = ctypes.c_void_p()
+    _lib.check(lib.qg_alloc(ctypes.byref(base), (len(amps) + 2) * 8))
+    try:
+        for shift in (0, 8):
+            ptr = ctypes.c_void_p(base.value + shift)
+            _lib.check(lib.qg_copy_h2d(ptr, amps.ctypes.data, amps.nbytes, None))
+            lib.qg_sync()
+            tot = ctypes.c_double()
+            _lib.check(lib.qg_sv32_calcTotalProb(ptr, n, ctypes.byref(tot), None))
+            assert abs(tot.value - want_sum) < 1e-12 * want_sum
+            _lib.check(lib.qg_sv32_normalise(ptr, n, 1.0, None))
+            got = np.empty_like(amps)
+            _lib.check(lib.qg_copy_d2h(got.ctypes.data, ptr, got.nbytes, None))
+            want = a64 / np.sqrt(want_sum)
+            assert np.max(np.abs(got.astype(np.complex128) - want)) <= 4 * np.finfo(np.float32).eps * np.max(np.abs(want))
+    finally:
+        lib.qg_free(base)
+
+
 @pytest.mark.parametrize("impl", [1, 2])
 def test_graph_replays_the_circuit(env, impl):
     """A CUDA graph of the block kernels gives the same bits as applying the circuit."""
