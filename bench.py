@@ -821,6 +821,72 @@ def run_gates(args, world, rank, local, dist):
         print(json.dumps(line), flush=True)
 
 
+def run_blocks(args, world, rank, local, dist):
+    """Per-target-set timing of one fused 5-qubit block on an FP32 register through the
+    tensor-core kernel (`Circuit` API, impl = tc): ms per apply from CUDA events over
+    `--steps` applies after `--warmup`.  `lines` is how many 128-byte lines one warp
+    instruction would touch loading 32 groups row by row; the kernel stages its loads
+    (16 lines) or its loads and stores (32 lines) through shared memory."""
+    import ctypes as C
+    from quest_gb300 import _lib
+    from quest_gb300.fused import Circuit, StateVector32, IMPL_TC
+    L = _lib.lib()
+    _lib.check(L.qg_init(local))
+    n = args.qubits
+    if args.block_targets:
+        sets = [[int(v) for v in ts.split(",")] for ts in args.block_targets.split(";")]
+    else:
+        sets = [[0, 1, 2, 3, 4], [1, 2, 3, 4, 5], [2, 3, 4, 5, 6], [0, 1, 7, 13, 19], [5, 6, 7, 8, 9],
+                list(range(n - 5, n))]
+    rng = np.random.default_rng(0x5155455354 + 7)
+    s = StateVector32(n)
+    s.init_zero()
+    e0, e1 = C.c_void_p(), C.c_void_p()
+    L.qg_event_create(C.byref(e0))
+    L.qg_event_create(C.byref(e1))
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    peak = peaks.get("hbm_gbs", 6800.0)
+    rows = []
+    for targs in sets:
+        c = Circuit(n)
+        c.add(targs, haar(32, rng))
+        c.fuse(5)
+        for _ in range(max(1, args.warmup)):
+            c.apply(s, impl=IMPL_TC)
+        L.qg_sync()
+        L.qg_event_record(e0, None)
+        for _ in range(args.steps):
+            c.apply(s, impl=IMPL_TC)
+        L.qg_event_record(e1, None)
+        L.qg_sync()
+        ms = C.c_float()
+        L.qg_event_elapsed_ms(e0, e1, C.byref(ms))
+        per = ms.value / args.steps
+        ts = sorted(targs)
+
+        def ins(v):
+            for t in ts:
+                lo = v & ((1 << t) - 1)
+                v = ((v ^ lo) << 1) | lo
+            return v
+        lines = len({ins(r) >> 4 for r in range(32)})
+        gbs = 2 * 8 * (1 << n) / per / 1e6
+        rows.append({"targets": targs, "lines": lines, "ms": round(per, 4), "gbs": round(gbs, 1),
+                     "frac_of_hbm": round(gbs / peak, 3)})
+    flag = C.c_int(0)
+    L.qg_tc_get_error_flag(C.byref(flag))
+    s.free()
+    line = {"metric": "per-block GB/s of the FP32 tensor-core block kernel, by target set", "value": rows[-1]["gbs"],
+            "unit": "GB/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (3xTF32 tensor-core products)",
+            "data": "synthetic (|0> state, seeded Haar 32x32 unitaries)",
+            "config": {"workload": f"{n}-qubit FP32 statevector, one 5-qubit block per launch", "qubits": n,
+                       "l2": "state larger than L2; no flush"},
+            "blocks": rows, "tc_error_flag": flag.value, "hbm_peak_gbs": peak}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -831,9 +897,11 @@ def main():
     ap.add_argument("--depth", type=int, default=20)
     ap.add_argument("--cpu-sample", type=int, default=45, help="gates of the circuit timed on the host CPU")
     ap.add_argument("--traffic", type=float, default=None, help="ncu DRAM bytes per dense launch, if captured")
-    ap.add_argument("--config", default="plain", choices=["plain", "precision", "serve", "gates"],
+    ap.add_argument("--config", default="plain", choices=["plain", "precision", "serve", "gates", "blocks"],
                     help="plain: the 30-qubit FP64 per-gate circuit (default); precision: FP32 fused blocks; "
-                         "serve: request stream, served vs plain; gates: per-gate-kind timing (28 qubits)")
+                         "serve: request stream, served vs plain; gates: per-gate-kind timing (28 qubits); "
+                         "blocks: one FP32 5-qubit block per target set")
+    ap.add_argument("--block-targets", default="", help="blocks: target sets, e.g. '0,1,2,3,4;5,6,7,8,9'")
     ap.add_argument("--requests", type=int, default=48)
     ap.add_argument("--min-qubits", type=int, default=8)
     ap.add_argument("--max-qubits", type=int, default=26)
@@ -851,6 +919,8 @@ def main():
         run_serve(args, world, rank, local, dist)
     elif args.config == "gates":
         run_gates(args, world, rank, local, dist)
+    elif args.config == "blocks":
+        run_blocks(args, world, rank, local, dist)
     elif args.config == "precision":
         if args.qubits == 30 and "--qubits" not in sys.argv:
             args.qubits = 32
