@@ -130,9 +130,12 @@ __device__ __forceinline__ void dense1_fx_pair(const qgfx::Op4& C, const Mat1& M
 }
 
 // The launch bound asks for half the SM's thread slots resident (4 blocks of 256):
-// it caps registers at 64 (one 8-byte spill), and the extra warps take the kernel from
-// 0.86 to 0.94 of the measured HBM rate at 30 qubits.
-template <int NB, int PPT, int THREADS>
+// it caps registers at 64, and the extra warps take the kernel from 0.86 to 0.94 of
+// the measured HBM rate at 30 qubits.  Each thread keeps NBUF rounds of PPT pairs in
+// registers: the loads of the next NBUF - 1 rounds are in flight while one round is
+// computed, and the loop is unrolled NBUF times so that no buffer is ever copied (a
+// register copy of a pending load would wait for it).
+template <int NB, int PPT, int THREADS, int NBUF = 2>
 __global__ void __launch_bounds__(THREADS, 2048 / THREADS / 2) k_dense1_fx(double2* __restrict__ a, qidx numIts, Ins ins, qidx mask,
                                                       qidx tbit, qgfx::Op4 C, Mat1 M) {
     const qidx stride = (qidx)gridDim.x * THREADS;
@@ -140,36 +143,34 @@ __global__ void __launch_bounds__(THREADS, 2048 / THREADS / 2) k_dense1_fx(doubl
     const qidx tid = blockIdx.x * (qidx)THREADS + threadIdx.x;
     const qidx groups = numIts / span;      // rounds in which all PPT pairs of every thread exist
     if (groups > 0) {
-        qidx i0[PPT];
-        double2 x[PPT], y[PPT];
-#pragma unroll
-        for (int k = 0; k < PPT; k++) {
-            i0[k] = insert_bits<NB>(tid + k * stride, ins) | mask;
-            x[k] = ld_amp(a + i0[k]);
-            y[k] = ld_amp(a + (i0[k] | tbit));
-        }
-        for (qidx g = 1;; g++) {
-            const bool more = g < groups;
-            qidx j0[PPT];
-            double2 xn[PPT], yn[PPT];
-            if (more) {
-#pragma unroll
-                for (int k = 0; k < PPT; k++) {
-                    j0[k] = insert_bits<NB>(g * span + tid + k * stride, ins) | mask;
-                    xn[k] = ld_amp(a + j0[k]);
-                    yn[k] = ld_amp(a + (j0[k] | tbit));
-                }
-            }
+        qidx i0[NBUF][PPT];
+        double2 x[NBUF][PPT], y[NBUF][PPT];
+        auto load = [&](qidx (&ib)[PPT], double2 (&xb)[PPT], double2 (&yb)[PPT], qidx g) {
 #pragma unroll
             for (int k = 0; k < PPT; k++) {
-                double2 o0, o1;
-                dense1_fx_pair(C, M, x[k], y[k], o0, o1);
-                st_amp(a + i0[k], o0);
-                st_amp(a + (i0[k] | tbit), o1);
+                ib[k] = insert_bits<NB>(g * span + tid + k * stride, ins) | mask;
+                xb[k] = ld_amp(a + ib[k]);
+                yb[k] = ld_amp(a + (ib[k] | tbit));
             }
-            if (!more) break;
+        };
 #pragma unroll
-            for (int k = 0; k < PPT; k++) { i0[k] = j0[k]; x[k] = xn[k]; y[k] = yn[k]; }
+        for (int b = 0; b < NBUF - 1; b++)
+            if (b < groups) load(i0[b], x[b], y[b], b);
+        for (qidx g0 = 0; g0 < groups; g0 += NBUF) {
+#pragma unroll
+            for (int b = 0; b < NBUF; b++) {
+                const qidx g = g0 + b;
+                if (g >= groups) break;
+                const int nb = (b + NBUF - 1) % NBUF;
+                if (g + NBUF - 1 < groups) load(i0[nb], x[nb], y[nb], g + NBUF - 1);
+#pragma unroll
+                for (int k = 0; k < PPT; k++) {
+                    double2 o0, o1;
+                    dense1_fx_pair(C, M, x[b][k], y[b][k], o0, o1);
+                    st_amp(a + i0[b][k], o0);
+                    st_amp(a + (i0[b][k] | tbit), o1);
+                }
+            }
         }
     }
     // the remaining pairs, one at a time
@@ -393,9 +394,10 @@ __device__ __forceinline__ double2 diag1_fx_amp(const qgfx::Op2& F, double2 f, d
 }
 
 // MODE 1: every visited amplitude times F0 (the target bit is part of the fixed mask);
-// MODE 0: F0 or F1 by the target bit.  PPT amplitudes per thread per round, the
-// next round's loads issued before this round's products.
-template <int NB, int MODE, int PPT, int THREADS>
+// MODE 0: F0 or F1 by the target bit.  PPT amplitudes per thread per round, NBUF rounds
+// in registers: the next NBUF - 1 rounds' loads are in flight while one round's
+// products are formed (the loop is unrolled NBUF times, so no buffer is copied).
+template <int NB, int MODE, int PPT, int THREADS, int NBUF = 2>
 __global__ void __launch_bounds__(THREADS) k_diag1_fx(double2* __restrict__ a, qidx numIts, Ins ins, qidx mask, qidx tbit,
                                                      double2 d0, double2 d1, qgfx::Op2 F0, qgfx::Op2 F1) {
     const qidx stride = (qidx)gridDim.x * THREADS;
@@ -403,32 +405,31 @@ __global__ void __launch_bounds__(THREADS) k_diag1_fx(double2* __restrict__ a, q
     const qidx tid = blockIdx.x * (qidx)THREADS + threadIdx.x;
     const qidx groups = numIts / span;
     if (groups > 0) {
-        qidx i[PPT];
-        double2 x[PPT];
-#pragma unroll
-        for (int k = 0; k < PPT; k++) {
-            i[k] = insert_bits<NB>(tid + k * stride, ins) | mask;
-            x[k] = ld_amp(a + i[k]);
-        }
-        for (qidx g = 1;; g++) {
-            const bool more = g < groups;
-            qidx j[PPT];
-            double2 xn[PPT];
-            if (more) {
-#pragma unroll
-                for (int k = 0; k < PPT; k++) {
-                    j[k] = insert_bits<NB>(g * span + tid + k * stride, ins) | mask;
-                    xn[k] = ld_amp(a + j[k]);
-                }
-            }
+        qidx i[NBUF][PPT];
+        double2 x[NBUF][PPT];
+        auto load = [&](qidx (&ib)[PPT], double2 (&xb)[PPT], qidx g) {
 #pragma unroll
             for (int k = 0; k < PPT; k++) {
-                const bool second = (MODE == 0) && (i[k] & tbit);
-                st_amp(a + i[k], diag1_fx_amp(second ? F1 : F0, second ? d1 : d0, x[k]));
+                ib[k] = insert_bits<NB>(g * span + tid + k * stride, ins) | mask;
+                xb[k] = ld_amp(a + ib[k]);
             }
-            if (!more) break;
+        };
 #pragma unroll
-            for (int k = 0; k < PPT; k++) { i[k] = j[k]; x[k] = xn[k]; }
+        for (int b = 0; b < NBUF - 1; b++)
+            if (b < groups) load(i[b], x[b], b);
+        for (qidx g0 = 0; g0 < groups; g0 += NBUF) {
+#pragma unroll
+            for (int b = 0; b < NBUF; b++) {
+                const qidx g = g0 + b;
+                if (g >= groups) break;
+                const int nb = (b + NBUF - 1) % NBUF;
+                if (g + NBUF - 1 < groups) load(i[nb], x[nb], g + NBUF - 1);
+#pragma unroll
+                for (int k = 0; k < PPT; k++) {
+                    const bool second = (MODE == 0) && (i[b][k] & tbit);
+                    st_amp(a + i[b][k], diag1_fx_amp(second ? F1 : F0, second ? d1 : d0, x[b][k]));
+                }
+            }
         }
     }
     for (qidx n = groups * span + tid; n < numIts; n += stride) {
