@@ -53,6 +53,12 @@ int  qg_get_version(void);                 /* 100*major + minor */
 int qg_init(int device);                                   /* gpu_bindLocalGPUsToNodes (gpu_config.cpp:332) + queries */
 int qg_get_num_devices(int* out);                          /* gpu_getNumberOfLocalGpus (gpu_config.cpp:124) */
 int qg_get_device_info(int* numSMs, int64_t* totalMem, int64_t* freeMem, int* ccMajor, int* ccMinor);
+/* The context's L2 fetch-granularity hint (cudaLimitMaxL2FetchGranularity): 0 (the
+ * driver's default), 32, 64 or 128 bytes.  qg_init sets 32: gates that visit every other
+ * short run of amplitudes then fetch only the sectors they use.  No reference
+ * counterpart (the reference leaves the limit at its default). */
+int qg_set_l2_fetch_granularity(int bytes);
+int qg_get_l2_fetch_granularity(int* bytes);
 int qg_alloc(void** out, int64_t numBytes);                /* gpu_allocArray (gpu_config.cpp:399-421) */
 int qg_free(void* ptr);                                    /* gpu_deallocArray (gpu_config.cpp:424-436) */
 int qg_copy_h2d(void* dst, const void* src, int64_t numBytes, void* stream);   /* gpu_copyCpuToGpu (gpu_config.cpp:535) */

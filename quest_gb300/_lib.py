@@ -50,6 +50,8 @@ ABI = {
     "qg_init": [I],
     "qg_get_num_devices": [c_int_p],
     "qg_get_device_info": [c_int_p, c_i64_p, c_i64_p, c_int_p, c_int_p],
+    "qg_set_l2_fetch_granularity": [I],
+    "qg_get_l2_fetch_granularity": [c_int_p],
     "qg_alloc": [ctypes.POINTER(vp), I64],
     "qg_free": [vp],
     "qg_copy_h2d": [vp, vp, I64, vp],

@@ -276,6 +276,24 @@ def test_abi_rejects_bad_arguments(env):
         env.Q.destroyQureg(q)
 
 
+def test_l2_fetch_granularity_hint(env):
+    # initialisation leaves the context at 32-byte L2 fetches; the setter takes only the
+    # documented values
+    import ctypes
+    from quest_gb300 import _lib
+    L = _lib.lib()
+    v = ctypes.c_int(-1)
+    _lib.check(L.qg_get_l2_fetch_granularity(ctypes.byref(v)))
+    assert v.value == 32
+    try:
+        _lib.check(L.qg_set_l2_fetch_granularity(128))
+        _lib.check(L.qg_get_l2_fetch_granularity(ctypes.byref(v)))
+        assert v.value == 128
+        assert L.qg_set_l2_fetch_granularity(48) == -2
+    finally:
+        _lib.check(L.qg_set_l2_fetch_granularity(32))
+
+
 @pytest.mark.parametrize("nq,is_dm,seed", [(1, 0, 61), (5, 0, 62), (12, 0, 63), (1, 1, 64), (4, 1, 65), (6, 1, 66)])
 def test_fullstate_diag_vs_oracle(env, nq, is_dm, seed):
     """FullStateDiagMatr: apply / multiply with and without powers, and the four
