@@ -8,11 +8,12 @@ pairs per layer, then the full QFT (30 H + 435 controlled phases + 15 swaps):
 applyFullQuantumFourierTransform).
 
 Metric: whole-job algorithmic HBM throughput of the gates (GB/s), with the
-per-gate algorithmic bytes 2*16*2^(n-c) for a dense gate and 2*16*2^(n-2) for a
-controlled phase or a swap (the amplitudes each gate must read and write).
-`value` is timed with the state resident in HBM; `e2e` adds the host->device
-copy of the input state (pinned) and the device->host copy of the final state
-to every step.  The 16 GiB state exceeds L2 (129 MB), so no flush is needed.
+per-gate algorithmic bytes 2*16*2^(n-c) for a dense gate, 2*16*2^(n-2) for a
+controlled phase and 2*16*2^(n-1) for a swap (the amplitudes each gate must read and
+write).  `value` is timed with the state resident in HBM; `e2e` adds, to every step,
+the host->device copy of the input state and the device->host copy of the final
+state, both through the register's pinned host mirror (syncQuregToGpu /
+syncQuregFromGpu).  The 16 GiB state exceeds L2 (129 MB), so no flush is needed.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--qubits n]
 """
@@ -266,7 +267,6 @@ def run_gb300(args, world, rank, local, dist):
     nbytes = (1 << nq) * AMP_BYTES
     host_in = np.ctypeslib.as_array(C.cast(q.cpuAmps, C.POINTER(C.c_double)), shape=(2 << nq,))
     host_in[:] = state.view(np.float64)       # the pinned host mirror holds the input
-    host_out = np.empty(1 << nq, dtype=np.complex128)
     api.set_amps(q, state)
 
     mats = [comp_matr1(g[2]) if g[0] == "U" else None for g in gates]
@@ -332,9 +332,9 @@ def run_gb300(args, world, rank, local, dist):
     L.qg_sync()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        Q.syncQuregToGpu(q)                                  # pinned host -> HBM (16 GiB)
+        Q.syncQuregToGpu(q)      # pinned host mirror -> HBM (16 GiB): this step's input
         run_step()
-        Q.getQuregAmps(host_out.ctypes.data, q, 0, 1 << nq)  # HBM -> host (16 GiB)
+        Q.syncQuregFromGpu(q)    # HBM -> pinned host mirror (16 GiB): the step's result
     L.qg_sync()
     t_e2e = max_over_ranks(dist, time.perf_counter() - t0)
     barrier(dist)
