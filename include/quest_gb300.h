@@ -286,6 +286,11 @@ int qg_circuit_get_block(const qg_circuit* circuit, int i, int* targs, int* numT
 /* impl: 0 automatic (tensor cores for 5-qubit blocks on >= 12 qubits), 1 SIMT FP32, 2 tensor cores */
 int qg_sv32_apply_circuit(qg_circuit* circuit, void* amps32, int numQubits, int impl, void* stream);
 int qg_tc_get_error_flag(int* out);    /* 1 if a tensor-core kernel's bounded wait ran out */
+/* Self-test of that failure path: one launch (12..20 qubits, five targets) in which no
+ * operand buffer is ever signalled full, so the kernel's bounded waits run out (about
+ * 2 s).  flagOut: the error flag it left (1 expected, then cleared); secondsOut: the
+ * launch's wall time; unchangedOut: 1 if the scratch register was left untouched. */
+int qg_tc_selftest_timeout(int numQubits, const int* targs, int* flagOut, double* secondsOut, int* unchangedOut);
 
 /* Fusion autotuner (no counterpart in the reference): times the circuit fused at each
  * width k from its widest gate to 5 with the SIMT kernel, and at k = 5 with the

@@ -109,6 +109,7 @@ ABI = {
     "qg_circuit_get_block": [vp, I, c_int_p, c_int_p, c_cplx_p],
     "qg_sv32_apply_circuit": [vp, vp, I, I, vp],
     "qg_tc_get_error_flag": [c_int_p],
+    "qg_tc_selftest_timeout": [I, c_int_p, c_int_p, ctypes.POINTER(ctypes.c_double), c_int_p],
     "qg_circuit_autotune": [vp, c_int_p, c_int_p, c_int_p, c_int_p, c_dbl_p, I, c_int_p],
     "qg_circuit_graph_create": [vp, vp, I, I, ctypes.POINTER(vp)],
     "qg_graph_launch": [vp, vp],

@@ -29,7 +29,8 @@
 // tensor-core operand builder, defined in qg_fused_tc.cu
 size_t qg_tc_operand_floats();
 void qg_tc_build_operands(const std::complex<double>* m32x32, float* out);
-int qg_tc_apply_block(float2* amps, int numQubits, const int* targs, const float* devOperands, cudaStream_t st);
+int qg_tc_apply_block(float2* amps, int numQubits, const int* targs, const float* devOperands, cudaStream_t st,
+                      bool holdOperands = false);
 bool qg_tc_supported(int numQubits);
 int qg_tc_prepare();
 

@@ -20,7 +20,9 @@
 // sets the error flag, waits for the tensor core, frees the TMEM and returns.
 #include "qg_common.cuh"
 
+#include <chrono>
 #include <mutex>
+#include <vector>
 
 #include <cmath>
 #include <complex>
@@ -171,6 +173,7 @@ struct TcArgs {
     qidx kp[16];       // producer element k: amplitude offset of the L bits above the producer index = k
     qidx ke[32];       // epilogue element k: amplitude offset of L bits 7..11 = k
     int sj[32];        // stage_slot of the L bits of matrix index j (the slot map is linear over XOR)
+    int holdOperands;  // self-test of the bounded waits: producers never signal "A full"
 };
 
 // ---------------------------------------------------------------- kernel
@@ -357,7 +360,7 @@ __global__ void __launch_bounds__(WsShape<TPR, NBUF>::THREADS, 1) k32_fused_tc(T
                     *(float4*)(sAl + o) = l;
                 }
                 asm volatile("fence.proxy.async.shared::cta;");
-                mbar_arrive(aFull + 8 * s);
+                if (!args.holdOperands) mbar_arrive(aFull + 8 * s);
             }
         }
     } else if (warp == S::MMA_WARP) {
@@ -509,7 +512,8 @@ int qg_tc_prepare() {
     return QG_OK;
 }
 
-int qg_tc_apply_block(float2* amps, int numQubits, const int* targs, const float* devOperands, cudaStream_t st) {
+int qg_tc_apply_block(float2* amps, int numQubits, const int* targs, const float* devOperands, cudaStream_t st,
+                      bool holdOperands = false) {
     if (numQubits < 12) return qg_fail(QG_ERR_ARG, "the tensor-core block kernel needs at least 12 qubits (one 128-group tile)");
     if (!g_tc_error) QG_TRY(qg_tc_prepare());
     int zeros[5] = {0, 0, 0, 0, 0};
@@ -526,6 +530,7 @@ int qg_tc_apply_block(float2* amps, int numQubits, const int* targs, const float
     }
     a.ops = devOperands;
     a.errorFlag = g_tc_error;
+    a.holdOperands = holdOperands ? 1 : 0;
     // Row-by-row access makes one warp instruction touch `lines` distinct 128-byte lines
     // (32 groups, one amplitude each).  Measured on GB300 at 30 qubits: 32 lines run
     // fastest fully staged (5.3 ms against 8.9 ms row by row), 16 lines with staged loads
@@ -591,4 +596,43 @@ extern "C" int qg_tc_get_error_flag(int* out) {
     if (!g_tc_error) { *out = 0; return QG_OK; }
     QG_CUDA(cudaMemcpy(out, g_tc_error, sizeof(int), cudaMemcpyDeviceToHost));
     return QG_OK;
+}
+
+// Self-test of the kernel's failure path.  One launch on a scratch FP32 register of
+// numQubits (12..20) with the given five targets, in which the producers never signal
+// that an operand buffer is full.  The MMA warp's and the epilogue's bounded waits then
+// run out: no MMA is issued, nothing is stored, the TMEM is freed, and the kernel
+// returns with the error flag set.  Reports that flag (1 expected), the launch's
+// wall time and whether the register came back unchanged, then clears the flag.
+extern "C" int qg_tc_selftest_timeout(int numQubits, const int* targs, int* flagOut, double* secondsOut,
+                                      int* unchangedOut) {
+    if (numQubits < 12 || numQubits > 20 || !targs || !flagOut) return qg_fail(QG_ERR_ARG, "self-test on 12..20 qubits");
+    QG_TRY(qg_tc_prepare());
+    const size_t n = (size_t)1 << numQubits;
+    std::vector<float2> host(n);
+    for (size_t i = 0; i < n; i++) host[i] = make_float2((float)(i % 7) * 0.125f, -(float)(i % 5) * 0.25f);
+    void* amps = nullptr;
+    void* ops = nullptr;
+    QG_TRY(qg_alloc(&amps, (int64_t)(n * sizeof(float2))));
+    int rc = qg_alloc(&ops, (int64_t)(qg_tc_operand_floats() * sizeof(float)));
+    if (rc == QG_OK && cudaMemcpy(amps, host.data(), n * sizeof(float2), cudaMemcpyHostToDevice) != cudaSuccess)
+        rc = qg_fail(QG_ERR_CUDA, "copy failed");
+    if (rc == QG_OK && cudaMemset(ops, 0, qg_tc_operand_floats() * sizeof(float)) != cudaSuccess)
+        rc = qg_fail(QG_ERR_CUDA, "memset failed");
+    const auto t0 = std::chrono::steady_clock::now();
+    if (rc == QG_OK) rc = qg_tc_apply_block((float2*)amps, numQubits, targs, (const float*)ops, nullptr, true);
+    if (rc == QG_OK && cudaDeviceSynchronize() != cudaSuccess) rc = qg_fail(QG_ERR_CUDA, "self-test launch failed");
+    const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (rc == QG_OK) rc = qg_tc_get_error_flag(flagOut);
+    if (rc == QG_OK && unchangedOut) {
+        std::vector<float2> back(n);
+        if (cudaMemcpy(back.data(), amps, n * sizeof(float2), cudaMemcpyDeviceToHost) != cudaSuccess)
+            rc = qg_fail(QG_ERR_CUDA, "copy failed");
+        *unchangedOut = rc == QG_OK && std::memcmp(back.data(), host.data(), n * sizeof(float2)) == 0;
+    }
+    if (rc == QG_OK && cudaMemset(g_tc_error, 0, sizeof(int)) != cudaSuccess) rc = qg_fail(QG_ERR_CUDA, "flag reset failed");
+    if (secondsOut) *secondsOut = secs;
+    qg_free(ops);
+    qg_free(amps);
+    return rc;
 }

@@ -230,3 +230,29 @@ def test_single_block_many_tiles_per_cta(env, targs):
     flag = ctypes.c_int(0)
     _lib.lib().qg_tc_get_error_flag(ctypes.byref(flag))
     assert flag.value == 0
+
+
+@pytest.mark.parametrize("targs", [[0, 1, 2, 3, 4], [1, 2, 3, 4, 5], [5, 6, 7, 8, 9]])
+def test_tensor_core_wait_runs_out_cleanly(env, targs):
+    # A launch in which no operand buffer is ever signalled full: the kernel's bounded
+    # waits run out, it stores nothing, raises the error flag and returns.  The context
+    # stays usable: a normal block right after matches the oracle.
+    from quest_gb300 import _lib
+    lib = _lib.lib()
+    t = (ctypes.c_int * 5)(*targs)
+    flag, secs, same = ctypes.c_int(0), ctypes.c_double(0), ctypes.c_int(0)
+    _lib.check(lib.qg_tc_selftest_timeout(14, t, ctypes.byref(flag), ctypes.byref(secs), ctypes.byref(same)))
+    assert flag.value == 1
+    assert same.value == 1
+    assert 1.0 < secs.value < 30.0
+    cleared = ctypes.c_int(1)
+    lib.qg_tc_get_error_flag(ctypes.byref(cleared))
+    assert cleared.value == 0
+    n = 14
+    u = qc.haar_unitary(32, np.random.default_rng(5))
+    amps = qc.random_statevector(n, 6)
+    ref = run_oracle(n, amps, [(targs, u)])
+    tc, _ = run_fused(env, n, amps, [(targs, u)], 5, 2)
+    assert np.max(np.abs(tc - ref)) <= 2e-6 * np.max(np.abs(ref))
+    lib.qg_tc_get_error_flag(ctypes.byref(cleared))
+    assert cleared.value == 0
