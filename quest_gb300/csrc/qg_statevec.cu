@@ -411,7 +411,7 @@ __global__ void __launch_bounds__(THREADS) k_diag1_fx(double2* __restrict__ a, q
 #pragma unroll
             for (int k = 0; k < PPT; k++) {
                 ib[k] = insert_bits<NB>(g * span + tid + k * stride, ins) | mask;
-                xb[k] = ld_amp(a + ib[k]);
+                xb[k] = a[ib[k]];   // default caching: the amplitude's sector stays in L2 until it is stored
             }
         };
 #pragma unroll
@@ -435,7 +435,7 @@ __global__ void __launch_bounds__(THREADS) k_diag1_fx(double2* __restrict__ a, q
     for (qidx n = groups * span + tid; n < numIts; n += stride) {
         const qidx ii = insert_bits<NB>(n, ins) | mask;
         const bool second = (MODE == 0) && (ii & tbit);
-        st_amp(a + ii, diag1_fx_amp(second ? F1 : F0, second ? d1 : d0, ld_amp(a + ii)));
+        st_amp(a + ii, diag1_fx_amp(second ? F1 : F0, second ? d1 : d0, a[ii]));
     }
 }
 
