@@ -245,10 +245,10 @@ def run_gb300(args, world, rank, local, dist):
     _lib.check(L.qg_init(local if dev_count.value > local else 0))
     api.init_env()
     _lib.check(L.qg_set_fp64_products(0 if args.fp64_products == "fixed" else 1))
-    # the library's launch-shape autotuner, on a 26-qubit scratch register, before any timing
+    # the library's launch-shape autotuner, on a 28-qubit scratch register (4 GiB), before any timing
     tune_ms = (C.c_double * 8)()
     tune_n = C.c_int(0)
-    _lib.check(L.qg_autotune_fp64(min(26, args.qubits), tune_ms, 8, C.byref(tune_n)))
+    _lib.check(L.qg_autotune_fp64(min(28, args.qubits), tune_ms, 8, C.byref(tune_n)))
     shapes = []
     for kern in (0, 1):
         tppt, tthr = C.c_int(), C.c_int()
@@ -735,7 +735,7 @@ def run_gates(args, world, rank, local, dist):
     api.init_env()
     n = args.qubits if "--qubits" in sys.argv else 28
     ms_buf, cnt = (C.c_double * 8)(), C.c_int(0)
-    _lib.check(L.qg_autotune_fp64(min(26, n), ms_buf, 8, C.byref(cnt)))
+    _lib.check(L.qg_autotune_fp64(min(28, n), ms_buf, 8, C.byref(cnt)))
     p = C.c_void_p()
     _lib.check(L.qg_alloc(C.byref(p), 16 << n))
     _lib.check(L.qg_sv_initUniformState(p, n, qg_cplx(1 / np.sqrt(2.0 ** n), 0), None))
