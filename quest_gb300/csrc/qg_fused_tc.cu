@@ -19,6 +19,7 @@
 // and writes the group's 32 outputs back.  Every wait is bounded: a wait that runs out
 // sets the error flag, waits for the tensor core, frees the TMEM and returns.
 #include "qg_common.cuh"
+#include "qg_tc_plan.h"
 
 #include <chrono>
 #include <mutex>
@@ -482,17 +483,6 @@ int* g_tc_error = nullptr;
 
 bool qg_tc_supported(int numQubits) { return numQubits >= 12; }
 
-namespace {
-// the host form of insert_bits: a zero opened at each listed position
-qidx insert_bits_host(qidx n, const Ins& ins) {
-    for (int i = 0; i < ins.num; i++) {
-        const qidx lo = n & ins.low[i];
-        n = ((n ^ lo) << 1) | lo;
-    }
-    return n;
-}
-}  // namespace
-
 // one-time set-up (the error flag's memory, the kernel's shared-memory limit); done
 // before the first launch and before any stream capture of one
 int qg_tc_prepare() {
@@ -531,54 +521,18 @@ int qg_tc_apply_block(float2* amps, int numQubits, const int* targs, const float
     a.ops = devOperands;
     a.errorFlag = g_tc_error;
     a.holdOperands = holdOperands ? 1 : 0;
-    // Row-by-row access makes one warp instruction touch `lines` distinct 128-byte lines
-    // (32 groups, one amplitude each).  Measured on GB300 at 30 qubits: 32 lines run
-    // fastest fully staged (5.3 ms against 8.9 ms row by row), 16 lines with staged loads
-    // only (4.7 against 5.1), 8 or fewer row by row (2.8-3.9 against 3.4-5.4 staged).
-    int lines = 0;
-    {
-        qidx seen[32];
-        for (int r = 0; r < 32; r++) {
-            const qidx line = insert_bits_host(r, p.ins) >> 4;   // 16 FP32 amplitudes per line
-            bool dup = false;
-            for (int q = 0; q < lines; q++) dup |= seen[q] == line;
-            if (!dup) seen[lines++] = line;
-        }
-    }
-    a.stage = lines >= 32 ? 2 : lines >= 16 ? 1 : 0;
-    {
-        // local bit positions: the targets and the seven lowest other bits, ascending
-        int pos[12], n = 0, rows = 0;
-        for (int q = 0; q < numQubits && n < 12; q++) {
-            bool isTarg = false;
-            for (int b = 0; b < 5; b++) isTarg |= targs[b] == q;
-            if (isTarg || rows < 7) {
-                if (!isTarg) rows++;
-                pos[n++] = q;
-            }
-        }
-        int r = 0;
-        for (int pb = 0; pb < 12; pb++) {
-            a.lbit[pb] = (qidx)1 << pos[pb];
-            int jb = -1;
-            for (int b = 0; b < 5; b++) if (targs[b] == pos[pb]) jb = b;
-            if (jb >= 0) a.lj[jb] = pb;
-            else a.lrow[r++] = pb;
-        }
-        constexpr int PB = WsShape<TC_TPR_STAGED, TC_NBUF_STAGED>::PBITS;
-        for (int k = 0; k < (1 << (12 - PB)); k++) {
-            a.kp[k] = 0;
-            for (int c = 0; c < 12 - PB; c++) if ((k >> c) & 1) a.kp[k] += a.lbit[PB + c];
-        }
-        for (int k = 0; k < 32; k++) {
-            a.ke[k] = 0;
-            int ej = 0;
-            for (int c = 0; c < 5; c++) {
-                if ((k >> c) & 1) a.ke[k] += a.lbit[7 + c];
-                if ((k >> c) & 1) ej |= 1 << a.lj[c];
-            }
-            a.sj[k] = ej ^ ((ej >> 5) & 31);
-        }
+    // the mode and the staged modes' index tables (qg_tc_plan.h)
+    qgtc::Plan plan;
+    if (!qgtc::make_plan(numQubits, targs, WsShape<TC_TPR_STAGED, TC_NBUF_STAGED>::PBITS, &plan))
+        return qg_fail(QG_ERR_ARG, "bad targets for a tensor-core block");
+    a.stage = plan.stage;
+    for (int i = 0; i < 12; i++) a.lbit[i] = plan.lbit[i];
+    for (int i = 0; i < 7; i++) a.lrow[i] = plan.lrow[i];
+    for (int i = 0; i < 5; i++) a.lj[i] = plan.lj[i];
+    for (int i = 0; i < 16; i++) a.kp[i] = plan.kp[i];
+    for (int i = 0; i < 32; i++) {
+        a.ke[i] = plan.ke[i];
+        a.sj[i] = plan.sj[i];
     }
     const unsigned grid = (unsigned)std::min<qidx>(a.numTiles, (qidx)qg_num_sms());
     using SS = WsShape<TC_TPR_STAGED, TC_NBUF_STAGED>;
