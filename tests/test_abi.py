@@ -49,3 +49,16 @@ def test_python_binding_covers_abi():
             names |= declared_functions(h)
     bound = set(_lib.ABI) | {"qg_get_last_error", "qg_get_error_string", "qg_get_version"}
     assert names <= bound, names - bound
+
+
+def test_new_entry_points_validate_arguments_before_any_device_call(built_lib):
+    # argument checks come before any CUDA call, so they hold without a GPU
+    from quest_gb300._lib import lib
+    L = lib()
+    assert L.qg_set_l2_fetch_granularity(48) == -2
+    assert L.qg_set_l2_fetch_granularity(-32) == -2
+    assert L.qg_get_l2_fetch_granularity(None) == -2
+    t = (ctypes.c_int * 5)(0, 1, 2, 3, 4)
+    flag = ctypes.c_int(0)
+    assert L.qg_tc_selftest_timeout(11, t, ctypes.byref(flag), None, None) == -2
+    assert L.qg_tc_selftest_timeout(14, None, ctypes.byref(flag), None, None) == -2
