@@ -821,6 +821,76 @@ def run_gates(args, world, rank, local, dist):
         print(json.dumps(line), flush=True)
 
 
+def run_expec(args, world, rank, local, dist):
+    """Batched Pauli expectation values on one FP64 statevector (`--qubits`, default 28):
+    16 random strings (I/X/Y/Z uniform per qubit) through the batched entry point, one
+    launch per call, beside the same strings one per call.  ms per call from CUDA events
+    over `--steps` calls after `--warmup`; GB/s counts one read of the state (16 B per
+    amplitude) per call, the bytes one pass must move."""
+    import ctypes as C
+    from quest_gb300 import _lib, api
+    from quest_gb300._lib import qg_cplx
+    L = _lib.lib()
+    _lib.check(L.qg_init(local))
+    api.init_env()
+    n = args.qubits if "--qubits" in sys.argv else 28
+    ns = 16
+    rng = np.random.default_rng(0x5155455354 + 8)
+    codes = [[int(v) for v in rng.integers(0, 4, n)] for _ in range(ns)]
+    mxy = (C.c_int64 * ns)(*[sum(1 << q for q, c in enumerate(cs) if c in (1, 2)) for cs in codes])
+    myz = (C.c_int64 * ns)(*[sum(1 << q for q, c in enumerate(cs) if c in (2, 3)) for cs in codes])
+    ny = (C.c_int * ns)(*[sum(1 for c in cs if c == 2) for cs in codes])
+    p = C.c_void_p()
+    _lib.check(L.qg_alloc(C.byref(p), 16 << n))
+    state = random_state(n, seed=0x5155455354 + 8)
+    _lib.check(L.qg_copy_h2d(p, state.ctypes.data, 16 << n, None))
+    out = (qg_cplx * ns)()
+    e0, e1 = C.c_void_p(), C.c_void_p()
+    L.qg_event_create(C.byref(e0))
+    L.qg_event_create(C.byref(e1))
+
+    def timed(fn):
+        for _ in range(max(1, args.warmup)):
+            fn()
+        L.qg_sync()
+        L.qg_event_record(e0, None)
+        for _ in range(args.steps):
+            fn()
+        L.qg_event_record(e1, None)
+        ms = C.c_float()
+        L.qg_event_elapsed_ms(e0, e1, C.byref(ms))
+        return ms.value / args.steps
+
+    ms_batch = timed(lambda: _lib.check(L.qg_sv_calcExpecPauliStrBatch(p, n, mxy, myz, ny, ns, out, None)))
+    batch_vals = [out[i].re for i in range(ns)]
+    one = (qg_cplx * 1)()
+
+    def per_string():
+        for s in range(ns):
+            x = [q for q, c in enumerate(codes[s]) if c == 1]
+            y = [q for q, c in enumerate(codes[s]) if c == 2]
+            z = [q for q, c in enumerate(codes[s]) if c == 3]
+            _lib.check(L.qg_sv_calcExpecPauliStr(p, n, _lib.ints(x), len(x), _lib.ints(y), len(y),
+                                                 _lib.ints(z), len(z), one, None))
+    ms_single = timed(per_string)
+    L.qg_free(p)
+    state_bytes = 16 << n
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    peak = peaks.get("hbm_gbs", 6800.0)
+    line = {"metric": "batched Pauli expectation values: ms per 16 strings on an FP64 statevector",
+            "value": round(ms_batch, 4), "unit": "ms", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded Gaussian state, 16 random I/X/Y/Z strings)",
+            "config": {"workload": f"{n}-qubit FP64 statevector, 16 Pauli strings per call", "qubits": n,
+                       "l2": "state larger than L2; no flush"},
+            "batch_ms": round(ms_batch, 4), "per_string_calls_ms": round(ms_single, 4),
+            "batch_one_pass_gbs": round(state_bytes / ms_batch / 1e6, 1),
+            "batch_one_pass_frac_of_hbm": round(state_bytes / ms_batch / 1e6 / peak, 3),
+            "values": batch_vals, "hbm_peak_gbs": peak}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def run_blocks(args, world, rank, local, dist):
     """Per-target-set timing of one fused 5-qubit block on an FP32 register through the
     tensor-core kernel (`Circuit` API, impl = tc): ms per apply from CUDA events over
@@ -897,10 +967,10 @@ def main():
     ap.add_argument("--depth", type=int, default=20)
     ap.add_argument("--cpu-sample", type=int, default=45, help="gates of the circuit timed on the host CPU")
     ap.add_argument("--traffic", type=float, default=None, help="ncu DRAM bytes per dense launch, if captured")
-    ap.add_argument("--config", default="plain", choices=["plain", "precision", "serve", "gates", "blocks"],
+    ap.add_argument("--config", default="plain", choices=["plain", "precision", "serve", "gates", "blocks", "expec"],
                     help="plain: the 30-qubit FP64 per-gate circuit (default); precision: FP32 fused blocks; "
                          "serve: request stream, served vs plain; gates: per-gate-kind timing (28 qubits); "
-                         "blocks: one FP32 5-qubit block per target set")
+                         "blocks: one FP32 5-qubit block per target set; expec: 16 Pauli strings per call (28 qubits)")
     ap.add_argument("--block-targets", default="", help="blocks: target sets, e.g. '0,1,2,3,4;5,6,7,8,9'")
     ap.add_argument("--requests", type=int, default=48)
     ap.add_argument("--min-qubits", type=int, default=8)
@@ -921,6 +991,8 @@ def main():
         run_gates(args, world, rank, local, dist)
     elif args.config == "blocks":
         run_blocks(args, world, rank, local, dist)
+    elif args.config == "expec":
+        run_expec(args, world, rank, local, dist)
     elif args.config == "precision":
         if args.qubits == 30 and "--qubits" not in sys.argv:
             args.qubits = 32

@@ -4,7 +4,7 @@
  * Each entry point replaces one GPU backend function of QuEST v4.1.0, named in
  * its comment (file:line within the QuEST project).  A QuEST build reaches these
  * through a thin shim that keeps the signatures of quest/src/gpu/gpu_subroutines.hpp
- * and quest/src/gpu/gpu_config.hpp; the localiser and the
+ * and quest/src/gpu/gpu_config.hpp (quest_gb300/shim/); the localiser and the
  * accelerator above it are unchanged.
  *
  * Conventions
@@ -53,12 +53,17 @@ int  qg_get_version(void);                 /* 100*major + minor */
 int qg_init(int device);                                   /* gpu_bindLocalGPUsToNodes (gpu_config.cpp:332) + queries */
 int qg_get_num_devices(int* out);                          /* gpu_getNumberOfLocalGpus (gpu_config.cpp:124) */
 int qg_get_device_info(int* numSMs, int64_t* totalMem, int64_t* freeMem, int* ccMajor, int* ccMinor);
-/* The context's L2 fetch-granularity hint (cudaLimitMaxL2FetchGranularity): 0 (the
- * driver's default), 32, 64 or 128 bytes.  qg_init sets 32: gates that visit every other
- * short run of amplitudes then fetch only the sectors they use.  No reference
- * counterpart (the reference leaves the limit at its default). */
+/* The context's L2 fetch-granularity hint (cudaLimitMaxL2FetchGranularity): 0, 32, 64
+ * or 128 bytes.  qg_init sets 32: gates that visit every other short run of amplitudes
+ * then fetch only the sectors they use.  The limit belongs to the device's primary
+ * context, so it applies to every library of the host process on that device until the
+ * process exits.  qg_init keeps the value it found; qg_restore_l2_fetch_granularity puts
+ * that value back on the current device (a host application that shares the context and
+ * wants its own setting calls it after qg_init).  No reference counterpart (the
+ * reference leaves the limit alone). */
 int qg_set_l2_fetch_granularity(int bytes);
 int qg_get_l2_fetch_granularity(int* bytes);
+int qg_restore_l2_fetch_granularity(void);
 int qg_alloc(void** out, int64_t numBytes);                /* gpu_allocArray (gpu_config.cpp:399-421) */
 int qg_free(void* ptr);                                    /* gpu_deallocArray (gpu_config.cpp:424-436) */
 int qg_copy_h2d(void* dst, const void* src, int64_t numBytes, void* stream);   /* gpu_copyCpuToGpu (gpu_config.cpp:535) */
@@ -208,6 +213,10 @@ int qg_dm_calcProbOfMultiQubitOutcome(const void* amps, int numKetQubits, const 
  * deterministic (no atomics on the probabilities). outProbs: HOST array of 2^num */
 int qg_sv_calcProbsOfAllMultiQubitOutcomes(double* outProbs, const void* amps, int numQubits, const int* qubits, int num,
                                            void* stream);
+/* gpu_densmatr_calcProbsOfAllMultiQubitOutcomes_sub<N> (gpu_subroutines.hpp:150; gpu_subroutines.cpp:1550-1580):
+ * the histogram of the diagonal, deterministic like the statevector form */
+int qg_dm_calcProbsOfAllMultiQubitOutcomes(double* outProbs, const void* amps, int numKetQubits, const int* qubits, int num,
+                                           void* stream);
 /* ------------------------------------------------------------------ all-target diagonals (FullStateDiagMatr)
  * elems: DEVICE array of 2^n complex (n ket qubits for a density matrix), 16-byte aligned.
  * With hasPower the elements are raised to `exponent` (complex pow, exp(w log z)). */
@@ -283,9 +292,18 @@ int qg_circuit_get_num_gates(const qg_circuit* circuit, int* out);
 int qg_circuit_get_num_blocks(const qg_circuit* circuit, int* out);
 /* block i: its ascending targets and (if matr != NULL) its 2^k x 2^k FP64 matrix */
 int qg_circuit_get_block(const qg_circuit* circuit, int i, int* targs, int* numTargs, qg_cplx* matr);
-/* impl: 0 automatic (tensor cores for 5-qubit blocks on >= 12 qubits), 1 SIMT FP32, 2 tensor cores */
+/* impl: 0 automatic (tensor cores for 5-qubit blocks on >= 12 qubits), 1 SIMT FP32, 2 tensor cores,
+ * 3 tensor cores in the self-test of their failure path (no operand buffer is ever signalled
+ * full: every 5-qubit block launch gives up after about 2 s and leaves the register untouched).
+ * Asynchronous.  A tensor-core launch whose bounded wait runs out sets the device's error flag;
+ * the next qg_sv32_apply_circuit or qg_graph_launch on that device returns QG_ERR_TIMEOUT for
+ * it (and clears the flag) before launching anything.  Callers that need the verdict of their
+ * own launches synchronise the stream and read qg_tc_get_error_flag. */
 int qg_sv32_apply_circuit(qg_circuit* circuit, void* amps32, int numQubits, int impl, void* stream);
-int qg_tc_get_error_flag(int* out);    /* 1 if a tensor-core kernel's bounded wait ran out */
+/* the current device's flag: 1 if a tensor-core launch gave up a bounded wait since it was
+ * last cleared (a host read of mapped memory: no copy, no synchronisation) */
+int qg_tc_get_error_flag(int* out);
+int qg_tc_clear_error_flag(void);
 /* Self-test of that failure path: one launch (12..20 qubits, five targets) in which no
  * operand buffer is ever signalled full, so the kernel's bounded waits run out (about
  * 2 s).  flagOut: the error flag it left (1 expected, then cleared); secondsOut: the
@@ -333,6 +351,7 @@ int qg_sv32_calcExpecPauliStrBatch(const void* amps32, int numQubits, const int6
 
 typedef struct qg_server qg_server;
 
+/* impl: the block kernel choice of qg_sv32_apply_circuit (0..3) for the large registers */
 int qg_server_create(qg_server** out, int64_t hbmBudgetBytes, int maxInFlight, int impl);
 int qg_server_destroy(qg_server* server);
 /* queues a request (the fused circuit must outlive it); returns its id */
@@ -342,7 +361,10 @@ int qg_server_submit(qg_server* server, qg_circuit* circuit, const int64_t* mask
 int qg_server_poll(qg_server* server, int* numDone);
 /* *done = 1 once finished; values = the request's expectation values.  When every gate of
    the circuit is unitary (max|U^dagger U - I| <= 1e-10) they are <P>/<psi|psi>, with the norm
-   of the final FP32 state summed in FP64; otherwise <psi|P|psi> unnormalised. */
+   of the final FP32 state summed in FP64; otherwise <psi|P|psi> unnormalised.  A finished
+   request one of whose tensor-core launches gave up a bounded wait returns QG_ERR_TIMEOUT
+   (with *done = 1 and no values); each request has a timeout word of its own, so the others
+   in flight are unaffected. */
 int qg_server_result(qg_server* server, int64_t id, double* values, int* done);
 int qg_server_release(qg_server* server, int64_t id);
 /* the client went away: a queued request is dropped at once (its circuit is no longer

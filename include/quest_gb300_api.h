@@ -122,6 +122,14 @@ typedef struct {
 /* quest/include/paulis.h:53-60: base-4 digits, 2 bits per qubit */
 typedef struct { PAULI_MASK_TYPE lowPaulis; PAULI_MASK_TYPE highPaulis; } PauliStr;
 
+/* quest/include/paulis.h:64-80 */
+typedef struct {
+    qindex numTerms;
+    PauliStr* strings;
+    qcomp_t* coeffs;
+    int* isApproxHermitian;
+} PauliStrSum;
+
 /* environment (quest/include/environment.h:48-56) */
 void initQuESTEnv(void);
 void initCustomQuESTEnv(int useDistrib, int useGpuAccel, int useMultithread);
@@ -145,6 +153,11 @@ void  syncQuregToGpu(Qureg qureg);                                              
 void  syncQuregFromGpu(Qureg qureg);                                             /* qureg.cpp:402 */
 void  getQuregAmps(qcomp_t* outAmps, Qureg qureg, qindex startInd, qindex numAmps);        /* qureg.cpp:451 */
 qcomp_t getQuregAmp(Qureg qureg, qindex index);
+/* 1 if the Qureg's host mirror (cpuAmps) is page-locked, so that syncQuregToGpu /
+ * syncQuregFromGpu copy at the host link's rate; 0 if the pinned allocation was refused
+ * and the mirror is pageable.  No reference counterpart (the reference's mirror is
+ * always pageable, qureg.cpp:157-168). */
+int   isQuregHostMirrorPinned(Qureg qureg);
 
 /* initialisations (quest/src/api/initialisations.cpp) */
 void initZeroState(Qureg qureg);
@@ -168,6 +181,8 @@ void setKrausMapFlat(KrausMap map, const qcomp_t* ops /* numOps x 2^k x 2^k row-
 void syncKrausMap(KrausMap map);
 void destroyKrausMap(KrausMap map);
 PauliStr getPauliStrFromCodes(const int* paulis, const int* indices, int numPaulis);  /* getPauliStr(int*,int*,int), paulis.h:151 */
+PauliStrSum createPauliStrSum(PauliStr* strings, qcomp_t* coeffs, qindex numTerms);    /* paulis.cpp:396-417 */
+void destroyPauliStrSum(PauliStrSum sum);                                               /* paulis.cpp */
 
 /* operations (quest/src/api/operations.cpp) */
 void applyCompMatr1(Qureg qureg, int target, CompMatr1 matrix);                                          /* :81 */
@@ -221,6 +236,10 @@ void applyQubitProjector(Qureg qureg, int target, int outcome);                 
 void applyMultiQubitProjector(Qureg qureg, int* qubits, int* outcomes, int numQubits);                   /* :1766 */
 int  applyQubitMeasurement(Qureg qureg, int target);                                                     /* :1796 */
 int  applyQubitMeasurementAndGetProb(Qureg qureg, int target, qreal* probability);                       /* :1804 */
+qreal applyForcedQubitMeasurement(Qureg qureg, int target, int outcome);                                 /* :1829 */
+qindex applyMultiQubitMeasurement(Qureg qureg, int* qubits, int numQubits);                              /* :1848 */
+qindex applyMultiQubitMeasurementAndGetProb(Qureg qureg, int* qubits, int numQubits, qreal* probability); /* :1858 */
+qreal applyForcedMultiQubitMeasurement(Qureg qureg, int* qubits, int* outcomes, int numQubits);           /* :1893 */
 
 /* decoherence (quest/src/api/decoherence.cpp) */
 void mixDephasing(Qureg qureg, int qubit, qreal prob);                                                   /* :31 */
@@ -233,6 +252,8 @@ void mixKrausMap(Qureg qureg, int* qubits, int numQubits, KrausMap map);        
 
 /* calculations (quest/src/api/calculations.cpp) */
 qreal calcExpecPauliStr(Qureg qureg, PauliStr str);                                                      /* :133 */
+/* :146; every term through the batched kernels (several strings per pass over the state) */
+qreal calcExpecPauliStrSum(Qureg qureg, PauliStrSum sum);
 /* many strings of one Qureg in as few passes as the backend allows (per-term loop of
  * localiser_statevec_calcExpecPauliStrSum, localiser.cpp:2052-2148) */
 void  calcExpecPauliStrs(qreal* out, Qureg qureg, const PauliStr* strs, int numStrs);

@@ -586,6 +586,16 @@ extern "C" void orc_sv_probsOfAllOutcomes(double* out, const double* amps, int n
     for (idx k = 0; k < N; k++) out[getValueOfBits(k, qubits, n)] += std::norm(a[k]);
 }
 
+/* cpu_densmatr_calcProbsOfAllMultiQubitOutcomes_sub: cpu_subroutines.cpp:1865-1904 (one diagonal
+ * element per column, added to the bin of its outcome) */
+extern "C" void orc_dm_probsOfAllOutcomes(double* out, const double* amps, int nKet, const int* qubits, int n) {
+    const cplx* a = C(amps);
+    idx numOut = pow2(n);
+    for (idx i = 0; i < numOut; i++) out[i] = 0;
+    idx dim = pow2(nKet);
+    for (idx k = 0; k < dim; k++) out[getValueOfBits(k, qubits, n)] += std::real(a[k * (dim + 1)]);
+}
+
 /* cpu_statevec_calcExpecAnyTargZ_sub: cpu_subroutines.cpp:2006-2025 */
 extern "C" double orc_sv_expecZ(const double* amps, int nq, const int* targs, int nt) {
     const cplx* a = C(amps);
@@ -817,6 +827,32 @@ struct Runner {
         return out[0];
     }
 
+    /* the complex term value of one string (localiser.cpp:1963-2049, the value before the
+     * real part is taken) */
+    cplx expecC(const vector<int>& codesIn) {
+        vector<int> codes(n, 0);
+        for (size_t q = 0; q < codesIn.size() && (int)q < n; q++) codes[q] = codesIn[q];
+        vector<int> x, y, z; split(codes, x, y, z);
+        double out[2] = {0, 0};
+        if (!isDM) {
+            if (x.empty() && y.empty() && z.empty()) return orc_sv_totalProb(amps, n);
+            if (x.empty() && y.empty()) return orc_sv_expecZ(amps, n, z.data(), (int)z.size());
+            orc_sv_expecPauli(out, amps, n, x.data(), (int)x.size(), y.data(), (int)y.size(), z.data(), (int)z.size());
+            return cplx(out[0], out[1]);
+        }
+        if (x.empty() && y.empty() && z.empty()) return orc_dm_totalProb(amps, n);
+        if (x.empty() && y.empty()) orc_dm_expecZ(out, amps, n, z.data(), (int)z.size());
+        else orc_dm_expecPauli(out, amps, n, x.data(), (int)x.size(), y.data(), (int)y.size(), z.data(), (int)z.size());
+        return cplx(out[0], out[1]);
+    }
+    /* calcProbsOfAllMultiQubitOutcomes: calculations.cpp:265-275 */
+    vector<double> probsOfAll(const vector<int>& q) {
+        vector<double> p(pow2((int)q.size()));
+        if (isDM) orc_dm_probsOfAllOutcomes(p.data(), amps, n, q.data(), (int)q.size());
+        else orc_sv_probsOfAllOutcomes(p.data(), amps, n, q.data(), (int)q.size());
+        return p;
+    }
+
     bool run(const std::string& text);
 };
 
@@ -980,6 +1016,48 @@ bool Runner::run(const std::string& text) {
             int outcome = sample > p0;
             projector({q}, {outcome}, outcome ? p1 : p0);
             outcomes.push_back(outcome);
+        } else if (op == "MEASM") {      /* applyMultiQubitMeasurementAndGetProb: operations.cpp:1858-1891 */
+            int k; is >> k; auto q = rdInts(is, k);
+            vector<double> probs = probsOfAll(q);
+            double total = 0, comp = 0;              /* util_getSum: Kahan (utilities.cpp:346-360) */
+            for (double x : probs) { double y = x - comp, t = total + y; comp = (t - total) - y; total = t; }
+            if (std::abs(total - 1) > 1e-12) { err = "MEASM: outcome probabilities do not sum to one"; return false; }
+            std::uniform_real_distribution<double> distrib(0, 1);   /* rand_getRandomMultiQubitOutcome: randomiser.cpp:140-166 */
+            double sample = distrib(gen), cum = 0;
+            idx outcome = (idx)probs.size();
+            for (size_t i = 0; i < probs.size(); i++) { cum += probs[i]; if (sample < cum) { outcome = (idx)i; break; } }
+            if (outcome == (idx)probs.size()) {
+                if (1 - cum <= 1e-12) outcome = (idx)probs.size() - 1;
+                else { err = "MEASM: non-normalised probabilities"; return false; }
+            }
+            vector<int> o(k);
+            for (int i = 0; i < k; i++) o[i] = (int)((outcome >> i) & 1);   /* getBitsFromInteger */
+            projector(q, o, probs[(size_t)outcome]);
+            outcomes.push_back((int)outcome);
+            results.push_back(probs[(size_t)outcome]);
+        } else if (op == "FMEAS") {      /* applyForcedQubitMeasurement: operations.cpp:1829-1846 */
+            int q, o; is >> q >> o;
+            double p = probOfOutcome({q}, {o});
+            if (p < 1e-12) { err = "FMEAS: outcome impossibly unlikely"; return false; }
+            projector({q}, {o}, p);
+            results.push_back(p);
+        } else if (op == "FMEASM") {     /* applyForcedMultiQubitMeasurement: operations.cpp:1893-1912 */
+            int k; is >> k; auto q = rdInts(is, k); auto o = rdInts(is, k);
+            double p = probOfOutcome(q, o);
+            if (p < 1e-12) { err = "FMEASM: outcome impossibly unlikely"; return false; }
+            projector(q, o, p);
+            results.push_back(p);
+        } else if (op == "PROBALL") {    /* calcProbsOfAllMultiQubitOutcomes: calculations.cpp:265-275 */
+            int k; is >> k; auto q = rdInts(is, k);
+            for (double v : probsOfAll(q)) results.push_back(v);
+        } else if (op == "EXPSUM") {     /* calcExpecPauliStrSum: calculations.cpp:146-159, localiser.cpp:2052-2148 */
+            int T; is >> T;
+            cplx total = 0;
+            for (int t = 0; t < T; t++) {
+                double cr, ci; std::string ps; is >> cr >> ci >> ps;
+                total += cplx(cr, ci) * expecC(parsePauli(ps));
+            }
+            results.push_back(total.real());
         } else if (op == "TOTALPROB") {  /* calcTotalProb: calculations.cpp:278-284 */
             results.push_back(isDM ? orc_dm_totalProb(amps, n) : orc_sv_totalProb(amps, n));
         } else if (op == "PURITY") {     /* calcPurity: calculations.cpp:293-300 */

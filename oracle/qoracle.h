@@ -10,7 +10,7 @@
  *
  * Parity is pinned: tests/golden/ holds final states and reduction results
  * produced by the reference library itself (built from its own sources by
- * oracle/build_ref.sh), and tests/test_oracle_golden.py checks this oracle
+ * `make -C oracle ref`), and tests/test_oracle_golden.py checks this oracle
  * against them.
  *
  * Complex numbers are interleaved (re, im) doubles, the layout of
@@ -59,6 +59,7 @@ double orc_dm_totalProb(const double* amps, int nKet);
 double orc_sv_probOfOutcome(const double* amps, int nq, const int* qubits, const int* outcomes, int n);
 double orc_dm_probOfOutcome(const double* amps, int nKet, const int* qubits, const int* outcomes, int n);
 void   orc_sv_probsOfAllOutcomes(double* out, const double* amps, int nq, const int* qubits, int n);
+void   orc_dm_probsOfAllOutcomes(double* out, const double* amps, int nKet, const int* qubits, int n);
 double orc_sv_expecZ(const double* amps, int nq, const int* targs, int nt);
 void   orc_dm_expecZ(double* out /*2*/, const double* amps, int nKet, const int* targs, int nt);
 void   orc_sv_expecPauli(double* out /*2*/, const double* amps, int nq, const int* x, int nx, const int* y, int ny, const int* z, int nz);

@@ -2,7 +2,7 @@
  * ref_harness.cpp -- runs the text circuit format of qoracle.h through the
  * REFERENCE QuEST v4.1.0 library itself (its OpenMP CPU build, FLOAT_PRECISION=2),
  * so that the oracle and the golden fixtures can be pinned to the reference's
- * own outputs.  TEST INFRASTRUCTURE ONLY: built by oracle/build_ref.sh into
+ * own outputs.  TEST INFRASTRUCTURE ONLY: built by `make -C oracle ref` into
  * oracle/_ref/ when the reference sources are present; never part of the product.
  *
  * Every op calls the public QuEST API function that the op names
@@ -128,6 +128,27 @@ extern "C" int ref_run_circuit(const char* text, int numQubits, int isDensMatr, 
         else if (op == "PROJ") { int k; is >> k; auto a = rdInts(is, k); auto o = rdInts(is, k); applyMultiQubitProjector(q, a.data(), o.data(), k); }
         else if (op == "SEED") { vector<unsigned> s; unsigned v; while (is >> v) s.push_back(v); setSeeds(s.data(), (int)s.size()); }
         else if (op == "MEAS") { int a; is >> a; outs.push_back(applyQubitMeasurement(q, a)); }
+        else if (op == "MEASM") {
+            int k; is >> k; auto a = rdInts(is, k); qreal p = 0;
+            qindex o = applyMultiQubitMeasurementAndGetProb(q, a.data(), k, &p);
+            outs.push_back((int)o); res.push_back(p);
+        }
+        else if (op == "FMEAS") { int a, o; is >> a >> o; res.push_back(applyForcedQubitMeasurement(q, a, o)); }
+        else if (op == "FMEASM") { int k; is >> k; auto a = rdInts(is, k); auto o = rdInts(is, k); res.push_back(applyForcedMultiQubitMeasurement(q, a.data(), o.data(), k)); }
+        else if (op == "PROBALL") {
+            int k; is >> k; auto a = rdInts(is, k);
+            vector<qreal> p((size_t)1 << k);
+            calcProbsOfAllMultiQubitOutcomes(p.data(), q, a.data(), k);
+            for (qreal v : p) res.push_back(v);
+        }
+        else if (op == "EXPSUM") {
+            int T; is >> T;
+            vector<PauliStr> strs; vector<qcomp> cs;
+            for (int t = 0; t < T; t++) { double cr, ci; std::string ps; is >> cr >> ci >> ps; cs.push_back(qcomp(cr, ci)); strs.push_back(pauliOf(ps)); }
+            PauliStrSum sum = createPauliStrSum(strs.data(), cs.data(), (qindex)T);
+            res.push_back(calcExpecPauliStrSum(q, sum));
+            destroyPauliStrSum(sum);
+        }
         else if (op == "TOTALPROB") res.push_back(calcTotalProb(q));
         else if (op == "PURITY") res.push_back(calcPurity(q));
         else if (op == "PROBQ") { int a, o; is >> a >> o; res.push_back(calcProbOfQubitOutcome(q, a, o)); }

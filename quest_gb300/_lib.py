@@ -52,6 +52,7 @@ ABI = {
     "qg_get_device_info": [c_int_p, c_i64_p, c_i64_p, c_int_p, c_int_p],
     "qg_set_l2_fetch_granularity": [I],
     "qg_get_l2_fetch_granularity": [c_int_p],
+    "qg_restore_l2_fetch_granularity": [],
     "qg_alloc": [ctypes.POINTER(vp), I64],
     "qg_free": [vp],
     "qg_copy_h2d": [vp, vp, I64, vp],
@@ -92,6 +93,7 @@ ABI = {
     "qg_sv_calcProbOfMultiQubitOutcome": [vp, I, c_int_p, c_int_p, I, c_dbl_p, vp],
     "qg_dm_calcProbOfMultiQubitOutcome": [vp, I, c_int_p, c_int_p, I, c_dbl_p, vp],
     "qg_sv_calcProbsOfAllMultiQubitOutcomes": [c_dbl_p, vp, I, c_int_p, I, vp],
+    "qg_dm_calcProbsOfAllMultiQubitOutcomes": [c_dbl_p, vp, I, c_int_p, I, vp],
     "qg_sv_calcExpecAnyTargZ": [vp, I, c_int_p, I, c_dbl_p, vp],
     "qg_dm_calcExpecAnyTargZ": [vp, I, c_int_p, I, c_cplx_p, vp],
     "qg_sv_calcExpecPauliStr": [vp, I, c_int_p, I, c_int_p, I, c_int_p, I, c_cplx_p, vp],
@@ -109,6 +111,7 @@ ABI = {
     "qg_circuit_get_block": [vp, I, c_int_p, c_int_p, c_cplx_p],
     "qg_sv32_apply_circuit": [vp, vp, I, I, vp],
     "qg_tc_get_error_flag": [c_int_p],
+    "qg_tc_clear_error_flag": [],
     "qg_tc_selftest_timeout": [I, c_int_p, c_int_p, ctypes.POINTER(ctypes.c_double), c_int_p],
     "qg_circuit_autotune": [vp, c_int_p, c_int_p, c_int_p, c_int_p, c_dbl_p, I, c_int_p],
     "qg_circuit_graph_create": [vp, vp, I, I, ctypes.POINTER(vp)],

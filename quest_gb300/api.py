@@ -81,6 +81,10 @@ class PauliStr(ctypes.Structure):
     _fields_ = [("lowPaulis", ctypes.c_ulonglong), ("highPaulis", ctypes.c_ulonglong)]
 
 
+class PauliStrSum(ctypes.Structure):
+    _fields_ = [("numTerms", qindex), ("strings", ctypes.POINTER(PauliStr)), ("coeffs", _CP), ("isApproxHermitian", _IP)]
+
+
 _HANDLER_T = ctypes.CFUNCTYPE(None, ctypes.c_char_p, ctypes.c_char_p)
 _errors = []
 
@@ -173,6 +177,10 @@ _PROTOS = {
     "applyMultiQubitProjector": (V, [Qureg, _IP, _IP, I]),
     "applyQubitMeasurement": (I, [Qureg, I]),
     "applyQubitMeasurementAndGetProb": (I, [Qureg, I, ctypes.POINTER(D)]),
+    "applyForcedQubitMeasurement": (D, [Qureg, I, I]),
+    "applyMultiQubitMeasurement": (qindex, [Qureg, _IP, I]),
+    "applyMultiQubitMeasurementAndGetProb": (qindex, [Qureg, _IP, I, ctypes.POINTER(D)]),
+    "applyForcedMultiQubitMeasurement": (D, [Qureg, _IP, _IP, I]),
     "mixDephasing": (V, [Qureg, I, D]),
     "mixTwoQubitDephasing": (V, [Qureg, I, I, D]),
     "mixDepolarising": (V, [Qureg, I, D]),
@@ -182,10 +190,14 @@ _PROTOS = {
     "mixKrausMap": (V, [Qureg, _IP, I, KrausMap]),
     "calcExpecPauliStr": (D, [Qureg, PauliStr]),
     "calcExpecPauliStrs": (V, [ctypes.POINTER(D), Qureg, ctypes.POINTER(PauliStr), I]),
+    "createPauliStrSum": (PauliStrSum, [ctypes.POINTER(PauliStr), _CP, qindex]),
+    "destroyPauliStrSum": (V, [PauliStrSum]),
+    "calcExpecPauliStrSum": (D, [Qureg, PauliStrSum]),
     "calcProbOfQubitOutcome": (D, [Qureg, I, I]),
     "calcProbOfMultiQubitOutcome": (D, [Qureg, _IP, _IP, I]),
     "calcProbsOfAllMultiQubitOutcomes": (V, [ctypes.POINTER(D), Qureg, _IP, I]),
     "calcTotalProb": (D, [Qureg]),
+    "isQuregHostMirrorPinned": (I, [Qureg]),
     "calcPurity": (D, [Qureg]),
     "createFullStateDiagMatr": (FullStateDiagMatr, [I]),
     "destroyFullStateDiagMatr": (V, [FullStateDiagMatr]),
@@ -353,3 +365,11 @@ def full_state_diag(elems):
     m = Q.createFullStateDiagMatr(n)
     Q.setFullStateDiagMatr(m, 0, e.ctypes.data, e.size)
     return m
+
+
+def pauli_str_sum(coeffs, strings):
+    """createPauliStrSum from complex coefficients and Pauli strings ('IXYZ...' text or codes)."""
+    n = len(strings)
+    strs = (PauliStr * n)(*[pauli_str(x) for x in strings])
+    cs = (qg_cplx * n)(*[qg_cplx(complex(c).real, complex(c).imag) for c in coeffs])
+    return Q.createPauliStrSum(strs, cs, n)

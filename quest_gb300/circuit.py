@@ -11,7 +11,7 @@ import numpy as np
 
 from ._lib import qg_cplx
 from .api import (Q, comp_matr, comp_matr1, comp_matr2, diag_matr, diag_matr1, diag_matr2, full_state_diag, ints,
-                  kraus_map, pauli_str, seeds)
+                  kraus_map, pauli_str, pauli_str_sum, seeds)
 
 
 def _f(tokens, k):
@@ -164,6 +164,30 @@ def run_text(text, qureg):
             seeds(*[int(v) for v in a])
         elif op == "MEAS":
             outcomes.append(Q.applyQubitMeasurement(qureg, int(a[0])))
+        elif op == "MEASM":
+            k = int(a[0])
+            p = ctypes.c_double(0)
+            outcomes.append(int(Q.applyMultiQubitMeasurementAndGetProb(qureg, ints(a[1:1 + k]), k, ctypes.byref(p))))
+            results.append(p.value)
+        elif op == "FMEAS":
+            results.append(Q.applyForcedQubitMeasurement(qureg, int(a[0]), int(a[1])))
+        elif op == "FMEASM":
+            k = int(a[0])
+            results.append(Q.applyForcedMultiQubitMeasurement(qureg, ints(a[1:1 + k]), ints(a[1 + k:1 + 2 * k]), k))
+        elif op == "PROBALL":
+            k = int(a[0])
+            out = (ctypes.c_double * (1 << k))()
+            Q.calcProbsOfAllMultiQubitOutcomes(out, qureg, ints(a[1:1 + k]), k)
+            results += list(out)
+        elif op == "EXPSUM":
+            T = int(a[0])
+            cs = [complex(float(a[1 + 3 * t]), float(a[2 + 3 * t])) for t in range(T)]
+            ps = [a[3 + 3 * t] for t in range(T)]
+            sm = pauli_str_sum(cs, ps)
+            try:
+                results.append(Q.calcExpecPauliStrSum(qureg, sm))
+            finally:
+                Q.destroyPauliStrSum(sm)
         elif op == "TOTALPROB":
             results.append(Q.calcTotalProb(qureg))
         elif op == "PURITY":

@@ -30,9 +30,10 @@
 size_t qg_tc_operand_floats();
 void qg_tc_build_operands(const std::complex<double>* m32x32, float* out);
 int qg_tc_apply_block(float2* amps, int numQubits, const int* targs, const float* devOperands, cudaStream_t st,
-                      bool holdOperands = false);
+                      bool holdOperands = false, int* errorFlag = nullptr);
 bool qg_tc_supported(int numQubits);
 int qg_tc_prepare();
+int qg_tc_take_error();
 
 namespace {
 
@@ -634,24 +635,34 @@ int qg_circuit_get_block(const qg_circuit* c, int i, int* targs, int* numTargs, 
     return QG_OK;
 }
 
-// impl: 0 = automatic (tensor cores for 5-qubit blocks on large states), 1 = SIMT FP32, 2 = tensor cores
-int qg_sv32_apply_circuit(qg_circuit* c, void* amps, int numQubits, int impl, void* stream) {
+// impl: 0 = automatic (tensor cores for 5-qubit blocks on large states), 1 = SIMT FP32, 2 = tensor cores,
+// 3 = tensor cores in the self-test of their failure path (operand buffers are never signalled
+// full, so every 5-qubit block launch gives up its bounded waits after about 2 s and leaves the
+// register untouched).  errorFlag: the device word a timed-out launch reports to (nullptr: the
+// device's own flag, reported by the next qg_sv32_apply_circuit or qg_graph_launch).
+int qg_sv32_apply_circuit_flag(qg_circuit* c, void* amps, int numQubits, int impl, cudaStream_t st, int* errorFlag) {
     QG_TRY(check32(amps, numQubits));
     if (!c) return qg_fail(QG_ERR_ARG, "null circuit");
-    if (!c->uploaded) QG_TRY(qg_circuit_upload(c, qg_stream(stream)));
+    if (impl < 0 || impl > 3) return qg_fail(QG_ERR_ARG, "unknown block kernel choice %d", impl);
+    if (!c->uploaded) QG_TRY(qg_circuit_upload(c, st));
     if (numQubits != c->numQubits) return qg_fail(QG_ERR_ARG, "circuit has %d qubits, state has %d", c->numQubits, numQubits);
     if (c->blocks.empty() && !c->gates.empty()) return qg_fail(QG_ERR_ARG, "circuit was not fused (qg_circuit_fuse)");
-    cudaStream_t st = qg_stream(stream);
     if (impl == 0 && c->preferredImpl != 0) impl = c->preferredImpl;
     for (const QgBlock& b : c->blocks) {
-        bool tc = b.targs.size() == 5 && (impl == 2 || (impl == 0 && qg_tc_supported(numQubits)));
+        bool tc = b.targs.size() == 5 && (impl >= 2 || (impl == 0 && qg_tc_supported(numQubits)));
         if (tc) {
-            QG_TRY(qg_tc_apply_block((float2*)amps, numQubits, b.targs.data(), c->devTC + b.offTC, st));
+            QG_TRY(qg_tc_apply_block((float2*)amps, numQubits, b.targs.data(), c->devTC + b.offTC, st, impl == 3, errorFlag));
         } else {
             QG_TRY(launch_fused_simt((float2*)amps, numQubits, b.targs, c->devF32 + b.off32, st));
         }
     }
     return QG_OK;
+}
+
+int qg_sv32_apply_circuit(qg_circuit* c, void* amps, int numQubits, int impl, void* stream) {
+    // a timeout left by an earlier launch on this device is reported here, before more work goes out
+    QG_TRY(qg_tc_take_error());
+    return qg_sv32_apply_circuit_flag(c, amps, numQubits, impl, qg_stream(stream), nullptr);
 }
 
 // ---------------------------------------------------------------- CUDA graphs of a circuit
@@ -678,7 +689,7 @@ int qg_circuit_graph_create(qg_circuit* c, void* amps, int numQubits, int impl, 
         cudaStreamDestroy(s);
         return qg_check_cuda(e, "cudaStreamBeginCapture");
     }
-    int rc = qg_sv32_apply_circuit(c, amps, numQubits, impl, s);
+    int rc = qg_sv32_apply_circuit_flag(c, amps, numQubits, impl, s, nullptr);
     cudaGraph_t graph = nullptr;
     e = cudaStreamEndCapture(s, &graph);
     qg_get_launch_count(&after);
@@ -701,6 +712,7 @@ int qg_circuit_graph_create(qg_circuit* c, void* amps, int numQubits, int impl, 
 
 int qg_graph_launch(qg_graph* g, void* stream) {
     if (!g) return qg_fail(QG_ERR_ARG, "null graph");
+    QG_TRY(qg_tc_take_error());
     QG_CUDA(cudaGraphLaunch(g->exec, qg_stream(stream)));
     qg_note_launch(g->numKernels);
     return QG_OK;

@@ -471,41 +471,86 @@ __global__ void __launch_bounds__(WsShape<TPR, NBUF>::THREADS, 1) k32_fused_tc(T
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
-    if (tid == 0 && *abortFlag) atomicExch(args.errorFlag, 1);
+    if (tid == 0 && *abortFlag) {
+        *(volatile int*)args.errorFlag = 1;     // a plain store: the word may be mapped host memory
+        __threadfence_system();
+    }
     if (warp == S::MMA_WARP) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(WS_TMEM_COLS));
 }
 
 // ---------------------------------------------------------------- host: launch
 
 namespace {
-int* g_tc_error = nullptr;
+// Per device: the error flag that launches without a flag of their own report to, and
+// whether the kernel's shared-memory limit has been raised there.  The flag lives in
+// mapped pinned host memory, so the host reads it without a copy or a synchronisation.
+struct TcDevice {
+    int* hostFlag = nullptr;   // host view
+    int* devFlag = nullptr;    // the same word as the device sees it
+    bool attr = false;
+};
+const int TC_MAX_DEVICES = 64;
+TcDevice g_tcdev[TC_MAX_DEVICES];
+std::mutex g_tcmu;
+
+int tc_current(TcDevice** out) {
+    int dev = 0;
+    QG_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= TC_MAX_DEVICES) return qg_fail(QG_ERR_NOTSUP, "device %d is beyond this build's device table", dev);
+    *out = &g_tcdev[dev];
+    return QG_OK;
 }
+}  // namespace
 
 bool qg_tc_supported(int numQubits) { return numQubits >= 12; }
 
-// one-time set-up (the error flag's memory, the kernel's shared-memory limit); done
-// before the first launch and before any stream capture of one
+// one-time set-up per device (the error flag, the kernel's shared-memory limit); done
+// before the first launch on that device and before any stream capture of one
 int qg_tc_prepare() {
-    static std::mutex mu;
-    static bool attr = false;
-    std::lock_guard<std::mutex> lock(mu);
-    if (!g_tc_error) {
-        QG_CUDA(cudaMalloc(&g_tc_error, sizeof(int)));
-        QG_CUDA(cudaMemset(g_tc_error, 0, sizeof(int)));
+    std::lock_guard<std::mutex> lock(g_tcmu);
+    TcDevice* d = nullptr;
+    QG_TRY(tc_current(&d));
+    if (!d->hostFlag) {
+        int* h = nullptr;
+        QG_CUDA(cudaHostAlloc((void**)&h, sizeof(int), cudaHostAllocMapped | cudaHostAllocPortable));
+        *(volatile int*)h = 0;
+        int* dp = nullptr;
+        cudaError_t e = cudaHostGetDevicePointer((void**)&dp, h, 0);
+        if (e != cudaSuccess) {
+            cudaFreeHost(h);
+            return qg_check_cuda(e, "cudaHostGetDevicePointer(tensor-core error flag)");
+        }
+        d->hostFlag = h;
+        d->devFlag = dp;
     }
-    if (!attr) {
+    if (!d->attr) {
         QG_CUDA(cudaFuncSetAttribute(k32_fused_tc<TC_TPR, TC_NBUF, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, WS_SMEM_BYTES(0)));
         QG_CUDA(cudaFuncSetAttribute(k32_fused_tc<TC_TPR_STAGED, TC_NBUF_STAGED, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, WS_SMEM_BYTES(1)));
         QG_CUDA(cudaFuncSetAttribute(k32_fused_tc<TC_TPR_STAGED, TC_NBUF_STAGED, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, WS_SMEM_BYTES(2)));
-        attr = true;
+        d->attr = true;
     }
     return QG_OK;
 }
 
+// Reports, and clears, a timeout that an earlier launch on the current device left in the
+// device's flag: QG_ERR_TIMEOUT if there was one.  A host read of mapped memory: no copy,
+// no synchronisation, so launches still in flight are not waited for.
+int qg_tc_take_error() {
+    TcDevice* d = nullptr;
+    QG_TRY(tc_current(&d));
+    if (!d->hostFlag || *(volatile int*)d->hostFlag == 0) return QG_OK;
+    *(volatile int*)d->hostFlag = 0;
+    return qg_fail(QG_ERR_TIMEOUT, "an earlier tensor-core block launch on this device gave up a bounded wait "
+                                   "(its register was left partly updated); the flag is now cleared");
+}
+
+// errorFlag: the device word a timeout is reported to (nullptr: the device's own flag)
 int qg_tc_apply_block(float2* amps, int numQubits, const int* targs, const float* devOperands, cudaStream_t st,
-                      bool holdOperands = false) {
+                      bool holdOperands = false, int* errorFlag = nullptr) {
     if (numQubits < 12) return qg_fail(QG_ERR_ARG, "the tensor-core block kernel needs at least 12 qubits (one 128-group tile)");
-    if (!g_tc_error) QG_TRY(qg_tc_prepare());
+    TcDevice* dev = nullptr;
+    QG_TRY(tc_current(&dev));
+    if (!dev->attr) QG_TRY(qg_tc_prepare());
     int zeros[5] = {0, 0, 0, 0, 0};
     QubitPlan p;
     QG_TRY(qg_make_plan(numQubits, nullptr, nullptr, 0, targs, zeros, 5, &p));
@@ -519,7 +564,7 @@ int qg_tc_apply_block(float2* amps, int numQubits, const int* targs, const float
         a.off[j] = o;
     }
     a.ops = devOperands;
-    a.errorFlag = g_tc_error;
+    a.errorFlag = errorFlag ? errorFlag : dev->devFlag;
     a.holdOperands = holdOperands ? 1 : 0;
     // the mode and the staged modes' index tables (qg_tc_plan.h)
     qgtc::Plan plan;
@@ -547,8 +592,17 @@ int qg_tc_apply_block(float2* amps, int numQubits, const int* targs, const float
 }
 
 extern "C" int qg_tc_get_error_flag(int* out) {
-    if (!g_tc_error) { *out = 0; return QG_OK; }
-    QG_CUDA(cudaMemcpy(out, g_tc_error, sizeof(int), cudaMemcpyDeviceToHost));
+    if (!out) return qg_fail(QG_ERR_ARG, "null argument");
+    TcDevice* d = nullptr;
+    QG_TRY(tc_current(&d));
+    *out = d->hostFlag ? *(volatile int*)d->hostFlag : 0;
+    return QG_OK;
+}
+
+extern "C" int qg_tc_clear_error_flag(void) {
+    TcDevice* d = nullptr;
+    QG_TRY(tc_current(&d));
+    if (d->hostFlag) *(volatile int*)d->hostFlag = 0;
     return QG_OK;
 }
 
@@ -584,7 +638,7 @@ extern "C" int qg_tc_selftest_timeout(int numQubits, const int* targs, int* flag
             rc = qg_fail(QG_ERR_CUDA, "copy failed");
         *unchangedOut = rc == QG_OK && std::memcmp(back.data(), host.data(), n * sizeof(float2)) == 0;
     }
-    if (rc == QG_OK && cudaMemset(g_tc_error, 0, sizeof(int)) != cudaSuccess) rc = qg_fail(QG_ERR_CUDA, "flag reset failed");
+    if (rc == QG_OK) qg_tc_clear_error_flag();
     if (secondsOut) *secondsOut = secs;
     qg_free(ops);
     qg_free(amps);

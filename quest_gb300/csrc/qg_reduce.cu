@@ -176,17 +176,25 @@ __global__ void __launch_bounds__(RED_THREADS) k_dm_expec_pauli_batch(const doub
     block_reduce_and_finish<2 * NS>(v, out);
 }
 
-// histogram of all outcomes of `num` qubits, one bin per blockIdx.y (deterministic)
-template <int NB>
+// histogram of all outcomes of `num` qubits, one bin per blockIdx.y (deterministic: no
+// atomics, a fixed assignment of terms to threads and a fixed addition order).
+// Statevector (DIAG = false): sum of |a_i|^2; density matrix (DIAG = true): sum of
+// Re rho_ii, the element i * diagStride of the Choi vector.
+template <int NB, bool DIAG>
 __global__ void __launch_bounds__(RED_THREADS) k_probs_all(const double2* __restrict__ a, qidx numIts, Ins ins,
-                                                          const qidx* __restrict__ binMasks, double* __restrict__ partials) {
+                                                          const qidx* __restrict__ binMasks, qidx diagStride,
+                                                          double* __restrict__ partials) {
     __shared__ double sh[RED_THREADS / 32];
     qidx mask = binMasks[blockIdx.y];
     double v = 0;
     qidx stride = (qidx)gridDim.x * RED_THREADS;
     for (qidx m = blockIdx.x * (qidx)RED_THREADS + threadIdx.x; m < numIts; m += stride) {
-        double2 x = ld_amp(a + (insert_bits<NB>(m, ins) | mask));
-        v = fma(x.x, x.x, fma(x.y, x.y, v));
+        if (DIAG) {
+            v += __ldg(&a[(insert_bits<NB>(m, ins) | mask) * diagStride].x);
+        } else {
+            double2 x = ld_amp(a + (insert_bits<NB>(m, ins) | mask));
+            v = fma(x.x, x.x, fma(x.y, x.y, v));
+        }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -282,10 +290,15 @@ int qg_dm_calcProbOfMultiQubitOutcome(const void* amps, int nKet, const int* qub
     return sum_diag(amps, nKet, p, out, qg_stream(stream));
 }
 
-int qg_sv_calcProbsOfAllMultiQubitOutcomes(double* outProbs, const void* amps, int numQubits, const int* qubits, int num,
-                                           void* stream) {
-    QG_TRY(qg_check_amps(amps, numQubits));
+}  // extern "C"
+
+namespace {
+
+// histogram over the outcomes of `num` qubits: statevector (nKet = 0) or the diagonal of a
+// density matrix of nKet qubits (its Choi vector has 2 nKet qubits)
+int probs_all(double* outProbs, const void* amps, int numQubits, bool dm, const int* qubits, int num, void* stream) {
     if (num < 1 || num > 20) return qg_fail(QG_ERR_ARG, "outcome histogram over %d qubits is unsupported", num);
+    if (!outProbs) return qg_fail(QG_ERR_ARG, "null output");
     std::vector<int> zeros(num, 0);
     QubitPlan p;
     QG_TRY(qg_make_plan(numQubits, nullptr, nullptr, 0, qubits, zeros.data(), num, &p));
@@ -298,6 +311,7 @@ int qg_sv_calcProbsOfAllMultiQubitOutcomes(double* outProbs, const void* amps, i
         masks[(size_t)b] = m;
     }
     qidx numIts = ((qidx)1 << numQubits) >> num;
+    qidx diagStride = dm ? ((qidx)1 << numQubits) + 1 : 1;
     int gx = (int)std::max<qidx>(1, std::min<qidx>((qidx)qg_num_sms() * 4 / numBins + 1, (numIts + RED_THREADS - 1) / RED_THREADS));
     cudaStream_t st = qg_stream(stream);
     void* s = nullptr;
@@ -305,15 +319,21 @@ int qg_sv_calcProbsOfAllMultiQubitOutcomes(double* outProbs, const void* amps, i
     QG_TRY(qg_scratch_get(&s, need + 512));
     // the first 512 bytes hold the completion ticket of the other reductions: keep clear of them
     qidx* dMasks = (qidx*)((char*)s + 512);
-    double* partials = (double*)((char*)s + 8 * numBins);
+    double* partials = (double*)((char*)s + 512 + 8 * numBins);
     double* result = partials + numBins * gx;
     QG_CUDA(cudaMemcpyAsync(dMasks, masks.data(), 8 * (size_t)numBins, cudaMemcpyHostToDevice, st));
     for (qidx b0 = 0; b0 < numBins; b0 += 65535) {
         unsigned gy = (unsigned)std::min<qidx>(65535, numBins - b0);
         dim3 grid(gx, gy);
-#define L(NBV) k_probs_all<NBV><<<grid, RED_THREADS, 0, st>>>((const double2*)amps, numIts, p.ins, dMasks + b0, partials + b0 * gx)
-        QG_DISPATCH_NB(p.numFixed, L)
+        if (dm) {
+#define L(NBV) k_probs_all<NBV, true><<<grid, RED_THREADS, 0, st>>>((const double2*)amps, numIts, p.ins, dMasks + b0, diagStride, partials + b0 * gx)
+            QG_DISPATCH_NB(p.numFixed, L)
 #undef L
+        } else {
+#define L(NBV) k_probs_all<NBV, false><<<grid, RED_THREADS, 0, st>>>((const double2*)amps, numIts, p.ins, dMasks + b0, diagStride, partials + b0 * gx)
+            QG_DISPATCH_NB(p.numFixed, L)
+#undef L
+        }
         qg_note_launch();
     }
     k_probs_all_finish<<<qg_blocks(numBins), QG_THREADS, 0, st>>>(partials, gx, numBins, result);
@@ -322,6 +342,22 @@ int qg_sv_calcProbsOfAllMultiQubitOutcomes(double* outProbs, const void* amps, i
     QG_CUDA(cudaMemcpyAsync(outProbs, result, 8 * (size_t)numBins, cudaMemcpyDeviceToHost, st));
     QG_CUDA(cudaStreamSynchronize(st));
     return QG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int qg_sv_calcProbsOfAllMultiQubitOutcomes(double* outProbs, const void* amps, int numQubits, const int* qubits, int num,
+                                           void* stream) {
+    QG_TRY(qg_check_amps(amps, numQubits));
+    return probs_all(outProbs, amps, numQubits, false, qubits, num, stream);
+}
+
+int qg_dm_calcProbsOfAllMultiQubitOutcomes(double* outProbs, const void* amps, int numKetQubits, const int* qubits, int num,
+                                           void* stream) {
+    QG_TRY(check_dm_amps(amps, numKetQubits));
+    return probs_all(outProbs, amps, numKetQubits, true, qubits, num, stream);
 }
 
 int qg_sv_calcExpecAnyTargZ(const void* amps, int numQubits, const int* targs, int numTargs, double* out, void* stream) {

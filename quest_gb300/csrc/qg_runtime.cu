@@ -178,6 +178,14 @@ const char* qg_get_error_string(int code) {
 
 int qg_get_version(void) { return 100; }
 
+namespace {
+// the context's L2 fetch-granularity limit as qg_init found it, per device (-1: not saved)
+const int L2_MAX_DEVICES = 64;
+int g_l2Saved[L2_MAX_DEVICES] = {};
+bool g_l2SavedInit = false;
+std::mutex g_l2mu;
+}  // namespace
+
 int qg_init(int device) {
     int n = 0;
     QG_CUDA(cudaGetDeviceCount(&n));
@@ -185,17 +193,44 @@ int qg_init(int device) {
     QG_CUDA(cudaSetDevice(device));
     QG_CUDA(cudaFree(0));  // create the primary context now
     qg_num_sms();
-    // L2 fetches of 32 bytes (a per-context hint, gone with the process): gates that
-    // visit every other 16-, 32- or 64-byte run (a controlled phase on qubits 1 or 2)
-    // otherwise pull whole 64- or 128-byte units for half their bytes.  Measured on
-    // GB300 at 28 qubits: 0.553 -> 0.372 ms for such a phase, streaming kernels unchanged.
+    // L2 fetches of 32 bytes: gates that visit every other 16-, 32- or 64-byte run (a
+    // controlled phase on qubits 1 or 2) otherwise pull whole 64- or 128-byte units for
+    // half their bytes.  Measured on GB300 at 28 qubits: 0.553 -> 0.372 ms for such a
+    // phase, streaming kernels unchanged.  The limit belongs to the primary context, which
+    // every library of the process shares, and lasts until the process exits; the value
+    // found here is kept so that qg_restore_l2_fetch_granularity can put it back.
+    {
+        std::lock_guard<std::mutex> lock(g_l2mu);
+        if (!g_l2SavedInit) {
+            for (int i = 0; i < L2_MAX_DEVICES; i++) g_l2Saved[i] = -1;
+            g_l2SavedInit = true;
+        }
+        if (device < L2_MAX_DEVICES && g_l2Saved[device] < 0) {
+            size_t v = 0;
+            QG_CUDA(cudaDeviceGetLimit(&v, cudaLimitMaxL2FetchGranularity));
+            g_l2Saved[device] = (int)v;
+        }
+    }
     return qg_set_l2_fetch_granularity(32);
 }
 
 int qg_set_l2_fetch_granularity(int bytes) {
     if (bytes != 0 && bytes != 32 && bytes != 64 && bytes != 128)
-        return qg_fail(QG_ERR_ARG, "L2 fetch granularity %d: use 0 (the driver's default), 32, 64 or 128", bytes);
+        return qg_fail(QG_ERR_ARG, "L2 fetch granularity %d: use 0, 32, 64 or 128", bytes);
     QG_CUDA(cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, (size_t)bytes));
+    return QG_OK;
+}
+
+int qg_restore_l2_fetch_granularity(void) {
+    int dev = 0;
+    QG_CUDA(cudaGetDevice(&dev));
+    int v = -1;
+    {
+        std::lock_guard<std::mutex> lock(g_l2mu);
+        if (g_l2SavedInit && dev < L2_MAX_DEVICES) v = g_l2Saved[dev];
+    }
+    if (v < 0) return QG_OK;    // qg_init never changed this device's limit
+    QG_CUDA(cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, (size_t)v));
     return QG_OK;
 }
 

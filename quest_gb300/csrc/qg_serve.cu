@@ -37,7 +37,7 @@
 #define SERVE_SMALL_THREADS 256
 #define SERVE_STREAMS 16
 
-int qg_sv32_apply_circuit(qg_circuit* c, void* amps, int numQubits, int impl, void* stream);
+extern "C" int qg_sv32_apply_circuit_flag(qg_circuit* c, void* amps, int numQubits, int impl, cudaStream_t st, int* errorFlag);
 
 // ============================================================== device: small registers in shared memory
 
@@ -202,6 +202,7 @@ struct Request {
     bool unitary = true;     // every gate of the circuit is unitary: results are normalised
     bool finished = false;
     bool cancelled = false;  // the client went away while it ran: dropped when it completes
+    bool timedOut = false;   // a tensor-core launch of it gave up a bounded wait: no values
     std::vector<double> values;
 };
 
@@ -222,6 +223,8 @@ struct qg_server {
     size_t inUse = 0;
     double* devResults = nullptr;             // [maxSlots][2*16]
     double* hostResults = nullptr;            // pinned mirror
+    int* devFlags = nullptr;                  // [maxSlots] tensor-core timeout word of the slot's request
+    int* hostFlags = nullptr;                 // pinned mirror
     std::vector<int> freeSlots;
     cudaStream_t streams[SERVE_STREAMS];
     cudaStream_t smallStream;
@@ -292,7 +295,9 @@ int launch_large(qg_server* s, Request& r) {
     float2* amps = (float2*)(s->arena + r.arenaOff);
     qidx n = (qidx)1 << r.nq;
     QG_TRY(qg_sv32_initClassicalState(amps, r.nq, 0, st));
-    QG_TRY(qg_sv32_apply_circuit(r.circ, amps, r.nq, s->impl, st));
+    int* flag = s->devFlags + r.slot;
+    QG_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), st));
+    QG_TRY(qg_sv32_apply_circuit_flag(r.circ, amps, r.nq, s->impl, st, flag));
     release_transient_copy(r.circ);
     // expectation values into the request's own reduction scratch, then its result slot
     char* scratch = s->arena + r.arenaOff + round_up((size_t)8 << r.nq, 256);
@@ -312,6 +317,7 @@ int launch_large(qg_server* s, Request& r) {
     QG_TRY(qg_check_launch("k_serve_expec"));
     QG_CUDA(cudaMemcpyAsync(s->hostResults + (size_t)r.slot * SERVE_RESULT_DOUBLES, ro.result,
                             sizeof(double) * SERVE_RESULT_DOUBLES, cudaMemcpyDeviceToHost, st));
+    QG_CUDA(cudaMemcpyAsync(s->hostFlags + r.slot, flag, sizeof(int), cudaMemcpyDeviceToHost, st));
     QG_CUDA(cudaEventCreateWithFlags(&r.done, cudaEventDisableTiming));
     QG_CUDA(cudaEventRecord(r.done, st));
     return QG_OK;
@@ -375,6 +381,8 @@ int launch_small_batch(qg_server* s) {
 
 void finish(qg_server* s, Request& r) {
     const double* h = s->hostResults + (size_t)r.slot * SERVE_RESULT_DOUBLES;
+    // small requests run in shared memory without tensor-core launches: no timeout word
+    r.timedOut = !r.small && s->hostFlags[r.slot] != 0;
     r.values.resize(r.numStrings);
     // A unitary circuit keeps the norm of |0>, so values are divided by the FP64 norm of
     // the final FP32 state: this removes the drift of the FP32 products to first order.
@@ -396,6 +404,7 @@ extern "C" {
 
 int qg_server_create(qg_server** out, int64_t hbmBudgetBytes, int maxInFlight, int impl) {
     if (!out || hbmBudgetBytes < (1 << 20) || maxInFlight < 1) return qg_fail(QG_ERR_ARG, "bad server arguments");
+    if (impl < 0 || impl > 3) return qg_fail(QG_ERR_ARG, "unknown block kernel choice %d", impl);
     qg_server* s = new qg_server();
     s->impl = impl;
     s->maxSlots = maxInFlight;
@@ -408,6 +417,9 @@ int qg_server_create(qg_server** out, int64_t hbmBudgetBytes, int maxInFlight, i
     s->freeList[0] = s->arenaBytes;
     QG_CUDA(cudaMalloc(&s->devResults, sizeof(double) * SERVE_RESULT_DOUBLES * maxInFlight));
     QG_CUDA(cudaMallocHost(&s->hostResults, sizeof(double) * SERVE_RESULT_DOUBLES * maxInFlight));
+    QG_CUDA(cudaMalloc(&s->devFlags, sizeof(int) * maxInFlight));
+    QG_CUDA(cudaMallocHost(&s->hostFlags, sizeof(int) * maxInFlight));
+    for (int i = 0; i < maxInFlight; i++) s->hostFlags[i] = 0;
     for (int i = maxInFlight - 1; i >= 0; i--) s->freeSlots.push_back(i);
     for (int i = 0; i < SERVE_STREAMS; i++) QG_CUDA(cudaStreamCreateWithFlags(&s->streams[i], cudaStreamNonBlocking));
     QG_CUDA(cudaStreamCreateWithFlags(&s->smallStream, cudaStreamNonBlocking));
@@ -425,6 +437,8 @@ int qg_server_destroy(qg_server* s) {
     cudaFree(s->arena);
     cudaFree(s->devResults);
     cudaFreeHost(s->hostResults);
+    cudaFree(s->devFlags);
+    cudaFreeHost(s->hostFlags);
     delete s;
     return QG_OK;
 }
@@ -520,6 +534,8 @@ int qg_server_result(qg_server* s, int64_t id, double* values, int* done) {
     auto it = s->reqs.find(id);
     if (it == s->reqs.end()) return qg_fail(QG_ERR_ARG, "unknown request %lld", (long long)id);
     *done = it->second.finished ? 1 : 0;
+    if (it->second.finished && it->second.timedOut)
+        return qg_fail(QG_ERR_TIMEOUT, "request %lld failed: a tensor-core block launch gave up a bounded wait", (long long)id);
     if (it->second.finished && values)
         for (int k = 0; k < it->second.numStrings; k++) values[k] = it->second.values[k];
     return QG_OK;

@@ -16,6 +16,8 @@
 #include <algorithm>
 #include <cmath>
 #include <complex>
+#include <map>
+#include <mutex>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -34,6 +36,10 @@ const double REDUCTION_EPS_FACTOR = 100;     // validation.cpp:1137
 double g_eps = DEFAULT_EPS;
 bool g_envInit = false;
 thread_local void* g_stream = nullptr;
+// how each Qureg's host mirror was allocated (keyed by cpuAmps)
+enum { MIRROR_PINNED = 0, MIRROR_REGISTERED = 1, MIRROR_PAGEABLE = 2 };
+std::map<void*, int> g_mirrorKind;
+std::mutex g_mirrorMu;
 std::mt19937_64 g_rng;
 
 void default_handler(const char* func, const char* msg) {
@@ -139,6 +145,21 @@ void applyDense(const Qureg& q, const int* ctrls, const int* states, int nc, con
     if (!check(nt >= 1, func, "At least one target qubit is required.")) return;
     if (checkUnitary && !check(isUnitaryDense(m, (qindex)1 << nt), func, "The given matrix was not (approximately) unitary.")) return;
     vector<int> c = V(ctrls, nc), s = V(states, nc), t = V(targs, nt);
+    if (q.isDensityMatrix && nt == 1 && nc == 0) {
+        // U rho U^dagger in one pass: U on the ket qubit and conj(U) on its bra partner commute,
+        // and together they are the 4x4 operator conj(U) (x) U on the pair (t, t + N) -- the
+        // same 16 complex products per 4 amplitudes as the reference's two passes
+        // (localiser_statevec_anyCtrlOneTargDenseMatr on the ket, then on the conjugated bra),
+        // with one read and one write of the state instead of two.
+        qcomp_t k[16];
+        for (int r1 = 0; r1 < 2; r1++)
+            for (int r0 = 0; r0 < 2; r0++)
+                for (int c1 = 0; c1 < 2; c1++)
+                    for (int c0 = 0; c0 < 2; c0++)
+                        k[((r1 << 1) | r0) * 4 + ((c1 << 1) | c0)] = Q(std::conj(C(m[r1 * 2 + c1])) * C(m[r0 * 2 + c0]));
+        backend(qg_sv_anyCtrlTwoTargDenseMatr(q.gpuAmps, nsv(q), nullptr, nullptr, 0, t[0], t[0] + q.numQubits, k, g_stream), func);
+        return;
+    }
     if (!denseSV(q, c, s, t, m, false, func)) return;
     if (!q.isDensityMatrix) return;
     denseSV(q, braOf(q, c), s, braOf(q, t), m, true, func);
@@ -340,15 +361,25 @@ Qureg createCustomQureg(int numQubits, int isDensMatr, int useDistrib, int useGp
         return q;
     }
     void* host = nullptr;
+    int kind = MIRROR_PINNED;
     if (cudaMallocHost(&host, bytes) != cudaSuccess) {
+        // pinned allocation refused (a memlock limit, say): page-lock ordinary memory, and
+        // only if that fails too keep a pageable mirror (copies then run through staging)
         cudaGetLastError();
         host = std::calloc(1, bytes);
+        kind = MIRROR_PAGEABLE;
+        if (host && cudaHostRegister(host, bytes, cudaHostRegisterDefault) == cudaSuccess) kind = MIRROR_REGISTERED;
+        else cudaGetLastError();
     }
     if (!host) {
         qg_free(dev);
         fail(func, "Could not allocate the host copy of the amplitudes.");
         std::memset(&q, 0, sizeof(q));
         return q;
+    }
+    {
+        std::lock_guard<std::mutex> lock(g_mirrorMu);
+        g_mirrorKind[host] = kind;
     }
     q.gpuAmps = (qcomp_t*)dev;
     q.cpuAmps = (qcomp_t*)host;
@@ -372,10 +403,30 @@ void destroyQureg(Qureg qureg) {
     if (!checkQureg(qureg, "destroyQureg")) return;
     qg_sync();
     qg_free(qureg.gpuAmps);
-    if (cudaFreeHost(qureg.cpuAmps) != cudaSuccess) {
-        cudaGetLastError();
-        std::free(qureg.cpuAmps);
+    int kind = MIRROR_PINNED;
+    {
+        std::lock_guard<std::mutex> lock(g_mirrorMu);
+        auto it = g_mirrorKind.find(qureg.cpuAmps);
+        if (it != g_mirrorKind.end()) {
+            kind = it->second;
+            g_mirrorKind.erase(it);
+        }
     }
+    if (kind == MIRROR_PINNED) {
+        if (cudaFreeHost(qureg.cpuAmps) != cudaSuccess) cudaGetLastError();
+        return;
+    }
+    if (kind == MIRROR_REGISTERED && cudaHostUnregister(qureg.cpuAmps) != cudaSuccess) cudaGetLastError();
+    std::free(qureg.cpuAmps);
+}
+
+// 1 if the Qureg's host mirror is page-locked (pinned or registered), so that
+// syncQuregToGpu / syncQuregFromGpu copy at the host link's rate; 0 if it is pageable
+int isQuregHostMirrorPinned(Qureg qureg) {
+    if (!checkQureg(qureg, "isQuregHostMirrorPinned")) return 0;
+    std::lock_guard<std::mutex> lock(g_mirrorMu);
+    auto it = g_mirrorKind.find(qureg.cpuAmps);
+    return it != g_mirrorKind.end() && it->second != MIRROR_PAGEABLE ? 1 : 0;
 }
 
 void syncQuregToGpu(Qureg q) {
@@ -786,6 +837,64 @@ int applyQubitMeasurementAndGetProb(Qureg q, int t, qreal* probability) {
 }
 int applyQubitMeasurement(Qureg q, int t) { qreal p = 0; return applyQubitMeasurementAndGetProb(q, t, &p); }
 
+// applyMultiQubitMeasurementAndGetProb: operations.cpp:1858-1891.  Every outcome's
+// probability (one deterministic histogram pass), a Kahan-summed normalisation check
+// (util_getSum, utilities.cpp:346-360), one uniform sample walked along the cumulative
+// probabilities (rand_getRandomMultiQubitOutcome, randomiser.cpp:140-166), then the
+// projector onto the outcome's bits (bit i of the outcome for qubits[i]).
+qindex applyMultiQubitMeasurementAndGetProb(Qureg q, int* qs, int n, qreal* probability) {
+    const char* func = "applyMultiQubitMeasurementAndGetProb";
+    if (!checkQureg(q, func) || !checkQubits(q, qs, n, func, "target qubits")) return -1;
+    if (!check(n >= 1 && n <= 20, func, "This build measures at most 20 qubits at once.")) return -1;
+    vector<double> probs((size_t)1 << n);
+    calcProbsOfAllMultiQubitOutcomes(probs.data(), q, qs, n);
+    double total = 0, comp = 0;
+    for (double x : probs) { double y = x - comp, t = total + y; comp = (t - total) - y; total = t; }
+    if (!check(std::abs(total - 1) <= g_eps, func, "The outcome probabilities do not sum to one; the state is not normalised.")) return -1;
+    std::uniform_real_distribution<double> distrib(0, 1);
+    double sample = distrib(g_rng), cum = 0;
+    qindex outcome = (qindex)probs.size();
+    for (size_t i = 0; i < probs.size(); i++) {
+        cum += probs[i];
+        if (sample < cum) { outcome = (qindex)i; break; }
+    }
+    if (outcome == (qindex)probs.size()) {
+        if (!check(1 - cum <= g_eps, func, "The outcome probabilities are not normalised.")) return -1;
+        outcome = (qindex)probs.size() - 1;
+    }
+    vector<int> qv(qs, qs + n), ov(n);
+    for (int i = 0; i < n; i++) ov[i] = (int)((outcome >> i) & 1);
+    if (probability) *probability = probs[(size_t)outcome];
+    project(q, qv, ov, probs[(size_t)outcome], func);
+    return outcome;
+}
+qindex applyMultiQubitMeasurement(Qureg q, int* qs, int n) { qreal p = 0; return applyMultiQubitMeasurementAndGetProb(q, qs, n, &p); }
+
+// applyForcedMultiQubitMeasurement: operations.cpp:1893-1912 (the outcome's probability must
+// be at least epsilon; the state is projected and renormalised by it)
+qreal applyForcedMultiQubitMeasurement(Qureg q, int* qs, int* os, int n) {
+    const char* func = "applyForcedMultiQubitMeasurement";
+    if (!checkQureg(q, func) || !checkQubits(q, qs, n, func, "target qubits")) return 0;
+    for (int i = 0; i < n; i++)
+        if (!check(os[i] == 0 || os[i] == 1, func, "Invalid measurement outcome; must be 0 or 1.")) return 0;
+    double p = 0;
+    if (!probOf(q, V(qs, n), V(os, n), &p, func)) return 0;
+    if (!check(p >= g_eps, func, "The forced measurement outcome is impossibly unlikely.")) return 0;
+    project(q, V(qs, n), V(os, n), p, func);
+    return p;
+}
+// applyForcedQubitMeasurement: operations.cpp:1829-1846
+qreal applyForcedQubitMeasurement(Qureg q, int t, int o) {
+    const char* func = "applyForcedQubitMeasurement";
+    if (!checkQureg(q, func) || !checkQubits(q, &t, 1, func, "target qubits")) return 0;
+    if (!check(o == 0 || o == 1, func, "Invalid measurement outcome; must be 0 or 1.")) return 0;
+    double p = 0;
+    if (!probOf(q, {t}, {o}, &p, func)) return 0;
+    if (!check(p >= g_eps, func, "The forced measurement outcome is impossibly unlikely.")) return 0;
+    project(q, {t}, {o}, p, func);
+    return p;
+}
+
 // ====================================================================== decoherence (decoherence.cpp:31-131)
 
 void mixDephasing(Qureg q, int qubit, qreal prob) {
@@ -1067,16 +1176,10 @@ qreal calcProbOfQubitOutcome(Qureg q, int qubit, int outcome) { return calcProbO
 void calcProbsOfAllMultiQubitOutcomes(qreal* out, Qureg q, int* qs, int n) {
     const char* func = "calcProbsOfAllMultiQubitOutcomes";
     if (!checkQureg(q, func) || !checkQubits(q, qs, n, func, "target qubits")) return;
-    if (!q.isDensityMatrix) {
+    if (q.isDensityMatrix)
+        backend(qg_dm_calcProbsOfAllMultiQubitOutcomes(out, q.gpuAmps, q.numQubits, qs, n, g_stream), func);
+    else
         backend(qg_sv_calcProbsOfAllMultiQubitOutcomes(out, q.gpuAmps, q.numQubits, qs, n, g_stream), func);
-        return;
-    }
-    // density matrix: one diagonal reduction per outcome
-    vector<int> qv(qs, qs + n), ov(n);
-    for (qindex b = 0; b < ((qindex)1 << n); b++) {
-        for (int i = 0; i < n; i++) ov[i] = (int)((b >> i) & 1);
-        if (!probOf(q, qv, ov, &out[b], func)) return;
-    }
 }
 
 // calcExpecPauliStr: calculations.cpp:133-144 and localiser.cpp:1963-2049
@@ -1095,32 +1198,114 @@ qreal calcExpecPauliStr(Qureg q, PauliStr str) {
     return v.re;
 }
 
-void calcExpecPauliStrs(qreal* out, Qureg q, const PauliStr* strs, int num) {
-    const char* func = "calcExpecPauliStrs";
-    if (!checkQureg(q, func)) return;
-    vector<int64_t> mxy(num), myz(num);
-    vector<int> ny(num);
-    for (int s = 0; s < num; s++) {
-        if (!check(strFits(strs[s], q.numQubits), func, "A Pauli string targets a qubit beyond the Qureg.")) return;
+}  // extern "C"
+
+namespace {
+
+// The complex value of every string (the term before its real part is taken), through the
+// batched kernels: many strings per pass over the amplitudes (statevector) or the columns
+// (density matrix).  The reference evaluates one pass per string
+// (localiser_statevec_calcExpecPauliStrSum, localiser.cpp:2052-2148; its density-matrix
+// form, :2151-2171); the values are the same terms.
+bool pauliValues(const Qureg& q, const PauliStr* strs, qindex num, vector<cd>& vals, const char* func) {
+    vector<int64_t> mxy((size_t)num), myz((size_t)num);
+    vector<int> ny((size_t)num);
+    for (qindex s = 0; s < num; s++) {
+        if (!check(strFits(strs[s], q.numQubits), func, "A Pauli string targets a qubit beyond the Qureg.")) return false;
         vector<int> codes = codesOf(strs[s], q.numQubits);
         int64_t a = 0, b = 0;
         for (int i = 0; i < q.numQubits; i++) {
             if (codes[i] == 1 || codes[i] == 2) a |= (int64_t)1 << i;
             if (codes[i] == 2 || codes[i] == 3) b |= (int64_t)1 << i;
         }
-        mxy[s] = a;
-        myz[s] = b;
-        ny[s] = numY(codes);
+        mxy[(size_t)s] = a;
+        myz[(size_t)s] = b;
+        ny[(size_t)s] = numY(codes);
     }
-    vector<qcomp_t> v(num);
-    int rc = q.isDensityMatrix
-                 ? qg_dm_calcExpecPauliStrBatch(q.gpuAmps, q.numQubits, mxy.data(), myz.data(), ny.data(), num, v.data(), g_stream)
-                 : qg_sv_calcExpecPauliStrBatch(q.gpuAmps, q.numQubits, mxy.data(), myz.data(), ny.data(), num, v.data(), g_stream);
-    if (!backend(rc, func)) return;
+    vector<qcomp_t> v((size_t)num);
+    const int CHUNK = 1 << 20;
+    for (qindex s0 = 0; s0 < num; s0 += CHUNK) {
+        int cnt = (int)std::min<qindex>(CHUNK, num - s0);
+        int rc = q.isDensityMatrix
+                     ? qg_dm_calcExpecPauliStrBatch(q.gpuAmps, q.numQubits, mxy.data() + s0, myz.data() + s0, ny.data() + s0, cnt, v.data() + s0, g_stream)
+                     : qg_sv_calcExpecPauliStrBatch(q.gpuAmps, q.numQubits, mxy.data() + s0, myz.data() + s0, ny.data() + s0, cnt, v.data() + s0, g_stream);
+        if (!backend(rc, func)) return false;
+    }
+    vals.resize((size_t)num);
+    for (qindex s = 0; s < num; s++) vals[(size_t)s] = C(v[(size_t)s]);
+    return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+void calcExpecPauliStrs(qreal* out, Qureg q, const PauliStr* strs, int num) {
+    const char* func = "calcExpecPauliStrs";
+    if (!checkQureg(q, func)) return;
+    if (!check(num >= 0 && (num == 0 || (strs && out)), func, "Invalid list of Pauli strings.")) return;
+    vector<cd> v;
+    if (!pauliValues(q, strs, num, v, func)) return;
     for (int s = 0; s < num; s++) {
-        if (!check(std::abs(v[s].im) <= REDUCTION_EPS_FACTOR * g_eps, func, "The expectation value was not approximately real.")) return;
-        out[s] = v[s].re;
+        if (!check(std::abs(v[s].imag()) <= REDUCTION_EPS_FACTOR * g_eps, func, "The expectation value was not approximately real.")) return;
+        out[s] = v[s].real();
     }
+}
+
+// createPauliStrSum: paulis.cpp:396-417 (the strings need not be unique)
+PauliStrSum createPauliStrSum(PauliStr* strings, qcomp_t* coeffs, qindex numTerms) {
+    const char* func = "createPauliStrSum";
+    PauliStrSum sum;
+    std::memset(&sum, 0, sizeof(sum));
+    if (!check(numTerms > 0, func, "The number of terms must be a positive integer.")) return sum;
+    if (!check(strings != nullptr && coeffs != nullptr, func, "Null list of Pauli strings or coefficients.")) return sum;
+    sum.numTerms = numTerms;
+    sum.strings = (PauliStr*)std::malloc(sizeof(PauliStr) * (size_t)numTerms);
+    sum.coeffs = (qcomp_t*)std::malloc(sizeof(qcomp_t) * (size_t)numTerms);
+    sum.isApproxHermitian = (int*)std::malloc(sizeof(int));
+    if (!sum.strings || !sum.coeffs || !sum.isApproxHermitian) {
+        std::free(sum.strings);
+        std::free(sum.coeffs);
+        std::free(sum.isApproxHermitian);
+        std::memset(&sum, 0, sizeof(sum));
+        fail(func, "Could not allocate the memory of the Pauli string sum.");
+        return sum;
+    }
+    std::memcpy(sum.strings, strings, sizeof(PauliStr) * (size_t)numTerms);
+    std::memcpy(sum.coeffs, coeffs, sizeof(qcomp_t) * (size_t)numTerms);
+    *sum.isApproxHermitian = -1;
+    return sum;
+}
+
+void destroyPauliStrSum(PauliStrSum sum) {
+    std::free(sum.strings);
+    std::free(sum.coeffs);
+    std::free(sum.isApproxHermitian);
+}
+
+// calcExpecPauliStrSum: calculations.cpp:146-159.  Validation as validate_pauliStrSumFields,
+// _pauliStrSumTargets and _pauliStrSumIsHermitian (validation.cpp:3255-3293: every coefficient
+// real within epsilon, the flag cached in the sum); the value is sum_t coeff_t * <P_t> added
+// in term order, and must be real within the reduction epsilon.
+qreal calcExpecPauliStrSum(Qureg q, PauliStrSum sum) {
+    const char* func = "calcExpecPauliStrSum";
+    if (!checkQureg(q, func)) return 0;
+    if (!check(sum.numTerms > 0 && sum.strings && sum.coeffs && sum.isApproxHermitian, func,
+               "Invalid PauliStrSum; it was not created, or was destroyed.")) return 0;
+    for (qindex t = 0; t < sum.numTerms; t++)
+        if (!check(strFits(sum.strings[t], q.numQubits), func, "The PauliStrSum targets a qubit beyond the Qureg.")) return 0;
+    if (*sum.isApproxHermitian == -1) {
+        int herm = 1;
+        for (qindex t = 0; t < sum.numTerms && herm; t++) herm = std::abs(sum.coeffs[t].im) <= g_eps;
+        *sum.isApproxHermitian = herm;
+    }
+    if (!check(*sum.isApproxHermitian == 1, func, "The PauliStrSum is not Hermitian (a coefficient is not real).")) return 0;
+    vector<cd> v;
+    if (!pauliValues(q, sum.strings, sum.numTerms, v, func)) return 0;
+    cd total = 0;
+    for (qindex t = 0; t < sum.numTerms; t++) total += C(sum.coeffs[t]) * v[(size_t)t];
+    if (!check(std::abs(total.imag()) <= REDUCTION_EPS_FACTOR * g_eps, func, "The expectation value was not approximately real.")) return 0;
+    return total.real();
 }
 
 }  // extern "C"

@@ -206,11 +206,7 @@ void gpu_statevec_calcProbsOfAllMultiQubitOutcomes_sub(qreal* out, Qureg q, vect
 }
 template <int NumQubits>
 void gpu_densmatr_calcProbsOfAllMultiQubitOutcomes_sub(qreal* out, Qureg q, vector<int> qs) {
-    vector<int> os(qs.size());
-    for (qindex b = 0; b < ((qindex)1 << qs.size()); b++) {
-        for (size_t i = 0; i < qs.size(); i++) os[i] = (int)((b >> i) & 1);
-        ok(qg_dm_calcProbOfMultiQubitOutcome(q.gpuAmps, q.numQubits, P(qs), P(os), (int)qs.size(), &out[b], nullptr), __func__);
-    }
+    ok(qg_dm_calcProbsOfAllMultiQubitOutcomes(out, q.gpuAmps, q.numQubits, P(qs), (int)qs.size(), nullptr), __func__);
 }
 INSTANTIATE_FUNC_OPTIMISED_FOR_NUM_TARGS(qreal, gpu_statevec_calcProbOfMultiQubitOutcome_sub, (Qureg, vector<int>, vector<int>))
 INSTANTIATE_FUNC_OPTIMISED_FOR_NUM_TARGS(qreal, gpu_densmatr_calcProbOfMultiQubitOutcome_sub, (Qureg, vector<int>, vector<int>))

@@ -31,6 +31,8 @@ CASES = [
     ("dm6_config3", 6, 1, "config3", 41),
     ("sv5_fullstate_diag", 5, 0, "fsd", 51),
     ("dm3_fullstate_diag", 3, 1, "fsd", 52),
+    ("sv7_measure_sum", 7, 0, "measure", 61),
+    ("dm4_measure_sum", 4, 1, "measure", 62),
 ]
 
 
@@ -86,6 +88,8 @@ def make_case(name, nq, is_dm, kind, seed):
         text = qc.config1_circuit(nq, 3, seed)
     elif kind == "fsd":
         text = qc.fullstate_diag_circuit(nq, is_dm, seed)
+    elif kind == "measure":
+        text = qc.measure_sum_circuit(nq, is_dm, seed)
     else:
         text = config3_circuit(nq, 3, seed)
     amps = qc.random_density_matrix(nq, seed) if is_dm else qc.random_statevector(nq, seed)

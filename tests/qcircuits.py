@@ -208,15 +208,55 @@ def every_op_circuit(nq, is_dm, seed, with_measure=True):
         L.append(f"EXPEC {pauli_text([int(v) for v in rng.integers(0, 4, size=nq)])}")
     L.append(f"EXPEC {pauli_text([int(v) * 3 for v in rng.integers(0, 2, size=nq)])}")
     L.append(f"EXPEC {'I' * nq}")
+    t = distinct(min(3, nq)); L.append(f"PROBALL {len(t)} {' '.join(map(str, t))}")
+    L.append(expsum_line(nq, 5, rng))
     if with_measure:
         L.append(f"SEED {int(rng.integers(1 << 31))} {int(rng.integers(1 << 31))}")
-        m = distinct(3)
+        m = distinct(min(nq, 4))
         L.append(f"MEAS {m[0]}")
         L.append(f"MEAS {m[1]}")
         L.append("TOTALPROB")
+        if nq >= 4:
+            L.append(f"FMEAS {m[3]} {int(rng.integers(2))}")
+            L.append(f"MEASM 2 {m[0]} {m[2]}")
+            L.append("TOTALPROB")
         # a projector on a qubit not measured keeps part of the state (unnormalised)
         L.append(f"PROJ 1 {m[2]} {int(rng.integers(2))}")
         L.append("TOTALPROB")
+    return "\n".join(L) + "\n"
+
+
+def expsum_line(nq, num_terms, rng):
+    """calcExpecPauliStrSum over `num_terms` random strings with real Gaussian coefficients."""
+    terms = " ".join(f"{fmt(rng.standard_normal())} 0.0 {pauli_text([int(v) for v in rng.integers(0, 4, size=nq)])}"
+                     for _ in range(num_terms))
+    return f"EXPSUM {num_terms} {terms}"
+
+
+def measure_sum_circuit(nq, is_dm, seed):
+    """Outcome histograms, Pauli-string sums and the multi-qubit and forced measurements,
+    on a register prepared by a few gates (nq >= 4)."""
+    rng = np.random.default_rng(seed)
+    L = [f"H {t}" for t in range(nq)]
+    for t in range(nq):
+        L.append(f"U1 {t} {mat_tokens(haar_unitary(2, rng))}")
+    L.append(f"U2 0 {nq - 1} {mat_tokens(haar_unitary(4, rng))}")
+    if is_dm:
+        L.append(f"DEPOL 1 {fmt(0.05)}")
+    L.append("PROBALL 1 0")
+    L.append(f"PROBALL 3 {nq - 1} 0 2")
+    L.append(f"PROBALL {nq} {' '.join(str(q) for q in range(nq))}")
+    L.append(expsum_line(nq, 7, rng))
+    L.append(f"EXPSUM 2 1.5 0.0 {'I' * nq} -0.5 0.0 {'Z' * nq}")
+    L.append(f"SEED {int(rng.integers(1 << 31))}")
+    L.append(f"MEASM 3 2 0 {nq - 1}")
+    L.append("TOTALPROB")
+    L.append(f"FMEAS 1 {int(rng.integers(2))}")
+    L.append(f"FMEASM 1 3 {int(rng.integers(2))}")
+    L.append("TOTALPROB")
+    L.append(f"MEASM 1 1")
+    L.append(f"MEASM {nq} {' '.join(str(q) for q in reversed(range(nq)))}")
+    L.append("TOTALPROB")
     return "\n".join(L) + "\n"
 
 

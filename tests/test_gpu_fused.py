@@ -256,3 +256,78 @@ def test_tensor_core_wait_runs_out_cleanly(env, targs):
     assert np.max(np.abs(tc - ref)) <= 2e-6 * np.max(np.abs(ref))
     lib.qg_tc_get_error_flag(ctypes.byref(cleared))
     assert cleared.value == 0
+
+
+def test_timed_out_launch_is_reported_by_the_next_apply(env):
+    # Kernel choice 3 makes every 5-qubit tensor-core launch give up its bounded waits
+    # (about 2 s) and leave the register untouched.  The apply itself returns at once
+    # (asynchronous); the device's flag is set once the launch ends, and the next apply
+    # reports the timeout with QG_ERR_TIMEOUT and clears the flag before launching
+    # anything.  The apply after that runs normally and matches the oracle.
+    from quest_gb300 import _lib
+    from quest_gb300.fused import Circuit, StateVector32
+    lib = _lib.lib()
+    n = 13
+    u = qc.haar_unitary(32, np.random.default_rng(8))
+    amps = qc.random_statevector(n, 9)
+    c = Circuit(n)
+    c.add([1, 3, 5, 7, 9], u)
+    c.fuse(5)
+    s = StateVector32(n)
+    try:
+        s.set(amps)
+        _lib.check(lib.qg_sv32_apply_circuit(c.h, s.ptr, n, 3, None))
+        _lib.check(lib.qg_sync())
+        flag = ctypes.c_int(0)
+        _lib.check(lib.qg_tc_get_error_flag(ctypes.byref(flag)))
+        assert flag.value == 1
+        assert np.array_equal(s.get(), amps.astype(np.complex64))       # nothing was stored
+        assert lib.qg_sv32_apply_circuit(c.h, s.ptr, n, 2, None) == -4     # QG_ERR_TIMEOUT
+        _lib.check(lib.qg_tc_get_error_flag(ctypes.byref(flag)))
+        assert flag.value == 0
+        _lib.check(lib.qg_sv32_apply_circuit(c.h, s.ptr, n, 2, None))
+        got = s.get().astype(np.complex128)
+    finally:
+        s.free()
+    ref = run_oracle(n, amps, [([1, 3, 5, 7, 9], u)])
+    assert np.max(np.abs(got - ref)) <= 2e-6 * np.max(np.abs(ref))
+
+
+def test_server_fails_only_the_request_that_timed_out(env):
+    # A server whose large registers run with kernel choice 3: each large request's
+    # tensor-core launch gives up and that request alone is failed with QG_ERR_TIMEOUT;
+    # small requests (shared memory, no tensor cores) in the same server finish normally,
+    # and the device's own flag is left clear.
+    from quest_gb300 import _lib, serve
+    lib = _lib.lib()
+    rng = np.random.default_rng(12)
+    from quest_gb300.fused import Circuit
+    big = Circuit(13).add([0, 2, 4, 6, 8], qc.haar_unitary(32, rng)).fuse(5)      # one tensor-core block
+    small = serve.circuit_of(8, serve.hea_request(8, 6, rng)[0])
+    codes = [[1] * 13, [3] * 13]
+    srv = serve.Server(1 << 28, 8, impl=3)
+    try:
+        rid_big = srv.submit(big, codes)
+        rid_small = srv.submit(small, [[3] * 8])
+        import time
+        t0 = time.time()
+        states = {}
+        while len(states) < 2 and time.time() - t0 < 60:
+            srv.poll()
+            for rid in (rid_big, rid_small):
+                if rid in states:
+                    continue
+                vals = (ctypes.c_double * 2)()
+                done = ctypes.c_int(0)
+                rc = lib.qg_server_result(srv.h, rid, vals, ctypes.byref(done))
+                if done.value:
+                    states[rid] = rc
+        assert states.get(rid_big) == -4
+        assert states.get(rid_small) == 0
+        srv.release(rid_big)
+        srv.release(rid_small)
+    finally:
+        srv.close()
+    flag = ctypes.c_int(1)
+    _lib.check(lib.qg_tc_get_error_flag(ctypes.byref(flag)))
+    assert flag.value == 0

@@ -290,6 +290,10 @@ def test_l2_fetch_granularity_hint(env):
         _lib.check(L.qg_get_l2_fetch_granularity(ctypes.byref(v)))
         assert v.value == 128
         assert L.qg_set_l2_fetch_granularity(48) == -2
+        # the restore puts back what the context had before initialisation changed it
+        _lib.check(L.qg_restore_l2_fetch_granularity())
+        _lib.check(L.qg_get_l2_fetch_granularity(ctypes.byref(v)))
+        assert v.value != 128
     finally:
         _lib.check(L.qg_set_l2_fetch_granularity(32))
 
