@@ -279,21 +279,22 @@ def run_gb300(args, world, rank, local, dist):
 
     timed_dense = []   # (start, stop) events around every Haar-gate kernel in the timed region
 
-    def run_step(record_dense=False):
+    def run_step(record_dense=False, reg=None):
+        r = q if reg is None else reg
         for g, m in zip(gates, mats):
             if g[0] == "U":
                 if record_dense:
                     a, b = new_event(), new_event()
                     L.qg_event_record(a, None)
-                    Q.applyCompMatr1(q, g[1], m)
+                    Q.applyCompMatr1(r, g[1], m)
                     L.qg_event_record(b, None)
                     timed_dense.append((a, b))
                 else:
-                    Q.applyCompMatr1(q, g[1], m)
+                    Q.applyCompMatr1(r, g[1], m)
             elif g[0] == "CP":
-                Q.applyTwoQubitPhaseShift(q, g[1], g[2], g[3])
+                Q.applyTwoQubitPhaseShift(r, g[1], g[2], g[3])
             else:
-                Q.applyFullQuantumFourierTransform(q)
+                Q.applyFullQuantumFourierTransform(r)
 
     for _ in range(args.warmup):
         run_step()
@@ -326,20 +327,89 @@ def run_gb300(args, world, rank, local, dist):
         L.qg_event_destroy(b)
     clk = clocks.summary()
 
-    # ---- end to end through the API with host buffers: H2D input, circuit, D2H result
+    # ---- end to end through the API with host buffers, double-buffered.  Step i runs its
+    # gates on register regs[i % 2] (compute stream) while the copy stream reads step
+    # i-1's result out of the other register and then writes step i+1's input into it.
+    # Every step's input (16 GiB, from q's pinned host mirror) and result (16 GiB, into
+    # q2's pinned host mirror) cross the host link inside the timed region; events on the
+    # two streams order each copy against the gates of its register.
+    q2 = Q.createQureg(nq)
+    regs = [q, q2]
+    namps = 1 << nq
+    in_ptr = C.cast(q.cpuAmps, C.c_void_p)
+    out_ptr = C.cast(q2.cpuAmps, C.c_void_p)
+    mirrors = ["pinned" if Q.isQuregHostMirrorPinned(r) else "pageable" for r in regs]
+    sc, sx = C.c_void_p(), C.c_void_p()
+    _lib.check(L.qg_stream_create(C.byref(sc)))
+    _lib.check(L.qg_stream_create(C.byref(sx)))
+    # the host link alone: one 16 GiB copy each way on the copy stream
+    a, b = new_event(), new_event()
+    Q.setQuESTStream(sx)
+    L.qg_event_record(a, sx)
+    Q.setQuregAmps(q2, 0, in_ptr, namps)
+    L.qg_event_record(b, sx)
+    h2d_ms = C.c_float(0)
+    L.qg_event_elapsed_ms(a, b, C.byref(h2d_ms))
+    L.qg_event_record(a, sx)
+    Q.getQuregAmps(out_ptr, q2, 0, namps)
+    L.qg_event_record(b, sx)
+    d2h_ms = C.c_float(0)
+    L.qg_event_elapsed_ms(a, b, C.byref(d2h_ms))
+    Q.setQuESTStream(None)
     e2e_steps = max(1, args.steps)
+    ev_up = [new_event() for _ in range(e2e_steps)]
+    ev_done = [new_event() for _ in range(e2e_steps)]
     barrier(dist)
     L.qg_sync()
     t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        Q.syncQuregToGpu(q)      # pinned host mirror -> HBM (16 GiB): this step's input
-        run_step()
-        Q.syncQuregFromGpu(q)    # HBM -> pinned host mirror (16 GiB): the step's result
+    Q.setQuESTStream(sx)
+    Q.setQuregAmps(regs[0], 0, in_ptr, namps)           # step 0's input
+    L.qg_event_record(ev_up[0], sx)
+    for i in range(e2e_steps):
+        L.qg_stream_wait_event(sc, ev_up[i])
+        Q.setQuESTStream(sc)
+        run_step(reg=regs[i % 2])
+        L.qg_event_record(ev_done[i], sc)
+        Q.setQuESTStream(sx)
+        if i >= 1:
+            L.qg_stream_wait_event(sx, ev_done[i - 1])
+            Q.getQuregAmps(out_ptr, regs[(i - 1) % 2], 0, namps)     # step i-1's result
+        if i + 1 < e2e_steps:
+            Q.setQuregAmps(regs[(i + 1) % 2], 0, in_ptr, namps)      # step i+1's input
+            L.qg_event_record(ev_up[i + 1], sx)
+    L.qg_stream_wait_event(sx, ev_done[e2e_steps - 1])
+    Q.getQuregAmps(out_ptr, regs[(e2e_steps - 1) % 2], 0, namps)     # the last step's result
     L.qg_sync()
     t_e2e = max_over_ranks(dist, time.perf_counter() - t0)
+    Q.setQuESTStream(None)
     barrier(dist)
+    for e in ev_up + ev_done + [a, b]:
+        L.qg_event_destroy(e)
+    L.qg_stream_destroy(sc)
+    L.qg_stream_destroy(sx)
 
+    # ---- both product modes on one step from the same input: final total probabilities,
+    # and the IEEE-FP64 dense kernel's launch time beside the fixed-point one
+    modes = {}
+    for mode_name, mode_val, reg in (("fixed", 0, q), ("fp64", 1, q2)):
+        _lib.check(L.qg_set_fp64_products(mode_val))
+        Q.setQuregAmps(reg, 0, in_ptr, namps)
+        timed_dense.clear()
+        run_step(record_dense=True, reg=reg)
+        L.qg_sync()
+        ms_list = []
+        for x, y in timed_dense:
+            v = C.c_float(0)
+            L.qg_event_elapsed_ms(x, y, C.byref(v))
+            ms_list.append(v.value)
+            L.qg_event_destroy(x)
+            L.qg_event_destroy(y)
+        timed_dense.clear()
+        modes[mode_name] = {"final_total_prob": Q.calcTotalProb(reg),
+                            "dense_kernel_ms": round(statistics.mean(ms_list), 4)}
+    _lib.check(L.qg_set_fp64_products(0 if args.fp64_products == "fixed" else 1))
     norm = Q.calcTotalProb(q)
+    Q.destroyQureg(q2)
     Q.destroyQureg(q)
 
     value = world * args.steps * step_bytes / t_dev / 1e9
@@ -397,15 +467,53 @@ def run_gb300(args, world, rank, local, dist):
                    "gates_per_step": step_gates, "algorithmic_bytes_per_step": step_bytes,
                    "l2": "state (16 GiB) larger than L2; no flush", "parallelism": f"replicas x{world}",
                    "fp64_products": args.fp64_products, "autotune": tuning},
-        "e2e": {"value": round(e2e_value, 2), "unit": "GB/s", "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
+        "e2e": {"value": round(e2e_value, 2), "unit": "GB/s", "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+                "steps": e2e_steps, "ms_per_step": round(t_e2e / e2e_steps * 1e3, 3),
+                "frac_of_value": round(e2e_value / value, 4),
+                "schedule": "double-buffered: two registers, gates on one stream, host copies on another",
+                "host_mirror": mirrors[0] if mirrors[0] == mirrors[1] else ",".join(mirrors),
+                "h2d_gbs": round(nbytes / (h2d_ms.value / 1e3) / 1e9, 1),
+                "d2h_gbs": round(nbytes / (d2h_ms.value / 1e3) / 1e9, 1)},
+        "product_modes": {**modes, "note": "one step of the circuit from the same input in each mode; "
+                                            "dense_kernel_ms = mean CUDA-event time of the Haar-gate launches"},
         "gpu_launches": int(launches1.value - launches0.value),
         "roofline": roofline,
         "cpu_baseline": cpu,
         "clocks": clk,
         "final_total_prob": norm,
     }
+    if world == 1 and not args.no_extras:
+        line["precision_form"], line["serving"] = extras_summary(args, world, rank, local, dist)
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def extras_summary(args, world, rank, local, dist):
+    """The precision form (32-qubit FP32 fused blocks on the tensor cores, accuracy at 28
+    qubits) and the serving form (a short request set, served vs plain) in small, so the
+    default line records them beside the FP64 circuit.  A failure here is reported in
+    the line and does not lose the headline."""
+    precision = serving = None
+    try:
+        pa = argparse.Namespace(**vars(args))
+        pa.qubits, pa.acc_qubits, pa.depth, pa.steps, pa.warmup, pa.fused_impl = 32, 28, 40, 2, 1, "tc"
+        pl = run_precision(pa, world, rank, local, dist, emit=False)
+        precision = {"workload": pl["config"]["workload"], "blocks": pl["config"]["blocks"], "steps": pa.steps,
+                     "value_gbs": pl["value"], "frac_of_hbm": pl["roofline"]["frac"],
+                     "ms_per_block_pass": pl["ms_per_block_pass"], "tensor_tflops": pl["roofline"]["tensor_tflops"],
+                     "accuracy": pl["accuracy"], "tc_error_flag": pl["tc_error_flag"]}
+    except Exception as e:          # noqa: BLE001 -- recorded in the line
+        precision = {"error": f"{type(e).__name__}: {e}"}
+    try:
+        sa = argparse.Namespace(**vars(args))
+        sa.requests, sa.min_qubits, sa.max_qubits, sa.load = 12, 8, 26, 0.8
+        sl = run_serve(sa, world, rank, local, dist, emit=False)
+        serving = {"requests": sa.requests, "data": sl["data"], "saturation": sl["saturation"],
+                   "poisson": sl["poisson"], "max_abs_expec_err_served_vs_fp64": sl["max_abs_expec_err_served_vs_fp64"],
+                   "plain_registers": sl["plain_registers"]}
+    except Exception as e:          # noqa: BLE001
+        serving = {"error": f"{type(e).__name__}: {e}"}
+    return precision, serving
 
 
 # ------------------------------------------------------------------ reference arm
@@ -497,7 +605,7 @@ def precision_accuracy(na, depth, impl):
     return fid, maxabs, experr, norm_drift
 
 
-def run_precision(args, world, rank, local, dist):
+def run_precision(args, world, rank, local, dist, emit=True):
     """FP32 statevector, brickwork circuit fused into 5-qubit blocks applied as 3xTF32
     tensor-core GEMM tiles, then an FP64-summed renormalisation (the circuit is unitary).
     Accuracy against the FP64 per-gate path (which is pinned to the FP64 oracle) at
@@ -580,8 +688,9 @@ def run_precision(args, world, rank, local, dist):
             "accuracy": accuracy,
             "gpu_launches": int(launches1.value - launches0.value), "tc_error_flag": flag.value,
             "final_total_prob": norm, "clocks": clocks.summary()}
-    if rank == 0:
+    if rank == 0 and emit:
         print(json.dumps(line), flush=True)
+    return line
 
 
 # ------------------------------------------------------------------ serving form
@@ -589,7 +698,7 @@ def run_precision(args, world, rank, local, dist):
 def log(msg):
     print(f"[bench {time.strftime('%H:%M:%S')}] {msg}", file=sys.stderr, flush=True)
 
-def run_serve(args, world, rank, local, dist):
+def run_serve(args, world, rank, local, dist, emit=True):
     """Poisson stream of hardware-efficient-ansatz requests (8-26 qubits, depth 10-100,
     16 Pauli expectations each).  Served: FP32 fused blocks through the continuous-
     batching server (circuits fused on a host thread pool as they arrive).  Plain:
@@ -611,8 +720,16 @@ def run_serve(args, world, rank, local, dist):
         reqs.append((n, depth, ops, codes))
     ngates = sum(len(r[2]) for r in reqs)
 
+    # one register per qubit count, made before any timing: the plain arm then times gate
+    # work and reductions, not allocation (the served arm carves its registers out of a
+    # pre-allocated arena the same way)
+    plain_regs = {}
+    for n in sorted({r[0] for r in reqs} | {10}):
+        plain_regs[n] = Q.createQureg(n)
+
     def plain_one(n, ops, codes):
-        q = Q.createQureg(n)
+        q = plain_regs[n]
+        Q.initZeroState(q)
         for op in ops:
             if op[0] == "RY":
                 Q.applyRotateY(q, op[1], op[2])
@@ -623,7 +740,6 @@ def run_serve(args, world, rank, local, dist):
         strs = (api.PauliStr * len(codes))(*[api.pauli_str(c) for c in codes])
         vals = (C.c_double * len(codes))()
         Q.calcExpecPauliStrs(vals, q, strs, len(codes))
-        Q.destroyQureg(q)
         return np.array(list(vals))
 
     def run_plain(arrivals):
@@ -717,9 +833,13 @@ def run_serve(args, world, rank, local, dist):
             "poisson": {"rate_per_s": round(lam, 3), "load_vs_plain_capacity": args.load,
                         "served_p50_ms": round(pct(lat_s, 50), 2), "served_p99_ms": round(pct(lat_s, 99), 2),
                         "plain_p50_ms": round(pct(lat_p, 50), 2), "plain_p99_ms": round(pct(lat_p, 99), 2)},
-            "max_abs_expec_err_served_vs_fp64": err}
-    if rank == 0:
+            "max_abs_expec_err_served_vs_fp64": err,
+            "plain_registers": "one pre-created register per qubit count, reset to |0> per request"}
+    for r in plain_regs.values():
+        Q.destroyQureg(r)
+    if rank == 0 and emit:
         print(json.dumps(line), flush=True)
+    return line
 
 
 def run_gates(args, world, rank, local, dist):
@@ -781,7 +901,7 @@ def run_gates(args, world, rank, local, dist):
 
     # density-matrix channels on an N-qubit density matrix (its 2N-qubit Choi vector has
     # the same bytes as the statevector above); every channel below streams the whole
-    # Choi vector once, a one-qubit unitary twice (ket and bra)
+    # Choi vector once
     from quest_gb300.api import Q, comp_matr1, kraus_map
     nd = n // 2
     dm = Q.createDensityQureg(nd)
@@ -791,7 +911,7 @@ def run_gates(args, world, rank, local, dist):
     k1 = kraus_map([np.sqrt(0.7) * np.eye(2), np.sqrt(0.3) * haar(2, rng)])
     iso = haar(16, rng)[:, :4]                                    # a 16x4 isometry: four 4x4 Kraus operators
     k2 = kraus_map([iso[4 * i:4 * i + 4, :] for i in range(4)])
-    dm_gates = [("applyCompMatr1 on the density matrix (2 passes)", 2, lambda: Q.applyCompMatr1(dm, 3, u1)),
+    dm_gates = [("applyCompMatr1 on the density matrix (one pass of conj(U) x U)", 1, lambda: Q.applyCompMatr1(dm, 3, u1)),
                 ("mixDepolarising", 1, lambda: Q.mixDepolarising(dm, 3, 0.01)),
                 ("mixTwoQubitDepolarising", 1, lambda: Q.mixTwoQubitDepolarising(dm, 3, 8, 0.01)),
                 ("mixDephasing (the off-diagonal half)", 0.5, lambda: Q.mixDephasing(dm, 3, 0.05)),
@@ -983,6 +1103,8 @@ def main():
                     help="plain: general complex 2x2 products in block-floating fixed point (default) or IEEE FP64")
     ap.add_argument("--acc-qubits", type=int, default=28, help="precision form: qubits of the accuracy check (0 skips it)")
     ap.add_argument("--fused-impl", default="tc", choices=["tc", "simt"])
+    ap.add_argument("--no-extras", action="store_true",
+                    help="plain: leave out the short precision-form and serving summaries of the default line")
     args = ap.parse_args()
     world, rank, local, dist = dist_setup()
     if args.config == "serve":

@@ -74,6 +74,14 @@ int qg_stream_sync(void* stream);
 int qg_get_cache_size(int64_t* out);                       /* getGpuCacheSize (quest/src/api/debug.cpp:180) */
 int qg_clear_cache(void);                                  /* gpu_clearCache (gpu_config.cpp:665) */
 int qg_get_launch_count(int64_t* out);                     /* kernels launched by this library so far */
+/* Streams and events for host harnesses (no reference counterpart; the reference runs
+ * everything on the legacy default stream): a non-blocking stream, so that work on it
+ * never waits implicitly for the legacy stream; a stream that waits for an event
+ * recorded on another, so that copies on one stream and gates on another can be
+ * overlapped and still ordered. */
+int qg_stream_create(void** out);
+int qg_stream_destroy(void* stream);
+int qg_stream_wait_event(void* stream, void* event);
 /* CUDA events on the launching stream, for timing kernels from a host harness */
 int qg_event_create(void** out);
 int qg_event_destroy(void* event);

@@ -63,6 +63,9 @@ ABI = {
     "qg_get_cache_size": [c_i64_p],
     "qg_clear_cache": [],
     "qg_get_launch_count": [c_i64_p],
+    "qg_stream_create": [ctypes.POINTER(vp)],
+    "qg_stream_destroy": [vp],
+    "qg_stream_wait_event": [vp, vp],
     "qg_event_create": [ctypes.POINTER(vp)],
     "qg_event_destroy": [vp],
     "qg_event_record": [vp, vp],

@@ -12,6 +12,7 @@
 // factors of quest/src/core/utilities.cpp:916-990.
 #include "qg_common.cuh"
 
+#include <algorithm>
 #include <cmath>
 
 namespace {
@@ -29,54 +30,63 @@ __device__ __forceinline__ double2 lin2(double c1, double2 x, double c2, double2
 
 }  // namespace
 
-// cpu_densmatr_oneQubitDepolarising_subA (cpu_subroutines.cpp:1183-1215)
-__global__ void k_depol1(double2* __restrict__ a, qidx numIts, int ket, int bra, double cAA, double cBB, double cAB) {
-    qidx n = blockIdx.x * (qidx)blockDim.x + threadIdx.x;
-    if (n >= numIts) return;
-    qidx i00 = insert_two_zeros(n, ket, bra);
-    qidx i01 = i00 | ((qidx)1 << ket), i10 = i00 | ((qidx)1 << bra), i11 = i01 | ((qidx)1 << bra);
-    double2 a00 = ld_amp(a + i00), a01 = ld_amp(a + i01), a10 = ld_amp(a + i10), a11 = ld_amp(a + i11);
-    st_amp(a + i00, lin2(cAA, a00, cBB, a11));
-    st_amp(a + i01, cscale(cAB, a01));
-    st_amp(a + i10, cscale(cAB, a10));
-    st_amp(a + i11, lin2(cAA, a11, cBB, a00));
-}
+// One-qubit channels on the 4-amplitude groups {i00, i01, i10, i11} over (ket q, bra q+N).
+// Each thread takes G groups per iteration of a grid-stride loop and issues all their
+// loads before any arithmetic, so that G x 64 B per thread are in flight.
+enum { CH_DEPOL = 0, CH_PAULI = 1, CH_DAMP = 2, CH_DEPHASE = 3 };
 
-// cpu_densmatr_oneQubitPauliChannel_subA (cpu_subroutines.cpp:1455-1496)
-__global__ void k_pauli_channel1(double2* __restrict__ a, qidx numIts, int ket, int bra, double fAA, double fBB, double fAB, double fBA) {
-    qidx n = blockIdx.x * (qidx)blockDim.x + threadIdx.x;
-    if (n >= numIts) return;
-    qidx i00 = insert_two_zeros(n, ket, bra);
-    qidx i01 = i00 | ((qidx)1 << ket), i10 = i00 | ((qidx)1 << bra), i11 = i01 | ((qidx)1 << bra);
-    double2 a00 = ld_amp(a + i00), a01 = ld_amp(a + i01), a10 = ld_amp(a + i10), a11 = ld_amp(a + i11);
-    st_amp(a + i00, lin2(fAA, a00, fBB, a11));
-    st_amp(a + i01, lin2(fAB, a01, fBA, a10));
-    st_amp(a + i10, lin2(fAB, a10, fBA, a01));
-    st_amp(a + i11, lin2(fAA, a11, fBB, a00));
-}
-
-// cpu_densmatr_oneQubitDamping_subA (cpu_subroutines.cpp:1550-1575)
-__global__ void k_damping1(double2* __restrict__ a, qidx numIts, int ket, int bra, double prob, double c1, double c2) {
-    qidx n = blockIdx.x * (qidx)blockDim.x + threadIdx.x;
-    if (n >= numIts) return;
-    qidx i00 = insert_two_zeros(n, ket, bra);
-    qidx i01 = i00 | ((qidx)1 << ket), i10 = i00 | ((qidx)1 << bra), i11 = i01 | ((qidx)1 << bra);
-    double2 a00 = ld_amp(a + i00), a01 = ld_amp(a + i01), a10 = ld_amp(a + i10), a11 = ld_amp(a + i11);
-    st_amp(a + i00, make_double2(fma(prob, a11.x, a00.x), fma(prob, a11.y, a00.y)));
-    st_amp(a + i01, cscale(c1, a01));
-    st_amp(a + i10, cscale(c1, a10));
-    st_amp(a + i11, cscale(c2, a11));
-}
-
-// cpu_densmatr_oneQubitDephasing_subA (cpu_subroutines.cpp:1072-1105): only the two
-// off-diagonal amplitudes of each group change.
-__global__ void k_dephase1(double2* __restrict__ a, qidx numIts, int ket, int bra, double fac) {
-    qidx n = blockIdx.x * (qidx)blockDim.x + threadIdx.x;
-    if (n >= numIts) return;
-    qidx i00 = insert_two_zeros(n, ket, bra);
-    qidx i01 = i00 | ((qidx)1 << ket), i10 = i00 | ((qidx)1 << bra);
-    st_amp(a + i01, cscale(fac, ld_amp(a + i01)));
-    st_amp(a + i10, cscale(fac, ld_amp(a + i10)));
+template <int KIND, int G>
+__global__ void __launch_bounds__(QG_THREADS) k_dm_channel1(double2* __restrict__ a, qidx numIts, int ket, int bra,
+                                                            double f0, double f1, double f2, double f3) {
+    const qidx bk = (qidx)1 << ket, bb = (qidx)1 << bra;
+    const qidx stride = (qidx)gridDim.x * QG_THREADS * G;
+    for (qidx n0 = blockIdx.x * (qidx)QG_THREADS * G + threadIdx.x; n0 < numIts; n0 += stride) {
+        qidx i00[G];
+        double2 x00[G], x01[G], x10[G], x11[G];
+#pragma unroll
+        for (int g = 0; g < G; g++) {
+            qidx n = n0 + (qidx)g * QG_THREADS;
+            i00[g] = insert_two_zeros(n < numIts ? n : n0, ket, bra);
+            if (KIND != CH_DEPHASE) {
+                x00[g] = ld_amp(a + i00[g]);
+                x11[g] = ld_amp(a + (i00[g] | bk | bb));
+            }
+            x01[g] = ld_amp(a + (i00[g] | bk));
+            x10[g] = ld_amp(a + (i00[g] | bb));
+        }
+#pragma unroll
+        for (int g = 0; g < G; g++) {
+            if (n0 + (qidx)g * QG_THREADS >= numIts) break;
+            const qidx i = i00[g];
+            if (KIND == CH_DEPOL) {
+                // cpu_densmatr_oneQubitDepolarising_subA (cpu_subroutines.cpp:1183-1215):
+                // a00' = cAA a00 + cBB a11 with cAA = 1 - cBB, written a00 + cBB (a11 - a00)
+                // (3 FP64 operations per real pair instead of 4); off-diagonals times cAB
+                double2 d = make_double2(x11[g].x - x00[g].x, x11[g].y - x00[g].y);
+                st_amp(a + i, make_double2(fma(f0, d.x, x00[g].x), fma(f0, d.y, x00[g].y)));
+                st_amp(a + (i | bk | bb), make_double2(fma(-f0, d.x, x11[g].x), fma(-f0, d.y, x11[g].y)));
+                st_amp(a + (i | bk), cscale(f1, x01[g]));
+                st_amp(a + (i | bb), cscale(f1, x10[g]));
+            } else if (KIND == CH_PAULI) {
+                // cpu_densmatr_oneQubitPauliChannel_subA (cpu_subroutines.cpp:1455-1496)
+                st_amp(a + i, lin2(f0, x00[g], f1, x11[g]));
+                st_amp(a + (i | bk), lin2(f2, x01[g], f3, x10[g]));
+                st_amp(a + (i | bb), lin2(f2, x10[g], f3, x01[g]));
+                st_amp(a + (i | bk | bb), lin2(f0, x11[g], f1, x00[g]));
+            } else if (KIND == CH_DAMP) {
+                // cpu_densmatr_oneQubitDamping_subA (cpu_subroutines.cpp:1550-1575)
+                st_amp(a + i, make_double2(fma(f0, x11[g].x, x00[g].x), fma(f0, x11[g].y, x00[g].y)));
+                st_amp(a + (i | bk), cscale(f1, x01[g]));
+                st_amp(a + (i | bb), cscale(f1, x10[g]));
+                st_amp(a + (i | bk | bb), cscale(f2, x11[g]));
+            } else {
+                // cpu_densmatr_oneQubitDephasing_subA (cpu_subroutines.cpp:1072-1105): only the two
+                // off-diagonal amplitudes of each group change
+                st_amp(a + (i | bk), cscale(f0, x01[g]));
+                st_amp(a + (i | bb), cscale(f0, x10[g]));
+            }
+        }
+    }
 }
 
 // cpu_densmatr_twoQubitDephasing_subB (cpu_subroutines.cpp:1143-1170): amplitudes
@@ -126,6 +136,18 @@ __global__ void k_dm_projector(double2* __restrict__ a, qidx numAmps, int nKet, 
 
 namespace {
 
+const int CH_G = 2;   // groups per thread per iteration
+
+template <int KIND>
+int launch_channel1(void* amps, int nKet, int qubit, double f0, double f1, double f2, double f3, void* stream, const char* what) {
+    qidx numIts = ((qidx)1 << (2 * nKet)) / 4;
+    qidx need = (numIts + (qidx)QG_THREADS * CH_G - 1) / ((qidx)QG_THREADS * CH_G);
+    unsigned grid = (unsigned)std::max<qidx>(1, std::min<qidx>(need, (qidx)qg_num_sms() * 16));
+    k_dm_channel1<KIND, CH_G><<<grid, QG_THREADS, 0, qg_stream(stream)>>>((double2*)amps, numIts, qubit, qubit + nKet, f0, f1, f2, f3);
+    qg_note_launch();
+    return qg_check_launch(what);
+}
+
 int check_dm(void* amps, int nKet, int qubit) {
     if (nKet < 1 || 2 * nKet > QG_MAX_QUBITS) return qg_fail(QG_ERR_ARG, "density matrix of %d qubits is unsupported", nKet);
     QG_TRY(qg_check_amps(amps, 2 * nKet));
@@ -140,11 +162,9 @@ extern "C" {
 int qg_dm_oneQubitDepolarising(void* amps, int nKet, int qubit, double prob, void* stream) {
     QG_TRY(check_dm(amps, nKet, qubit));
     // util_getOneQubitDepolarisingFactors (utilities.cpp:932-947)
-    double cAA = 1 - (2 * prob / 3), cBB = 2 * prob / 3, cAB = 1 - (4 * prob / 3);
-    qidx numIts = ((qidx)1 << (2 * nKet)) / 4;
-    k_depol1<<<qg_blocks(numIts), QG_THREADS, 0, qg_stream(stream)>>>((double2*)amps, numIts, qubit, qubit + nKet, cAA, cBB, cAB);
-    qg_note_launch();
-    return qg_check_launch("depol1");
+    // (cAA = 1 - cBB is folded into the kernel's arithmetic)
+    double cBB = 2 * prob / 3, cAB = 1 - (4 * prob / 3);
+    return launch_channel1<CH_DEPOL>(amps, nKet, qubit, cBB, cAB, 0, 0, stream, "depol1");
 }
 
 int qg_dm_twoQubitDepolarising(void* amps, int nKet, int qubit1, int qubit2, double prob, void* stream) {
@@ -169,10 +189,7 @@ int qg_dm_twoQubitDepolarising(void* amps, int nKet, int qubit1, int qubit2, dou
 int qg_dm_oneQubitDephasing(void* amps, int nKet, int qubit, double prob, void* stream) {
     QG_TRY(check_dm(amps, nKet, qubit));
     double fac = 1 - (2 * prob);   // util_getOneQubitDephasingFactor (utilities.cpp:918-921)
-    qidx numIts = ((qidx)1 << (2 * nKet)) / 4;
-    k_dephase1<<<qg_blocks(numIts), QG_THREADS, 0, qg_stream(stream)>>>((double2*)amps, numIts, qubit, qubit + nKet, fac);
-    qg_note_launch();
-    return qg_check_launch("dephase1");
+    return launch_channel1<CH_DEPHASE>(amps, nKet, qubit, fac, 0, 0, 0, stream, "dephase1");
 }
 
 int qg_dm_twoQubitDephasing(void* amps, int nKet, int qubit1, int qubit2, double prob, void* stream) {
@@ -189,10 +206,7 @@ int qg_dm_twoQubitDephasing(void* amps, int nKet, int qubit1, int qubit2, double
 int qg_dm_oneQubitDamping(void* amps, int nKet, int qubit, double prob, void* stream) {
     QG_TRY(check_dm(amps, nKet, qubit));
     double c1 = std::sqrt(1 - prob), c2 = 1 - prob;   // util_getOneQubitDampingFactors (utilities.cpp:977-988)
-    qidx numIts = ((qidx)1 << (2 * nKet)) / 4;
-    k_damping1<<<qg_blocks(numIts), QG_THREADS, 0, qg_stream(stream)>>>((double2*)amps, numIts, qubit, qubit + nKet, prob, c1, c2);
-    qg_note_launch();
-    return qg_check_launch("damping1");
+    return launch_channel1<CH_DAMP>(amps, nKet, qubit, prob, c1, c2, 0, stream, "damping1");
 }
 
 int qg_dm_oneQubitPauliChannel(void* amps, int nKet, int qubit, double pX, double pY, double pZ, void* stream) {
@@ -200,10 +214,7 @@ int qg_dm_oneQubitPauliChannel(void* amps, int nKet, int qubit, double pX, doubl
     double pI = 1 - pX - pY - pZ;   // localiser.cpp:1575-1585
     // util_getOneQubitPauliChannelFactors (utilities.cpp:962-975)
     double fAA = pI + pZ, fBB = pX + pY, fAB = pI - pZ, fBA = pX - pY;
-    qidx numIts = ((qidx)1 << (2 * nKet)) / 4;
-    k_pauli_channel1<<<qg_blocks(numIts), QG_THREADS, 0, qg_stream(stream)>>>((double2*)amps, numIts, qubit, qubit + nKet, fAA, fBB, fAB, fBA);
-    qg_note_launch();
-    return qg_check_launch("pauli_channel1");
+    return launch_channel1<CH_PAULI>(amps, nKet, qubit, fAA, fBB, fAB, fBA, stream, "pauli_channel1");
 }
 
 int qg_dm_multiQubitProjector(void* amps, int nKet, const int* qubits, const int* outcomes, int num, double prob, void* stream) {

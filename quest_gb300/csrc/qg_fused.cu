@@ -34,6 +34,9 @@ int qg_tc_apply_block(float2* amps, int numQubits, const int* targs, const float
 bool qg_tc_supported(int numQubits);
 int qg_tc_prepare();
 int qg_tc_take_error();
+template <typename AMP>
+int qg_pauli_tile_batch(const AMP* amps, int n, const int64_t* mXY, const int64_t* mYZ, const int* numsY, int num,
+                        qg_cplx* out, cudaStream_t st);
 
 namespace {
 
@@ -398,37 +401,6 @@ __global__ void __launch_bounds__(256) k32_scale_to_norm(float2* __restrict__ a,
         x.x *= f; x.y *= f; x.z *= f; x.w *= f;
         __stcs(a4 + i, x);
     }
-}
-
-// batched Pauli expectation (FP64 accumulation), the reference's per-n term
-template <int NS>
-__global__ void __launch_bounds__(RED_THREADS) k32_expec_pauli_batch(const float2* __restrict__ a, qidx n,
-                                                                    const qidx* __restrict__ mXY, const qidx* __restrict__ mYZ,
-                                                                    int numStrings, RedOut out) {
-    double v[2 * NS];
-#pragma unroll
-    for (int k = 0; k < 2 * NS; k++) v[k] = 0.0;
-    __shared__ qidx sXY[NS], sYZ[NS];
-    if (threadIdx.x < NS) {
-        sXY[threadIdx.x] = threadIdx.x < numStrings ? mXY[threadIdx.x] : 0;
-        sYZ[threadIdx.x] = threadIdx.x < numStrings ? mYZ[threadIdx.x] : 0;
-    }
-    __syncthreads();
-    qidx stride = (qidx)gridDim.x * RED_THREADS;
-    for (qidx i = blockIdx.x * (qidx)RED_THREADS + threadIdx.x; i < n; i += stride) {
-        float2 an = __ldg(a + i);
-#pragma unroll
-        for (int s = 0; s < NS; s++) {
-            if (s < numStrings) {
-                qidx j = i ^ sXY[s];
-                float2 aj = __ldg(a + j);
-                double sg = parity64(j & sYZ[s]) ? -1.0 : 1.0;
-                v[2 * s] += sg * ((double)an.x * aj.x + (double)an.y * aj.y);
-                v[2 * s + 1] += sg * ((double)an.x * aj.y - (double)an.y * aj.x);
-            }
-        }
-    }
-    block_reduce_and_finish<2 * NS>(v, out);
 }
 
 // ============================================================== host side
@@ -860,32 +832,11 @@ int qg_sv32_calcExpecPauliStrBatch(const void* amps, int numQubits, const int64_
     qidx lim = ((qidx)1 << numQubits) - 1;
     for (int s = 0; s < numStrings; s++)
         if ((masksXY[s] & ~lim) || (masksYZ[s] & ~lim)) return qg_fail(QG_ERR_ARG, "Pauli string %d targets a qubit beyond %d", s, numQubits);
-    cudaStream_t st = qg_stream(stream);
-    const int NS = 16;
-    qidx n = (qidx)1 << numQubits;
-    for (int s0 = 0; s0 < numStrings; s0 += NS) {
-        int cnt = std::min(NS, numStrings - s0);
-        int grid = red_grid(n);
-        void* s = nullptr;
-        QG_TRY(qg_scratch_get(&s, red_scratch_bytes(grid, 2 * NS) + 512));
-        RedOut r;
-        red_setup_at((char*)s + 512, grid, 2 * NS, &r);
-        r.ticket = (unsigned int*)s;              // the ticket stays at the start of scratch
-        qidx* dm = (qidx*)((char*)s + 256);       // masks right after it
-        std::vector<qidx> hm(2 * NS, 0);
-        for (int k = 0; k < cnt; k++) { hm[k] = masksXY[s0 + k]; hm[NS + k] = masksYZ[s0 + k]; }
-        QG_CUDA(cudaMemcpyAsync(dm, hm.data(), 8 * 2 * NS, cudaMemcpyHostToDevice, st));
-        k32_expec_pauli_batch<NS><<<grid, RED_THREADS, 0, st>>>((const float2*)amps, n, dm, dm + NS, cnt, r);
-        double v[2 * NS];
-        QG_TRY(red_fetch(r, 2 * NS, v, st));
-        for (int k = 0; k < cnt; k++) {
-            double re = v[2 * k], im = v[2 * k + 1];
-            times_power_of_i(&re, &im, numsY[s0 + k]);
-            out[s0 + k].re = re;
-            out[s0 + k].im = im;
-        }
-    }
-    return QG_OK;
+    if (numStrings > 0 && (!masksXY || !masksYZ || !numsY || !out)) return qg_fail(QG_ERR_ARG, "null argument");
+    // the tiled kernel of qg_pauli_tile.cu: FP32 amplitudes, FP64 products and sums
+    return numStrings ? qg_pauli_tile_batch<float2>((const float2*)amps, numQubits, masksXY, masksYZ, numsY, numStrings, out,
+                                                    qg_stream(stream))
+                      : QG_OK;
 }
 
 }  // extern "C"

@@ -113,38 +113,6 @@ __global__ void __launch_bounds__(RED_THREADS) k_dm_expec_pauli(const double2* _
     block_reduce_and_finish<2>(v, out);
 }
 
-// Many Pauli strings in one pass: each thread reads a_n once and, per string,
-// the partner a_{n ^ maskXY}; the full sum over n of the reference's term is kept.
-template <int NS>
-__global__ void __launch_bounds__(RED_THREADS) k_expec_pauli_batch(const double2* __restrict__ a, qidx numAmps,
-                                                                  const qidx* __restrict__ mXY, const qidx* __restrict__ mYZ,
-                                                                  int numStrings, RedOut out) {
-    double v[2 * NS];
-#pragma unroll
-    for (int k = 0; k < 2 * NS; k++) v[k] = 0.0;
-    __shared__ qidx sXY[NS], sYZ[NS];
-    if (threadIdx.x < NS) {
-        sXY[threadIdx.x] = threadIdx.x < numStrings ? mXY[threadIdx.x] : 0;
-        sYZ[threadIdx.x] = threadIdx.x < numStrings ? mYZ[threadIdx.x] : 0;
-    }
-    __syncthreads();
-    qidx stride = (qidx)gridDim.x * RED_THREADS;
-    for (qidx n = blockIdx.x * (qidx)RED_THREADS + threadIdx.x; n < numAmps; n += stride) {
-        double2 an = __ldg(a + n);
-#pragma unroll
-        for (int s = 0; s < NS; s++) {
-            if (s < numStrings) {
-                qidx j = n ^ sXY[s];
-                double2 aj = __ldg(a + j);
-                double sg = parity64(j & sYZ[s]) ? -1.0 : 1.0;
-                v[2 * s] += sg * fma(an.x, aj.x, an.y * aj.y);
-                v[2 * s + 1] += sg * fma(an.x, aj.y, -an.y * aj.x);
-            }
-        }
-    }
-    block_reduce_and_finish<2 * NS>(v, out);
-}
-
 // Density-matrix form of the batch: per column n and string s the element
 // rho[n ^ maskXY_s][n] with its sign; NS strings per pass over the 2^N columns.
 template <int NS>
@@ -477,9 +445,15 @@ int qg_dm_calcExpecPauliStrBatch(const void* amps, int numKetQubits, const int64
 
 }  // extern "C"
 
+template <typename AMP>
+int qg_pauli_tile_batch(const AMP* amps, int n, const int64_t* mXY, const int64_t* mYZ, const int* numsY, int num,
+                        qg_cplx* out, cudaStream_t st);
+
 namespace {
 
-// up to 16 strings per pass; numQubits = the ket qubits of a density matrix
+// statevector: the tiled kernel of qg_pauli_tile.cu (each amplitude read once per group
+// of strings); density matrix: up to 16 strings per pass over the columns, where each
+// string reads one element per column; numQubits = the ket qubits of a density matrix
 int expec_pauli_batch(const void* amps, int numQubits, bool dm, const int64_t* masksXY, const int64_t* masksYZ,
                       const int* numsY, int numStrings, qg_cplx* out, void* stream) {
     if (numStrings < 0) return qg_fail(QG_ERR_ARG, "negative string count");
@@ -488,6 +462,7 @@ int expec_pauli_batch(const void* amps, int numQubits, bool dm, const int64_t* m
     for (int s = 0; s < numStrings; s++)
         if ((masksXY[s] & ~lim) || (masksYZ[s] & ~lim)) return qg_fail(QG_ERR_ARG, "Pauli string %d targets a qubit beyond %d", s, numQubits);
     cudaStream_t st = qg_stream(stream);
+    if (!dm) return numStrings ? qg_pauli_tile_batch<double2>((const double2*)amps, numQubits, masksXY, masksYZ, numsY, numStrings, out, st) : QG_OK;
     const int NS = 16;
     qidx n = (qidx)1 << numQubits;
     for (int s0 = 0; s0 < numStrings; s0 += NS) {
@@ -506,10 +481,7 @@ int expec_pauli_batch(const void* amps, int numQubits, bool dm, const int64_t* m
         std::vector<qidx> hm(2 * NS, 0);
         for (int k = 0; k < cnt; k++) { hm[k] = masksXY[s0 + k]; hm[NS + k] = masksYZ[s0 + k]; }
         QG_CUDA(cudaMemcpyAsync(dmask, hm.data(), 8 * 2 * NS, cudaMemcpyHostToDevice, st));
-        if (dm)
-            k_dm_expec_pauli_batch<NS><<<grid, RED_THREADS, 0, st>>>((const double2*)amps, n, dmask, dmask + NS, cnt, r);
-        else
-            k_expec_pauli_batch<NS><<<grid, RED_THREADS, 0, st>>>((const double2*)amps, n, dmask, dmask + NS, cnt, r);
+        k_dm_expec_pauli_batch<NS><<<grid, RED_THREADS, 0, st>>>((const double2*)amps, n, dmask, dmask + NS, cnt, r);
         qg_note_launch();
         double v[2 * NS];
         QG_TRY(red_fetch(r, 2 * NS, v, st));

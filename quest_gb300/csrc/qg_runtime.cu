@@ -334,6 +334,25 @@ int qg_clear_cache(void) {
     return QG_OK;
 }
 
+int qg_stream_create(void** out) {
+    if (!out) return qg_fail(QG_ERR_ARG, "null output");
+    cudaStream_t s;
+    QG_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    *out = (void*)s;
+    return QG_OK;
+}
+
+int qg_stream_destroy(void* stream) {
+    if (stream) QG_CUDA(cudaStreamDestroy((cudaStream_t)stream));
+    return QG_OK;
+}
+
+int qg_stream_wait_event(void* stream, void* ev) {
+    if (!ev) return qg_fail(QG_ERR_ARG, "null event");
+    QG_CUDA(cudaStreamWaitEvent(qg_stream(stream), (cudaEvent_t)ev, 0));
+    return QG_OK;
+}
+
 int qg_event_create(void** out) {
     cudaEvent_t e;
     QG_CUDA(cudaEventCreate(&e));

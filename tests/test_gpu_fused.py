@@ -302,9 +302,11 @@ def test_server_fails_only_the_request_that_timed_out(env):
     lib = _lib.lib()
     rng = np.random.default_rng(12)
     from quest_gb300.fused import Circuit
-    big = Circuit(13).add([0, 2, 4, 6, 8], qc.haar_unitary(32, rng)).fuse(5)      # one tensor-core block
+    # 15 qubits: above the shared-memory path (at most 14), so the request runs as
+    # whole-state passes with one tensor-core block
+    big = Circuit(15).add([0, 2, 4, 6, 8], qc.haar_unitary(32, rng)).fuse(5)
     small = serve.circuit_of(8, serve.hea_request(8, 6, rng)[0])
-    codes = [[1] * 13, [3] * 13]
+    codes = [[1] * 15, [3] * 15]
     srv = serve.Server(1 << 28, 8, impl=3)
     try:
         rid_big = srv.submit(big, codes)

@@ -359,3 +359,46 @@ def test_pauli_batch_matches_oracle(env, nq, is_dm):
     finally:
         Q.destroyQureg(q)
     assert np.max(np.abs(np.array(list(got)) - want)) <= TOL
+
+
+def _string_set(nq, count, style, rng):
+    codes = []
+    for s in range(count):
+        c = [int(v) for v in rng.integers(0, 4, nq)]
+        if style == "low":        # X/Y only on the lowest qubits (partners in the same row)
+            c = [v if q < 3 or v in (0, 3) else 3 for q, v in enumerate(c)]
+        elif style == "high":     # X/Y only on the highest qubits (partners far away)
+            c = [v if q >= nq - 3 or v in (0, 3) else 0 for q, v in enumerate(c)]
+        elif style == "zi":       # Z-only and identity strings between general ones
+            if s % 2 == 0:
+                c = [3 * (v & 1) if s % 4 == 0 else 0 for v in c]
+        elif style == "repeat" and s % 2 == 1:
+            c = codes[-1]
+        codes.append(c)
+    return codes
+
+
+@pytest.mark.parametrize("nq", [1, 3, 6, 12, 17, 22])
+@pytest.mark.parametrize("style", ["random", "low", "high", "zi", "repeat"])
+def test_tiled_pauli_batch_string_shapes(env, nq, style):
+    """The statevector batch (tiles of 2^t contiguous columns times the span of the
+    strings' row parts, every amplitude read once per pass) on strings whose partners
+    are near, far, absent (Z/I) or repeated, 1 to 22 qubits, against the oracle."""
+    import ctypes
+    rng = np.random.default_rng(hash((nq, style)) & 0xffff)
+    codes = _string_set(nq, 37, style, rng)
+    amps = qc.random_statevector(nq, 80 + nq)
+    _, want, _ = qc.oracle().run("".join(f"EXPEC {qc.pauli_text(c)}\n" for c in codes), nq, 0, amps)
+    Q = env.Q
+    q = Q.createQureg(nq)
+    try:
+        env.set_amps(q, amps)
+        strs = (env.PauliStr * len(codes))(*[env.pauli_str(c) for c in codes])
+        got = (ctypes.c_double * len(codes))()
+        Q.calcExpecPauliStrs(got, q, strs, len(codes))
+        again = (ctypes.c_double * len(codes))()
+        Q.calcExpecPauliStrs(again, q, strs, len(codes))
+    finally:
+        Q.destroyQureg(q)
+    assert np.max(np.abs(np.array(list(got)) - want)) <= TOL
+    assert bytes(got) == bytes(again)       # deterministic
