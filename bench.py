@@ -246,15 +246,15 @@ def run_gb300(args, world, rank, local, dist):
     api.init_env()
     _lib.check(L.qg_set_fp64_products(0 if args.fp64_products == "fixed" else 1))
     # the library's launch-shape autotuner, on a 28-qubit scratch register (4 GiB), before any timing
-    tune_ms = (C.c_double * 8)()
+    tune_ms = (C.c_double * 12)()
     tune_n = C.c_int(0)
-    _lib.check(L.qg_autotune_fp64(min(28, args.qubits), tune_ms, 8, C.byref(tune_n)))
+    _lib.check(L.qg_autotune_fp64(min(28, args.qubits), tune_ms, 12, C.byref(tune_n)))
     shapes = []
-    for kern in (0, 1):
+    for kern in (0, 1, 2):
         tppt, tthr = C.c_int(), C.c_int()
         _lib.check(L.qg_get_kernel_shape(kern, C.byref(tppt), C.byref(tthr)))
         shapes.append([tppt.value, tthr.value])
-    tuning = {"dense1_fx_shape": shapes[0], "diag1_fx_shape": shapes[1],
+    tuning = {"dense1_fx_shape": shapes[0], "diag1_fx_shape": shapes[1], "dense2_fx_shape": shapes[2],
               "candidates_ms": [round(tune_ms[i], 4) for i in range(tune_n.value)]}
 
     nq = args.qubits
@@ -854,8 +854,8 @@ def run_gates(args, world, rank, local, dist):
     _lib.check(L.qg_init(local))
     api.init_env()
     n = args.qubits if "--qubits" in sys.argv else 28
-    ms_buf, cnt = (C.c_double * 8)(), C.c_int(0)
-    _lib.check(L.qg_autotune_fp64(min(28, n), ms_buf, 8, C.byref(cnt)))
+    ms_buf, cnt = (C.c_double * 12)(), C.c_int(0)
+    _lib.check(L.qg_autotune_fp64(min(28, n), ms_buf, 12, C.byref(cnt)))
     p = C.c_void_p()
     _lib.check(L.qg_alloc(C.byref(p), 16 << n))
     _lib.check(L.qg_sv_initUniformState(p, n, qg_cplx(1 / np.sqrt(2.0 ** n), 0), None))

@@ -106,11 +106,13 @@ int qg_get_fp64_products(int* mode);
 /* ------------------------------------------------------------------ launch-shape autotuner
  * (no counterpart in the reference, whose launch sizes are fixed formulas,
  * gpu_subroutines.cpp getNumBlocks)  Kernel 0 = the one-target dense kernel, 1 = the
- * one-target diagonal kernel, both with fixed-point products.  A shape is (items per
- * thread per iteration, threads per block) from {(1,256), (1,128), (2,256), (2,128)};
+ * one-target diagonal kernel, 2 = the two-target dense kernel, all with fixed-point
+ * products.  A shape is (items per thread per iteration -- for kernel 2, groups in
+ * flight per thread -- , threads per block) from {(1,256), (1,128), (2,256), (2,128)};
  * default (1,256). */
 #define QG_TUNE_KERNEL_DENSE1 0
 #define QG_TUNE_KERNEL_DIAG1 1
+#define QG_TUNE_KERNEL_DENSE2 2
 int qg_set_kernel_shape(int kernel, int pairsPerThread, int threadsPerBlock);
 int qg_get_kernel_shape(int kernel, int* pairsPerThread, int* threadsPerBlock);
 /* times every candidate of every tunable kernel on a scratch register of numQubits

@@ -93,6 +93,38 @@ static inline idx insertWithMask(idx n, const QubitSet& s) {
     return s.stateMask | insertZeroBits(n, s.sorted.data(), (int)s.sorted.size());
 }
 
+/* The reference unrolls insertBits at compile time for up to five bits
+ * (SET_VAR_AT_COMPILE_TIME with the NumCtrls template parameter, cpu_subroutines.cpp);
+ * the same here, so that the port runs as fast as the reference's CPU build. */
+struct FixedSet {
+    int num;
+    int sorted[64];
+    idx mask;
+    explicit FixedSet(const QubitSet& s) : num((int)s.sorted.size()), mask(s.stateMask) {
+        for (int i = 0; i < num; i++) sorted[i] = s.sorted[i];
+    }
+};
+template <int K>
+static inline idx insertK(idx n, const FixedSet& f) {
+    if (K >= 0) {
+        for (int i = 0; i < (K >= 0 ? K : 0); i++) n = insertBit(n, f.sorted[i], 0);
+    } else {
+        for (int i = 0; i < f.num; i++) n = insertBit(n, f.sorted[i], 0);
+    }
+    return n | f.mask;
+}
+#define ORC_DISPATCH_K(num, ...)                          \
+    switch (num) {                                        \
+        case 0: { constexpr int K = 0; __VA_ARGS__ } break;  \
+        case 1: { constexpr int K = 1; __VA_ARGS__ } break;  \
+        case 2: { constexpr int K = 2; __VA_ARGS__ } break;  \
+        case 3: { constexpr int K = 3; __VA_ARGS__ } break;  \
+        case 4: { constexpr int K = 4; __VA_ARGS__ } break;  \
+        case 5: { constexpr int K = 5; __VA_ARGS__ } break;  \
+        default: { constexpr int K = -1; __VA_ARGS__ } break; \
+    }
+#define ORC_PARALLEL_FOR _Pragma("omp parallel for num_threads(orc_get_num_threads())")
+
 static inline cplx* C(double* a) { return reinterpret_cast<cplx*>(a); }
 static inline const cplx* C(const double* a) { return reinterpret_cast<const cplx*>(a); }
 
@@ -116,32 +148,35 @@ extern "C" int orc_get_num_threads(void) {
 extern "C" void orc_sv_swap(double* amps, int nq, const int* ctrls, const int* states, int nc, int t1, int t2) {
     if (t1 > t2) std::swap(t1, t2);
     int targs[2] = {t2, t1}, ts[2] = {0, 1};
-    QubitSet s = makeSet(ctrls, states, nc, targs, ts, 2);
+    FixedSet f(makeSet(ctrls, states, nc, targs, ts, 2));
     idx numIts = pow2(nq) >> (nc + 2);
     cplx* a = C(amps);
-    #pragma omp parallel for NT
-    for (idx n = 0; n < numIts; n++) {
-        idx i01 = insertWithMask(n, s);
-        idx i10 = flipBit(flipBit(i01, t2), t1);
-        std::swap(a[i01], a[i10]);
-    }
+    ORC_DISPATCH_K(f.num,
+        ORC_PARALLEL_FOR
+        for (idx n = 0; n < numIts; n++) {
+            idx i01 = insertK<K>(n, f);
+            idx i10 = flipBit(flipBit(i01, t2), t1);
+            std::swap(a[i01], a[i10]);
+        })
 }
 
 /* cpu_statevec_anyCtrlOneTargDenseMatr_subA: cpu_subroutines.cpp:355-383 */
 extern "C" void orc_sv_dense1(double* amps, int nq, const int* ctrls, const int* states, int nc, int t, const double* mm) {
     const cplx* m = C(mm);
     int ts = 0;
-    QubitSet s = makeSet(ctrls, states, nc, &t, &ts, 1);
+    FixedSet f(makeSet(ctrls, states, nc, &t, &ts, 1));
     idx numIts = pow2(nq) >> (nc + 1);
     cplx* a = C(amps);
-    #pragma omp parallel for NT
-    for (idx n = 0; n < numIts; n++) {
-        idx i0 = insertWithMask(n, s);
-        idx i1 = flipBit(i0, t);
-        cplx a0 = a[i0], a1 = a[i1];
-        a[i0] = m[0] * a0 + m[1] * a1;
-        a[i1] = m[2] * a0 + m[3] * a1;
-    }
+    const cplx m0 = m[0], m1 = m[1], m2 = m[2], m3 = m[3];
+    ORC_DISPATCH_K(f.num,
+        ORC_PARALLEL_FOR
+        for (idx n = 0; n < numIts; n++) {
+            idx i0 = insertK<K>(n, f);
+            idx i1 = flipBit(i0, t);
+            cplx a0 = a[i0], a1 = a[i1];
+            a[i0] = m0 * a0 + m1 * a1;
+            a[i1] = m2 * a0 + m3 * a1;
+        })
 }
 
 /* cpu_statevec_anyCtrlTwoTargDenseMatr_sub: cpu_subroutines.cpp:433-470 */
@@ -195,14 +230,16 @@ extern "C" void orc_sv_denseK(double* amps, int nq, const int* ctrls, const int*
 /* cpu_statevec_anyCtrlOneTargDiagMatr_sub: cpu_subroutines.cpp:581-610 */
 extern "C" void orc_sv_diag1(double* amps, int nq, const int* ctrls, const int* states, int nc, int t, const double* dd) {
     const cplx* d = C(dd);
-    QubitSet s = makeSet(ctrls, states, nc, nullptr, nullptr, 0);
+    FixedSet f(makeSet(ctrls, states, nc, nullptr, nullptr, 0));
     idx numIts = pow2(nq) >> nc;
     cplx* a = C(amps);
-    #pragma omp parallel for NT
-    for (idx n = 0; n < numIts; n++) {
-        idx j = insertWithMask(n, s);
-        a[j] *= d[getBit(j, t)];
-    }
+    const cplx d2[2] = {d[0], d[1]};
+    ORC_DISPATCH_K(f.num,
+        ORC_PARALLEL_FOR
+        for (idx n = 0; n < numIts; n++) {
+            idx j = insertK<K>(n, f);
+            a[j] *= d2[getBit(j, t)];
+        })
 }
 
 /* cpu_statevec_anyCtrlTwoTargDiagMatr_sub: cpu_subroutines.cpp:622-651 (k = bit t2 bit t1) */

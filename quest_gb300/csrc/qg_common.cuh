@@ -40,7 +40,8 @@ int qg_fp64_products_mode();
 struct QgShape { int ppt; int threads; };
 #define QG_TUNE_DENSE1 0
 #define QG_TUNE_DIAG1 1
-#define QG_TUNE_NUM 2
+#define QG_TUNE_DENSE2 2
+#define QG_TUNE_NUM 3
 QgShape qg_tuned_shape(int kernel);
 
 #define QG_CUDA(call)                                                      \

@@ -47,7 +47,7 @@ __device__ __forceinline__ double flip_sign(double x, unsigned long long s) {
 }
 
 template <typename AMP>
-__global__ void __launch_bounds__(PT_THREADS, 2) k_expec_pauli_tile(const AMP* __restrict__ a, qidx numTiles,
+__global__ void __launch_bounds__(PT_THREADS, 3) k_expec_pauli_tile(const AMP* __restrict__ a, qidx numTiles,
                                                                     const qgpt::Tile P, RedOut out) {
     extern __shared__ __align__(16) unsigned char pt_smem[];
     double2* tile = (double2*)pt_smem;
@@ -115,10 +115,13 @@ int qg_pauli_tile_batch(const AMP* amps, int n, const int64_t* mXY, const int64_
     for (const qgpt::Pass& ps : passes) {
         const qgpt::Tile& P = ps.tile;
         const size_t smem = (sizeof(double2) << (P.d + P.t)) + sizeof(qidx) * ((size_t)1 << P.d);
-        const int grid = (int)std::max<qidx>(1, std::min<qidx>(ps.numTiles, (qidx)qg_num_sms() * 2));
+        QG_CUDA(cudaFuncSetAttribute(k_expec_pauli_tile<AMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        // every resident block busy: while some load their tile, the others keep the FP64 pipe fed
+        int perSM = 0;
+        QG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_expec_pauli_tile<AMP>, PT_THREADS, smem));
+        const int grid = (int)std::max<qidx>(1, std::min<qidx>(ps.numTiles, (qidx)qg_num_sms() * std::max(1, perSM)));
         RedOut r;
         QG_TRY(red_setup(grid, qgpt::NS, &r));
-        QG_CUDA(cudaFuncSetAttribute(k_expec_pauli_tile<AMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         k_expec_pauli_tile<AMP><<<grid, PT_THREADS, smem, st>>>(amps, ps.numTiles, P, r);
         qg_note_launch();
         QG_TRY(red_fetch(r, qgpt::NS, raw, st));

@@ -208,31 +208,65 @@ __global__ void k_dense2(double2* __restrict__ a, qidx numIts, Ins ins, qidx mas
 // k_dense2 through the integer pipes: the real 8x8 form of the matrix on each group
 // of four amplitudes in block-floating fixed point (qg_fixed.cuh); groups holding
 // Inf/NaN or with results outside the normal range take the FP64 products.
-// 4 resident blocks of 256 (registers capped at 64, a 40-byte spill): 3 % faster than 3.
-template <int NB>
-__global__ void __launch_bounds__(QG_THREADS, 4) k_dense2_fx(double2* __restrict__ a, qidx numIts, Ins ins, qidx mask,
-                                                         qidx b1, qidx b2, qgfx::OpN<8> C, Mat2 M) {
-    const qidx stride = (qidx)gridDim.x * blockDim.x;
-    for (qidx n = blockIdx.x * (qidx)blockDim.x + threadIdx.x; n < numIts; n += stride) {
-        const qidx i00 = insert_bits<NB>(n, ins) | mask;
+// NBUF = 1: one group per thread at a time (registers capped at 64 for 4 resident
+// blocks of 256).  NBUF = 2: two groups per thread in rotating register buffers, the
+// next group's loads in flight while the current one is computed (the loop is unrolled
+// over the buffers, so no buffer is copied: a register copy of a pending load would
+// wait for it); 3 resident blocks of 256.  The autotuner picks the shape per GPU.
+__device__ __forceinline__ void dense2_fx_group(double2* __restrict__ a, qidx i00, qidx b1, qidx b2, const double2 (&v)[4],
+                                                const qgfx::OpN<8>& C, const Mat2& M) {
+    const double in[8] = {v[0].x, v[0].y, v[1].x, v[1].y, v[2].x, v[2].y, v[3].x, v[3].y};
+    double out[8];
+    if (qgfx::apply_op_best<8>(C, in, out)) {
+        st_amp(a + i00, make_double2(out[0], out[1]));
+        st_amp(a + (i00 | b1), make_double2(out[2], out[3]));
+        st_amp(a + (i00 | b2), make_double2(out[4], out[5]));
+        st_amp(a + (i00 | b1 | b2), make_double2(out[6], out[7]));
+    } else {
         const qidx idx[4] = {i00, i00 | b1, i00 | b2, i00 | b1 | b2};
-        double2 v[4];
 #pragma unroll
-        for (int j = 0; j < 4; j++) v[j] = ld_amp(a + idx[j]);
-        const double in[8] = {v[0].x, v[0].y, v[1].x, v[1].y, v[2].x, v[2].y, v[3].x, v[3].y};
-        double out[8];
-        if (qgfx::apply_op_best<8>(C, in, out)) {
+        for (int r = 0; r < 4; r++) {
+            double2 acc = cmul(M.m[4 * r], v[0]);
 #pragma unroll
-            for (int r = 0; r < 4; r++) st_amp(a + idx[r], make_double2(out[2 * r], out[2 * r + 1]));
-        } else {
-#pragma unroll
-            for (int r = 0; r < 4; r++) {
-                double2 acc = cmul(M.m[4 * r], v[0]);
-#pragma unroll
-                for (int j = 1; j < 4; j++) acc = cfma(M.m[4 * r + j], v[j], acc);
-                st_amp(a + idx[r], acc);
-            }
+            for (int j = 1; j < 4; j++) acc = cfma(M.m[4 * r + j], v[j], acc);
+            st_amp(a + idx[r], acc);
         }
+    }
+}
+
+template <int NB, int NBUF, int THREADS>
+__global__ void __launch_bounds__(THREADS, (NBUF == 1 ? 1024 : 768) / THREADS) k_dense2_fx(double2* __restrict__ a, qidx numIts,
+                                                                                         Ins ins, qidx mask, qidx b1, qidx b2,
+                                                                                         qgfx::OpN<8> C, Mat2 M) {
+    const qidx stride = (qidx)gridDim.x * THREADS;
+    const qidx tid = blockIdx.x * (qidx)THREADS + threadIdx.x;
+    auto load = [&](qidx& i00, double2 (&v)[4], qidx n) {
+        i00 = insert_bits<NB>(n, ins) | mask;
+        v[0] = ld_amp(a + i00);
+        v[1] = ld_amp(a + (i00 | b1));
+        v[2] = ld_amp(a + (i00 | b2));
+        v[3] = ld_amp(a + (i00 | b1 | b2));
+    };
+    if (NBUF == 1) {
+        for (qidx n = tid; n < numIts; n += stride) {
+            qidx i00;
+            double2 v[4];
+            load(i00, v, n);
+            dense2_fx_group(a, i00, b1, b2, v, C, M);
+        }
+        return;
+    }
+    // rounds g = 0, 1, ...: this thread's group of round g is tid + g * stride
+    const qidx rounds = numIts > tid ? (numIts - tid + stride - 1) / stride : 0;
+    qidx i0[2];
+    double2 v[2][4];
+    if (rounds > 0) load(i0[0], v[0], tid);
+    for (qidx g = 0; g < rounds; g += 2) {
+        if (g + 1 < rounds) load(i0[1], v[1], tid + (g + 1) * stride);
+        dense2_fx_group(a, i0[0], b1, b2, v[0], C, M);
+        if (g + 1 >= rounds) break;
+        if (g + 2 < rounds) load(i0[0], v[0], tid + (g + 2) * stride);
+        dense2_fx_group(a, i0[1], b1, b2, v[1], C, M);
     }
 }
 
@@ -274,6 +308,140 @@ template <int K>
 struct DenseKOp { typedef qgfx::OpN<2 << K> type; static constexpr bool complex = false; };
 template <>
 struct DenseKOp<3> { typedef qgfx::CopN<8> type; static constexpr bool complex = true; };
+
+// k_denseK_fx with the work of a group shared by G/4 threads (K = 3, 4; G = 2^K
+// amplitudes, N = 2G reals per group).  Thread part p of a group loads amplitudes
+// 4p..4p+3 and forms outputs 4p..4p+3 (real rows 8p..8p+7 of the operator).  The
+// threads of a part sit in one warp, 32 groups side by side, so every operator
+// coefficient a warp reads is one compile-time constant-bank operand (the per-thread
+// kernel indexes rows at run time and spends its issue on constant-bank address
+// loads), and the G/4 warps of a group set exchange the group's scale and limbs
+// through shared memory.  The arithmetic is fx_prepare_e / fx_row's: the same limbs,
+// the same integer sums, so the same bits as k_denseK_fx.
+template <int K>
+struct CoopShape {
+    static constexpr int G = 1 << K, N = 2 * G, TPG = G / 4, SETS = 8 / TPG;
+};
+
+template <int PART, int N>
+__device__ __forceinline__ void coop_rows(const qgfx::OpN<N>& C, const int2 (*limbs)[32], int lane, int64_t (&R)[8]) {
+    int64_t hh[8], mid[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) { hh[i] = 0; mid[i] = 0; }
+#pragma unroll 4
+    for (int j = 0; j < N; j++) {
+        const int2 L = limbs[j][lane];
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+            hh[i] += (int64_t)L.x * C.h[8 * PART + i][j];
+            mid[i] += (int64_t)L.x * C.l[8 * PART + i][j];
+            mid[i] += (int64_t)L.y * C.h[8 * PART + i][j];
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 8; i++) R[i] = hh[i] + (mid[i] >> 32);
+}
+
+template <int K, int NB>
+__global__ void __launch_bounds__(256, 3) k_denseK_coop(double2* __restrict__ a, qidx numIts, Ins ins, qidx mask, MatK<K> M,
+                                                        qgfx::OpN<2 << K> C) {
+    typedef CoopShape<K> SH;
+    constexpr int G = SH::G, N = SH::N, TPG = SH::TPG, SETS = SH::SETS;
+    constexpr int S = qgfx::FxShift<N>::S;
+    __shared__ double2 raw[SETS][G][32];      // the inputs (for the FP64 path)
+    __shared__ int2 limbs[SETS][N][32];       // (high, low) limbs of every real of every group
+    __shared__ int4 stat[SETS][TPG][32];      // per part: largest exponent, smallest, largest effective, any nonzero
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int part = warp % TPG, set = warp / TPG;
+    const qidx step = (qidx)gridDim.x * SETS * 32;
+    for (qidx g0 = (qidx)blockIdx.x * SETS * 32; g0 < numIts; g0 += step) {
+        const qidx gi = g0 + set * 32 + lane;
+        const bool valid = gi < numIts;
+        const qidx base = insert_bits<NB>(valid ? gi : 0, ins) | mask;
+        double2 v[4];
+        int e = 0, emin = 4096, eg = 1, any = 0;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            v[k] = valid ? ld_amp(a + base + M.off[4 * part + k]) : make_double2(0.0, 0.0);
+            const double re[2] = {v[k].x, v[k].y};
+#pragma unroll
+            for (int c = 0; c < 2; c++) {
+                const uint64_t u = qgfx::f64_bits(re[c]);
+                any |= (u << 1) != 0;
+                const int ej = (int)((u >> 52) & 0x7FF);
+                e = ej > e ? ej : e;
+                emin = ej < emin ? ej : emin;
+                const int ejg = ej + (ej == 0);
+                eg = ejg > eg ? ejg : eg;
+            }
+        }
+        __syncthreads();   // the previous iteration's reads of the shared arrays are done
+#pragma unroll
+        for (int k = 0; k < 4; k++) raw[set][4 * part + k][lane] = v[k];
+        stat[set][part][lane] = make_int4(e, emin, eg, any);
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < TPG; q++) {
+            const int4 st = stat[set][q][lane];
+            e = st.x > e ? st.x : e;
+            emin = st.y < emin ? st.y : emin;
+            eg = st.z > eg ? st.z : eg;
+            any |= st.w;
+        }
+        // fx_prepare_e's choice, made alike by the group's threads
+        const int t = e + C.expo - qgfx::FxShift<N>::TOFF;
+        const int tg = eg + C.expo - qgfx::FxShift<N>::TOFF;
+        int path;          // 0: near form, 1: general form, 2: all zero, 3: FP64
+        if (emin >= 1 && e <= 2046 && e - emin <= 31 && 1023 + t >= 1 && 1023 + qgfx::FxShift<N>::RL + t <= 2046) path = 0;
+        else if (1023 + tg < 1 || 1023 + qgfx::FxShift<N>::RL + tg > 2046 || eg == 2047) path = any ? 3 : 2;
+        else path = 1;
+        if (path <= 1) {
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const double re[2] = {v[k].x, v[k].y};
+#pragma unroll
+                for (int c = 0; c < 2; c++) {
+                    const uint64_t u = qgfx::f64_bits(re[c]);
+                    int32_t xh, xl;
+                    if (path == 0) {
+                        const uint32_t hi = (uint32_t)(u >> 32);
+                        qgfx::to_limbs_near<S>(hi, (uint32_t)u, e - (int)((hi >> 20) & 0x7FFu), xh, xl);
+                    } else {
+                        qgfx::to_limbs(u, eg, xh, xl, S);
+                    }
+                    limbs[set][8 * part + 2 * k + c][lane] = make_int2(xh, xl);
+                }
+            }
+        }
+        __syncthreads();
+        if (!valid) continue;
+        if (path <= 1) {
+            int64_t R[8];
+            if (part == 0) coop_rows<0, N>(C, limbs[set], lane, R);
+            else if (TPG > 1 && part == 1) coop_rows<(TPG > 1 ? 1 : 0), N>(C, limbs[set], lane, R);
+            else if (TPG > 2 && part == 2) coop_rows<(TPG > 2 ? 2 : 0), N>(C, limbs[set], lane, R);
+            else coop_rows<(TPG > 3 ? 3 : 0), N>(C, limbs[set], lane, R);
+            const uint32_t down = (uint32_t)(path == 0 ? t : tg) << 20;
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                st_amp(a + base + M.off[4 * part + k],
+                       make_double2(qgfx::fx_to_double(R[2 * k], down), qgfx::fx_to_double(R[2 * k + 1], down)));
+        } else if (path == 2) {
+#pragma unroll
+            for (int k = 0; k < 4; k++) st_amp(a + base + M.off[4 * part + k], make_double2(0.0, 0.0));
+        } else {
+            // FP64 products from the group's inputs in shared memory
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const int r = 4 * part + k;
+                double2 acc = cmul(M.m[r * G], raw[set][0][lane]);
+#pragma unroll
+                for (int j = 1; j < G; j++) acc = cfma(M.m[r * G + j], raw[set][j][lane], acc);
+                st_amp(a + base + M.off[r], acc);
+            }
+        }
+    }
+}
 
 template <int K, int NB>
 __global__ void __launch_bounds__(128) k_denseK_fx(double2* __restrict__ a, qidx numIts, Ins ins, qidx mask, MatK<K> M,
@@ -657,6 +825,26 @@ int launch_dense1_fx(QgShape shape, const QubitPlan& p, qidx numIts, double2* am
     }
 }
 
+// k_dense2_fx with a launch shape (groups in flight per thread, threads per block)
+template <int NBUF, int THREADS>
+int launch_dense2_fx_shape(const QubitPlan& p, qidx numIts, double2* amps, qidx b1, qidx b2, const qgfx::OpN<8>& C,
+                           const Mat2& M, cudaStream_t st) {
+#define L(NBV) k_dense2_fx<NBV, NBUF, THREADS><<<resident_blocks(k_dense2_fx<NBV, NBUF, THREADS>, numIts, THREADS), THREADS, 0, st>>>(amps, numIts, p.ins, p.stateMask, b1, b2, C, M)
+    QG_DISPATCH_NB(p.numFixed, L)
+#undef L
+    return QG_OK;
+}
+
+int launch_dense2_fx(QgShape shape, const QubitPlan& p, qidx numIts, double2* amps, qidx b1, qidx b2, const qgfx::OpN<8>& C,
+                     const Mat2& M, cudaStream_t st) {
+    switch (shape.ppt * 1000 + shape.threads) {
+        case 1128: return launch_dense2_fx_shape<1, 128>(p, numIts, amps, b1, b2, C, M, st);
+        case 2128: return launch_dense2_fx_shape<2, 128>(p, numIts, amps, b1, b2, C, M, st);
+        case 2256: return launch_dense2_fx_shape<2, 256>(p, numIts, amps, b1, b2, C, M, st);
+        default: return launch_dense2_fx_shape<1, 256>(p, numIts, amps, b1, b2, C, M, st);
+    }
+}
+
 template <int MODE, int PPT, int THREADS>
 int launch_diag1_fx_shape(const QubitPlan& p, qidx numIts, double2* amps, qidx tbit, double2 d0, double2 d1,
                           const qgfx::Op2& F0, const qgfx::Op2& F1, cudaStream_t st) {
@@ -783,9 +971,7 @@ int qg_sv_anyCtrlTwoTargDenseMatr(void* amps, int numQubits, const int* ctrls, c
     qgfx::real_form(u, 4, R);
     qgfx::OpN<8> C;
     if (qg_fp64_products_mode() == QG_FP64_PRODUCTS_FIXED && qgfx::make_op<8>(R, C)) {
-#define L(NBV) k_dense2_fx<NBV><<<resident_blocks(k_dense2_fx<NBV>, numIts), QG_THREADS, 0, st>>>((double2*)amps, numIts, p.ins, p.stateMask, b1, b2, C, M)
-        QG_DISPATCH_NB(p.numFixed, L)
-#undef L
+        QG_TRY(launch_dense2_fx(qg_tuned_shape(QG_TUNE_DENSE2), p, numIts, (double2*)amps, b1, b2, C, M, st));
     } else {
 #define L(NBV) QG_LAUNCH_PLAIN(k_dense2, NBV, (double2*)amps, numIts, p.ins, p.stateMask, b1, b2, M)
         QG_DISPATCH_NB(p.numFixed, L)
@@ -822,7 +1008,22 @@ int launch_denseK(double2* amps, qidx numIts, const QubitPlan& p, const qg_cplx*
                 qgfx::real_form(u.data(), D, R.data());
                 ok = qgfx::make_op<2 * D>(R.data(), C);
             }
-            if (ok) {
+            if (ok && K == 4) {
+                // the cooperative form (real operator), 64 groups per block and iteration
+                qgfx::OpN<2 * D> CR;
+                if (!DenseKOp<K>::complex) std::memcpy(&CR, &C, sizeof(CR));
+                else {
+                    qgfx::real_form(u.data(), D, R.data());
+                    ok = qgfx::make_op<2 * D>(R.data(), CR);
+                }
+                if (ok) {
+                    const qidx items = (numIts + CoopShape<K>::SETS * 32 - 1) / (CoopShape<K>::SETS * 32) * 256;
+#define L(NBV) k_denseK_coop<K, NBV><<<resident_blocks(k_denseK_coop<K, NBV>, items, 256), 256, 0, st>>>(amps, numIts, p.ins, p.stateMask, M, CR)
+                    QG_DISPATCH_NB(p.numFixed, L)
+#undef L
+                    return QG_OK;
+                }
+            } else if (ok) {
 #define L(NBV) k_denseK_fx<K, NBV><<<resident_blocks(k_denseK_fx<K, NBV>, numIts, 128), 128, 0, st>>>(amps, numIts, p.ins, p.stateMask, M, C)
                 QG_DISPATCH_NB(p.numFixed, L)
 #undef L

@@ -17,9 +17,9 @@ namespace {
 
 struct Candidate { int ppt, threads; };
 const Candidate kCandidates[] = {{1, 256}, {1, 128}, {2, 256}, {2, 128}};
-const char* kKernelNames[QG_TUNE_NUM] = {"dense1_fx", "diag1_fx"};
+const char* kKernelNames[QG_TUNE_NUM] = {"dense1_fx", "diag1_fx", "dense2_fx"};
 
-std::atomic<int> g_shape[QG_TUNE_NUM] = {{1 * 1000 + 256}, {1 * 1000 + 256}};
+std::atomic<int> g_shape[QG_TUNE_NUM] = {{1 * 1000 + 256}, {1 * 1000 + 256}, {1 * 1000 + 256}};
 
 bool is_candidate(int ppt, int threads) {
     for (const auto& c : kCandidates)
@@ -65,9 +65,10 @@ int qg_get_kernel_shape(int kernel, int* ppt, int* threads) {
 // Times every candidate shape of the tunable kernels on a scratch register of
 // numQubits (16 B x 2^numQubits of device memory, freed before returning): the
 // one-target dense kernel (fixed-point products) on a fixed unitary, and the
-// one-target diagonal kernel on a controlled phase.  Keeps the fastest shape per kernel
-// and reports milliseconds per launch in msOut, kernel-major: msOut[k * 4 + c] for
-// candidate c (up to maxOut entries).
+// one-target diagonal kernel on a controlled phase, the two-target dense kernel
+// (fixed-point products) on near and far target pairs.  Keeps the fastest shape per
+// kernel and reports milliseconds per launch in msOut, kernel-major: msOut[k * 4 + c]
+// for candidate c (up to maxOut entries).
 int qg_autotune_fp64(int numQubits, double* msOut, int maxOut, int* numOut) {
     if (numQubits < 10 || numQubits > 32) return qg_fail(QG_ERR_ARG, "tune on 10..32 qubits, not %d", numQubits);
     const int64_t bytes = (int64_t)16 << numQubits;
@@ -79,6 +80,12 @@ int qg_autotune_fp64(int numQubits, double* msOut, int maxOut, int* numOut) {
     const double c = std::cos(0.37), s = std::sin(0.37), pc = std::cos(0.11), ps = std::sin(0.11);
     const qg_cplx m[4] = {{c * pc, c * ps}, {-s * pc, -s * ps}, {s * pc, s * ps}, {c * pc, c * ps}};
     const qg_cplx phase[2] = {{1.0, 0.0}, {std::cos(0.23), std::sin(0.23)}};
+    qg_cplx m4[16];   // the Kronecker product of the 2x2 above with itself (unitary)
+    for (int r = 0; r < 4; r++)
+        for (int q = 0; q < 4; q++) {
+            const qg_cplx x = m[(r >> 1) * 2 + (q >> 1)], y = m[(r & 1) * 2 + (q & 1)];
+            m4[r * 4 + q] = qg_cplx{x.re * y.re - x.im * y.im, x.re * y.im + x.im * y.re};
+        }
     void* ev0 = nullptr;
     void* ev1 = nullptr;
     int saved[QG_TUNE_NUM], best[QG_TUNE_NUM];
@@ -95,6 +102,12 @@ int qg_autotune_fp64(int numQubits, double* msOut, int maxOut, int* numOut) {
                 const int t = (r * 7) % (numQubits - 2) + 2;
                 if (kern == QG_TUNE_DENSE1)
                     return qg_sv_anyCtrlOneTargDenseMatr(amps, numQubits, nullptr, nullptr, 0, t, m, nullptr);
+                if (kern == QG_TUNE_DENSE2) {
+                    // near pairs and pairs half the register apart (a density matrix's ket/bra pair)
+                    const int t2 = (r & 1) ? (t + numQubits / 2) % numQubits : (t + 1) % numQubits;
+                    return qg_sv_anyCtrlTwoTargDenseMatr(amps, numQubits, nullptr, nullptr, 0, t, t2 == t ? (t + 1) % numQubits : t2,
+                                                         m4, nullptr);
+                }
                 const int ctrl = (t + 3) % numQubits == t ? 0 : (t + 3) % numQubits;
                 return qg_sv_anyCtrlOneTargDiagMatr(amps, numQubits, &ctrl, nullptr, 1, t, phase, nullptr);
             };

@@ -44,16 +44,17 @@ def test_kernel_shape_table_and_tuning_file(built_lib, tmp_path):
     assert L.qg_get_kernel_shape(0, ctypes.byref(ppt), ctypes.byref(thr)) == 0
     assert (ppt.value, thr.value) == (1, 256)
     assert L.qg_set_kernel_shape(0, 3, 256) != 0          # not a compiled shape
-    assert L.qg_set_kernel_shape(2, 1, 256) != 0          # no such kernel
+    assert L.qg_set_kernel_shape(3, 1, 256) != 0          # no such kernel
     assert L.qg_set_kernel_shape(0, 2, 128) == 0
     path = str(tmp_path / "tune.txt").encode()
     assert L.qg_tune_save(path) == 0
     text = open(path.decode()).read().splitlines()
     assert text[0] == "qg-tune 1" and text[1].split()[1:] == ["dense1_fx", "2", "128"]
     assert text[2].split()[1:] == ["diag1_fx", "1", "256"]
+    assert text[3].split()[1:] == ["dense2_fx", "1", "256"]
     assert L.qg_set_kernel_shape(0, 1, 256) == 0
     n = ctypes.c_int(-1)
-    assert L.qg_tune_load(path, ctypes.byref(n)) == 0 and n.value == 2
+    assert L.qg_tune_load(path, ctypes.byref(n)) == 0 and n.value == 3
     assert L.qg_get_kernel_shape(0, ctypes.byref(ppt), ctypes.byref(thr)) == 0
     assert (ppt.value, thr.value) == (2, 128)
     # lines for another device are skipped

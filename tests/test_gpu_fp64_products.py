@@ -134,17 +134,19 @@ def test_every_launch_shape_gives_the_same_bits(env):
     want, _, _ = qc.oracle().run(text, nq, 0, amps)
     outs = []
     text += "".join(f"CPS {c} {t} {0.1 + 0.3 * c}\n" for c, t in [(0, 5), (3, 9), (12, 2)])
+    rng = np.random.default_rng(19)
+    text += "".join(f"U2 {a} {b} {qc.mat_tokens(qc.haar_unitary(4, rng))}\n" for a, b in [(0, 1), (15, 2), (4, 12), (9, 8)])
     want, _, _ = qc.oracle().run(text, nq, 0, amps)
     try:
         for ppt, thr in [(1, 256), (1, 128), (2, 256), (2, 128)]:
-            assert L.qg_set_kernel_shape(0, ppt, thr) == 0
-            assert L.qg_set_kernel_shape(1, ppt, thr) == 0
+            for kern in (0, 1, 2):
+                assert L.qg_set_kernel_shape(kern, ppt, thr) == 0
             out, _ = _run(env, text, nq, amps)
             assert np.max(np.abs(out - want)) <= TOL
             outs.append(out)
     finally:
-        L.qg_set_kernel_shape(0, 1, 256)
-        L.qg_set_kernel_shape(1, 1, 256)
+        for kern in (0, 1, 2):
+            L.qg_set_kernel_shape(kern, 1, 256)
     for o in outs[1:]:
         assert np.array_equal(o.view(np.float64), outs[0].view(np.float64))
 
@@ -153,17 +155,17 @@ def test_autotune_picks_the_fastest_candidate(env):
     import ctypes
     from quest_gb300._lib import lib
     L = lib()
-    ms = (ctypes.c_double * 8)()
+    ms = (ctypes.c_double * 12)()
     n = ctypes.c_int()
     try:
-        assert L.qg_autotune_fp64(22, ms, 8, ctypes.byref(n)) == 0
-        assert n.value == 8 and all(ms[i] > 0 for i in range(8))
+        assert L.qg_autotune_fp64(22, ms, 12, ctypes.byref(n)) == 0
+        assert n.value == 12 and all(ms[i] > 0 for i in range(12))
         cands = [(1, 256), (1, 128), (2, 256), (2, 128)]
-        for kernel in (0, 1):
+        for kernel in (0, 1, 2):
             ppt, thr = ctypes.c_int(), ctypes.c_int()
             assert L.qg_get_kernel_shape(kernel, ctypes.byref(ppt), ctypes.byref(thr)) == 0
             best = min(range(4), key=lambda i: ms[4 * kernel + i])
             assert (ppt.value, thr.value) == cands[best]
     finally:
-        L.qg_set_kernel_shape(0, 1, 256)
-        L.qg_set_kernel_shape(1, 1, 256)
+        for kernel in (0, 1, 2):
+            L.qg_set_kernel_shape(kernel, 1, 256)

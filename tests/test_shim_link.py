@@ -9,7 +9,7 @@ import subprocess
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = "/root/reference"
+REF = os.environ.get("QUEST_SOURCES", "/root/reference")   # a checkout of the QuEST sources, where one exists
 
 
 @pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "quest", "src")), reason="QuEST sources not present")
