@@ -856,6 +856,12 @@ def run_gates(args, world, rank, local, dist):
     n = args.qubits if "--qubits" in sys.argv else 28
     ms_buf, cnt = (C.c_double * 12)(), C.c_int(0)
     _lib.check(L.qg_autotune_fp64(min(28, n), ms_buf, 12, C.byref(cnt)))
+    tuned = {}
+    for kern, name in ((0, "dense1_fx"), (1, "diag1_fx"), (2, "dense2_fx")):
+        tppt, tthr = C.c_int(), C.c_int()
+        _lib.check(L.qg_get_kernel_shape(kern, C.byref(tppt), C.byref(tthr)))
+        tuned[name] = {"shape": [tppt.value, tthr.value],
+                       "candidates_ms": [round(ms_buf[4 * kern + i], 4) for i in range(4)]}
     p = C.c_void_p()
     _lib.check(L.qg_alloc(C.byref(p), 16 << n))
     _lib.check(L.qg_sv_initUniformState(p, n, qg_cplx(1 / np.sqrt(2.0 ** n), 0), None))
@@ -911,12 +917,19 @@ def run_gates(args, world, rank, local, dist):
     k1 = kraus_map([np.sqrt(0.7) * np.eye(2), np.sqrt(0.3) * haar(2, rng)])
     iso = haar(16, rng)[:, :4]                                    # a 16x4 isometry: four 4x4 Kraus operators
     k2 = kraus_map([iso[4 * i:4 * i + 4, :] for i in range(4)])
-    dm_gates = [("applyCompMatr1 on the density matrix (one pass of conj(U) x U)", 1, lambda: Q.applyCompMatr1(dm, 3, u1)),
-                ("mixDepolarising", 1, lambda: Q.mixDepolarising(dm, 3, 0.01)),
+    # one-qubit unitaries and channels on a density matrix are deferred (multiplied into a
+    # pending superoperator per qubit); syncQuESTEnv applies them, one pass each
+    def now(fn):
+        def run():
+            fn()
+            Q.syncQuESTEnv()
+        return run
+    dm_gates = [("applyCompMatr1 on the density matrix (one pass of conj(U) x U)", 1, now(lambda: Q.applyCompMatr1(dm, 3, u1))),
+                ("mixDepolarising", 1, now(lambda: Q.mixDepolarising(dm, 3, 0.01))),
                 ("mixTwoQubitDepolarising", 1, lambda: Q.mixTwoQubitDepolarising(dm, 3, 8, 0.01)),
-                ("mixDephasing (the off-diagonal half)", 0.5, lambda: Q.mixDephasing(dm, 3, 0.05)),
-                ("mixDamping", 1, lambda: Q.mixDamping(dm, 3, 0.05)),
-                ("mixKrausMap, 1 qubit (2-target superoperator)", 1, lambda: Q.mixKrausMap(dm, (C.c_int * 1)(3), 1, k1)),
+                ("mixDephasing (the off-diagonal half)", 0.5, now(lambda: Q.mixDephasing(dm, 3, 0.05))),
+                ("mixDamping", 1, now(lambda: Q.mixDamping(dm, 3, 0.05))),
+                ("mixKrausMap, 1 qubit (2-target superoperator)", 1, now(lambda: Q.mixKrausMap(dm, (C.c_int * 1)(3), 1, k1))),
                 ("mixKrausMap, 2 qubits (4-target superoperator)", 1,
                  lambda: Q.mixKrausMap(dm, (C.c_int * 2)(3, 8), 2, k2))]
     for mode in ("fixed", "fp64"):
@@ -936,7 +949,8 @@ def run_gates(args, world, rank, local, dist):
             "scaling": "weak", "vs_baseline": None, "dtype": "f64 storage", "data": "synthetic (uniform state, seeded Haar gates)",
             "config": {"workload": f"{n}-qubit FP64 statevector, one gate per launch", "qubits": n,
                        "l2": "state larger than L2; no flush"},
-            "gates": rows, "hbm_peak_gbs": peak}
+            "gates": rows, "hbm_peak_gbs": peak,
+            "autotune": {"candidates": "(1,256), (1,128), (2,256), (2,128)", **tuned}}
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -1007,6 +1021,204 @@ def run_expec(args, world, rank, local, dist):
             "batch_one_pass_gbs": round(state_bytes / ms_batch / 1e6, 1),
             "batch_one_pass_frac_of_hbm": round(state_bytes / ms_batch / 1e6 / peak, 3),
             "values": batch_vals, "hbm_peak_gbs": peak}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def dm_layers(nq, layers, seed):
+    """The density-matrix method's circuit: per layer, Haar 2x2 unitaries on every qubit
+    (even layers) or Haar 4x4 unitaries on disjoint random pairs (odd layers), then
+    mixDepolarising(0.01) on every qubit and one 2-qubit 4-operator Kraus map (the 4x4
+    blocks of a random 16x4 isometry) on a random pair.  Returns a list of ops:
+    ("U1", t, m) / ("U2", a, b, m) / ("DEPOL", t, p) / ("KRAUS", a, b, [K0..K3])."""
+    rng = np.random.default_rng(seed)
+    ops = []
+    for layer in range(layers):
+        if layer % 2 == 0:
+            for t in range(nq):
+                ops.append(("U1", t, haar(2, rng)))
+        else:
+            perm = rng.permutation(nq)
+            for i in range(0, nq - 1, 2):
+                ops.append(("U2", int(perm[i]), int(perm[i + 1]), haar(4, rng)))
+        for t in range(nq):
+            ops.append(("DEPOL", t, 0.01))
+        a, b = (int(v) for v in rng.choice(nq, size=2, replace=False))
+        g = rng.standard_normal((16, 4)) + 1j * rng.standard_normal((16, 4))
+        qm, r = np.linalg.qr(g)
+        qm = qm * (np.diag(r) / np.abs(np.diag(r)))
+        ops.append(("KRAUS", a, b, [qm[4 * i:4 * i + 4, :] for i in range(4)]))
+    return ops
+
+
+def random_mixed_state(nq, seed, num_pure=8):
+    """sum_j w_j |psi_j><psi_j| (Dirichlet weights, Gaussian states) as a column-major flat
+    Choi vector (row = low bits)."""
+    rng = np.random.default_rng(seed)
+    w = rng.dirichlet(np.ones(num_pure))
+    dim = 1 << nq
+    psi = rng.standard_normal((dim, num_pure)) + 1j * rng.standard_normal((dim, num_pure))
+    psi /= np.linalg.norm(psi, axis=0)
+    rho = (psi * w) @ psi.conj().T
+    return np.ascontiguousarray(rho.T).reshape(-1)
+
+
+def run_dm(args, world, rank, local, dist):
+    """The density-matrix method (14-qubit density matrix: a 28-qubit Choi vector, 4 GiB)
+    through the QuEST-named API: 30 layers of unitaries, depolarising on every qubit and a
+    2-qubit Kraus map, then calcPurity and 16 Pauli expectation values.  One step is the
+    whole circuit from the same input state.  Also the time of each kind of operation on
+    its own (per call, from CUDA events), and the CPU oracle on the first layer."""
+    import ctypes as C
+    from quest_gb300 import _lib, api
+    from quest_gb300.api import Q, comp_matr1, comp_matr2, kraus_map
+    L = _lib.lib()
+    _lib.check(L.qg_init(local))
+    api.init_env()
+    ms_buf, cnt = (C.c_double * 12)(), C.c_int(0)
+    _lib.check(L.qg_autotune_fp64(28, ms_buf, 12, C.byref(cnt)))
+    nq = args.qubits if "--qubits" in sys.argv else 14
+    layers = args.depth if "--depth" in sys.argv else 30
+    ops = dm_layers(nq, layers, seed=0x5155455354 + 3)
+    rng = np.random.default_rng(0x5155455354 + 3)
+    codes = [[int(v) for v in rng.integers(0, 4, nq)] for _ in range(16)]
+    state = random_mixed_state(nq, seed=0x5155455354 + 3)
+    nbytes = 16 << (2 * nq)
+    prepared = []
+    for op in ops:
+        if op[0] == "U1":
+            prepared.append((0, op[1], comp_matr1(op[2])))
+        elif op[0] == "U2":
+            prepared.append((1, (op[1], op[2]), comp_matr2(op[3])))
+        elif op[0] == "DEPOL":
+            prepared.append((2, op[1], op[2]))
+        else:
+            prepared.append((3, (C.c_int * 2)(op[1], op[2]), kraus_map(op[3])))
+    strs = (api.PauliStr * 16)(*[api.pauli_str(c) for c in codes])
+    vals = (C.c_double * 16)()
+    q = Q.createDensityQureg(nq)
+    host = np.ctypeslib.as_array(C.cast(q.cpuAmps, C.POINTER(C.c_double)), shape=(2 << (2 * nq),))
+    host[:] = state.view(np.float64)
+    in_ptr = C.cast(q.cpuAmps, C.c_void_p)
+
+    def apply(op):
+        k = op[0]
+        if k == 0:
+            Q.applyCompMatr1(q, op[1], op[2])
+        elif k == 1:
+            Q.applyCompMatr2(q, op[1][0], op[1][1], op[2])
+        elif k == 2:
+            Q.mixDepolarising(q, op[1], op[2])
+        else:
+            Q.mixKrausMap(q, op[1], 2, op[2])
+
+    def step():
+        Q.setDensityQuregFlatAmps(q, 0, in_ptr, 1 << (2 * nq))
+        for op in prepared:
+            apply(op)
+        purity = Q.calcPurity(q)
+        Q.calcExpecPauliStrs(vals, q, strs, 16)
+        return purity
+
+    for _ in range(args.warmup):
+        step()
+    L.qg_sync()
+    e0, e1 = C.c_void_p(), C.c_void_p()
+    L.qg_event_create(C.byref(e0))
+    L.qg_event_create(C.byref(e1))
+    launches0 = C.c_int64(0)
+    L.qg_get_launch_count(C.byref(launches0))
+    with ClockSampler(local) as clocks:
+        barrier(dist)
+        L.qg_sync()
+        L.qg_event_record(e0, None)
+        for _ in range(args.steps):
+            purity = step()
+        L.qg_event_record(e1, None)
+        L.qg_sync()
+        barrier(dist)
+    launches1 = C.c_int64(0)
+    L.qg_get_launch_count(C.byref(launches1))
+    ms = C.c_float(0)
+    L.qg_event_elapsed_ms(e0, e1, C.byref(ms))
+    t = max_over_ranks(dist, ms.value / 1e3)
+    # each kind of operation alone, per call (a deferred one-qubit op is applied by the sync)
+    per_op = {}
+    kinds = {0: "applyCompMatr1 (one-qubit unitary)", 1: "applyCompMatr2 (two-qubit unitary, ket and bra passes)",
+             2: "mixDepolarising", 3: "mixKrausMap (2 qubits, 4 operators: a 4-target superoperator)"}
+    for k, name in kinds.items():
+        sample = [op for op in prepared if op[0] == k][:8]
+        L.qg_sync()
+        L.qg_event_record(e0, None)
+        for op in sample:
+            apply(op)
+            if k in (0, 2):
+                Q.syncQuESTEnv()        # applies the op now (it is deferred otherwise)
+        L.qg_event_record(e1, None)
+        L.qg_event_elapsed_ms(e0, e1, C.byref(ms))
+        per = ms.value / len(sample)
+        passes = 2 if k == 1 else 1
+        per_op[name] = {"ms": round(per, 4), "gbs": round(passes * 2 * nbytes / per / 1e6, 1)}
+    # the fused pair the circuit produces most: a one-qubit unitary followed by depolarising
+    L.qg_sync()
+    L.qg_event_record(e0, None)
+    for t_ in range(8):
+        Q.applyCompMatr1(q, t_ % nq, prepared[0][2])
+        Q.mixDepolarising(q, t_ % nq, 0.01)
+        Q.syncQuESTEnv()
+    L.qg_event_record(e1, None)
+    L.qg_event_elapsed_ms(e0, e1, C.byref(ms))
+    per_op["applyCompMatr1 + mixDepolarising on one qubit (one fused pass)"] = {
+        "ms": round(ms.value / 8, 4), "gbs": round(2 * nbytes / (ms.value / 8) / 1e6, 1)}
+    Q.destroyQureg(q)
+    ops_count = {name: sum(1 for op in prepared if op[0] == k) for k, name in kinds.items()}
+    alg_bytes = sum((2 if op[0] == 1 else 1) * 2 * nbytes for op in prepared) + nbytes * 2   # + purity and the state load
+    cpu = None
+    if rank == 0 and args.cpu_sample > 0:
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import qcircuits as qc
+        lines = []
+        first = [op for op in ops][:2 * nq + 1] if ops[0][0] == "U1" else ops[:nq]
+        cbytes = 0
+        for op in first:
+            if op[0] == "U1":
+                lines.append(f"U1 {op[1]} {qc.mat_tokens(op[2])}"); cbytes += 2 * 2 * nbytes
+            elif op[0] == "DEPOL":
+                lines.append(f"DEPOL {op[1]} {qc.fmt(op[2])}"); cbytes += 2 * nbytes
+            elif op[0] == "U2":
+                lines.append(f"U2 {op[1]} {op[2]} {qc.mat_tokens(op[3])}"); cbytes += 2 * 2 * nbytes
+            else:
+                lines.append(f"KRAUS 2 {op[1]} {op[2]} 4 " + " ".join(qc.mat_tokens(m) for m in op[3])); cbytes += 2 * nbytes
+        orc = qc.oracle()
+        threads = host_threads()
+        orc.lib.orc_set_num_threads(threads)
+        amps = state.copy()
+        res, outs = np.zeros(8), np.zeros(8, dtype=np.int32)
+        nr, no = C.c_int(0), C.c_int(0)
+        t0 = time.perf_counter()
+        orc.fn(("\n".join(lines) + "\n").encode(), nq, 1, amps.ctypes.data, res.ctypes.data, 8, C.byref(nr),
+               outs.ctypes.data, 8, C.byref(no))
+        secs = time.perf_counter() - t0
+        cpu = {"value": round(cbytes / secs / 1e9, 3), "unit": "GB/s", "cores": threads, "kind": "port",
+               "sample": f"the first {len(lines)} operations (unitaries and depolarising of layer 1, the reference's "
+                         f"two passes per unitary) in {secs:.1f} s on {threads} host threads with the OpenMP oracle"}
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    peak = peaks.get("hbm_gbs", 6800.0)
+    gbs = world * args.steps * alg_bytes / t / 1e9
+    line = {"metric": "density-matrix method: GB/s of the whole circuit (algorithmic bytes of the reference's passes) and ms per layer",
+            "value": round(gbs, 1), "unit": "GB/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(t / args.steps * 1e3, 2), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64 (storage; products in block-floating fixed point)",
+            "data": "synthetic (seeded mixed state of 8 Gaussian pure states, Dirichlet weights; seeded Haar gates and Kraus maps)",
+            "config": {"workload": f"{nq}-qubit FP64 density matrix ({2 * nq}-qubit Choi vector), {layers} layers of "
+                                   f"unitaries + mixDepolarising(0.01) on every qubit + a 2-qubit 4-operator Kraus map, then "
+                                   f"calcPurity and 16 Pauli expectations", "qubits": nq, "layers": layers,
+                       "ops": ops_count, "l2": "state larger than L2; no flush",
+                       "bytes": "per op 2 x 16 B x 4^N (the reference's passes: two for a unitary) + state load + purity"},
+            "ms_per_layer": round(t / args.steps / layers * 1e3, 3),
+            "frac_of_hbm": round(gbs / world / peak, 4), "per_op": per_op,
+            "final_purity": purity, "expec": list(vals), "gpu_launches": int(launches1.value - launches0.value),
+            "cpu_baseline": cpu, "clocks": clocks.summary()}
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -1087,10 +1299,11 @@ def main():
     ap.add_argument("--depth", type=int, default=20)
     ap.add_argument("--cpu-sample", type=int, default=45, help="gates of the circuit timed on the host CPU")
     ap.add_argument("--traffic", type=float, default=None, help="ncu DRAM bytes per dense launch, if captured")
-    ap.add_argument("--config", default="plain", choices=["plain", "precision", "serve", "gates", "blocks", "expec"],
+    ap.add_argument("--config", default="plain", choices=["plain", "precision", "serve", "gates", "blocks", "expec", "dm"],
                     help="plain: the 30-qubit FP64 per-gate circuit (default); precision: FP32 fused blocks; "
                          "serve: request stream, served vs plain; gates: per-gate-kind timing (28 qubits); "
-                         "blocks: one FP32 5-qubit block per target set; expec: 16 Pauli strings per call (28 qubits)")
+                         "blocks: one FP32 5-qubit block per target set; expec: 16 Pauli strings per call (28 qubits); "
+                         "dm: the density-matrix method (14-qubit density matrix, 30 layers)")
     ap.add_argument("--block-targets", default="", help="blocks: target sets, e.g. '0,1,2,3,4;5,6,7,8,9'")
     ap.add_argument("--requests", type=int, default=48)
     ap.add_argument("--min-qubits", type=int, default=8)
@@ -1115,6 +1328,8 @@ def main():
         run_blocks(args, world, rank, local, dist)
     elif args.config == "expec":
         run_expec(args, world, rank, local, dist)
+    elif args.config == "dm":
+        run_dm(args, world, rank, local, dist)
     elif args.config == "precision":
         if args.qubits == 30 and "--qubits" not in sys.argv:
             args.qubits = 32

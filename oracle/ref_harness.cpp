@@ -57,13 +57,21 @@ static CompMatr mK(int k, const vector<double>& d) {
 }
 static DiagMatr dK(int k, const vector<double>& d) { DiagMatr m = createDiagMatr(k); setDiagMatr(m, toC(d)); return m; }
 
+// REF_HARNESS_GPU=1 builds the same runner against a QuEST built with its GPU backend
+// (the drop-in of this repository): GPU-accelerated Quregs, amplitudes moved through the
+// host mirror with syncQuregToGpu / syncQuregFromGpu (no-ops for CPU Quregs).
+#ifndef REF_HARNESS_GPU
+#define REF_HARNESS_GPU 0
+#endif
+
 extern "C" int ref_run_circuit(const char* text, int numQubits, int isDensMatr, double* amps,
                                double* results, int maxResults, int* numResults,
                                int* outcomes, int maxOutcomes, int* numOutcomes) {
     static bool envUp = false;
-    if (!envUp) { initCustomQuESTEnv(0, 0, 1); envUp = true; }
-    Qureg q = createCustomQureg(numQubits, isDensMatr, 0, 0, 1);
+    if (!envUp) { initCustomQuESTEnv(0, REF_HARNESS_GPU, !REF_HARNESS_GPU); envUp = true; }
+    Qureg q = createCustomQureg(numQubits, isDensMatr, 0, REF_HARNESS_GPU, !REF_HARNESS_GPU);
     std::memcpy(q.cpuAmps, amps, sizeof(qcomp) * q.numAmps);
+    syncQuregToGpu(q);
     vector<double> res; vector<int> outs;
     { unsigned s0 = 0; setSeeds(&s0, 1); }
 
@@ -186,6 +194,7 @@ extern "C" int ref_run_circuit(const char* text, int numQubits, int isDensMatr, 
         }
         else { g_err = "unknown op " + op; rc = -1; break; }
     }
+    syncQuregFromGpu(q);
     std::memcpy(amps, q.cpuAmps, sizeof(qcomp) * q.numAmps);
     destroyQureg(q);
     if (numResults) *numResults = (int)res.size();

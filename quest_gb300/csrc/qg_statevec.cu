@@ -328,7 +328,9 @@ __device__ __forceinline__ void coop_rows(const qgfx::OpN<N>& C, const int2 (*li
     int64_t hh[8], mid[8];
 #pragma unroll
     for (int i = 0; i < 8; i++) { hh[i] = 0; mid[i] = 0; }
-#pragma unroll 4
+    // fully unrolled: every coefficient is a compile-time constant-bank operand (a run-time
+    // index would turn each into a constant-bank load)
+#pragma unroll
     for (int j = 0; j < N; j++) {
         const int2 L = limbs[j][lane];
 #pragma unroll

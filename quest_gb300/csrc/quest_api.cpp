@@ -67,9 +67,109 @@ inline qcomp_t Q(cd c) { return qcomp_t{c.real(), c.imag()}; }
 
 bool checkEnv(const char* func) { return check(g_envInit, func, "The QuEST environment has not been initialised."); }
 
-bool checkQureg(const Qureg& q, const char* func) {
+// ------------------------------------------------------------------ deferred one-qubit superoperators
+// On a density matrix, a one-qubit unitary and a one-qubit channel act on the pair
+// (ket q, bra q+N) of the Choi vector as a 4x4 superoperator (matrix index bit 0 = ket,
+// bit 1 = bra).  Such operations are not applied at once: per ket qubit they are
+// multiplied into one pending 4x4 in FP64 on the host, and the product is applied in
+// one pass when something needs the state -- any other API call on the Qureg (all
+// pending qubits), or a multi-qubit operation (only the qubits it touches: operations on
+// other qubits commute with it).  A unitary followed by depolarising on the same qubit
+// then costs one pass instead of two.  A qubit whose only pending operation is a single
+// channel is applied with that channel's own kernel.
+enum { PEND_GENERAL = 0, PEND_DEPOL, PEND_DEPHASE, PEND_DAMP, PEND_PAULIS };
+struct PendingOp {
+    int kind;
+    double p[3];      // the channel's parameters when kind is not PEND_GENERAL
+    cd m[16];         // the product of the qubit's pending superoperators, row-major
+};
+struct PendingSet {
+    int numQubits;                      // the Qureg's (ket) qubits
+    std::map<int, PendingOp> ops;       // ket qubit -> its pending op
+};
+std::map<const void*, PendingSet> g_pending;   // keyed by gpuAmps
+std::mutex g_pendingMu;
+
+bool backend(int rc, const char* func);
+
+bool applyPendingOp(const Qureg& q, int qubit, const PendingOp& op, const char* func) {
+    const int N = q.numQubits;
+    switch (op.kind) {
+        case PEND_DEPOL: return backend(qg_dm_oneQubitDepolarising(q.gpuAmps, N, qubit, op.p[0], g_stream), func);
+        case PEND_DEPHASE: return backend(qg_dm_oneQubitDephasing(q.gpuAmps, N, qubit, op.p[0], g_stream), func);
+        case PEND_DAMP: return backend(qg_dm_oneQubitDamping(q.gpuAmps, N, qubit, op.p[0], g_stream), func);
+        case PEND_PAULIS: return backend(qg_dm_oneQubitPauliChannel(q.gpuAmps, N, qubit, op.p[0], op.p[1], op.p[2], g_stream), func);
+        default: {
+            qcomp_t k[16];
+            for (int i = 0; i < 16; i++) k[i] = qcomp_t{op.m[i].real(), op.m[i].imag()};
+            return backend(qg_sv_anyCtrlTwoTargDenseMatr(q.gpuAmps, 2 * N, nullptr, nullptr, 0, qubit, qubit + N, k, g_stream), func);
+        }
+    }
+}
+
+// applies the pending ops of the listed ket qubits (all of them when `qubits` is null)
+bool flushPending(const Qureg& q, const std::vector<int>* qubits, const char* func) {
+    std::vector<std::pair<int, PendingOp>> todo;
+    {
+        std::lock_guard<std::mutex> lock(g_pendingMu);
+        auto it = g_pending.find(q.gpuAmps);
+        if (it == g_pending.end()) return true;
+        if (!qubits) {
+            for (auto& kv : it->second.ops) todo.push_back(kv);
+            g_pending.erase(it);
+        } else {
+            for (int b : *qubits) {
+                auto jt = it->second.ops.find(b);
+                if (jt == it->second.ops.end()) continue;
+                todo.push_back(*jt);
+                it->second.ops.erase(jt);
+            }
+            if (it->second.ops.empty()) g_pending.erase(it);
+        }
+    }
+    for (auto& kv : todo)
+        if (!applyPendingOp(q, kv.first, kv.second, func)) return false;
+    return true;
+}
+
+// forgets the pending ops of a Qureg whose state is about to be overwritten or freed
+void discardPending(const Qureg& q) {
+    std::lock_guard<std::mutex> lock(g_pendingMu);
+    g_pending.erase(q.gpuAmps);
+}
+
+// S applied after the qubit's pending op: pending = S * pending
+void addPending(const Qureg& q, int qubit, const cd (&S)[16], int kind, double p0 = 0, double p1 = 0, double p2 = 0) {
+    std::lock_guard<std::mutex> lock(g_pendingMu);
+    PendingSet& set = g_pending[q.gpuAmps];
+    set.numQubits = q.numQubits;
+    auto& ops = set.ops;
+    auto it = ops.find(qubit);
+    if (it == ops.end()) {
+        PendingOp op;
+        op.kind = kind;
+        op.p[0] = p0; op.p[1] = p1; op.p[2] = p2;
+        for (int i = 0; i < 16; i++) op.m[i] = S[i];
+        ops[qubit] = op;
+        return;
+    }
+    PendingOp& op = it->second;
+    cd prod[16];
+    for (int r = 0; r < 4; r++)
+        for (int c = 0; c < 4; c++) {
+            cd acc = 0;
+            for (int k = 0; k < 4; k++) acc += S[r * 4 + k] * op.m[k * 4 + c];
+            prod[r * 4 + c] = acc;
+        }
+    for (int i = 0; i < 16; i++) op.m[i] = prod[i];
+    op.kind = PEND_GENERAL;
+}
+
+// checks the Qureg and, unless `keepPending`, applies its deferred ops first
+bool checkQureg(const Qureg& q, const char* func, bool keepPending = false) {
     if (!checkEnv(func)) return false;
-    return check(q.gpuAmps != nullptr && q.numQubits >= 1, func, "Invalid Qureg; it was not created, or was destroyed.");
+    if (!check(q.gpuAmps != nullptr && q.numQubits >= 1, func, "Invalid Qureg; it was not created, or was destroyed.")) return false;
+    return keepPending || flushPending(q, nullptr, func);
 }
 
 bool checkQubits(const Qureg& q, const int* qs, int n, const char* func, const char* what) {
@@ -139,26 +239,31 @@ bool denseSV(const Qureg& q, const vector<int>& c, const vector<int>& s, const v
 
 // validateAndApplyAnyCtrlAnyTargUnitaryMatrix: operations.cpp:36-63
 void applyDense(const Qureg& q, const int* ctrls, const int* states, int nc, const int* targs, int nt, const qcomp_t* m, bool checkUnitary, const char* func) {
-    if (!checkQureg(q, func)) return;
+    if (!checkQureg(q, func, q.isDensityMatrix != 0)) return;
     if (!checkCtrlsTargs(q, ctrls, nc, targs, nt, func)) return;
     if (!checkStates(states, nc, func)) return;
     if (!check(nt >= 1, func, "At least one target qubit is required.")) return;
     if (checkUnitary && !check(isUnitaryDense(m, (qindex)1 << nt), func, "The given matrix was not (approximately) unitary.")) return;
     vector<int> c = V(ctrls, nc), s = V(states, nc), t = V(targs, nt);
     if (q.isDensityMatrix && nt == 1 && nc == 0) {
-        // U rho U^dagger in one pass: U on the ket qubit and conj(U) on its bra partner commute,
-        // and together they are the 4x4 operator conj(U) (x) U on the pair (t, t + N) -- the
-        // same 16 complex products per 4 amplitudes as the reference's two passes
-        // (localiser_statevec_anyCtrlOneTargDenseMatr on the ket, then on the conjugated bra),
-        // with one read and one write of the state instead of two.
-        qcomp_t k[16];
+        // U rho U^dagger as one superoperator: U on the ket qubit and conj(U) on its bra
+        // partner commute, and together they are the 4x4 operator conj(U) (x) U on the pair
+        // (t, t + N) -- the same 16 complex products per 4 amplitudes as the reference's two
+        // passes (localiser_statevec_anyCtrlOneTargDenseMatr on the ket, then on the
+        // conjugated bra).  It joins the qubit's pending superoperator (applied in one pass).
+        cd k[16];
         for (int r1 = 0; r1 < 2; r1++)
             for (int r0 = 0; r0 < 2; r0++)
                 for (int c1 = 0; c1 < 2; c1++)
                     for (int c0 = 0; c0 < 2; c0++)
-                        k[((r1 << 1) | r0) * 4 + ((c1 << 1) | c0)] = Q(std::conj(C(m[r1 * 2 + c1])) * C(m[r0 * 2 + c0]));
-        backend(qg_sv_anyCtrlTwoTargDenseMatr(q.gpuAmps, nsv(q), nullptr, nullptr, 0, t[0], t[0] + q.numQubits, k, g_stream), func);
+                        k[((r1 << 1) | r0) * 4 + ((c1 << 1) | c0)] = std::conj(C(m[r1 * 2 + c1])) * C(m[r0 * 2 + c0]);
+        addPending(q, t[0], k, PEND_GENERAL);
         return;
+    }
+    if (q.isDensityMatrix) {
+        vector<int> touched = c;
+        touched.insert(touched.end(), t.begin(), t.end());
+        if (!flushPending(q, &touched, func)) return;
     }
     if (!denseSV(q, c, s, t, m, false, func)) return;
     if (!q.isDensityMatrix) return;
@@ -307,7 +412,25 @@ void finalizeQuESTEnv(void) {
 
 int isQuESTEnvInit(void) { return g_envInit ? 1 : 0; }
 
-void syncQuESTEnv(void) { backend(qg_sync(), "syncQuESTEnv"); }
+void syncQuESTEnv(void) {
+    // deferred one-qubit superoperators of every density matrix are applied first
+    std::vector<std::pair<const void*, PendingSet>> all;
+    {
+        std::lock_guard<std::mutex> lock(g_pendingMu);
+        for (auto& kv : g_pending) all.push_back(kv);
+        g_pending.clear();
+    }
+    for (auto& kv : all) {
+        Qureg q;
+        std::memset(&q, 0, sizeof(q));
+        q.gpuAmps = (qcomp_t*)kv.first;
+        q.numQubits = kv.second.numQubits;
+        q.isDensityMatrix = 1;
+        for (auto& op : kv.second.ops)
+            if (!applyPendingOp(q, op.first, op.second, "syncQuESTEnv")) return;
+    }
+    backend(qg_sync(), "syncQuESTEnv");
+}
 
 void setInputErrorHandler(void (*callback)(const char*, const char*)) { g_handler = callback ? callback : default_handler; }
 
@@ -400,7 +523,8 @@ Qureg createCloneQureg(Qureg qureg) {
 }
 
 void destroyQureg(Qureg qureg) {
-    if (!checkQureg(qureg, "destroyQureg")) return;
+    if (!checkQureg(qureg, "destroyQureg", true)) return;
+    discardPending(qureg);
     qg_sync();
     qg_free(qureg.gpuAmps);
     int kind = MIRROR_PINNED;
@@ -430,7 +554,8 @@ int isQuregHostMirrorPinned(Qureg qureg) {
 }
 
 void syncQuregToGpu(Qureg q) {
-    if (!checkQureg(q, "syncQuregToGpu")) return;
+    if (!checkQureg(q, "syncQuregToGpu", true)) return;
+    discardPending(q);      // the host copy replaces the whole state
     backend(qg_copy_h2d(q.gpuAmps, q.cpuAmps, (int64_t)(sizeof(qcomp_t) * q.numAmps), g_stream), "syncQuregToGpu");
 }
 
@@ -458,36 +583,43 @@ void initZeroState(Qureg q) { initClassicalState(q, 0); }
 
 void initPlusState(Qureg q) {
     const char* func = "initPlusState";
-    if (!checkQureg(q, func)) return;
+    if (!checkQureg(q, func, true)) return;
+    discardPending(q);
     double v = q.isDensityMatrix ? 1.0 / (double)((qindex)1 << q.numQubits) : 1.0 / std::sqrt((double)((qindex)1 << q.numQubits));
     backend(qg_sv_initUniformState(q.gpuAmps, nsv(q), qcomp_t{v, 0}, g_stream), func);
 }
 
 void initClassicalState(Qureg q, qindex ind) {
     const char* func = "initClassicalState";
-    if (!checkQureg(q, func)) return;
+    if (!checkQureg(q, func, true)) return;
     qindex dim = (qindex)1 << q.numQubits;
     if (!check(ind >= 0 && ind < dim, func, "Invalid basis state index.")) return;
     qindex flat = q.isDensityMatrix ? ind * (dim + 1) : ind;
+    discardPending(q);
     backend(qg_sv_initClassicalState(q.gpuAmps, nsv(q), flat, g_stream), func);
 }
 
 void initDebugState(Qureg q) {
-    if (!checkQureg(q, "initDebugState")) return;
+    if (!checkQureg(q, "initDebugState", true)) return;
+    discardPending(q);
     backend(qg_sv_initDebugState(q.gpuAmps, nsv(q), g_stream), "initDebugState");
 }
 
 void setQuregAmps(Qureg q, qindex start, qcomp_t* amps, qindex num) {
     const char* func = "setQuregAmps";
-    if (!checkQureg(q, func)) return;
+    if (!checkQureg(q, func, true)) return;
     if (!check(start >= 0 && num >= 0 && start + num <= q.numAmps, func, "Invalid amplitude range.")) return;
+    if (start == 0 && num == q.numAmps) discardPending(q);      // every amplitude is overwritten
+    else if (!flushPending(q, nullptr, func)) return;
     backend(qg_copy_h2d(q.gpuAmps + start, amps, (int64_t)(sizeof(qcomp_t) * num), g_stream), func);
 }
 
 void setDensityQuregFlatAmps(Qureg q, qindex start, qcomp_t* amps, qindex num) {
     const char* func = "setDensityQuregFlatAmps";
-    if (!checkQureg(q, func) || !checkDensMatr(q, func)) return;
+    if (!checkQureg(q, func, true) || !checkDensMatr(q, func)) return;
     if (!check(start >= 0 && num >= 0 && start + num <= q.numAmps, func, "Invalid amplitude range.")) return;
+    if (start == 0 && num == q.numAmps) discardPending(q);
+    else if (!flushPending(q, nullptr, func)) return;
     backend(qg_copy_h2d(q.gpuAmps + start, amps, (int64_t)(sizeof(qcomp_t) * num), g_stream), func);
 }
 
@@ -897,57 +1029,79 @@ qreal applyForcedQubitMeasurement(Qureg q, int t, int o) {
 
 // ====================================================================== decoherence (decoherence.cpp:31-131)
 
+// The one-qubit channels join the qubit's pending superoperator (index bit 0 = ket,
+// bit 1 = bra); their factors are those of the reference's kernels
+// (utilities.cpp:916-990, cpu_subroutines.cpp:1060-1600).
 void mixDephasing(Qureg q, int qubit, qreal prob) {
     const char* func = "mixDephasing";
-    if (!checkQureg(q, func) || !checkQubits(q, &qubit, 1, func, "target qubits") || !checkProb(prob, 0.5, func)) return;
+    if (!checkQureg(q, func, q.isDensityMatrix != 0) || !checkQubits(q, &qubit, 1, func, "target qubits") || !checkProb(prob, 0.5, func)) return;
     if (prob == 0) return;
     if (!checkDensMatr(q, func)) return;
-    backend(qg_dm_oneQubitDephasing(q.gpuAmps, q.numQubits, qubit, prob, g_stream), func);
+    const double f = 1 - 2 * prob;    // util_getOneQubitDephasingFactor (utilities.cpp:918-921)
+    cd S[16] = {};
+    S[0] = 1; S[5] = f; S[10] = f; S[15] = 1;
+    addPending(q, qubit, S, PEND_DEPHASE, prob);
 }
 void mixTwoQubitDephasing(Qureg q, int a, int b, qreal prob) {
     const char* func = "mixTwoQubitDephasing";
     int t[2] = {a, b};
-    if (!checkQureg(q, func) || !checkQubits(q, t, 2, func, "target qubits") || !checkProb(prob, 0.75, func)) return;
+    if (!checkQureg(q, func, q.isDensityMatrix != 0) || !checkQubits(q, t, 2, func, "target qubits") || !checkProb(prob, 0.75, func)) return;
     if (prob == 0) return;
     if (!checkDensMatr(q, func)) return;
+    vector<int> touched = {a, b};
+    if (!flushPending(q, &touched, func)) return;
     backend(qg_dm_twoQubitDephasing(q.gpuAmps, q.numQubits, a, b, prob, g_stream), func);
 }
 void mixDepolarising(Qureg q, int qubit, qreal prob) {
     const char* func = "mixDepolarising";
-    if (!checkQureg(q, func) || !checkQubits(q, &qubit, 1, func, "target qubits") || !checkProb(prob, 0.75, func)) return;
+    if (!checkQureg(q, func, q.isDensityMatrix != 0) || !checkQubits(q, &qubit, 1, func, "target qubits") || !checkProb(prob, 0.75, func)) return;
     if (prob == 0) return;
     if (!checkDensMatr(q, func)) return;
-    backend(qg_dm_oneQubitDepolarising(q.gpuAmps, q.numQubits, qubit, prob, g_stream), func);
+    // util_getOneQubitDepolarisingFactors (utilities.cpp:932-947)
+    const double c1 = 1 - 2 * prob / 3, c2 = 2 * prob / 3, c3 = 1 - 4 * prob / 3;
+    cd S[16] = {};
+    S[0] = c1; S[3] = c2; S[5] = c3; S[10] = c3; S[12] = c2; S[15] = c1;
+    addPending(q, qubit, S, PEND_DEPOL, prob);
 }
 void mixTwoQubitDepolarising(Qureg q, int a, int b, qreal prob) {
     const char* func = "mixTwoQubitDepolarising";
     int t[2] = {a, b};
-    if (!checkQureg(q, func) || !checkQubits(q, t, 2, func, "target qubits") || !checkProb(prob, 15.0 / 16, func)) return;
+    if (!checkQureg(q, func, q.isDensityMatrix != 0) || !checkQubits(q, t, 2, func, "target qubits") || !checkProb(prob, 15.0 / 16, func)) return;
     if (prob == 0) return;
     if (!checkDensMatr(q, func)) return;
+    vector<int> touched = {a, b};
+    if (!flushPending(q, &touched, func)) return;
     backend(qg_dm_twoQubitDepolarising(q.gpuAmps, q.numQubits, a, b, prob, g_stream), func);
 }
 void mixDamping(Qureg q, int qubit, qreal prob) {
     const char* func = "mixDamping";
-    if (!checkQureg(q, func) || !checkQubits(q, &qubit, 1, func, "target qubits") || !checkProb(prob, 1.0, func)) return;
+    if (!checkQureg(q, func, q.isDensityMatrix != 0) || !checkQubits(q, &qubit, 1, func, "target qubits") || !checkProb(prob, 1.0, func)) return;
     if (prob == 0) return;
     if (!checkDensMatr(q, func)) return;
-    backend(qg_dm_oneQubitDamping(q.gpuAmps, q.numQubits, qubit, prob, g_stream), func);
+    const double c1 = std::sqrt(1 - prob), c2 = 1 - prob;   // util_getOneQubitDampingFactors (utilities.cpp:977-988)
+    cd S[16] = {};
+    S[0] = 1; S[3] = prob; S[5] = c1; S[10] = c1; S[15] = c2;
+    addPending(q, qubit, S, PEND_DAMP, prob);
 }
 void mixPaulis(Qureg q, int qubit, qreal px, qreal py, qreal pz) {
     const char* func = "mixPaulis";
-    if (!checkQureg(q, func) || !checkQubits(q, &qubit, 1, func, "target qubits")) return;
+    if (!checkQureg(q, func, q.isDensityMatrix != 0) || !checkQubits(q, &qubit, 1, func, "target qubits")) return;
     if (!checkProb(px, 1, func) || !checkProb(py, 1, func) || !checkProb(pz, 1, func)) return;
     if (px == 0 && py == 0 && pz == 0) return;
     if (!checkDensMatr(q, func)) return;
-    backend(qg_dm_oneQubitPauliChannel(q.gpuAmps, q.numQubits, qubit, px, py, pz, g_stream), func);
+    // util_getOneQubitPauliChannelFactors (utilities.cpp:962-975)
+    const double pI = 1 - px - py - pz;
+    const double fAA = pI + pz, fBB = px + py, fAB = pI - pz, fBA = px - py;
+    cd S[16] = {};
+    S[0] = fAA; S[3] = fBB; S[5] = fAB; S[6] = fBA; S[9] = fBA; S[10] = fAB; S[12] = fBB; S[15] = fAA;
+    addPending(q, qubit, S, PEND_PAULIS, px, py, pz);
 }
 
 // mixKrausMap: the superoperator as a dense matrix on targets {ket..., bra...}
 // (localiser_densmatr_superoperator, localiser.cpp:1670-1686), not conjugated
 void mixKrausMap(Qureg q, int* qubits, int n, KrausMap map) {
     const char* func = "mixKrausMap";
-    if (!checkQureg(q, func) || !checkDensMatr(q, func) || !checkQubits(q, qubits, n, func, "target qubits")) return;
+    if (!checkQureg(q, func, q.isDensityMatrix != 0) || !checkDensMatr(q, func) || !checkQubits(q, qubits, n, func, "target qubits")) return;
     if (!check(map.numQubits == n && map.superop.cpuElemsFlat, func, "The Kraus map size does not match the number of targets.")) return;
     // util_isCPTP (utilities.cpp:729-768): sum_n K_n^dagger K_n = I within eps (squared distance)
     if (*map.isApproxCPTP == -1) {
@@ -962,6 +1116,15 @@ void mixKrausMap(Qureg q, int* qubits, int n, KrausMap map) {
         *map.isApproxCPTP = ok;
     }
     if (!check(*map.isApproxCPTP == 1, func, "The Kraus map is not (approximately) completely positive and trace preserving.")) return;
+    if (n == 1) {
+        // a one-qubit map joins the qubit's pending superoperator
+        cd S[16];
+        for (int i = 0; i < 16; i++) S[i] = C(map.superop.cpuElemsFlat[i]);
+        addPending(q, qubits[0], S, PEND_GENERAL);
+        return;
+    }
+    vector<int> touched(qubits, qubits + n);
+    if (!flushPending(q, &touched, func)) return;
     vector<int> t(qubits, qubits + n);
     for (int i = 0; i < n; i++) t.push_back(qubits[i] + q.numQubits);
     denseSV(q, {}, {}, t, map.superop.cpuElemsFlat, false, func);

@@ -187,3 +187,84 @@ def test_pauli_str_sum_validation(env):
         Q.destroyPauliStrSum(wide)
     finally:
         Q.destroyQureg(q)
+
+
+@pytest.mark.parametrize("nq,seed", [(3, 1), (6, 2), (9, 3)])
+def test_deferred_density_matrix_superoperators(env, nq, seed):
+    """One-qubit unitaries and channels on a density matrix are multiplied into one
+    pending superoperator per qubit and applied when something needs the state; random
+    interleavings with two-qubit operations (which apply only the qubits they touch),
+    controlled gates, rotations and reductions in between, against the oracle applying
+    every operation at once."""
+    rng = np.random.default_rng(900 + seed)
+    L = []
+    for step in range(60):
+        q = int(rng.integers(nq))
+        kind = int(rng.integers(12))
+        if kind == 0:
+            L.append(f"U1 {q} {qc.mat_tokens(qc.haar_unitary(2, rng))}")
+        elif kind == 1:
+            L.append(f"DEPOL {q} {qc.fmt(rng.uniform(0, 0.3))}")
+        elif kind == 2:
+            L.append(f"DEPHASE {q} {qc.fmt(rng.uniform(0, 0.3))}")
+        elif kind == 3:
+            L.append(f"DAMP {q} {qc.fmt(rng.uniform(0, 0.5))}")
+        elif kind == 4:
+            px, py, pz = rng.uniform(0, 0.1, 3)
+            L.append(f"PAULIS {q} {qc.fmt(px)} {qc.fmt(py)} {qc.fmt(pz)}")
+        elif kind == 5:
+            L.append(f"KRAUS 1 {q} 3 " + " ".join(qc.mat_tokens(o) for o in qc.random_kraus(1, 3, rng)))
+        elif kind == 6:
+            L.append(f"H {q}")
+        elif kind == 7 and nq >= 2:
+            a, b = (int(v) for v in rng.choice(nq, 2, replace=False))
+            L.append(f"U2 {a} {b} {qc.mat_tokens(qc.haar_unitary(4, rng))}")
+        elif kind == 8 and nq >= 2:
+            a, b = (int(v) for v in rng.choice(nq, 2, replace=False))
+            L.append(rng.choice([f"DEPOL2 {a} {b} {qc.fmt(rng.uniform(0, 0.3))}",
+                                 f"DEPHASE2 {a} {b} {qc.fmt(rng.uniform(0, 0.3))}",
+                                 f"KRAUS 2 {a} {b} 2 " + " ".join(qc.mat_tokens(o) for o in qc.random_kraus(2, 2, rng))]))
+        elif kind == 9 and nq >= 2:
+            a, b = (int(v) for v in rng.choice(nq, 2, replace=False))
+            L.append(f"CU1 1 {a} 1 {b} {qc.mat_tokens(qc.haar_unitary(2, rng))}")
+        elif kind == 10:
+            L.append(f"RY {q} {qc.fmt(rng.uniform(0, 6.3))}")
+        else:
+            L.append(rng.choice(["TOTALPROB", "PURITY", f"PROBQ {q} 0",
+                                 f"EXPEC {qc.pauli_text([int(v) for v in rng.integers(0, 4, nq)])}"]))
+    L += ["PURITY", f"EXPEC {'X' * nq}", "TOTALPROB"]
+    text = "\n".join(L) + "\n"
+    amps = qc.random_density_matrix(nq, 950 + seed)
+    a1, r1, _ = qc.oracle().run(text, nq, 1, amps)
+    a2, r2, _ = run_gpu(env, text, nq, 1, amps)
+    assert np.max(np.abs(a1 - a2)) <= TOL
+    assert np.max(np.abs(r1 - r2)) <= TOL
+
+
+def test_deferred_superoperators_applied_by_sync_and_overwritten_by_set(env):
+    """syncQuESTEnv applies the pending superoperators of every density matrix; a full
+    setDensityQuregFlatAmps replaces the state, pending operations included."""
+    import ctypes
+    Q = env.Q
+    nq = 4
+    amps = qc.random_density_matrix(nq, 77)
+    rng = np.random.default_rng(78)
+    u = qc.haar_unitary(2, rng)
+    text = f"U1 2 {qc.mat_tokens(u)}\nDEPOL 2 0.125\nDAMP 0 0.25\n"
+    want, _, _ = qc.oracle().run(text, nq, 1, amps)
+    q = Q.createDensityQureg(nq)
+    try:
+        env.set_amps(q, amps)
+        Q.applyCompMatr1(q, 2, env.comp_matr1(u))
+        Q.mixDepolarising(q, 2, 0.125)
+        Q.mixDamping(q, 0, 0.25)
+        Q.syncQuESTEnv()
+        raw = np.empty(1 << (2 * nq), dtype=np.complex128)     # the device state, read without the API
+        from quest_gb300 import _lib
+        _lib.check(_lib.lib().qg_copy_d2h(raw.ctypes.data, ctypes.cast(q.gpuAmps, ctypes.c_void_p), raw.nbytes, None))
+        assert np.max(np.abs(raw - want)) <= TOL
+        Q.mixDepolarising(q, 1, 0.3)         # pending, then overwritten
+        env.set_amps(q, amps)
+        assert np.max(np.abs(env.get_amps(q) - amps)) == 0
+    finally:
+        Q.destroyQureg(q)
