@@ -483,16 +483,17 @@ def run_gb300(args, world, rank, local, dist):
         "final_total_prob": norm,
     }
     if world == 1 and not args.no_extras:
-        line["precision_form"], line["serving"] = extras_summary(args, world, rank, local, dist)
+        line["precision_form"], line["serving"], line["density_matrix"] = extras_summary(args, world, rank, local, dist)
     if rank == 0:
         print(json.dumps(line), flush=True)
 
 
 def extras_summary(args, world, rank, local, dist):
     """The precision form (32-qubit FP32 fused blocks on the tensor cores, accuracy at 28
-    qubits) and the serving form (a short request set, served vs plain) in small, so the
-    default line records them beside the FP64 circuit.  A failure here is reported in
-    the line and does not lose the headline."""
+    qubits), the serving form (a short request set, served vs plain) and the
+    density-matrix method (14 qubits, 30 layers, one step) in small, so the default line
+    records them beside the FP64 circuit.  A failure here is reported in the line and does
+    not lose the headline."""
     precision = serving = None
     try:
         pa = argparse.Namespace(**vars(args))
@@ -513,7 +514,16 @@ def extras_summary(args, world, rank, local, dist):
                    "plain_registers": sl["plain_registers"]}
     except Exception as e:          # noqa: BLE001
         serving = {"error": f"{type(e).__name__}: {e}"}
-    return precision, serving
+    try:
+        da = argparse.Namespace(**vars(args))
+        da.steps, da.warmup, da.cpu_sample, da.dm_qubits, da.dm_layers = 1, 1, 1, 14, 30
+        dl = run_dm(da, world, rank, local, dist, emit=False)
+        dm = {"workload": dl["config"]["workload"], "steps": 1, "value_gbs": dl["value"], "frac_of_hbm": dl["frac_of_hbm"],
+              "ms_per_step": dl["ms_per_step"], "ms_per_layer": dl["ms_per_layer"], "per_op": dl["per_op"],
+              "final_purity": dl["final_purity"], "cpu_baseline": dl["cpu_baseline"]}
+    except Exception as e:          # noqa: BLE001
+        dm = {"error": f"{type(e).__name__}: {e}"}
+    return precision, serving, dm
 
 
 # ------------------------------------------------------------------ reference arm
@@ -1063,7 +1073,7 @@ def random_mixed_state(nq, seed, num_pure=8):
     return np.ascontiguousarray(rho.T).reshape(-1)
 
 
-def run_dm(args, world, rank, local, dist):
+def run_dm(args, world, rank, local, dist, emit=True):
     """The density-matrix method (14-qubit density matrix: a 28-qubit Choi vector, 4 GiB)
     through the QuEST-named API: 30 layers of unitaries, depolarising on every qubit and a
     2-qubit Kraus map, then calcPurity and 16 Pauli expectation values.  One step is the
@@ -1077,8 +1087,7 @@ def run_dm(args, world, rank, local, dist):
     api.init_env()
     ms_buf, cnt = (C.c_double * 12)(), C.c_int(0)
     _lib.check(L.qg_autotune_fp64(28, ms_buf, 12, C.byref(cnt)))
-    nq = args.qubits if "--qubits" in sys.argv else 14
-    layers = args.depth if "--depth" in sys.argv else 30
+    nq, layers = args.dm_qubits, args.dm_layers
     ops = dm_layers(nq, layers, seed=0x5155455354 + 3)
     rng = np.random.default_rng(0x5155455354 + 3)
     codes = [[int(v) for v in rng.integers(0, 4, nq)] for _ in range(16)]
@@ -1219,8 +1228,9 @@ def run_dm(args, world, rank, local, dist):
             "frac_of_hbm": round(gbs / world / peak, 4), "per_op": per_op,
             "final_purity": purity, "expec": list(vals), "gpu_launches": int(launches1.value - launches0.value),
             "cpu_baseline": cpu, "clocks": clocks.summary()}
-    if rank == 0:
+    if rank == 0 and emit:
         print(json.dumps(line), flush=True)
+    return line
 
 
 def run_blocks(args, world, rank, local, dist):
@@ -1329,6 +1339,8 @@ def main():
     elif args.config == "expec":
         run_expec(args, world, rank, local, dist)
     elif args.config == "dm":
+        args.dm_qubits = args.qubits if "--qubits" in sys.argv else 14
+        args.dm_layers = args.depth if "--depth" in sys.argv else 30
         run_dm(args, world, rank, local, dist)
     elif args.config == "precision":
         if args.qubits == 30 and "--qubits" not in sys.argv:

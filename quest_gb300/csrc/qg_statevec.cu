@@ -309,139 +309,115 @@ struct DenseKOp { typedef qgfx::OpN<2 << K> type; static constexpr bool complex 
 template <>
 struct DenseKOp<3> { typedef qgfx::CopN<8> type; static constexpr bool complex = true; };
 
-// k_denseK_fx with the work of a group shared by G/4 threads (K = 3, 4; G = 2^K
-// amplitudes, N = 2G reals per group).  Thread part p of a group loads amplitudes
-// 4p..4p+3 and forms outputs 4p..4p+3 (real rows 8p..8p+7 of the operator).  The
-// threads of a part sit in one warp, 32 groups side by side, so every operator
-// coefficient a warp reads is one compile-time constant-bank operand (the per-thread
-// kernel indexes rows at run time and spends its issue on constant-bank address
-// loads), and the G/4 warps of a group set exchange the group's scale and limbs
-// through shared memory.  The arithmetic is fx_prepare_e / fx_row's: the same limbs,
-// the same integer sums, so the same bits as k_denseK_fx.
-template <int K>
-struct CoopShape {
-    static constexpr int G = 1 << K, N = 2 * G, TPG = G / 4, SETS = 8 / TPG;
-};
+// Four targets (a 16-amplitude group, the real 32x32 operator) with the operator
+// stationary in registers: lane l of a warp owns real row l (its 32 high and 32 low
+// coefficient limbs, loaded once), and a warp works through its groups in batches of 32.
+//  1. Loads: each instruction takes amplitude j = l % 16 of two groups (l / 16 picks the
+//     group); the 16 lanes of a group find its scale with shuffles (fx_prepare_e's rules)
+//     and write their limbs to the warp's shared tile.
+//  2. Rows: for each group of the batch every lane reads the group's 32 limb pairs
+//     (broadcasts) and forms its own output real with 96 integer products, then stores it.
+// The sums are fx_row's (the same limbs and integer sums), so the bits equal k_denseK_fx's.
+// A group that needs FP64 is reloaded from global memory by the warp (nothing of that
+// group has been stored yet) and evaluated with the complex matrix.
+#define ROWS_WARPS 4
+#define ROWS_BATCH 32
 
-template <int PART, int N>
-__device__ __forceinline__ void coop_rows(const qgfx::OpN<N>& C, const int2 (*limbs)[32], int lane, int64_t (&R)[8]) {
-    int64_t hh[8], mid[8];
-#pragma unroll
-    for (int i = 0; i < 8; i++) { hh[i] = 0; mid[i] = 0; }
-    // fully unrolled: every coefficient is a compile-time constant-bank operand (a run-time
-    // index would turn each into a constant-bank load)
-#pragma unroll
-    for (int j = 0; j < N; j++) {
-        const int2 L = limbs[j][lane];
-#pragma unroll
-        for (int i = 0; i < 8; i++) {
-            hh[i] += (int64_t)L.x * C.h[8 * PART + i][j];
-            mid[i] += (int64_t)L.x * C.l[8 * PART + i][j];
-            mid[i] += (int64_t)L.y * C.h[8 * PART + i][j];
-        }
-    }
-#pragma unroll
-    for (int i = 0; i < 8; i++) R[i] = hh[i] + (mid[i] >> 32);
-}
-
-template <int K, int NB>
-__global__ void __launch_bounds__(256, 3) k_denseK_coop(double2* __restrict__ a, qidx numIts, Ins ins, qidx mask, MatK<K> M,
-                                                        qgfx::OpN<2 << K> C) {
-    typedef CoopShape<K> SH;
-    constexpr int G = SH::G, N = SH::N, TPG = SH::TPG, SETS = SH::SETS;
-    constexpr int S = qgfx::FxShift<N>::S;
-    __shared__ double2 raw[SETS][G][32];      // the inputs (for the FP64 path)
-    __shared__ int2 limbs[SETS][N][32];       // (high, low) limbs of every real of every group
-    __shared__ int4 stat[SETS][TPG][32];      // per part: largest exponent, smallest, largest effective, any nonzero
+template <int NB>
+__global__ void __launch_bounds__(32 * ROWS_WARPS, 6) k_dense4_rows(double2* __restrict__ a, qidx numIts, Ins ins, qidx mask,
+                                                                    MatK<4> M, qgfx::OpN<32> C) {
+    constexpr int N = 32, S = qgfx::FxShift<N>::S;
+    __shared__ int2 limbs[ROWS_WARPS][ROWS_BATCH][N];          // [warp][group][real]
+    __shared__ int meta[ROWS_WARPS][ROWS_BATCH][2];             // path, exponent shift of each group
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int part = warp % TPG, set = warp / TPG;
-    const qidx step = (qidx)gridDim.x * SETS * 32;
-    for (qidx g0 = (qidx)blockIdx.x * SETS * 32; g0 < numIts; g0 += step) {
-        const qidx gi = g0 + set * 32 + lane;
-        const bool valid = gi < numIts;
-        const qidx base = insert_bits<NB>(valid ? gi : 0, ins) | mask;
-        double2 v[4];
-        int e = 0, emin = 4096, eg = 1, any = 0;
+    const int half = lane >> 4, j = lane & 15;
+    // this lane's row of the operator
+    int32_t ch[N], cl[N];
 #pragma unroll
-        for (int k = 0; k < 4; k++) {
-            v[k] = valid ? ld_amp(a + base + M.off[4 * part + k]) : make_double2(0.0, 0.0);
-            const double re[2] = {v[k].x, v[k].y};
+    for (int k = 0; k < N; k++) { ch[k] = C.h[lane][k]; cl[k] = C.l[lane][k]; }
+    const qidx offJ = M.off[j];
+    const qidx numBatches = (numIts + ROWS_BATCH - 1) / ROWS_BATCH;
+    const qidx warpsTotal = (qidx)gridDim.x * ROWS_WARPS;
+    for (qidx b = blockIdx.x * (qidx)ROWS_WARPS + warp; b < numBatches; b += warpsTotal) {
+        const qidx g0 = b * ROWS_BATCH;
+        // ---- 1: limbs of the batch's groups, two groups per load instruction
+#pragma unroll 4
+        for (int p = 0; p < ROWS_BATCH / 2; p++) {
+            const int gl = 2 * p + half;
+            const qidx gi = g0 + gl;
+            const bool valid = gi < numIts;
+            const qidx base = insert_bits<NB>(valid ? gi : g0, ins) | mask;
+            const double2 v = valid ? ld_amp(a + base + offJ) : make_double2(0.0, 0.0);
+            const uint64_t u0 = qgfx::f64_bits(v.x), u1 = qgfx::f64_bits(v.y);
+            const int e0 = (int)((u0 >> 52) & 0x7FF), e1 = (int)((u1 >> 52) & 0x7FF);
+            int e = e0 > e1 ? e0 : e1;
+            int emin = e0 < e1 ? e0 : e1;
+            int eg = (e0 + (e0 == 0)) > (e1 + (e1 == 0)) ? (e0 + (e0 == 0)) : (e1 + (e1 == 0));
+            int any = ((u0 << 1) | (u1 << 1)) != 0;
 #pragma unroll
-            for (int c = 0; c < 2; c++) {
-                const uint64_t u = qgfx::f64_bits(re[c]);
-                any |= (u << 1) != 0;
-                const int ej = (int)((u >> 52) & 0x7FF);
-                e = ej > e ? ej : e;
-                emin = ej < emin ? ej : emin;
-                const int ejg = ej + (ej == 0);
-                eg = ejg > eg ? ejg : eg;
+            for (int o = 1; o < 16; o <<= 1) {
+                const int e2 = __shfl_xor_sync(0xffffffffu, e, o), m2 = __shfl_xor_sync(0xffffffffu, emin, o);
+                const int g2 = __shfl_xor_sync(0xffffffffu, eg, o), a2 = __shfl_xor_sync(0xffffffffu, any, o);
+                e = e2 > e ? e2 : e;
+                emin = m2 < emin ? m2 : emin;
+                eg = g2 > eg ? g2 : eg;
+                any |= a2;
+            }
+            const int t = e + C.expo - qgfx::FxShift<N>::TOFF;
+            const int tg = eg + C.expo - qgfx::FxShift<N>::TOFF;
+            int path;          // 0: near form, 1: general form, 2: all zero, 3: FP64
+            if (emin >= 1 && e <= 2046 && e - emin <= 31 && 1023 + t >= 1 && 1023 + qgfx::FxShift<N>::RL + t <= 2046) path = 0;
+            else if (1023 + tg < 1 || 1023 + qgfx::FxShift<N>::RL + tg > 2046 || eg == 2047) path = any ? 3 : 2;
+            else path = 1;
+            int32_t xh0 = 0, xl0 = 0, xh1 = 0, xl1 = 0;
+            if (path == 0) {
+                qgfx::to_limbs_near<S>((uint32_t)(u0 >> 32), (uint32_t)u0, e - e0, xh0, xl0);
+                qgfx::to_limbs_near<S>((uint32_t)(u1 >> 32), (uint32_t)u1, e - e1, xh1, xl1);
+            } else if (path == 1) {
+                qgfx::to_limbs(u0, eg, xh0, xl0, S);
+                qgfx::to_limbs(u1, eg, xh1, xl1, S);
+            }
+            limbs[warp][gl][2 * j] = make_int2(xh0, xl0);
+            limbs[warp][gl][2 * j + 1] = make_int2(xh1, xl1);
+            if (j == 0) {
+                meta[warp][gl][0] = valid ? path : 2;
+                meta[warp][gl][1] = path == 0 ? t : tg;
             }
         }
-        __syncthreads();   // the previous iteration's reads of the shared arrays are done
+        __syncwarp();
+        // ---- 2: every lane forms its output real of each group
+        const int k = lane >> 1, c = lane & 1;
+        const qidx offK = M.off[k];
+        for (int gl = 0; gl < ROWS_BATCH; gl++) {
+            const qidx gi = g0 + gl;
+            if (gi >= numIts) break;
+            const qidx base = insert_bits<NB>(gi, ins) | mask;
+            const int path = meta[warp][gl][0];
+            double* dst = (double*)(a + base + offK) + c;
+            if (path <= 1) {
+                int64_t hh = 0, mid = 0;
+                const int4* row = (const int4*)limbs[warp][gl];
 #pragma unroll
-        for (int k = 0; k < 4; k++) raw[set][4 * part + k][lane] = v[k];
-        stat[set][part][lane] = make_int4(e, emin, eg, any);
-        __syncthreads();
-#pragma unroll
-        for (int q = 0; q < TPG; q++) {
-            const int4 st = stat[set][q][lane];
-            e = st.x > e ? st.x : e;
-            emin = st.y < emin ? st.y : emin;
-            eg = st.z > eg ? st.z : eg;
-            any |= st.w;
-        }
-        // fx_prepare_e's choice, made alike by the group's threads
-        const int t = e + C.expo - qgfx::FxShift<N>::TOFF;
-        const int tg = eg + C.expo - qgfx::FxShift<N>::TOFF;
-        int path;          // 0: near form, 1: general form, 2: all zero, 3: FP64
-        if (emin >= 1 && e <= 2046 && e - emin <= 31 && 1023 + t >= 1 && 1023 + qgfx::FxShift<N>::RL + t <= 2046) path = 0;
-        else if (1023 + tg < 1 || 1023 + qgfx::FxShift<N>::RL + tg > 2046 || eg == 2047) path = any ? 3 : 2;
-        else path = 1;
-        if (path <= 1) {
-#pragma unroll
-            for (int k = 0; k < 4; k++) {
-                const double re[2] = {v[k].x, v[k].y};
-#pragma unroll
-                for (int c = 0; c < 2; c++) {
-                    const uint64_t u = qgfx::f64_bits(re[c]);
-                    int32_t xh, xl;
-                    if (path == 0) {
-                        const uint32_t hi = (uint32_t)(u >> 32);
-                        qgfx::to_limbs_near<S>(hi, (uint32_t)u, e - (int)((hi >> 20) & 0x7FFu), xh, xl);
-                    } else {
-                        qgfx::to_limbs(u, eg, xh, xl, S);
-                    }
-                    limbs[set][8 * part + 2 * k + c][lane] = make_int2(xh, xl);
+                for (int q = 0; q < N / 2; q++) {
+                    const int4 L = row[q];                 // limbs of reals 2q and 2q+1 (a broadcast)
+                    hh += (int64_t)L.x * ch[2 * q];
+                    mid += (int64_t)L.x * cl[2 * q];
+                    mid += (int64_t)L.y * ch[2 * q];
+                    hh += (int64_t)L.z * ch[2 * q + 1];
+                    mid += (int64_t)L.z * cl[2 * q + 1];
+                    mid += (int64_t)L.w * ch[2 * q + 1];
                 }
+                __stcs(dst, qgfx::fx_to_double(hh + (mid >> 32), (uint32_t)meta[warp][gl][1] << 20));
+            } else if (path == 2) {
+                __stcs(dst, 0.0);
+            } else {
+                double2 acc = make_double2(0.0, 0.0);
+                for (int q = 0; q < 16; q++) acc = cfma(M.m[k * 16 + q], a[base + M.off[q]], acc);
+                __syncwarp();      // every lane has read the group before any lane stores
+                __stcs(dst, c ? acc.y : acc.x);
             }
         }
-        __syncthreads();
-        if (!valid) continue;
-        if (path <= 1) {
-            int64_t R[8];
-            if (part == 0) coop_rows<0, N>(C, limbs[set], lane, R);
-            else if (TPG > 1 && part == 1) coop_rows<(TPG > 1 ? 1 : 0), N>(C, limbs[set], lane, R);
-            else if (TPG > 2 && part == 2) coop_rows<(TPG > 2 ? 2 : 0), N>(C, limbs[set], lane, R);
-            else coop_rows<(TPG > 3 ? 3 : 0), N>(C, limbs[set], lane, R);
-            const uint32_t down = (uint32_t)(path == 0 ? t : tg) << 20;
-#pragma unroll
-            for (int k = 0; k < 4; k++)
-                st_amp(a + base + M.off[4 * part + k],
-                       make_double2(qgfx::fx_to_double(R[2 * k], down), qgfx::fx_to_double(R[2 * k + 1], down)));
-        } else if (path == 2) {
-#pragma unroll
-            for (int k = 0; k < 4; k++) st_amp(a + base + M.off[4 * part + k], make_double2(0.0, 0.0));
-        } else {
-            // FP64 products from the group's inputs in shared memory
-#pragma unroll
-            for (int k = 0; k < 4; k++) {
-                const int r = 4 * part + k;
-                double2 acc = cmul(M.m[r * G], raw[set][0][lane]);
-#pragma unroll
-                for (int j = 1; j < G; j++) acc = cfma(M.m[r * G + j], raw[set][j][lane], acc);
-                st_amp(a + base + M.off[r], acc);
-            }
-        }
+        __syncwarp();      // the tile is read before the next batch writes it
     }
 }
 
@@ -1010,17 +986,11 @@ int launch_denseK(double2* amps, qidx numIts, const QubitPlan& p, const qg_cplx*
                 qgfx::real_form(u.data(), D, R.data());
                 ok = qgfx::make_op<2 * D>(R.data(), C);
             }
-            if (ok && K == 4) {
-                // the cooperative form (real operator), 64 groups per block and iteration
-                qgfx::OpN<2 * D> CR;
-                if (!DenseKOp<K>::complex) std::memcpy(&CR, &C, sizeof(CR));
-                else {
-                    qgfx::real_form(u.data(), D, R.data());
-                    ok = qgfx::make_op<2 * D>(R.data(), CR);
-                }
+            if constexpr (K == 4) {
                 if (ok) {
-                    const qidx items = (numIts + CoopShape<K>::SETS * 32 - 1) / (CoopShape<K>::SETS * 32) * 256;
-#define L(NBV) k_denseK_coop<K, NBV><<<resident_blocks(k_denseK_coop<K, NBV>, items, 256), 256, 0, st>>>(amps, numIts, p.ins, p.stateMask, M, CR)
+                    // the row-stationary form: 32 groups per warp and batch
+                    const qidx items = (numIts + ROWS_BATCH - 1) / ROWS_BATCH * 32;
+#define L(NBV) k_dense4_rows<NBV><<<resident_blocks(k_dense4_rows<NBV>, items, 32 * ROWS_WARPS), 32 * ROWS_WARPS, 0, st>>>(amps, numIts, p.ins, p.stateMask, M, C)
                     QG_DISPATCH_NB(p.numFixed, L)
 #undef L
                     return QG_OK;
