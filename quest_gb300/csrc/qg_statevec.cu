@@ -324,17 +324,26 @@ struct DenseKOp<3> { typedef qgfx::CopN<8> type; static constexpr bool complex =
 #define ROWS_BATCH 32
 
 template <int NB>
-__global__ void __launch_bounds__(32 * ROWS_WARPS, 6) k_dense4_rows(double2* __restrict__ a, qidx numIts, Ins ins, qidx mask,
+__global__ void __launch_bounds__(32 * ROWS_WARPS, 4) k_dense4_rows(double2* __restrict__ a, qidx numIts, Ins ins, qidx mask,
                                                                     MatK<4> M, qgfx::OpN<32> C) {
     constexpr int N = 32, S = qgfx::FxShift<N>::S;
     __shared__ int2 limbs[ROWS_WARPS][ROWS_BATCH][N];          // [warp][group][real]
     __shared__ int meta[ROWS_WARPS][ROWS_BATCH][2];             // path, exponent shift of each group
+    __shared__ int2 coef[N][N + 1];                             // (high, low) limbs of the operator
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int half = lane >> 4, j = lane & 15;
-    // this lane's row of the operator
+    // this lane's row of the operator, held in registers for the whole kernel.  It goes
+    // through shared memory once: read straight from the parameter bank with a per-lane
+    // row, any reload the register allocator chose would be a divergent constant load.
+    for (int e = threadIdx.x; e < N * N; e += 32 * ROWS_WARPS) coef[e / N][e % N] = make_int2(C.h[e / N][e % N], C.l[e / N][e % N]);
+    __syncthreads();
     int32_t ch[N], cl[N];
 #pragma unroll
-    for (int k = 0; k < N; k++) { ch[k] = C.h[lane][k]; cl[k] = C.l[lane][k]; }
+    for (int k = 0; k < N; k++) {
+        const int2 v = coef[lane][k];
+        ch[k] = v.x;
+        cl[k] = v.y;
+    }
     const qidx offJ = M.off[j];
     const qidx numBatches = (numIts + ROWS_BATCH - 1) / ROWS_BATCH;
     const qidx warpsTotal = (qidx)gridDim.x * ROWS_WARPS;
