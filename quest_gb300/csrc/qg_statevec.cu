@@ -309,124 +309,69 @@ struct DenseKOp { typedef qgfx::OpN<2 << K> type; static constexpr bool complex 
 template <>
 struct DenseKOp<3> { typedef qgfx::CopN<8> type; static constexpr bool complex = true; };
 
-// Four targets (a 16-amplitude group, the real 32x32 operator) with the operator
-// stationary in registers: lane l of a warp owns real row l (its 32 high and 32 low
-// coefficient limbs, loaded once), and a warp works through its groups in batches of 32.
-//  1. Loads: each instruction takes amplitude j = l % 16 of two groups (l / 16 picks the
-//     group); the 16 lanes of a group find its scale with shuffles (fx_prepare_e's rules)
-//     and write their limbs to the warp's shared tile.
-//  2. Rows: for each group of the batch every lane reads the group's 32 limb pairs
-//     (broadcasts) and forms its own output real with 96 integer products, then stores it.
-// The sums are fx_row's (the same limbs and integer sums), so the bits equal k_denseK_fx's.
-// A group that needs FP64 is reloaded from global memory by the warp (nothing of that
-// group has been stored yet) and evaluated with the complex matrix.
-#define ROWS_WARPS 4
-#define ROWS_BATCH 32
-
+// Four targets (a 16-amplitude group, the real 32x32 operator): each thread owns a group,
+// as k_denseK_fx does, and forms its 32 outputs one row at a time; the operator sits in
+// shared memory and every row is read as 16-byte broadcasts (all threads of a warp are on
+// the same row), not from the parameter bank, where a row chosen at run time becomes a
+// constant-bank load per coefficient.  The limbs and the integer sums are fx_prepare /
+// fx_row's, so the bits equal k_denseK_fx's.
 template <int NB>
-__global__ void __launch_bounds__(32 * ROWS_WARPS, 4) k_dense4_rows(double2* __restrict__ a, qidx numIts, Ins ins, qidx mask,
-                                                                    MatK<4> M, qgfx::OpN<32> C) {
-    constexpr int N = 32, S = qgfx::FxShift<N>::S;
-    __shared__ int2 limbs[ROWS_WARPS][ROWS_BATCH][N];          // [warp][group][real]
-    __shared__ int meta[ROWS_WARPS][ROWS_BATCH][2];             // path, exponent shift of each group
-    __shared__ int2 coef[N][N + 1];                             // (high, low) limbs of the operator
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int half = lane >> 4, j = lane & 15;
-    // this lane's row of the operator, held in registers for the whole kernel.  It goes
-    // through shared memory once: read straight from the parameter bank with a per-lane
-    // row, any reload the register allocator chose would be a divergent constant load.
-    for (int e = threadIdx.x; e < N * N; e += 32 * ROWS_WARPS) coef[e / N][e % N] = make_int2(C.h[e / N][e % N], C.l[e / N][e % N]);
-    __syncthreads();
-    int32_t ch[N], cl[N];
-#pragma unroll
-    for (int k = 0; k < N; k++) {
-        const int2 v = coef[lane][k];
-        ch[k] = v.x;
-        cl[k] = v.y;
+__global__ void __launch_bounds__(128) k_dense4_fx(double2* __restrict__ a, qidx numIts, Ins ins, qidx mask, MatK<4> M,
+                                                   qgfx::OpN<32> C) {
+    constexpr int D = 16, N = 32;
+    __shared__ __align__(16) int32_t sh[N][N], sl[N][N];
+    for (int e = threadIdx.x; e < N * N; e += blockDim.x) {
+        sh[e / N][e % N] = C.h[e / N][e % N];
+        sl[e / N][e % N] = C.l[e / N][e % N];
     }
-    const qidx offJ = M.off[j];
-    const qidx numBatches = (numIts + ROWS_BATCH - 1) / ROWS_BATCH;
-    const qidx warpsTotal = (qidx)gridDim.x * ROWS_WARPS;
-    for (qidx b = blockIdx.x * (qidx)ROWS_WARPS + warp; b < numBatches; b += warpsTotal) {
-        const qidx g0 = b * ROWS_BATCH;
-        // ---- 1: limbs of the batch's groups, two groups per load instruction
-#pragma unroll 4
-        for (int p = 0; p < ROWS_BATCH / 2; p++) {
-            const int gl = 2 * p + half;
-            const qidx gi = g0 + gl;
-            const bool valid = gi < numIts;
-            const qidx base = insert_bits<NB>(valid ? gi : g0, ins) | mask;
-            const double2 v = valid ? ld_amp(a + base + offJ) : make_double2(0.0, 0.0);
-            const uint64_t u0 = qgfx::f64_bits(v.x), u1 = qgfx::f64_bits(v.y);
-            const int e0 = (int)((u0 >> 52) & 0x7FF), e1 = (int)((u1 >> 52) & 0x7FF);
-            int e = e0 > e1 ? e0 : e1;
-            int emin = e0 < e1 ? e0 : e1;
-            int eg = (e0 + (e0 == 0)) > (e1 + (e1 == 0)) ? (e0 + (e0 == 0)) : (e1 + (e1 == 0));
-            int any = ((u0 << 1) | (u1 << 1)) != 0;
+    __syncthreads();
+    const qidx stride = (qidx)gridDim.x * blockDim.x;
+    for (qidx n = blockIdx.x * (qidx)blockDim.x + threadIdx.x; n < numIts; n += stride) {
+        const qidx base = insert_bits<NB>(n, ins) | mask;
+        double in[N];
 #pragma unroll
-            for (int o = 1; o < 16; o <<= 1) {
-                const int e2 = __shfl_xor_sync(0xffffffffu, e, o), m2 = __shfl_xor_sync(0xffffffffu, emin, o);
-                const int g2 = __shfl_xor_sync(0xffffffffu, eg, o), a2 = __shfl_xor_sync(0xffffffffu, any, o);
-                e = e2 > e ? e2 : e;
-                emin = m2 < emin ? m2 : emin;
-                eg = g2 > eg ? g2 : eg;
-                any |= a2;
-            }
-            const int t = e + C.expo - qgfx::FxShift<N>::TOFF;
-            const int tg = eg + C.expo - qgfx::FxShift<N>::TOFF;
-            int path;          // 0: near form, 1: general form, 2: all zero, 3: FP64
-            if (emin >= 1 && e <= 2046 && e - emin <= 31 && 1023 + t >= 1 && 1023 + qgfx::FxShift<N>::RL + t <= 2046) path = 0;
-            else if (1023 + tg < 1 || 1023 + qgfx::FxShift<N>::RL + tg > 2046 || eg == 2047) path = any ? 3 : 2;
-            else path = 1;
-            int32_t xh0 = 0, xl0 = 0, xh1 = 0, xl1 = 0;
-            if (path == 0) {
-                qgfx::to_limbs_near<S>((uint32_t)(u0 >> 32), (uint32_t)u0, e - e0, xh0, xl0);
-                qgfx::to_limbs_near<S>((uint32_t)(u1 >> 32), (uint32_t)u1, e - e1, xh1, xl1);
-            } else if (path == 1) {
-                qgfx::to_limbs(u0, eg, xh0, xl0, S);
-                qgfx::to_limbs(u1, eg, xh1, xl1, S);
-            }
-            limbs[warp][gl][2 * j] = make_int2(xh0, xl0);
-            limbs[warp][gl][2 * j + 1] = make_int2(xh1, xl1);
-            if (j == 0) {
-                meta[warp][gl][0] = valid ? path : 2;
-                meta[warp][gl][1] = path == 0 ? t : tg;
-            }
+        for (int j = 0; j < D; j++) {
+            const double2 v = ld_amp(a + base + M.off[j]);
+            in[2 * j] = v.x;
+            in[2 * j + 1] = v.y;
         }
-        __syncwarp();
-        // ---- 2: every lane forms its output real of each group
-        const int k = lane >> 1, c = lane & 1;
-        const qidx offK = M.off[k];
-        for (int gl = 0; gl < ROWS_BATCH; gl++) {
-            const qidx gi = g0 + gl;
-            if (gi >= numIts) break;
-            const qidx base = insert_bits<NB>(gi, ins) | mask;
-            const int path = meta[warp][gl][0];
-            double* dst = (double*)(a + base + offK) + c;
-            if (path <= 1) {
-                int64_t hh = 0, mid = 0;
-                const int4* row = (const int4*)limbs[warp][gl];
+        int32_t xh[N], xl[N];
+        uint32_t down;
+        bool zero;
+        if (qgfx::fx_prepare<N>(C, in, xh, xl, down, zero)) {
+#pragma unroll 1
+            for (int r = 0; r < D; r++) {
+                double out[2];
 #pragma unroll
-                for (int q = 0; q < N / 2; q++) {
-                    const int4 L = row[q];                 // limbs of reals 2q and 2q+1 (a broadcast)
-                    hh += (int64_t)L.x * ch[2 * q];
-                    mid += (int64_t)L.x * cl[2 * q];
-                    mid += (int64_t)L.y * ch[2 * q];
-                    hh += (int64_t)L.z * ch[2 * q + 1];
-                    mid += (int64_t)L.z * cl[2 * q + 1];
-                    mid += (int64_t)L.w * ch[2 * q + 1];
+                for (int c = 0; c < 2; c++) {
+                    const int4* hr = (const int4*)sh[2 * r + c];
+                    const int4* lr = (const int4*)sl[2 * r + c];
+                    int64_t hh = 0, mid = 0;
+#pragma unroll
+                    for (int q = 0; q < N / 4; q++) {
+                        const int4 H = hr[q], Lo = lr[q];
+                        hh += (int64_t)xh[4 * q] * H.x;     mid += (int64_t)xh[4 * q] * Lo.x;     mid += (int64_t)xl[4 * q] * H.x;
+                        hh += (int64_t)xh[4 * q + 1] * H.y; mid += (int64_t)xh[4 * q + 1] * Lo.y; mid += (int64_t)xl[4 * q + 1] * H.y;
+                        hh += (int64_t)xh[4 * q + 2] * H.z; mid += (int64_t)xh[4 * q + 2] * Lo.z; mid += (int64_t)xl[4 * q + 2] * H.z;
+                        hh += (int64_t)xh[4 * q + 3] * H.w; mid += (int64_t)xh[4 * q + 3] * Lo.w; mid += (int64_t)xl[4 * q + 3] * H.w;
+                    }
+                    out[c] = zero ? 0.0 : qgfx::fx_to_double(hh + (mid >> 32), down);
                 }
-                __stcs(dst, qgfx::fx_to_double(hh + (mid >> 32), (uint32_t)meta[warp][gl][1] << 20));
-            } else if (path == 2) {
-                __stcs(dst, 0.0);
-            } else {
-                double2 acc = make_double2(0.0, 0.0);
-                for (int q = 0; q < 16; q++) acc = cfma(M.m[k * 16 + q], a[base + M.off[q]], acc);
-                __syncwarp();      // every lane has read the group before any lane stores
-                __stcs(dst, c ? acc.y : acc.x);
+                st_amp(a + base + M.off[r], make_double2(out[0], out[1]));
+            }
+        } else {
+            // nothing has been stored: reload the group and use FP64
+            double2 v[D];
+#pragma unroll
+            for (int j = 0; j < D; j++) v[j] = a[base + M.off[j]];
+#pragma unroll 1
+            for (int r = 0; r < D; r++) {
+                double2 acc = cmul(M.m[r * D], v[0]);
+#pragma unroll
+                for (int j = 1; j < D; j++) acc = cfma(M.m[r * D + j], v[j], acc);
+                st_amp(a + base + M.off[r], acc);
             }
         }
-        __syncwarp();      // the tile is read before the next batch writes it
     }
 }
 
@@ -997,9 +942,8 @@ int launch_denseK(double2* amps, qidx numIts, const QubitPlan& p, const qg_cplx*
             }
             if constexpr (K == 4) {
                 if (ok) {
-                    // the row-stationary form: 32 groups per warp and batch
-                    const qidx items = (numIts + ROWS_BATCH - 1) / ROWS_BATCH * 32;
-#define L(NBV) k_dense4_rows<NBV><<<resident_blocks(k_dense4_rows<NBV>, items, 32 * ROWS_WARPS), 32 * ROWS_WARPS, 0, st>>>(amps, numIts, p.ins, p.stateMask, M, C)
+                    // the operator as shared-memory broadcasts
+#define L(NBV) k_dense4_fx<NBV><<<resident_blocks(k_dense4_fx<NBV>, numIts, 128), 128, 0, st>>>(amps, numIts, p.ins, p.stateMask, M, C)
                     QG_DISPATCH_NB(p.numFixed, L)
 #undef L
                     return QG_OK;
