@@ -6,8 +6,9 @@ compared with QuEST's own CPU build.
 
 Sample: the first `--gates` gates (Haar 2x2 unitaries and controlled phases) of the
 benchmark circuit on an n-qubit FP64 statevector.  Each runner's time is the median over
-`--reps` runs of the sample minus the median of an empty circuit (the runners' own
-copies of the state in and out are not gate work).
+`--reps` runs, timed by each runner around its ops only (the reference runner creates a
+Qureg and copies the state in and out on every call, which is not gate work); the two
+runners alternate.
 
     python oracle/compare_port_speed.py [--qubits 28] [--gates 45] [--threads N] [--reps 3]
 """
@@ -16,7 +17,6 @@ import ctypes
 import os
 import statistics
 import sys
-import time
 
 import numpy as np
 
@@ -57,25 +57,42 @@ def main():
     res = np.zeros(8)
     outs = np.zeros(8, dtype=np.int32)
 
+    seconds = {id(orc): orc.lib.orc_last_run_seconds, id(ref): ref.lib.ref_last_run_seconds}
+    for f in seconds.values():
+        f.restype = ctypes.c_double
+
+    # both runners work on memory allocated the way QuEST allocates a Qureg (calloc), so
+    # that page sizes do not differ between them (numpy asks for transparent huge pages)
+    libc = ctypes.CDLL(None)
+    libc.calloc.restype = ctypes.c_void_p
+    libc.calloc.argtypes = [ctypes.c_size_t, ctypes.c_size_t]
+    raw = libc.calloc(1, state.nbytes)
+    work = np.ctypeslib.as_array(ctypes.cast(raw, ctypes.POINTER(ctypes.c_double)), shape=(2 * state.size,)).view(np.complex128)
+
     def timed(runner, body):
-        amps = state.copy()
+        amps = work
+        amps[:] = state
         nr, no = ctypes.c_int(0), ctypes.c_int(0)
-        t0 = time.perf_counter()
         rc = runner.fn(body.encode(), n, 0, amps.ctypes.data, res.ctypes.data, 8, ctypes.byref(nr), outs.ctypes.data, 8,
                        ctypes.byref(no))
-        dt = time.perf_counter() - t0
         if rc != 0:
             raise RuntimeError("runner failed")
-        return dt, amps
+        return seconds[id(runner)](), amps
 
-    out = {}
-    for name, runner in (("port", orc), ("reference", ref)):
+    runners = (("port", orc), ("reference", ref))
+    for _, runner in runners:
         timed(runner, text)                                        # warm-up (first-touch, thread pool)
-        full = statistics.median(timed(runner, text)[0] for _ in range(a.reps))
-        empty = statistics.median(timed(runner, "\n")[0] for _ in range(a.reps))
-        out[name] = (full - empty, nbytes / (full - empty) / 1e9)
-    _, a_port = timed(orc, text)
-    _, a_ref = timed(ref, text)
+    # the two runners alternate, so that a change in the machine's load falls on both
+    times = {name: [] for name, _ in runners}
+    for _ in range(a.reps):
+        for name, runner in runners:
+            times[name].append(timed(runner, text)[0])
+    out = {}
+    for name, _ in runners:
+        secs = statistics.median(times[name])
+        out[name] = (secs, nbytes / secs / 1e9)
+    a_port = timed(orc, text)[1].copy()
+    a_ref = timed(ref, text)[1].copy()
     diff = float(np.max(np.abs(a_port - a_ref)))
     print(f"{n}-qubit FP64 statevector, first {len(lines)} gates of the benchmark circuit, {a.threads} threads, "
           f"median of {a.reps}")

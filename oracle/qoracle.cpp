@@ -11,6 +11,7 @@
 #include "qoracle.h"
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <complex>
 #include <cstdio>
@@ -1120,6 +1121,10 @@ thread_local std::string g_err;
 
 extern "C" const char* orc_last_error(void) { return g_err.c_str(); }
 
+static double g_lastSeconds = 0;
+/* seconds spent in the ops of the last orc_run_circuit call (no state copies) */
+extern "C" double orc_last_run_seconds(void) { return g_lastSeconds; }
+
 extern "C" int orc_run_circuit(const char* text, int numQubits, int isDensMatr, double* amps,
                                double* results, int maxResults, int* numResults,
                                int* outcomes, int maxOutcomes, int* numOutcomes) {
@@ -1130,7 +1135,9 @@ extern "C" int orc_run_circuit(const char* text, int numQubits, int isDensMatr, 
     r.amps = amps;
     std::seed_seq seq{0u};
     r.gen.seed(seq);
+    const auto t0 = std::chrono::steady_clock::now();
     bool ok = r.run(text ? std::string(text) : std::string());
+    g_lastSeconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     if (numResults) *numResults = (int)r.results.size();
     if (numOutcomes) *numOutcomes = (int)r.outcomes.size();
     for (int i = 0; i < (int)r.results.size() && i < maxResults; i++) results[i] = r.results[i];

@@ -77,6 +77,7 @@ int orc_run_circuit(const char* text, int numQubits, int isDensMatr, double* amp
                     double* results, int maxResults, int* numResults,
                     int* outcomes, int maxOutcomes, int* numOutcomes);
 const char* orc_last_error(void);
+double orc_last_run_seconds(void);   /* time in the ops of the last run (no state copies) */
 void orc_set_num_threads(int n);
 int  orc_get_num_threads(void);
 

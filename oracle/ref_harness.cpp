@@ -22,6 +22,7 @@
 #include "quest/include/initialisations.h"
 #include "quest/include/debug.h"
 
+#include <chrono>
 #include <cstring>
 #include <sstream>
 #include <string>
@@ -30,6 +31,10 @@
 using std::vector;
 
 static std::string g_err;
+static double g_lastSeconds = 0;
+
+// seconds spent in the ops of the last ref_run_circuit call (no Qureg creation or copies)
+extern "C" double ref_last_run_seconds(void) { return g_lastSeconds; }
 
 static vector<int> rdInts(std::istringstream& is, int k) { vector<int> v(k); for (int i = 0; i < k; i++) is >> v[i]; return v; }
 static vector<double> rdDbl(std::istringstream& is, int k) { vector<double> v(k); for (int i = 0; i < k; i++) is >> v[i]; return v; }
@@ -78,6 +83,7 @@ extern "C" int ref_run_circuit(const char* text, int numQubits, int isDensMatr, 
     std::istringstream lines(text);
     std::string line;
     int rc = 0;
+    const auto t0 = std::chrono::steady_clock::now();
     while (std::getline(lines, line)) {
         std::istringstream is(line);
         std::string op;
@@ -194,6 +200,8 @@ extern "C" int ref_run_circuit(const char* text, int numQubits, int isDensMatr, 
         }
         else { g_err = "unknown op " + op; rc = -1; break; }
     }
+    syncQuESTEnv();
+    g_lastSeconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     syncQuregFromGpu(q);
     std::memcpy(amps, q.cpuAmps, sizeof(qcomp) * q.numAmps);
     destroyQureg(q);

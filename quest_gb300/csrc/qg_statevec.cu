@@ -346,16 +346,18 @@ __global__ void __launch_bounds__(128) k_dense4_fx(double2* __restrict__ a, qidx
                 for (int c = 0; c < 2; c++) {
                     const int4* hr = (const int4*)sh[2 * r + c];
                     const int4* lr = (const int4*)sl[2 * r + c];
-                    int64_t hh = 0, mid = 0;
+                    // four independent integer sums (exact, so their order does not matter):
+                    // short dependency chains for the integer multiply-add pipe
+                    int64_t h0 = 0, h1 = 0, m0 = 0, m1 = 0;
 #pragma unroll
                     for (int q = 0; q < N / 4; q++) {
                         const int4 H = hr[q], Lo = lr[q];
-                        hh += (int64_t)xh[4 * q] * H.x;     mid += (int64_t)xh[4 * q] * Lo.x;     mid += (int64_t)xl[4 * q] * H.x;
-                        hh += (int64_t)xh[4 * q + 1] * H.y; mid += (int64_t)xh[4 * q + 1] * Lo.y; mid += (int64_t)xl[4 * q + 1] * H.y;
-                        hh += (int64_t)xh[4 * q + 2] * H.z; mid += (int64_t)xh[4 * q + 2] * Lo.z; mid += (int64_t)xl[4 * q + 2] * H.z;
-                        hh += (int64_t)xh[4 * q + 3] * H.w; mid += (int64_t)xh[4 * q + 3] * Lo.w; mid += (int64_t)xl[4 * q + 3] * H.w;
+                        h0 += (int64_t)xh[4 * q] * H.x;     m0 += (int64_t)xh[4 * q] * Lo.x;     m1 += (int64_t)xl[4 * q] * H.x;
+                        h1 += (int64_t)xh[4 * q + 1] * H.y; m0 += (int64_t)xh[4 * q + 1] * Lo.y; m1 += (int64_t)xl[4 * q + 1] * H.y;
+                        h0 += (int64_t)xh[4 * q + 2] * H.z; m0 += (int64_t)xh[4 * q + 2] * Lo.z; m1 += (int64_t)xl[4 * q + 2] * H.z;
+                        h1 += (int64_t)xh[4 * q + 3] * H.w; m0 += (int64_t)xh[4 * q + 3] * Lo.w; m1 += (int64_t)xl[4 * q + 3] * H.w;
                     }
-                    out[c] = zero ? 0.0 : qgfx::fx_to_double(hh + (mid >> 32), down);
+                    out[c] = zero ? 0.0 : qgfx::fx_to_double((h0 + h1) + ((m0 + m1) >> 32), down);
                 }
                 st_amp(a + base + M.off[r], make_double2(out[0], out[1]));
             }
