@@ -1106,9 +1106,11 @@ def run_dm(args, world, rank, local, dist, emit=True):
     strs = (api.PauliStr * 16)(*[api.pauli_str(c) for c in codes])
     vals = (C.c_double * 16)()
     q = Q.createDensityQureg(nq)
-    host = np.ctypeslib.as_array(C.cast(q.cpuAmps, C.POINTER(C.c_double)), shape=(2 << (2 * nq),))
-    host[:] = state.view(np.float64)
-    in_ptr = C.cast(q.cpuAmps, C.c_void_p)
+    api.set_amps(q, state)
+    # the input stays on the device: each step starts from a device-to-device copy of it
+    src = C.c_void_p()
+    _lib.check(L.qg_alloc(C.byref(src), nbytes))
+    _lib.check(L.qg_copy_d2d(src, C.cast(q.gpuAmps, C.c_void_p), nbytes, None))
 
     def apply(op):
         k = op[0]
@@ -1122,7 +1124,9 @@ def run_dm(args, world, rank, local, dist, emit=True):
             Q.mixKrausMap(q, op[1], 2, op[2])
 
     def step():
-        Q.setDensityQuregFlatAmps(q, 0, in_ptr, 1 << (2 * nq))
+        # nothing is pending here: the previous step ended with reductions, which apply
+        # every deferred operation first
+        _lib.check(L.qg_copy_d2d(C.cast(q.gpuAmps, C.c_void_p), src, nbytes, None))
         for op in prepared:
             apply(op)
         purity = Q.calcPurity(q)
@@ -1180,8 +1184,9 @@ def run_dm(args, world, rank, local, dist, emit=True):
     per_op["applyCompMatr1 + mixDepolarising on one qubit (one fused pass)"] = {
         "ms": round(ms.value / 8, 4), "gbs": round(2 * nbytes / (ms.value / 8) / 1e6, 1)}
     Q.destroyQureg(q)
+    L.qg_free(src)
     ops_count = {name: sum(1 for op in prepared if op[0] == k) for k, name in kinds.items()}
-    alg_bytes = sum((2 if op[0] == 1 else 1) * 2 * nbytes for op in prepared) + nbytes * 2   # + purity and the state load
+    alg_bytes = sum((2 if op[0] == 1 else 1) * 2 * nbytes for op in prepared) + nbytes * 3   # + purity and the state reset
     cpu = None
     if rank == 0 and args.cpu_sample > 0:
         sys.path.insert(0, os.path.join(ROOT, "tests"))
@@ -1223,7 +1228,8 @@ def run_dm(args, world, rank, local, dist, emit=True):
                                    f"unitaries + mixDepolarising(0.01) on every qubit + a 2-qubit 4-operator Kraus map, then "
                                    f"calcPurity and 16 Pauli expectations", "qubits": nq, "layers": layers,
                        "ops": ops_count, "l2": "state larger than L2; no flush",
-                       "bytes": "per op 2 x 16 B x 4^N (the reference's passes: two for a unitary) + state load + purity"},
+                       "bytes": "per op 2 x 16 B x 4^N (the reference's passes: two for a unitary) + the state reset (a device copy) + purity",
+                       "start": "each step from a device copy of the input state"},
             "ms_per_layer": round(t / args.steps / layers * 1e3, 3),
             "frac_of_hbm": round(gbs / world / peak, 4), "per_op": per_op,
             "final_purity": purity, "expec": list(vals), "gpu_launches": int(launches1.value - launches0.value),
