@@ -310,72 +310,35 @@ template <>
 struct DenseKOp<3> { typedef qgfx::CopN<8> type; static constexpr bool complex = true; };
 
 // Four targets (a 16-amplitude group, the real 32x32 operator): each thread owns a group,
-// as k_denseK_fx does, and forms its 32 outputs one row at a time.
-//  * The operator sits in shared memory and every row is read as 16-byte broadcasts (all
-//    threads of a warp are on the same row), not from the parameter bank, where a row
-//    chosen at run time becomes a constant-bank load per coefficient.
-//  * The group's 16 amplitudes pass through the warp's shared stage (each load
-//    instruction takes amplitude j of the warp's 32 groups) while the thread scans its
-//    own group's exponents; the limbs are then made from the stage, so the inputs never
-//    sit in registers beside the limbs, and 4 blocks of 128 fit on an SM instead of 2.
-//  * Each output is four independent integer sums (exact, so their order does not
-//    matter): short dependency chains for the integer multiply-add pipe.
-// The limbs and the sums are fx_prepare_e / fx_row's, so the bits equal k_denseK_fx's.
-#define D4_THREADS 128
+// as k_denseK_fx does, and forms its 32 outputs one row at a time; the operator sits in
+// shared memory and every row is read as 16-byte broadcasts (all threads of a warp are on
+// the same row), not from the parameter bank, where a row chosen at run time becomes a
+// constant-bank load per coefficient.  The limbs and the integer sums are fx_prepare /
+// fx_row's, so the bits equal k_denseK_fx's.
 template <int NB>
-__global__ void __launch_bounds__(D4_THREADS, 4) k_dense4_fx(double2* __restrict__ a, qidx numIts, Ins ins, qidx mask,
-                                                             MatK<4> M, qgfx::OpN<32> C) {
-    constexpr int D = 16, N = 32, S = qgfx::FxShift<N>::S;
+__global__ void __launch_bounds__(128) k_dense4_fx(double2* __restrict__ a, qidx numIts, Ins ins, qidx mask, MatK<4> M,
+                                                   qgfx::OpN<32> C) {
+    constexpr int D = 16, N = 32;
     __shared__ __align__(16) int32_t sh[N][N], sl[N][N];
-    __shared__ double2 stage[D4_THREADS / 32][D][32];           // [warp][amplitude j][lane]
-    for (int e = threadIdx.x; e < N * N; e += D4_THREADS) {
+    for (int e = threadIdx.x; e < N * N; e += blockDim.x) {
         sh[e / N][e % N] = C.h[e / N][e % N];
         sl[e / N][e % N] = C.l[e / N][e % N];
     }
     __syncthreads();
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const qidx stride = (qidx)gridDim.x * D4_THREADS;
-    // every thread of a warp runs the same number of iterations (the loop bound is rounded
-    // to whole warps), so the warp-wide synchronisation below is always reached by all
-    const qidx numWarpIts = (numIts + 31) / 32 * 32;
-    for (qidx n = blockIdx.x * (qidx)D4_THREADS + threadIdx.x; n - lane < numWarpIts; n += stride) {
-        const bool valid = n < numIts;
-        const qidx base = insert_bits<NB>(valid ? n : 0, ins) | mask;
-        int e = 0, emin = 4096, eg = 1, any = 0;
+    const qidx stride = (qidx)gridDim.x * blockDim.x;
+    for (qidx n = blockIdx.x * (qidx)blockDim.x + threadIdx.x; n < numIts; n += stride) {
+        const qidx base = insert_bits<NB>(n, ins) | mask;
+        double in[N];
 #pragma unroll
         for (int j = 0; j < D; j++) {
-            const double2 v = valid ? ld_amp(a + base + M.off[j]) : make_double2(0.0, 0.0);
-            stage[warp][j][lane] = v;
-            const uint64_t u0 = qgfx::f64_bits(v.x), u1 = qgfx::f64_bits(v.y);
-            const int e0 = (int)((u0 >> 52) & 0x7FF), e1 = (int)((u1 >> 52) & 0x7FF);
-            e = max(e, max(e0, e1));
-            emin = min(emin, min(e0, e1));
-            eg = max(eg, max(e0 + (e0 == 0), e1 + (e1 == 0)));
-            any |= ((u0 << 1) | (u1 << 1)) != 0;
+            const double2 v = ld_amp(a + base + M.off[j]);
+            in[2 * j] = v.x;
+            in[2 * j + 1] = v.y;
         }
-        __syncwarp();
-        // fx_prepare_e's choice for this group
-        const int t = e + C.expo - qgfx::FxShift<N>::TOFF;
-        const int tg = eg + C.expo - qgfx::FxShift<N>::TOFF;
-        int path;          // 0: near form, 1: general form, 2: all zero, 3: FP64
-        if (emin >= 1 && e <= 2046 && e - emin <= 31 && 1023 + t >= 1 && 1023 + qgfx::FxShift<N>::RL + t <= 2046) path = 0;
-        else if (1023 + tg < 1 || 1023 + qgfx::FxShift<N>::RL + tg > 2046 || eg == 2047) path = any ? 3 : 2;
-        else path = 1;
-        if (valid && path <= 2) {
-            int32_t xh[N], xl[N];
-#pragma unroll
-            for (int j = 0; j < D; j++) {
-                const double2 v = stage[warp][j][lane];
-                const uint64_t u0 = qgfx::f64_bits(v.x), u1 = qgfx::f64_bits(v.y);
-                if (path == 0) {
-                    qgfx::to_limbs_near<S>((uint32_t)(u0 >> 32), (uint32_t)u0, e - (int)((u0 >> 52) & 0x7FF), xh[2 * j], xl[2 * j]);
-                    qgfx::to_limbs_near<S>((uint32_t)(u1 >> 32), (uint32_t)u1, e - (int)((u1 >> 52) & 0x7FF), xh[2 * j + 1], xl[2 * j + 1]);
-                } else {
-                    qgfx::to_limbs(u0, eg, xh[2 * j], xl[2 * j], S);
-                    qgfx::to_limbs(u1, eg, xh[2 * j + 1], xl[2 * j + 1], S);
-                }
-            }
-            const uint32_t down = (uint32_t)(path == 0 ? t : tg) << 20;
+        int32_t xh[N], xl[N];
+        uint32_t down;
+        bool zero;
+        if (qgfx::fx_prepare<N>(C, in, xh, xl, down, zero)) {
 #pragma unroll 1
             for (int r = 0; r < D; r++) {
                 double out[2];
@@ -383,6 +346,8 @@ __global__ void __launch_bounds__(D4_THREADS, 4) k_dense4_fx(double2* __restrict
                 for (int c = 0; c < 2; c++) {
                     const int4* hr = (const int4*)sh[2 * r + c];
                     const int4* lr = (const int4*)sl[2 * r + c];
+                    // four independent integer sums (exact, so their order does not matter):
+                    // short dependency chains for the integer multiply-add pipe
                     int64_t h0 = 0, h1 = 0, m0 = 0, m1 = 0;
 #pragma unroll
                     for (int q = 0; q < N / 4; q++) {
@@ -392,21 +357,23 @@ __global__ void __launch_bounds__(D4_THREADS, 4) k_dense4_fx(double2* __restrict
                         h0 += (int64_t)xh[4 * q + 2] * H.z; m0 += (int64_t)xh[4 * q + 2] * Lo.z; m1 += (int64_t)xl[4 * q + 2] * H.z;
                         h1 += (int64_t)xh[4 * q + 3] * H.w; m0 += (int64_t)xh[4 * q + 3] * Lo.w; m1 += (int64_t)xl[4 * q + 3] * H.w;
                     }
-                    out[c] = path == 2 ? 0.0 : qgfx::fx_to_double((h0 + h1) + ((m0 + m1) >> 32), down);
+                    out[c] = zero ? 0.0 : qgfx::fx_to_double((h0 + h1) + ((m0 + m1) >> 32), down);
                 }
                 st_amp(a + base + M.off[r], make_double2(out[0], out[1]));
             }
-        } else if (valid) {
-            // FP64 products from the staged inputs
+        } else {
+            // nothing has been stored: reload the group and use FP64
+            double2 v[D];
+#pragma unroll
+            for (int j = 0; j < D; j++) v[j] = a[base + M.off[j]];
 #pragma unroll 1
             for (int r = 0; r < D; r++) {
-                double2 acc = cmul(M.m[r * D], stage[warp][0][lane]);
+                double2 acc = cmul(M.m[r * D], v[0]);
 #pragma unroll
-                for (int j = 1; j < D; j++) acc = cfma(M.m[r * D + j], stage[warp][j][lane], acc);
+                for (int j = 1; j < D; j++) acc = cfma(M.m[r * D + j], v[j], acc);
                 st_amp(a + base + M.off[r], acc);
             }
         }
-        __syncwarp();      // the stage is read before the next iteration writes it
     }
 }
 
@@ -978,7 +945,7 @@ int launch_denseK(double2* amps, qidx numIts, const QubitPlan& p, const qg_cplx*
             if constexpr (K == 4) {
                 if (ok) {
                     // the operator as shared-memory broadcasts
-#define L(NBV) k_dense4_fx<NBV><<<resident_blocks(k_dense4_fx<NBV>, numIts, D4_THREADS), D4_THREADS, 0, st>>>(amps, numIts, p.ins, p.stateMask, M, C)
+#define L(NBV) k_dense4_fx<NBV><<<resident_blocks(k_dense4_fx<NBV>, numIts, 128), 128, 0, st>>>(amps, numIts, p.ins, p.stateMask, M, C)
                     QG_DISPATCH_NB(p.numFixed, L)
 #undef L
                     return QG_OK;
