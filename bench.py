@@ -903,8 +903,20 @@ def run_gates(args, world, rank, local, dist):
             m = (qg_cplx * (D * D))(*[qg_cplx(v.real, v.imag) for v in u])
             t = (C.c_int * k)(*range(3, 3 + k))
             ms = timed(lambda: _lib.check(L.qg_sv_anyCtrlAnyTargDenseMatr(p, n, None, None, 0, t, k, m, 0, None)))
-            rows.append({"gate": f"dense, {k} target(s)", "products": mode, "ms": round(ms, 4),
+            label = "fixed (tensor-core slices)" if mode == "fixed" and k >= 3 else mode
+            rows.append({"gate": f"dense, {k} target(s)", "products": label, "ms": round(ms, 4),
                          "gbs": round(2 * state_bytes / ms / 1e6, 1)})
+            if mode == "fixed" and k >= 3:
+                # the same gate on the lowest qubits, and through the integer-pipe kernels
+                t0 = (C.c_int * k)(*range(k))
+                ms = timed(lambda: _lib.check(L.qg_sv_anyCtrlAnyTargDenseMatr(p, n, None, None, 0, t0, k, m, 0, None)))
+                rows.append({"gate": f"dense, {k} target(s) on qubits 0..{k - 1}", "products": label, "ms": round(ms, 4),
+                             "gbs": round(2 * state_bytes / ms / 1e6, 1)})
+                _lib.check(L.qg_set_tensor_slices(0))
+                ms = timed(lambda: _lib.check(L.qg_sv_anyCtrlAnyTargDenseMatr(p, n, None, None, 0, t, k, m, 0, None)))
+                _lib.check(L.qg_set_tensor_slices(1))
+                rows.append({"gate": f"dense, {k} target(s)", "products": "fixed (integer pipes)", "ms": round(ms, 4),
+                             "gbs": round(2 * state_bytes / ms / 1e6, 1)})
         ctrl = C.c_int(2)
         ms = timed(lambda: _lib.check(L.qg_sv_anyCtrlOneTargDiagMatr(p, n, C.byref(ctrl), None, 1, 7, phase, None)))
         rows.append({"gate": "controlled phase (quarter of the amplitudes)", "products": mode, "ms": round(ms, 4),
@@ -946,8 +958,15 @@ def run_gates(args, world, rank, local, dist):
         _lib.check(L.qg_set_fp64_products(0 if mode == "fixed" else 1))
         for name, passes, fn in dm_gates:
             ms = timed(fn)
-            rows.append({"gate": f"DM {nd}q: {name}", "products": mode, "ms": round(ms, 4),
-                         "gbs": round(passes * pass_bytes / ms / 1e6, 1)})
+            four = "2 qubits" in name
+            rows.append({"gate": f"DM {nd}q: {name}", "products": "fixed (tensor-core slices)" if mode == "fixed" and four else mode,
+                         "ms": round(ms, 4), "gbs": round(passes * pass_bytes / ms / 1e6, 1)})
+            if mode == "fixed" and four:
+                _lib.check(L.qg_set_tensor_slices(0))
+                ms = timed(fn)
+                _lib.check(L.qg_set_tensor_slices(1))
+                rows.append({"gate": f"DM {nd}q: {name}", "products": "fixed (integer pipes)", "ms": round(ms, 4),
+                             "gbs": round(passes * pass_bytes / ms / 1e6, 1)})
     _lib.check(L.qg_set_fp64_products(0))
     Q.destroyQureg(dm)
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}

@@ -102,6 +102,20 @@ int qg_measure_fp64_fma_rate(double* fmaPerSecond);
  * process-wide. */
 int qg_set_fp64_products(int mode);
 int qg_get_fp64_products(int* mode);
+/* Three- and four-target dense gates in product mode 0 (no counterpart in the reference):
+ *   1 (default) on the bf16 tensor cores as exact 8-bit slices when the register holds at
+ *     least one tile of 128 amplitude groups per SM: each group's inputs share one exponent,
+ *     are cut into seven signed 8-bit digits and multiplied with the matrix's eight digits,
+ *     every digit product and sum exact (FP32 sums of integers below 2^22), and combined in
+ *     int64; per output the error is below (2^(K+1) + 2) 2^-53 of (largest |amp| in the
+ *     group) x (largest |matrix entry|), as for mode 0's integer form; groups holding Inf/NaN
+ *     or with extreme scales are evaluated in FP64;
+ *   2 the same at every register size;
+ *   0 the integer-pipe fixed-point kernels.
+ * A launch whose bounded wait runs out sets the tensor-core error flag (qg_tc_get_error_flag);
+ * the next such launch returns QG_ERR_TIMEOUT.  Process-wide. */
+int qg_set_tensor_slices(int mode);
+int qg_get_tensor_slices(int* mode);
 
 /* ------------------------------------------------------------------ launch-shape autotuner
  * (no counterpart in the reference, whose launch sizes are fixed formulas,

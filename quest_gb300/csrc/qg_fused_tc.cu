@@ -20,6 +20,7 @@
 // sets the error flag, waits for the tensor core, frees the TMEM and returns.
 #include "qg_common.cuh"
 #include "qg_tc_plan.h"
+#include "qg_tcgen05.cuh"
 
 #include <chrono>
 #include <mutex>
@@ -93,17 +94,6 @@ void qg_tc_build_operands(const std::complex<double>* m, float* out) {
 
 // ---------------------------------------------------------------- device helpers
 
-__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ uint64_t make_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
-    uint64_t d = 0;
-    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
-    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
-    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
-    d |= (uint64_t)1 << 46;   // descriptor version for tcgen05
-    return d;                 // base offset 0, relative LBO, no swizzle
-}
-
 // kind::tf32 instruction descriptor: D=F32, A=B=TF32, both K-major, N=64, M=128
 __device__ __forceinline__ uint32_t make_idesc() {
     return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(TC_N >> 3) << 17) | ((uint32_t)(TC_M >> 4) << 24);
@@ -122,37 +112,8 @@ __device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t adesc, uint64
         :: "r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc));
 }
 
-__device__ __forceinline__ uint64_t globaltimer_ns() {
-    uint64_t t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
-        : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
-    return ok != 0;
-}
-
-// bounded wait on an mbarrier phase; false if it ran out.  The clock is read once
-// per 256 polls, not per poll.
-__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
-    if (mbar_try_wait(bar, parity)) return true;
-    const uint64_t t0 = globaltimer_ns();
-    for (;;) {
-        for (int i = 0; i < 256; i++)
-            if (mbar_try_wait(bar, parity)) return true;
-        if (globaltimer_ns() - t0 > TC_WAIT_NS) return false;
-    }
-}
-
-#define TMEM_LD16(taddr, r)                                                                              \
-    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];" \
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),    \
-                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]) \
-                 : "r"(taddr))
+// bounded wait with this kernel's limit
+__device__ __forceinline__ bool mbar_wait_tc(uint32_t bar, uint32_t parity) { return mbar_wait_bounded(bar, parity, TC_WAIT_NS); }
 
 // ---------------------------------------------------------------- kernel
 
@@ -204,25 +165,6 @@ struct TcArgs {
 // Shared memory and L1 share one array per SM, and L1 holds the loads in flight, so a
 // launch asks only for what its mode uses.
 #define WS_SMEM_BYTES(nstage) (4 * TC_A_BYTES + 2 * TC_B_BYTES + (nstage) * WS_STAGE_BYTES + 128 + 1024)
-
-__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(bar) : "memory");
-}
-
-// named barrier over `count` threads (a multiple of 32)
-__device__ __forceinline__ void named_sync(int id, int count) {
-    asm volatile("bar.sync %0, %1;" :: "r"(id), "r"(count) : "memory");
-}
-
-// named barrier that also ORs a flag over the `count` threads: every thread gets the
-// same answer, so a group that must leave a loop leaves it together
-__device__ __forceinline__ bool named_sync_or(int id, int count, bool flag) {
-    uint32_t r;
-    asm volatile(
-        "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\tbar.red.or.pred q, %2, %3, p;\n\tselp.u32 %0, 1, 0, q;\n\t}\n"
-        : "=r"(r) : "r"((uint32_t)flag), "r"(id), "r"(count) : "memory");
-    return r != 0;
-}
 
 // staging-buffer slot of local index e: the low five bits are XORed with the next
 // five, so that both address-order and group-row-order accesses of a warp spread
@@ -325,7 +267,7 @@ __global__ void __launch_bounds__(WsShape<TPR, NBUF>::THREADS, 1) k32_fused_tc(T
                 if (i + NBUF - 1 < nLocal) load(x[(b + NBUF - 1) % NBUF], i + NBUF - 1);
                 const int s = (int)(i & 1);
                 const uint32_t u = (uint32_t)(i >> 1);
-                bool bad = u >= 1 && !mbar_wait_bounded(mmaDone + 8 * s, (u - 1) & 1);
+                bool bad = u >= 1 && !mbar_wait_tc(mmaDone + 8 * s, (u - 1) & 1);
                 if (bad) *abortFlag = 1;
                 if constexpr (STAGED) {
                     // all producers have finished reading the previous tile's staging
@@ -374,8 +316,8 @@ __global__ void __launch_bounds__(WsShape<TPR, NBUF>::THREADS, 1) k32_fused_tc(T
             for (qidx i = 0; i < nLocal; i++) {
                 const int s = (int)(i & 1);
                 const uint32_t u = (uint32_t)(i >> 1);
-                if (!mbar_wait_bounded(aFull + 8 * s, u & 1)) *abortFlag = 1;
-                if (!*abortFlag && u >= 1 && !mbar_wait_bounded(tmemEmpty + 8 * s, (u - 1) & 1)) *abortFlag = 1;
+                if (!mbar_wait_tc(aFull + 8 * s, u & 1)) *abortFlag = 1;
+                if (!*abortFlag && u >= 1 && !mbar_wait_tc(tmemEmpty + 8 * s, (u - 1) & 1)) *abortFlag = 1;
                 if (*abortFlag) break;
                 asm volatile("tcgen05.fence::after_thread_sync;");
                 const uint32_t aH = smem_addr(smem + (2 * s) * TC_A_BYTES), aL = aH + TC_A_BYTES;
@@ -397,7 +339,7 @@ __global__ void __launch_bounds__(WsShape<TPR, NBUF>::THREADS, 1) k32_fused_tc(T
             // no MMA may still be running when the accumulators are freed
             if (issued > 0) {
                 const qidx l = issued - 1;
-                if (!mbar_wait_bounded(mmaDone + 8 * (int)(l & 1), (uint32_t)(l >> 1) & 1)) *abortFlag = 1;
+                if (!mbar_wait_tc(mmaDone + 8 * (int)(l & 1), (uint32_t)(l >> 1) & 1)) *abortFlag = 1;
             }
         }
         __syncwarp();
@@ -424,7 +366,7 @@ __global__ void __launch_bounds__(WsShape<TPR, NBUF>::THREADS, 1) k32_fused_tc(T
         for (qidx i = 0; i < nLocal; i++) {
             const int s = (int)(i & 1);
             const uint32_t u = (uint32_t)(i >> 1);
-            const bool waited = mbar_wait_bounded(mmaDone + 8 * s, u & 1);
+            const bool waited = mbar_wait_tc(mmaDone + 8 * s, u & 1);
             if constexpr (STAGED_OUT) {
                 // the whole epilogue leaves together (named barriers below); this barrier
                 // also orders the previous tile's staging reads before this tile's writes
@@ -529,6 +471,15 @@ int qg_tc_prepare() {
         QG_CUDA(cudaFuncSetAttribute(k32_fused_tc<TC_TPR_STAGED, TC_NBUF_STAGED, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, WS_SMEM_BYTES(2)));
         d->attr = true;
     }
+    return QG_OK;
+}
+
+// the current device's error flag as the device sees it (prepared on first use)
+int qg_tc_device_flag(int** out) {
+    TcDevice* d = nullptr;
+    QG_TRY(tc_current(&d));
+    if (!d->hostFlag) QG_TRY(qg_tc_prepare());
+    *out = d->devFlag;
     return QG_OK;
 }
 

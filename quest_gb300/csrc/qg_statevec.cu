@@ -917,6 +917,11 @@ int qg_sv_anyCtrlTwoTargDenseMatr(void* amps, int numQubits, const int* ctrls, c
 
 }  // extern "C"
 
+bool qg_dense_tc_wanted(qidx numIts);
+template <int K>
+int qg_dense_tc_launch(double2* amps, qidx numIts, const Ins& ins, qidx mask, const double2* m, const qidx* off,
+                       cudaStream_t st, bool* used);
+
 namespace {
 
 template <int K>
@@ -929,6 +934,14 @@ int launch_denseK(double2* amps, qidx numIts, const QubitPlan& p, const qg_cplx*
         for (int b = 0; b < K; b++)
             if ((j >> b) & 1) o |= (qidx)1 << targs[b];
         M.off[j] = o;
+    }
+    if constexpr (K == 3 || K == 4) {
+        // exact 8-bit slices on the tensor cores (qg_dense_tc.cu)
+        if (qg_fp64_products_mode() == QG_FP64_PRODUCTS_FIXED && qg_dense_tc_wanted(numIts)) {
+            bool used = false;
+            QG_TRY(qg_dense_tc_launch<K>(amps, numIts, p.ins, p.stateMask, M.m, M.off, st, &used));
+            if (used) return QG_OK;
+        }
     }
     if constexpr (K <= 4) {
         if (qg_fp64_products_mode() == QG_FP64_PRODUCTS_FIXED) {

@@ -1,0 +1,191 @@
+"""Three- and four-target dense gates on the tensor cores as exact 8-bit slices
+(quest_gb300/csrc/qg_dense_tc.cu).
+
+* Bit for bit the host restatement of the kernel's arithmetic (tests/slices_ref.cpp over
+  qg_slices.h): this shows that every digit product and digit sum on the tensor cores is
+  exact, for every target placement (lowest bits included), with controls, for registers
+  of less than one tile of 128 groups, and for groups that go to FP64 (Inf, NaN, denormal
+  and extreme scales), which must give the FP64 path's bits.
+* Within the FP64 bar (max-abs <= 1e-12) of the oracle, in the automatic mode at sizes where
+  it picks the tensor cores, for state vectors and a density matrix's two-qubit Kraus map.
+* The switch and the error flag: no bounded wait runs out."""
+import ctypes
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+import qcircuits as qc
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-12
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "..", "quest_gb300", "csrc")
+
+
+@pytest.fixture(scope="module")
+def host_ref(tmp_path_factory):
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("g++ not available")
+    so = str(tmp_path_factory.mktemp("slices") / "libslices_ref.so")
+    subprocess.run([gxx, "-O2", "-std=c++17", "-shared", "-fPIC", "-I", CSRC, os.path.join(HERE, "slices_ref.cpp"),
+                    "-o", so], check=True)
+    L = ctypes.CDLL(so)
+    ip = ctypes.POINTER(ctypes.c_int)
+    dp = ctypes.POINTER(ctypes.c_double)
+    L.slices_apply_state.argtypes = [ctypes.c_int, ctypes.c_int, ip, ctypes.c_int, ip, ip, dp, dp]
+    L.slices_apply_state.restype = ctypes.c_int
+    return L
+
+
+def _ints(v):
+    a = (ctypes.c_int * max(1, len(v)))()
+    for i, x in enumerate(v):
+        a[i] = int(x)
+    return a
+
+
+def host_apply(L, nq, targs, ctrls, states, u, amps):
+    a = np.ascontiguousarray(amps, dtype=np.complex128).copy()
+    m = np.ascontiguousarray(u, dtype=np.complex128)
+    dp = ctypes.POINTER(ctypes.c_double)
+    rc = L.slices_apply_state(nq, len(targs), _ints(targs), len(ctrls), _ints(ctrls), _ints(states),
+                              m.ctypes.data_as(dp), a.ctypes.data_as(dp))
+    assert rc == 0
+    return a
+
+
+def gate_text(targs, ctrls, states, u):
+    k = len(targs)
+    t = " ".join(map(str, targs))
+    if ctrls:
+        return (f"CUK {len(ctrls)} {' '.join(map(str, ctrls))} {' '.join(map(str, states))} {k} {t} "
+                f"{qc.mat_tokens(u)}\n")
+    return f"UK {k} {t} {qc.mat_tokens(u)}\n"
+
+
+def run_gpu(env, text, nq, amps, is_dm=False):
+    from quest_gb300.circuit import run_text
+    Q = env.Q
+    q = Q.createDensityQureg(nq) if is_dm else Q.createQureg(nq)
+    try:
+        env.set_amps(q, amps)
+        res, _ = run_text(text, q)
+        return env.get_amps(q), res
+    finally:
+        Q.destroyQureg(q)
+
+
+def _lib():
+    from quest_gb300._lib import lib
+    return lib()
+
+
+def _set_slices(mode):
+    assert _lib().qg_set_tensor_slices(mode) == 0
+
+
+def _flag():
+    f = ctypes.c_int(-1)
+    assert _lib().qg_tc_get_error_flag(ctypes.byref(f)) == 0
+    return f.value
+
+
+def _same_bits(a, b):
+    x, y = a.view(np.float64), b.view(np.float64)
+    return np.array_equal(x, y) or bool(np.all((x == y) | (np.isnan(x) & np.isnan(y))))
+
+
+CASES = [
+    # nq, targets, controls, control states
+    (12, [5, 9, 1, 11], [], []),
+    (13, [0, 1, 2, 3], [], []),            # the four lowest bits: each group is 16 adjacent amplitudes
+    (10, [3, 0, 8, 6], [], []),            # 64 groups: less than one tile
+    (16, [15, 9, 4, 12], [2], [1]),
+    (15, [7, 0, 13, 2], [5, 10], [0, 1]),
+    (12, [2, 7, 0], [], []),
+    (14, [13, 1, 6], [3], [0]),
+    (11, [0, 1, 2], [], []),
+]
+
+
+@pytest.mark.parametrize("nq,targs,ctrls,states", CASES, ids=[f"{c[0]}q-{len(c[1])}t-{len(c[2])}c" for c in CASES])
+def test_bits_equal_the_host_restatement(env, host_ref, nq, targs, ctrls, states):
+    rng = np.random.default_rng(nq * 100 + len(targs) * 10 + len(ctrls))
+    u = qc.haar_unitary(1 << len(targs), rng)
+    amps = qc.random_statevector(nq, nq + 7)
+    want = host_apply(host_ref, nq, targs, ctrls, states, u, amps)
+    try:
+        _set_slices(2)
+        got, _ = run_gpu(env, gate_text(targs, ctrls, states, u), nq, amps)
+    finally:
+        _set_slices(1)
+    assert _same_bits(got, want)
+    ref, _, _ = qc.oracle().run(gate_text(targs, ctrls, states, u), nq, 0, amps)
+    assert np.max(np.abs(got - ref)) <= TOL
+    assert _flag() == 0
+
+
+@pytest.mark.parametrize("k", [3, 4])
+def test_special_groups_take_the_fp64_path(env, host_ref, k):
+    """Groups holding Inf/NaN, denormals only, magnitudes from 1e-300 to 1e300, and zeros."""
+    nq = 12
+    rng = np.random.default_rng(40 + k)
+    amps = qc.random_statevector(nq, 41) * 10.0 ** rng.integers(-300, 300, 1 << nq)
+    amps[3] = complex(np.inf, 0)
+    amps[100] = complex(np.nan, 1.0)
+    amps[200:232] = 0
+    amps[300:340] = complex(3e-312, -1e-310)
+    amps[500] = complex(1e-310, 0)
+    targs = [int(v) for v in rng.choice(nq, k, replace=False)]
+    u = qc.haar_unitary(1 << k, rng)
+    want = host_apply(host_ref, nq, targs, [], [], u, amps)
+    try:
+        _set_slices(2)
+        got, _ = run_gpu(env, gate_text(targs, [], [], u), nq, amps)
+    finally:
+        _set_slices(1)
+    assert _same_bits(got, want)
+    assert _flag() == 0
+
+
+@pytest.mark.parametrize("nq,k", [(20, 4), (21, 3), (19, 4)])
+def test_automatic_mode_meets_the_fp64_bar(env, nq, k):
+    """Sizes where mode 1 picks the tensor cores (at least one tile per SM); the integer
+    kernels (mode 0) on the same gates for comparison."""
+    rng = np.random.default_rng(nq + k)
+    text = ""
+    for _ in range(3):
+        t = [int(v) for v in rng.choice(nq, k, replace=False)]
+        text += gate_text(t, [], [], qc.haar_unitary(1 << k, rng))
+    text += "TOTALPROB\n"
+    amps = qc.random_statevector(nq, nq)
+    want, wres, _ = qc.oracle().run(text, nq, 0, amps)
+    outs = {}
+    try:
+        for mode in (1, 0):
+            _set_slices(mode)
+            outs[mode], res = run_gpu(env, text, nq, amps)
+            assert np.max(np.abs(outs[mode] - want)) <= TOL
+            assert np.max(np.abs(res - wres)) <= TOL
+    finally:
+        _set_slices(1)
+    assert _flag() == 0
+
+
+def test_density_matrix_kraus_map_on_the_tensor_cores(env):
+    """A two-qubit Kraus map on a 10-qubit density matrix: a four-target superoperator on
+    2^20 amplitudes, in the automatic mode."""
+    nq = 10
+    rng = np.random.default_rng(77)
+    ops = qc.random_kraus(2, 4, rng)
+    text = f"KRAUS 2 3 8 4 {' '.join(qc.mat_tokens(o) for o in ops)}\nPURITY\nTOTALPROB\n"
+    amps = qc.random_density_matrix(nq, 78)
+    want, wres, _ = qc.oracle().run(text, nq, 1, amps)
+    got, res = run_gpu(env, text, nq, amps, is_dm=True)
+    assert np.max(np.abs(got - want)) <= TOL
+    assert np.max(np.abs(res - wres)) <= TOL
+    assert _flag() == 0
