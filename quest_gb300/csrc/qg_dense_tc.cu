@@ -98,38 +98,40 @@ __device__ __forceinline__ void mma_f16(uint32_t tmem_d, uint64_t adesc, uint64_
         :: "r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc));
 }
 
-// W of a real with high and low words (hi, lo) at group scale Eg (qg_slices.h input_word;
-// Eg >= 2047 + 64 gives W = CX, all digits zero)
+// |V| + CX of a real with high and low words (hi, lo) at group scale Eg (qg_slices.h
+// input_word; Eg >= 2047 + 64 gives CX, all digits zero)
 __device__ __forceinline__ uint64_t dt_word(uint32_t hi, uint32_t lo, int Eg) {
     const int d = Eg - (int)((hi >> 20) & 0x7FFu);
     const uint64_t m2 = ((uint64_t)((hi & 0xFFFFFu) | 0x100000u) << 33) | ((uint64_t)lo << 1);
-    const uint64_t V = d < 64 ? m2 >> d : 0ull;
-    const uint64_t sg = (uint64_t)(int64_t)((int32_t)hi >> 31);      // 0 or all ones
-    return (V ^ sg) + qgsl::CX - sg;                                  // CX + V or CX - V
+    return (d < 64 ? m2 >> d : 0ull) + qgsl::CX;
 }
 
-// fp16x2 (byte b0 of g - 128, byte b1 of g - 128): 0x64XX is 1024 + XX in fp16, exactly,
-// and 1024 + XX - 1152 = XX - 128
-__device__ __forceinline__ uint32_t dt_pair(uint32_t g, uint32_t sel) {
+// fp16x2 (sign0 (byte b0 of g - 128), sign1 (byte b1 of g - 128)): 0x64XX is 1024 + XX in
+// fp16, exactly, and sgn (1024 + XX) - sgn 1152 = sgn (XX - 128) in one exact FMA
+__device__ __forceinline__ uint32_t dt_pair(uint32_t g, uint32_t sel, __half2 sgn, __half2 nc) {
     const uint32_t h = __byte_perm(g, 0x64646464u, sel);
-    const __half2 v = __hsub2(*reinterpret_cast<const __half2*>(&h), __halves2half2(__ushort_as_half(0x6480), __ushort_as_half(0x6480)));
+    const __half2 v = __hfma2(*reinterpret_cast<const __half2*>(&h), sgn, nc);
     return *reinterpret_cast<const uint32_t*>(&v);
 }
 
-// the 7 digit words (fp16x2: digit i of real k, digit i of real k + 1) of two words
-__device__ __forceinline__ void dt_digits2(uint64_t w0, uint64_t w1, uint32_t (&out)[qgsl::XD]) {
-    const uint32_t lo0 = (uint32_t)w0, lo1 = (uint32_t)w1, hi0 = (uint32_t)(w0 >> 32), hi1 = (uint32_t)(w1 >> 32);
-    const uint32_t gl01 = __byte_perm(lo0, lo1, 0x5140u);   // lo bytes 0, 1 of both: digits 6, 5
-    const uint32_t gl23 = __byte_perm(lo0, lo1, 0x7362u);   // lo bytes 2, 3: digits 4, 3
-    const uint32_t gh01 = __byte_perm(hi0, hi1, 0x5140u);   // hi bytes 0, 1 (W bytes 4, 5): digits 2, 1
-    const uint32_t gh2 = __byte_perm(hi0, hi1, 0x6262u);    // hi byte 2 (W byte 6): digit 0
-    out[0] = dt_pair(gh2, 0x4140u);
-    out[1] = dt_pair(gh01, 0x4342u);
-    out[2] = dt_pair(gh01, 0x4140u);
-    out[3] = dt_pair(gl23, 0x4342u);
-    out[4] = dt_pair(gl23, 0x4140u);
-    out[5] = dt_pair(gl01, 0x4342u);
-    out[6] = dt_pair(gl01, 0x4140u);
+// the 7 digit words (fp16x2: digit i of real k, digit i of real k + 1) of two reals with
+// high words hi0, hi1 (their signs) and magnitude words w0, w1
+__device__ __forceinline__ void dt_digits2(uint32_t hi0, uint32_t hi1, uint64_t w0, uint64_t w1, uint32_t (&out)[qgsl::XD]) {
+    const uint32_t sb = 0x3C003C00u | ((hi0 >> 16) & 0x8000u) | (hi1 & 0x80000000u);   // (+-1, +-1)
+    const uint32_t nb = 0xE480E480u ^ (sb & 0x80008000u);                              // (-+1152, -+1152)
+    const __half2 sgn = *reinterpret_cast<const __half2*>(&sb), nc = *reinterpret_cast<const __half2*>(&nb);
+    const uint32_t lo0 = (uint32_t)w0, lo1 = (uint32_t)w1, h0 = (uint32_t)(w0 >> 32), h1 = (uint32_t)(w1 >> 32);
+    const uint32_t gl01 = __byte_perm(lo0, lo1, 0x5140u);   // W bytes 0, 1 of both: digits 6, 5
+    const uint32_t gl23 = __byte_perm(lo0, lo1, 0x7362u);   // W bytes 2, 3: digits 4, 3
+    const uint32_t gh01 = __byte_perm(h0, h1, 0x5140u);     // W bytes 4, 5: digits 2, 1
+    const uint32_t gh2 = __byte_perm(h0, h1, 0x6262u);      // W byte 6: digit 0
+    out[0] = dt_pair(gh2, 0x4140u, sgn, nc);
+    out[1] = dt_pair(gh01, 0x4342u, sgn, nc);
+    out[2] = dt_pair(gh01, 0x4140u, sgn, nc);
+    out[3] = dt_pair(gl23, 0x4342u, sgn, nc);
+    out[4] = dt_pair(gl23, 0x4140u, sgn, nc);
+    out[5] = dt_pair(gl01, 0x4342u, sgn, nc);
+    out[6] = dt_pair(gl01, 0x4140u, sgn, nc);
 }
 
 // the output from this lane's eight digit sums (column q of each).  Each sum s is an
@@ -251,8 +253,8 @@ __global__ void __launch_bounds__(DtShape<KR>::THREADS, 1) k_dense_tc(const __gr
 #pragma unroll
                 for (int a = 0; a < 4; a++) {
                     const double2 v = x[4 * c + a];
-                    dt_digits2(dt_word((uint32_t)__double2hiint(v.x), (uint32_t)__double2loint(v.x), Ew),
-                               dt_word((uint32_t)__double2hiint(v.y), (uint32_t)__double2loint(v.y), Ew), dg[a]);
+                    const uint32_t hx = (uint32_t)__double2hiint(v.x), hy = (uint32_t)__double2hiint(v.y);
+                    dt_digits2(hx, hy, dt_word(hx, (uint32_t)__double2loint(v.x), Ew), dt_word(hy, (uint32_t)__double2loint(v.y), Ew), dg[a]);
                 }
                 if (i + 1 < nLocal) load4(i + 1, c);
                 unsigned char* dst = aBuf + dt_core_offset(row, part * S::NV + 8 * c, 128);

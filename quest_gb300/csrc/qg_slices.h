@@ -13,17 +13,17 @@
 //
 //  * Inputs share one scale per group: Eg = the largest biased exponent among the group's
 //    KR reals.  Each real v (biased exponent e, 53-bit significand m with the implicit bit)
-//    becomes V = trunc(m 2^(1 - (Eg - e))) = trunc(v 2^(1076 - Eg)), |V| < 2^54, and
-//    W = V + CX (CX = 0x80 in each of 7 bytes), 0 <= W < 2^56.  Digit i (i = 0 most
-//    significant) is byte 6 - i of W minus 128, in [-128, 127], and V = sum_i d_i 2^(8(6-i)).
-//    Zeros and denormals enter as V = 0 (Eg >= 56 below, so a denormal is below 2^-55 of
-//    the group's largest value).
+//    becomes |V| = trunc(m 2^(1 - (Eg - e))) = trunc(|v| 2^(1076 - Eg)) < 2^54, and
+//    W = |V| + CX (CX = 0x80 in each of 7 bytes), 0 <= W < 2^56.  Digit i (i = 0 most
+//    significant) is sign(v) (byte 6 - i of W minus 128), in [-128, 128], and
+//    V = sign(v) |V| = sum_i d_i 2^(8(6-i)).  Zeros and denormals enter as V = 0 (Eg >= 56
+//    below, so a denormal is below 2^-55 of the group's largest value).
 //  * The operator shares one scale: eR with every |R| < 2^eR; Vr = round(R * 2^(61 - eR)),
 //    |Vr| <= 2^61, Wr = Vr + CR (0x80 in each of 8 bytes), digit j = byte 7 - j of Wr minus
 //    128, and Vr = sum_j r_j 2^(8(7-j)).
 //  * sum_k V_k Vr_nk = sum_s acc_s 2^(104 - 8s) with acc_s = sum over i + j = s of
 //    sum_k d_i[k] r_j[n][k].  The sums s = 0..7 are kept (s = i + j >= 8 is dropped).
-//    Each acc_s has at most 7 digit pairs of KR <= 32 products of magnitude <= 2^14:
+//    Each acc_s has at most 7 digit pairs of KR <= 32 products of magnitude <= 128 x 128:
 //    |acc_s| < 2^22, exact in FP32 and through the tensor cores' FP32 sums.
 //  * Y = sum_{s<=7} acc_s 2^(8(7-s)) (|Y| <= 2^72), Y' = floor(Y / 2^11) in int64, and
 //    y = (double)Y' * 2^(Eg + eR - 1078), the conversion rounding to nearest even and the
@@ -62,16 +62,18 @@ const int YSHIFT = 11;                       // Y' = floor(Y / 2^11)
 const int SCALE_OFF = 1078;                  // y = Y' * 2^(Eg + eR - 1078)
 const int EMIN = 56, EMAX = 2039;            // normal groups: EMIN <= Eg + eR <= EMAX
 
-// W of the real with bits u at the group scale Eg (Eg >= its biased exponent)
+// W = |V| + CX of the real with bits u at the group scale Eg (Eg >= its biased exponent)
 QG_HD uint64_t input_word(uint64_t u, int Eg) {
     const int d = Eg - (int)((u >> 52) & 0x7FF);
     const uint64_t m2 = ((u & 0xFFFFFFFFFFFFFull) | (1ull << 52)) << 1;
-    const uint64_t V = d < 64 ? m2 >> d : 0ull;
-    return (u >> 63) ? CX - V : CX + V;
+    return (d < 64 ? m2 >> d : 0ull) + CX;
 }
 
-// digit i of an input word
-QG_HD int input_digit(uint64_t W, int i) { return (int)((W >> (8 * (6 - i))) & 0xFF) - 128; }
+// digit i of the real with bits u and word W
+QG_HD int input_digit(uint64_t u, uint64_t W, int i) {
+    const int b = (int)((W >> (8 * (6 - i))) & 0xFF) - 128;
+    return (u >> 63) ? -b : b;
+}
 
 // Y' from the eight exact digit sums acc[0..7] (acc[s] for s = i + j)
 QG_HD int64_t combine(const int32_t* acc) {
@@ -139,14 +141,17 @@ inline bool apply_group(const int8_t* dig, int eR, int KR, const double* x, doub
     } else if (Eg < EMIN || Eg + eR < EMIN || Eg + eR > EMAX) {
         return false;
     }
-    int64_t W[64];
-    for (int k = 0; k < KR; k++) W[k] = (int64_t)input_word(qgfx::f64_bits(x[k]), Eg);
+    uint64_t U[64], W[64];
+    for (int k = 0; k < KR; k++) {
+        U[k] = qgfx::f64_bits(x[k]);
+        W[k] = input_word(U[k], Eg);
+    }
     for (int n = 0; n < KR; n++) {
         int32_t acc[NSUM] = {0, 0, 0, 0, 0, 0, 0, 0};
         for (int i = 0; i < XD; i++)
             for (int j = 0; j < RD && i + j < NSUM; j++) {
                 int32_t s = 0;
-                for (int k = 0; k < KR; k++) s += input_digit((uint64_t)W[k], i) * dig[(j * KR + n) * KR + k];
+                for (int k = 0; k < KR; k++) s += input_digit(U[k], W[k], i) * dig[(j * KR + n) * KR + k];
                 acc[i + j] += s;
             }
         y[n] = to_output(combine(acc), Eg + eR - SCALE_OFF);

@@ -80,9 +80,13 @@ static void check_group(const std::vector<double>& R, int KR, const std::vector<
     }
     // digits of the inputs add back to V = trunc(x 2^(1076 - Eg))
     for (int k = 0; k < KR; k++) {
-        const uint64_t W = qgsl::input_word(qgfx::f64_bits(x[k]), Eg);
+        const uint64_t u = qgfx::f64_bits(x[k]), W = qgsl::input_word(u, Eg);
         int64_t sum = 0;
-        for (int i = 0; i < qgsl::XD; i++) sum = sum * 256 + qgsl::input_digit(W, i);
+        for (int i = 0; i < qgsl::XD; i++) {
+            const int dgt = qgsl::input_digit(u, W, i);
+            if (dgt < -128 || dgt > 128) fail("input digit out of range");
+            sum = sum * 256 + dgt;
+        }
         const ld V = std::trunc(std::ldexp((ld)x[k], 1076 - Eg));
         if ((ld)sum != V) fail("input digits do not add back");
         if (std::fabs(V) >= std::ldexp((ld)1, 54)) fail("input value above 2^54");
@@ -95,7 +99,8 @@ static void check_group(const std::vector<double>& R, int KR, const std::vector<
                 const int j = s - i;
                 if (j < 0 || j >= qgsl::RD) continue;
                 for (int k = 0; k < KR; k++)
-                    acc += (int64_t)qgsl::input_digit(qgsl::input_word(qgfx::f64_bits(x[k]), Eg), i) * dig[(j * KR + n) * KR + k];
+                    acc += (int64_t)qgsl::input_digit(qgfx::f64_bits(x[k]), qgsl::input_word(qgfx::f64_bits(x[k]), Eg), i) *
+                           dig[(j * KR + n) * KR + k];
             }
             if (acc >= ((int64_t)1 << 22) || acc <= -((int64_t)1 << 22)) fail("digit sum reached 2^22");
         }
