@@ -40,9 +40,13 @@
 #include <vector>
 
 #define DT_WAIT_NS 2000000000ull   // a tile takes microseconds; 2 s means it never completes
+#define DT_STAGE_MIN_BIT 1         // staged inputs when the lowest target or control is at least this qubit
 #define DT_SKIP INT_MIN            // epilogue: nothing to store for this group (else the scale << 20)
 
-template <int KR>
+// KR reals per group; STG: the producers' inputs pass through a shared-memory stage
+// filled by cp.async (else they load into registers, the next tile's loads issued per
+// k-core as its digits are formed)
+template <int KR, bool STG>
 struct DtShape {
     static constexpr int D = KR / 2;                      // amplitudes per group
     static constexpr int AMPS = D / 2;                    // amplitudes per producer thread
@@ -58,9 +62,18 @@ struct DtShape {
     static constexpr int DCOLS = qgsl::NSUM * KR;         // accumulator columns per tile
     static constexpr int TMEM_COLS = 2 * DCOLS;           // 512 (KR = 32) or 256
     static constexpr int INFO_BYTES = 4 * 128 * 4 + 8 * (KR / 2);   // + the offsets off[j]
+    // the producers' input staging: NSTAGE tiles of their amplitudes (NSTAGE - 1 in flight
+    // while one is cut into digits), filled by cp.async, so the bytes in flight per SM do
+    // not depend on registers
+    static constexpr int TILE_IN = 128 * D * 16;          // input bytes of one tile
+    static constexpr int NSTAGE = (96 * 1024) / TILE_IN;  // 3 (four targets) or 6 (three)
+    static constexpr int STAGE_BYTES = STG ? NSTAGE * TILE_IN : 0;
+    static constexpr int CHUNK = STG ? 8 : 4;             // output reals per TMEM-load round of the epilogue
+    // 128 bytes of barriers, TMEM address and abort flag; 128 of alignment slack
+    static constexpr int SMEM_USED = 2 * A_BYTES + B_BYTES + STAGE_BYTES + INFO_BYTES + 128 + 128;
     // one CTA per SM: at least 120 KiB asked for, so that a second never fits beside it
-    static constexpr int SMEM_USED = 2 * A_BYTES + B_BYTES + INFO_BYTES + 128 + 1024;
     static constexpr int SMEM = SMEM_USED > 120 * 1024 ? SMEM_USED : 120 * 1024;
+    static_assert(SMEM_USED <= 232448, "shared memory per block");
 };
 
 template <int KR>
@@ -75,7 +88,7 @@ struct DtArgs {
     int eR;                       // the operator's scale
     int* errorFlag;
     double2 m[(KR / 2) * (KR / 2)];                 // the matrix, for groups evaluated in FP64
-    uint4 bops[DtShape<KR>::B_BYTES / 16];         // the operator's digits in the B tile layout
+    uint4 bops[DtShape<KR, false>::B_BYTES / 16];  // the operator's digits in the B tile layout
 };
 
 // byte offset of element (row, k) in the K-major no-swizzle layout of a tile of `rows`
@@ -142,7 +155,8 @@ __device__ __forceinline__ void dt_digits2(uint32_t hi0, uint32_t hi1, uint64_t 
 // Y' = h1 2^37 + h2 2^21 + l1 2^5 + floor(l2 / 2^11) is formed from them modulo 2^64
 // with one constant, DT_K, taken off (qg_slices.h combine states the same value).
 #define DT_K 0x6811681168116800ull
-__device__ __forceinline__ double dt_output(const uint32_t (&r)[qgsl::NSUM][4], int q, int shift20) {
+template <int W>
+__device__ __forceinline__ double dt_output(const uint32_t (&r)[qgsl::NSUM][W], int q, int shift20) {
     uint32_t t[qgsl::NSUM];
 #pragma unroll
     for (int s = 0; s < qgsl::NSUM; s++) t[s] = __float_as_uint(__uint_as_float(r[s][q]) + 12582912.0f);
@@ -153,17 +167,18 @@ __device__ __forceinline__ double dt_output(const uint32_t (&r)[qgsl::NSUM][4], 
     return hi == 0 ? 0.0 : __hiloint2double(hi + shift20, __double2loint(d));
 }
 
-template <int KR>
-__global__ void __launch_bounds__(DtShape<KR>::THREADS, 1) k_dense_tc(const __grid_constant__ DtArgs<KR> args) {
-    using S = DtShape<KR>;
+template <int KR, bool STG>
+__global__ void __launch_bounds__(DtShape<KR, STG>::THREADS, 1) k_dense_tc(const __grid_constant__ DtArgs<KR> args) {
+    using S = DtShape<KR, STG>;
     constexpr int D = S::D, AMPS = S::AMPS;
-    extern __shared__ __align__(1024) unsigned char dt_smem_raw[];
-    unsigned char* smem = (unsigned char*)(((uintptr_t)dt_smem_raw + 1023) & ~(uintptr_t)1023);
+    extern __shared__ __align__(128) unsigned char dt_smem_raw[];
+    unsigned char* smem = (unsigned char*)(((uintptr_t)dt_smem_raw + 127) & ~(uintptr_t)127);
     unsigned char* sA = smem;                                   // A[2], XD slices each
     unsigned char* sB = smem + 2 * S::A_BYTES;
-    int* sInfo = (int*)(sB + S::B_BYTES);                       // [tile & 3][row]: output scale or DT_SKIP
+    double2* sStage = (double2*)(sB + S::B_BYTES);              // [stage][amplitude a][producer]
+    int* sInfo = (int*)(sB + S::B_BYTES + S::STAGE_BYTES);      // [tile & 3][row]: output scale or DT_SKIP
     qidx* sOff = (qidx*)(sInfo + 4 * 128);                      // off[j] (a per-lane index into the parameters would be a serial constant load)
-    uint64_t* bars = (uint64_t*)(sB + S::B_BYTES + S::INFO_BYTES);   // aFull[2], infoReady[2], mmaDone[2], tmemEmpty[2]
+    uint64_t* bars = (uint64_t*)(sB + S::B_BYTES + S::STAGE_BYTES + S::INFO_BYTES);   // aFull[2], infoReady[2], mmaDone[2], tmemEmpty[2]
     uint32_t* tmemSlot = (uint32_t*)(bars + 8);
     volatile int* abortFlag = (volatile int*)(tmemSlot + 1);
 
@@ -203,16 +218,35 @@ __global__ void __launch_bounds__(DtShape<KR>::THREADS, 1) k_dense_tc(const __gr
         // lanes of each shared-store phase write 8 consecutive rows of one core column
         const int row = warp * 16 + (lane & 15), part = lane >> 4;
         const qidx rowOff = insert_bits<-1>((qidx)row, args.ins);
+        // STG: tile i's amplitudes of this thread go to stage i % NSTAGE by cp.async, NSTAGE - 1
+        // tiles ahead; each thread reads back only what it copied, so one wait_group per
+        // tile orders them (one commit per tile, empty past the last).  Otherwise the loads of
+        // tile i + 1 go into the registers of a k-core of tile i as soon as its digits are
+        // formed.  (Staging gains where consecutive groups are adjacent amplitudes; with qubit
+        // 0 among the targets or controls, a thread's own loads share sectors, which the
+        // register loads take from L1 and the L2-only copies do not.)
+        auto issue = [&](qidx i) {
+            if (i < nLocal && (first + i * step) * 128 + row < args.numIts) {
+                const double2* src = args.amps + (tile_base(i) + rowOff);
+                double2* dst = sStage + (size_t)(i % S::NSTAGE) * AMPS * S::PRODUCERS + tid;
+#pragma unroll
+                for (int a = 0; a < AMPS; a++)
+                    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;"
+                                 :: "r"(smem_addr(dst + a * S::PRODUCERS)), "l"(src + sOff[part * AMPS + a]) : "memory");
+            }
+            asm volatile("cp.async.commit_group;" ::: "memory");
+        };
         double2 x[AMPS];
-        // the loads of tile i + 1 go into the registers of a k-core of tile i as soon as its
-        // digits are formed, so a load has a whole tile of work to arrive in
         auto load4 = [&](qidx i, int c) {
             const bool ok = (first + i * step) * 128 + row < args.numIts;
-            const double2* p = args.amps + (tile_base(i) + rowOff);
+            const double2* src = args.amps + (tile_base(i) + rowOff);
 #pragma unroll
-            for (int a = 4 * c; a < 4 * c + 4; a++) x[a] = ok ? __ldcs(p + sOff[part * AMPS + a]) : make_double2(0.0, 0.0);
+            for (int a = 4 * c; a < 4 * c + 4; a++) x[a] = ok ? __ldcs(src + sOff[part * AMPS + a]) : make_double2(0.0, 0.0);
         };
-        if (nLocal > 0) {
+        if constexpr (STG) {
+#pragma unroll 1
+            for (int j = 0; j < S::NSTAGE - 1; j++) issue(j);
+        } else if (nLocal > 0) {
 #pragma unroll
             for (int c = 0; c < AMPS / 4; c++) load4(0, c);
         }
@@ -220,6 +254,13 @@ __global__ void __launch_bounds__(DtShape<KR>::THREADS, 1) k_dense_tc(const __gr
             const qidx g = (first + i * step) * 128 + row;
             const bool valid = g < args.numIts;
             double2* p = args.amps + (tile_base(i) + rowOff);
+            if constexpr (STG) {
+                issue(i + S::NSTAGE - 1);
+                asm volatile("cp.async.wait_group %0;" :: "n"(S::NSTAGE - 1) : "memory");
+                const double2* src = sStage + (size_t)(i % S::NSTAGE) * AMPS * S::PRODUCERS + tid;
+#pragma unroll
+                for (int a = 0; a < AMPS; a++) x[a] = valid ? src[a * S::PRODUCERS] : make_double2(0.0, 0.0);
+            }
             const int s = (int)(i & 1);
             const uint32_t u = (uint32_t)(i >> 1);
             // the group's scale: the largest biased exponent of this half, then of the partner's
@@ -256,7 +297,9 @@ __global__ void __launch_bounds__(DtShape<KR>::THREADS, 1) k_dense_tc(const __gr
                     const uint32_t hx = (uint32_t)__double2hiint(v.x), hy = (uint32_t)__double2hiint(v.y);
                     dt_digits2(hx, hy, dt_word(hx, (uint32_t)__double2loint(v.x), Ew), dt_word(hy, (uint32_t)__double2loint(v.y), Ew), dg[a]);
                 }
-                if (i + 1 < nLocal) load4(i + 1, c);
+                if constexpr (!STG) {
+                    if (i + 1 < nLocal) load4(i + 1, c);
+                }
                 unsigned char* dst = aBuf + dt_core_offset(row, part * S::NV + 8 * c, 128);
 #pragma unroll
                 for (int d = 0; d < qgsl::XD; d++) *(uint4*)(dst + d * S::SLICE) = make_uint4(dg[0][d], dg[1][d], dg[2][d], dg[3][d]);
@@ -280,6 +323,7 @@ __global__ void __launch_bounds__(DtShape<KR>::THREADS, 1) k_dense_tc(const __gr
                 for (int a = 0; a < AMPS; a++) p[sOff[part * AMPS + a]] = out[a];
             }
         }
+        if constexpr (STG) asm volatile("cp.async.wait_all;" ::: "memory");      // none left in flight at exit
     } else if (warp == S::MMA_WARP) {
         // ---------------- MMA issue (one thread)
         if (lane == 0) {
@@ -333,22 +377,26 @@ __global__ void __launch_bounds__(DtShape<KR>::THREADS, 1) k_dense_tc(const __gr
             const int shift20 = sInfo[(i & 3) * 128 + row];
             double2* dst = args.amps + (tile_base(i) + rowOff);
             const uint32_t taddr = tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)(s * S::DCOLS + half * (KR / 2));
-            // chunks of 4 output reals (2 amplitudes): 8 digit sums x 4 columns in registers
-            // (a loop, not unrolled: the smaller body was measured faster)
+            // chunks of CHUNK output reals: 8 digit sums x CHUNK columns in registers (a loop,
+            // not unrolled: the smaller body was measured faster)
+            constexpr int CH = S::CHUNK;
 #pragma unroll 1
-            for (int c = 0; c < KR / 8; c++) {
-                uint32_t r[qgsl::NSUM][4];
+            for (int c = 0; c < KR / 2 / CH; c++) {
+                uint32_t r[qgsl::NSUM][CH];
 #pragma unroll
-                for (int sd = 0; sd < qgsl::NSUM; sd++) TMEM_LD4(taddr + (uint32_t)(sd * KR + 4 * c), r[sd]);
+                for (int sd = 0; sd < qgsl::NSUM; sd++) {
+                    if constexpr (CH == 8) TMEM_LD8(taddr + (uint32_t)(sd * KR + CH * c), r[sd]);
+                    else TMEM_LD4(taddr + (uint32_t)(sd * KR + CH * c), r[sd]);
+                }
                 tmem_wait_ld();
-                if (c == KR / 8 - 1) {
+                if (c == KR / 2 / CH - 1) {
                     asm volatile("tcgen05.fence::before_thread_sync;");
                     mbar_arrive(tmemEmpty + 8 * s);
                 }
                 if (shift20 != DT_SKIP) {
 #pragma unroll
-                    for (int q = 0; q < 2; q++)
-                        __stcs(dst + offs[2 * c + q],
+                    for (int q = 0; q < CH / 2; q++)
+                        __stcs(dst + offs[CH / 2 * c + q],
                                make_double2(dt_output(r, 2 * q, shift20), dt_output(r, 2 * q + 1, shift20)));
                 }
             }
@@ -373,7 +421,7 @@ int qg_tc_device_flag(int** out);
 namespace {
 std::atomic<int> g_slices{1};
 
-template <int KR>
+template <int KR, bool STG>
 int dt_set_attr() {
     static std::mutex mu;
     static bool done[64] = {};
@@ -382,7 +430,7 @@ int dt_set_attr() {
     if (dev < 0 || dev >= 64) return qg_fail(QG_ERR_NOTSUP, "device %d is beyond this build's device table", dev);
     std::lock_guard<std::mutex> lock(mu);
     if (!done[dev]) {
-        QG_CUDA(cudaFuncSetAttribute(k_dense_tc<KR>, cudaFuncAttributeMaxDynamicSharedMemorySize, DtShape<KR>::SMEM));
+        QG_CUDA(cudaFuncSetAttribute(k_dense_tc<KR, STG>, cudaFuncAttributeMaxDynamicSharedMemorySize, DtShape<KR, STG>::SMEM));
         done[dev] = true;
     }
     return QG_OK;
@@ -404,7 +452,7 @@ template <int K>
 int qg_dense_tc_launch(double2* amps, qidx numIts, const Ins& ins, qidx mask, const double2* m, const qidx* off,
                        cudaStream_t st, bool* used) {
     constexpr int KR = 2 << K, D = 1 << K;
-    using S = DtShape<KR>;
+    using S = DtShape<KR, false>;
     *used = false;
     std::vector<double> u(2 * D * D), R(KR * KR);
     for (int i = 0; i < D * D; i++) { u[2 * i] = m[i].x; u[2 * i + 1] = m[i].y; }
@@ -414,7 +462,6 @@ int qg_dense_tc_launch(double2* amps, qidx numIts, const Ins& ins, qidx mask, co
     if (!qgsl::operator_digits(R.data(), KR, dig.data(), &eR)) return QG_OK;
     QG_TRY(qg_tc_take_error());
     QG_TRY(qg_tc_prepare());
-    QG_TRY(dt_set_attr<KR>());
     std::unique_ptr<DtArgs<KR>> a(new DtArgs<KR>());
     a->amps = amps;
     a->numIts = numIts;
@@ -434,7 +481,20 @@ int qg_dense_tc_launch(double2* amps, qidx numIts, const Ins& ins, qidx mask, co
                 bt[dt_core_offset(j * KR + n, k, S::B_ROWS) / 2] = qgsl::digit_half(dig[(j * KR + n) * KR + k]);
     std::memcpy(a->bops, bt.data(), S::B_BYTES);
     const unsigned grid = (unsigned)std::min<qidx>(a->numTiles, (qidx)qg_num_sms());
-    k_dense_tc<KR><<<grid, S::THREADS, S::SMEM, st>>>(*a);
+    // staged inputs for four targets when qubits 0..DT_STAGE_MIN_BIT-1 are neither targets
+    // nor controls (ins.low[0] = 2^p - 1 for the lowest of them, p)
+    bool staged = false;
+    if constexpr (KR == 32) {
+        staged = ins.num == 0 || ins.low[0] >= ((qidx)1 << DT_STAGE_MIN_BIT) - 1;
+        if (staged) {
+            QG_TRY((dt_set_attr<KR, true>()));
+            k_dense_tc<KR, true><<<grid, DtShape<KR, true>::THREADS, DtShape<KR, true>::SMEM, st>>>(*a);
+        }
+    }
+    if (!staged) {
+        QG_TRY((dt_set_attr<KR, false>()));
+        k_dense_tc<KR, false><<<grid, S::THREADS, S::SMEM, st>>>(*a);
+    }
     qg_note_launch();
     *used = true;
     return qg_check_launch("k_dense_tc");
