@@ -28,6 +28,11 @@
 using std::vector;
 typedef std::complex<double> cd;
 
+// backend internals (quest_gb300/csrc): the product mode, and whether a gate on numIts
+// amplitude groups takes the tensor-core slices
+int qg_fp64_products_mode();
+bool qg_dense_tc_wanted(long long numIts);
+
 namespace {
 
 const int QG_MAX_QUBITS_API = 40;    // 2^40 FP64 amplitudes = 16 TiB: far above one GPU
@@ -107,6 +112,54 @@ bool applyPendingOp(const Qureg& q, int qubit, const PendingOp& op, const char* 
     }
 }
 
+// Two qubits' superoperators, or a two-qubit unitary's, as one 16x16 superoperator on the
+// Choi targets (a, b, a + N, b + N): matrix index bit 0 = ket a, 1 = ket b, 2 = bra a,
+// 3 = bra b.  One pass of the four-target tensor-core kernel costs about what one pass of a
+// one-qubit superoperator does, so when that kernel runs (product mode 0, registers of at
+// least one tile per SM) pairs of pending qubits are applied together.
+bool pairSuperops(const Qureg& q) {
+    return q.isDensityMatrix && q.numQubits >= 3 && qg_fp64_products_mode() == 0 &&
+           qg_dense_tc_wanted((long long)1 << (2 * q.numQubits - 4));
+}
+
+bool applyPairOp(const Qureg& q, int a, int b, const cd (&M)[256], const char* func) {
+    qcomp_t k[256];
+    for (int i = 0; i < 256; i++) k[i] = qcomp_t{M[i].real(), M[i].imag()};
+    const int t[4] = {a, b, a + q.numQubits, b + q.numQubits};
+    return backend(qg_sv_anyCtrlAnyTargDenseMatr(q.gpuAmps, 2 * q.numQubits, nullptr, nullptr, 0, t, 4, k, 0, g_stream), func);
+}
+
+// Sa on qubit a and Sb on qubit b (4x4, index bit 0 = ket, bit 1 = bra), as the 16x16 above
+void kronPair(const cd (&Sa)[16], const cd (&Sb)[16], cd (&M)[256]) {
+    for (int j = 0; j < 16; j++)
+        for (int k = 0; k < 16; k++) {
+            const int ja = (j & 1) | (((j >> 2) & 1) << 1), jb = ((j >> 1) & 1) | (((j >> 3) & 1) << 1);
+            const int ka = (k & 1) | (((k >> 2) & 1) << 1), kb = ((k >> 1) & 1) | (((k >> 3) & 1) << 1);
+            M[j * 16 + k] = Sa[ja * 4 + ka] * Sb[jb * 4 + kb];
+        }
+}
+
+// applies a list of pending ops: in pairs when that pays (general superoperators first,
+// a remaining one with a channel), the rest one by one
+bool applyPendingList(const Qureg& q, std::vector<std::pair<int, PendingOp>>& todo, const char* func) {
+    if (todo.size() >= 2 && pairSuperops(q)) {
+        std::stable_partition(todo.begin(), todo.end(), [](const std::pair<int, PendingOp>& x) { return x.second.kind == PEND_GENERAL; });
+        size_t i = 0;
+        for (; i + 1 < todo.size(); i += 2) {
+            if (todo[i].second.kind != PEND_GENERAL) break;    // two channels: their own kernels are cheaper
+            cd M[256];
+            kronPair(todo[i].second.m, todo[i + 1].second.m, M);
+            if (!applyPairOp(q, todo[i].first, todo[i + 1].first, M, func)) return false;
+        }
+        for (; i < todo.size(); i++)
+            if (!applyPendingOp(q, todo[i].first, todo[i].second, func)) return false;
+        return true;
+    }
+    for (auto& kv : todo)
+        if (!applyPendingOp(q, kv.first, kv.second, func)) return false;
+    return true;
+}
+
 // applies the pending ops of the listed ket qubits (all of them when `qubits` is null)
 bool flushPending(const Qureg& q, const std::vector<int>* qubits, const char* func) {
     std::vector<std::pair<int, PendingOp>> todo;
@@ -127,9 +180,7 @@ bool flushPending(const Qureg& q, const std::vector<int>* qubits, const char* fu
             if (it->second.ops.empty()) g_pending.erase(it);
         }
     }
-    for (auto& kv : todo)
-        if (!applyPendingOp(q, kv.first, kv.second, func)) return false;
-    return true;
+    return applyPendingList(q, todo, func);
 }
 
 // forgets the pending ops of a Qureg whose state is about to be overwritten or freed
@@ -264,6 +315,16 @@ void applyDense(const Qureg& q, const int* ctrls, const int* states, int nc, con
         vector<int> touched = c;
         touched.insert(touched.end(), t.begin(), t.end());
         if (!flushPending(q, &touched, func)) return;
+        if (nt == 2 && nc == 0 && pairSuperops(q)) {
+            // U rho U^dagger in one pass: conj(U) (x) U on (t0, t1, t0 + N, t1 + N), the
+            // reference's two passes (ket, then conjugated bra) as one superoperator
+            cd M[256];
+            for (int j = 0; j < 16; j++)
+                for (int k = 0; k < 16; k++)
+                    M[j * 16 + k] = C(m[(j & 3) * 4 + (k & 3)]) * std::conj(C(m[(j >> 2) * 4 + (k >> 2)]));
+            applyPairOp(q, t[0], t[1], M, func);
+            return;
+        }
     }
     if (!denseSV(q, c, s, t, m, false, func)) return;
     if (!q.isDensityMatrix) return;
@@ -426,8 +487,8 @@ void syncQuESTEnv(void) {
         q.gpuAmps = (qcomp_t*)kv.first;
         q.numQubits = kv.second.numQubits;
         q.isDensityMatrix = 1;
-        for (auto& op : kv.second.ops)
-            if (!applyPendingOp(q, op.first, op.second, "syncQuESTEnv")) return;
+        std::vector<std::pair<int, PendingOp>> todo(kv.second.ops.begin(), kv.second.ops.end());
+        if (!applyPendingList(q, todo, "syncQuESTEnv")) return;
     }
     backend(qg_sync(), "syncQuESTEnv");
 }
