@@ -295,6 +295,18 @@ def run_gb300(args, world, rank, local, dist):
                 Q.applyTwoQubitPhaseShift(r, g[1], g[2], g[3])
             else:
                 Q.applyFullQuantumFourierTransform(r)
+        # one-qubit gates deferred by the API (applied four qubits per tensor-core pass)
+        # are applied now, on this step's stream, so the step's result is complete
+        Q.flushQuregDeferredOps(r)
+
+    def tc_times():
+        # durations of the tensor-core dense launches recorded since qg_dense_tc_timing(1)
+        n = C.c_int(0)
+        _lib.check(L.qg_dense_tc_timing_read(None, 0, C.byref(n)))
+        buf = (C.c_float * max(1, n.value))()
+        _lib.check(L.qg_dense_tc_timing_read(buf, n.value, C.byref(n)))
+        _lib.check(L.qg_dense_tc_timing(0))
+        return [buf[i] for i in range(n.value)]
 
     for _ in range(args.warmup):
         run_step()
@@ -304,6 +316,7 @@ def run_gb300(args, world, rank, local, dist):
     launches0 = C.c_int64(0)
     L.qg_get_launch_count(C.byref(launches0))
     start, stop = new_event(), new_event()
+    _lib.check(L.qg_dense_tc_timing(1))
     with ClockSampler(local) as clocks:
         barrier(dist)
         L.qg_sync()
@@ -313,6 +326,7 @@ def run_gb300(args, world, rank, local, dist):
         L.qg_event_record(stop, None)
         L.qg_sync()
         barrier(dist)
+    tc_ms = tc_times()
     launches1 = C.c_int64(0)
     L.qg_get_launch_count(C.byref(launches1))
     ms = C.c_float(0)
@@ -395,8 +409,10 @@ def run_gb300(args, world, rank, local, dist):
         _lib.check(L.qg_set_fp64_products(mode_val))
         Q.setQuregAmps(reg, 0, in_ptr, namps)
         timed_dense.clear()
+        _lib.check(L.qg_dense_tc_timing(1))
         run_step(record_dense=True, reg=reg)
         L.qg_sync()
+        mode_tc = tc_times()
         ms_list = []
         for x, y in timed_dense:
             v = C.c_float(0)
@@ -405,8 +421,12 @@ def run_gb300(args, world, rank, local, dist):
             L.qg_event_destroy(x)
             L.qg_event_destroy(y)
         timed_dense.clear()
-        modes[mode_name] = {"final_total_prob": Q.calcTotalProb(reg),
-                            "dense_kernel_ms": round(statistics.mean(ms_list), 4)}
+        modes[mode_name] = {"final_total_prob": Q.calcTotalProb(reg)}
+        if mode_tc:
+            modes[mode_name]["fused_pass_ms"] = round(statistics.mean(mode_tc), 4)
+            modes[mode_name]["fused_passes"] = len(mode_tc)
+        else:
+            modes[mode_name]["dense_kernel_ms"] = round(statistics.mean(ms_list), 4)
     _lib.check(L.qg_set_fp64_products(0 if args.fp64_products == "fixed" else 1))
     norm = Q.calcTotalProb(q)
     Q.destroyQureg(q2)
@@ -414,7 +434,11 @@ def run_gb300(args, world, rank, local, dist):
 
     value = world * args.steps * step_bytes / t_dev / 1e9
     e2e_value = world * e2e_steps * step_bytes / t_e2e / 1e9
-    avg_dense = statistics.mean(dense_ms) / 1e3
+    # the dominant kernel: the tensor-core passes of deferred one-qubit gates (four per
+    # pass) when the API defers them, else the per-gate dense kernel; either streams the
+    # state once per launch
+    fused = len(tc_ms) > 0
+    avg_dense = statistics.mean(tc_ms if fused else dense_ms) / 1e3
     dense_bytes = 2 * AMP_BYTES * (1 << nq)
     peaks = {}
     pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -434,15 +458,25 @@ def run_gb300(args, world, rank, local, dist):
     # = 8.530e9 B for 2^27 pairs: 63.55 B per pair; the FP64-FMA kernel's capture: 8.53e9 B too)
     if args.traffic is not None:
         traffic, traffic_src = args.traffic, "command line"
+    elif fused:
+        # the 26-qubit capture of the four-target kernel: 1.0739e9 + 1.0131e9 B for 2^26
+        # amplitudes (31.10 B per amplitude), profiles/k_dense_tc_26q_ncu.md
+        traffic = round(31.10 * (1 << nq))
+        traffic_src = "ncu capture of k_dense_tc at 26 qubits (31.10 B per amplitude) scaled to this size"
     else:
         traffic = round(63.55 * (1 << (nq - 1)))
         traffic_src = "ncu capture at 28 qubits (63.55 B per amplitude pair) scaled to this size"
-    kname = ("k_dense1_fx (applyCompMatr1, general complex 2x2, FP64 storage, fixed-point products)"
-             if args.fp64_products == "fixed" else "k_dense1 (applyCompMatr1, general complex 2x2, FP64)")
+    if fused:
+        kname = ("k_dense_tc (deferred one-qubit gates, four per pass, as one 16x16 operator: exact 8-bit "
+                 "slices on the fp16 tensor cores)")
+    elif args.fp64_products == "fixed":
+        kname = "k_dense1_fx (applyCompMatr1, general complex 2x2, FP64 storage, fixed-point products)"
+    else:
+        kname = "k_dense1 (applyCompMatr1, general complex 2x2, FP64)"
     roofline = {"bound": "hbm", "kernel": kname,
                 "achieved": round(achieved, 1), "peak": peak, "peak_source": peak_src, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": traffic, "traffic_source": traffic_src,
-                "launches_timed": len(dense_ms), "avg_launch_ms": round(avg_dense * 1e3, 4),
+                "launches_timed": len(tc_ms) if fused else len(dense_ms), "avg_launch_ms": round(avg_dense * 1e3, 4),
                 "fp64_fma_per_s": round(fma_rate.value, -8), "fp64_ceiling_gbs": round(fp64_ceiling_gbs, 1),
                 "fp64_ceiling_frac": round(achieved / fp64_ceiling_gbs, 4)}
 
@@ -460,7 +494,8 @@ def run_gb300(args, world, rank, local, dist):
         "ms_per_step": round(t_dev / args.steps * 1e3, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f64" if args.fp64_products == "fp64" else
-                 "f64 (storage and all other ops; general 2x2 products in 60-bit block-floating fixed point)",
+                 "f64 (storage and all other ops; general 2x2 products in 60-bit block-floating fixed point, "
+                 "deferred one-qubit gates four per pass as exact 8-bit slices on the fp16 tensor cores)",
         "data": "synthetic (seeded Gaussian state, seeded Haar gates)",
         "config": {"workload": f"{nq}-qubit FP64 statevector (16 GiB at 30 qubits), depth {args.depth} Haar 1q "
                                f"+ 15 CPhase per layer, then full QFT", "qubits": nq, "depth": args.depth,
@@ -475,7 +510,9 @@ def run_gb300(args, world, rank, local, dist):
                 "h2d_gbs": round(nbytes / (h2d_ms.value / 1e3) / 1e9, 1),
                 "d2h_gbs": round(nbytes / (d2h_ms.value / 1e3) / 1e9, 1)},
         "product_modes": {**modes, "note": "one step of the circuit from the same input in each mode; "
-                                            "dense_kernel_ms = mean CUDA-event time of the Haar-gate launches"},
+                                            "fused_pass_ms = mean CUDA-event time of the tensor-core passes of "
+                                            "deferred one-qubit gates (fixed point); dense_kernel_ms = mean time of "
+                                            "the per-gate Haar launches (IEEE FP64, not deferred)"},
         "gpu_launches": int(launches1.value - launches0.value),
         "roofline": roofline,
         "cpu_baseline": cpu,

@@ -116,6 +116,12 @@ int qg_get_fp64_products(int* mode);
  * the next such launch returns QG_ERR_TIMEOUT.  Process-wide. */
 int qg_set_tensor_slices(int mode);
 int qg_get_tensor_slices(int* mode);
+/* CUDA events around every tensor-core dense launch, for a caller's roofline: enable = 1
+ * starts recording (dropping earlier records), 0 stops; _read waits for the recorded
+ * launches and returns their durations in ms (numOut = how many were recorded, of which
+ * the first maxOut are written). */
+int qg_dense_tc_timing(int enable);
+int qg_dense_tc_timing_read(float* msOut, int maxOut, int* numOut);
 
 /* ------------------------------------------------------------------ launch-shape autotuner
  * (no counterpart in the reference, whose launch sizes are fixed formulas,

@@ -158,6 +158,14 @@ qcomp_t getQuregAmp(Qureg qureg, qindex index);
  * and the mirror is pageable.  No reference counterpart (the reference's mirror is
  * always pageable, qureg.cpp:157-168). */
 int   isQuregHostMirrorPinned(Qureg qureg);
+/* Applies the Qureg's deferred operations now, on the current stream, without waiting for
+ * them.  One-qubit unitaries and channels on density matrices, and one-qubit dense
+ * unitaries on statevectors of at least one tensor-core tile of amplitude groups per SM,
+ * are deferred and applied together (two or four qubits per pass) when any other call on
+ * the Qureg needs its state; every API call that reads or changes the state does that
+ * itself, so this is for callers that hand the amplitudes to other code (the C ABI, their
+ * own kernels, a stream-ordered copy).  No reference counterpart. */
+void  flushQuregDeferredOps(Qureg qureg);
 
 /* initialisations (quest/src/api/initialisations.cpp) */
 void initZeroState(Qureg qureg);

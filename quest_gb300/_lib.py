@@ -135,6 +135,8 @@ ABI = {
     "qg_get_fp64_products": [c_int_p],
     "qg_set_tensor_slices": [I],
     "qg_get_tensor_slices": [c_int_p],
+    "qg_dense_tc_timing": [I],
+    "qg_dense_tc_timing_read": [ctypes.POINTER(ctypes.c_float), I, c_int_p],
     "qg_set_kernel_shape": [I, I, I],
     "qg_get_kernel_shape": [I, c_int_p, c_int_p],
     "qg_autotune_fp64": [I, c_dbl_p, I, c_int_p],

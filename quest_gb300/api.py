@@ -198,6 +198,7 @@ _PROTOS = {
     "calcProbsOfAllMultiQubitOutcomes": (V, [ctypes.POINTER(D), Qureg, _IP, I]),
     "calcTotalProb": (D, [Qureg]),
     "isQuregHostMirrorPinned": (I, [Qureg]),
+    "flushQuregDeferredOps": (V, [Qureg]),
     "calcPurity": (D, [Qureg]),
     "createFullStateDiagMatr": (FullStateDiagMatr, [I]),
     "destroyFullStateDiagMatr": (V, [FullStateDiagMatr]),

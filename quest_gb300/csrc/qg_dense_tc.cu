@@ -421,6 +421,11 @@ int qg_tc_device_flag(int** out);
 namespace {
 std::atomic<int> g_slices{1};
 
+// optional CUDA events around each launch (qg_dense_tc_timing), for a caller's roofline
+std::mutex g_timeMu;
+bool g_timing = false;
+std::vector<std::pair<cudaEvent_t, cudaEvent_t>> g_times;
+
 template <int KR, bool STG>
 int dt_set_attr() {
     static std::mutex mu;
@@ -483,6 +488,16 @@ int qg_dense_tc_launch(double2* amps, qidx numIts, const Ins& ins, qidx mask, co
     const unsigned grid = (unsigned)std::min<qidx>(a->numTiles, (qidx)qg_num_sms());
     // staged inputs for four targets when qubits 0..DT_STAGE_MIN_BIT-1 are neither targets
     // nor controls (ins.low[0] = 2^p - 1 for the lowest of them, p)
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_timeMu);
+        if (g_timing) {
+            QG_CUDA(cudaEventCreate(&ev0));
+            QG_CUDA(cudaEventCreate(&ev1));
+            g_times.push_back({ev0, ev1});
+            QG_CUDA(cudaEventRecord(ev0, st));
+        }
+    }
     bool staged = false;
     if constexpr (KR == 32) {
         staged = ins.num == 0 || ins.low[0] >= ((qidx)1 << DT_STAGE_MIN_BIT) - 1;
@@ -495,6 +510,7 @@ int qg_dense_tc_launch(double2* amps, qidx numIts, const Ins& ins, qidx mask, co
         QG_TRY((dt_set_attr<KR, false>()));
         k_dense_tc<KR, false><<<grid, S::THREADS, S::SMEM, st>>>(*a);
     }
+    if (ev1) QG_CUDA(cudaEventRecord(ev1, st));
     qg_note_launch();
     *used = true;
     return qg_check_launch("k_dense_tc");
@@ -514,6 +530,32 @@ int qg_set_tensor_slices(int enable) {
 int qg_get_tensor_slices(int* enable) {
     if (!enable) return qg_fail(QG_ERR_ARG, "null argument");
     *enable = g_slices.load();
+    return QG_OK;
+}
+
+int qg_dense_tc_timing(int enable) {
+    std::lock_guard<std::mutex> lock(g_timeMu);
+    for (auto& e : g_times) {
+        cudaEventDestroy(e.first);
+        cudaEventDestroy(e.second);
+    }
+    g_times.clear();
+    g_timing = enable != 0;
+    return QG_OK;
+}
+
+int qg_dense_tc_timing_read(float* msOut, int maxOut, int* numOut) {
+    if (!numOut || (maxOut > 0 && !msOut)) return qg_fail(QG_ERR_ARG, "null argument");
+    std::lock_guard<std::mutex> lock(g_timeMu);
+    int n = 0;
+    for (auto& e : g_times) {
+        float ms = 0;
+        QG_CUDA(cudaEventSynchronize(e.second));
+        QG_CUDA(cudaEventElapsedTime(&ms, e.first, e.second));
+        if (n < maxOut) msOut[n] = ms;
+        n++;
+    }
+    *numOut = n;
     return QG_OK;
 }
 

@@ -82,7 +82,7 @@ bool checkEnv(const char* func) { return check(g_envInit, func, "The QuEST envir
 // other qubits commute with it).  A unitary followed by depolarising on the same qubit
 // then costs one pass instead of two.  A qubit whose only pending operation is a single
 // channel is applied with that channel's own kernel.
-enum { PEND_GENERAL = 0, PEND_DEPOL, PEND_DEPHASE, PEND_DAMP, PEND_PAULIS };
+enum { PEND_GENERAL = 0, PEND_DEPOL, PEND_DEPHASE, PEND_DAMP, PEND_PAULIS, PEND_SV };
 struct PendingOp {
     int kind;
     double p[3];      // the channel's parameters when kind is not PEND_GENERAL
@@ -90,6 +90,7 @@ struct PendingOp {
 };
 struct PendingSet {
     int numQubits;                      // the Qureg's (ket) qubits
+    bool dm;                            // a density matrix (else a statevector: PEND_SV ops)
     std::map<int, PendingOp> ops;       // ket qubit -> its pending op
 };
 std::map<const void*, PendingSet> g_pending;   // keyed by gpuAmps
@@ -104,6 +105,11 @@ bool applyPendingOp(const Qureg& q, int qubit, const PendingOp& op, const char* 
         case PEND_DEPHASE: return backend(qg_dm_oneQubitDephasing(q.gpuAmps, N, qubit, op.p[0], g_stream), func);
         case PEND_DAMP: return backend(qg_dm_oneQubitDamping(q.gpuAmps, N, qubit, op.p[0], g_stream), func);
         case PEND_PAULIS: return backend(qg_dm_oneQubitPauliChannel(q.gpuAmps, N, qubit, op.p[0], op.p[1], op.p[2], g_stream), func);
+        case PEND_SV: {
+            const qcomp_t k[4] = {qcomp_t{op.m[0].real(), op.m[0].imag()}, qcomp_t{op.m[1].real(), op.m[1].imag()},
+                                  qcomp_t{op.m[2].real(), op.m[2].imag()}, qcomp_t{op.m[3].real(), op.m[3].imag()}};
+            return backend(qg_sv_anyCtrlOneTargDenseMatr(q.gpuAmps, N, nullptr, nullptr, 0, qubit, k, g_stream), func);
+        }
         default: {
             qcomp_t k[16];
             for (int i = 0; i < 16; i++) k[i] = qcomp_t{op.m[i].real(), op.m[i].imag()};
@@ -139,9 +145,66 @@ void kronPair(const cd (&Sa)[16], const cd (&Sb)[16], cd (&M)[256]) {
         }
 }
 
+// Statevectors: one-qubit dense unitaries are deferred the same way (a pending 2x2 per
+// qubit, composed on the host) when the tensor-core kernel runs for four targets, and the
+// pending qubits are applied four at a time as the Kronecker product of their unitaries
+// (one pass instead of four), then three, two or one.
+bool deferSV(const Qureg& q) {
+    return !q.isDensityMatrix && q.numQubits >= 5 && qg_fp64_products_mode() == 0 &&
+           qg_dense_tc_wanted((long long)1 << (q.numQubits - 4));
+}
+
+// U applied after the qubit's pending unitary: pending = U * pending
+void addPendingSV(const Qureg& q, int qubit, const cd (&U)[4]) {
+    std::lock_guard<std::mutex> lock(g_pendingMu);
+    PendingSet& set = g_pending[q.gpuAmps];
+    set.numQubits = q.numQubits;
+    set.dm = false;
+    auto it = set.ops.find(qubit);
+    if (it == set.ops.end()) {
+        PendingOp op;
+        op.kind = PEND_SV;
+        op.p[0] = op.p[1] = op.p[2] = 0;
+        for (int i = 0; i < 16; i++) op.m[i] = i < 4 ? U[i] : cd(0);
+        set.ops[qubit] = op;
+        return;
+    }
+    cd* P = it->second.m;
+    const cd r0 = U[0] * P[0] + U[1] * P[2], r1 = U[0] * P[1] + U[1] * P[3];
+    const cd r2 = U[2] * P[0] + U[3] * P[2], r3 = U[2] * P[1] + U[3] * P[3];
+    P[0] = r0; P[1] = r1; P[2] = r2; P[3] = r3;
+}
+
+// pending unitaries of k statevector qubits as one 2^k x 2^k matrix (bit b of an index =
+// qubit b of the group), applied in one pass
+bool applySVGroup(const Qureg& q, const std::pair<int, PendingOp>* g, int k, const char* func) {
+    if (k == 1) return applyPendingOp(q, g[0].first, g[0].second, func);
+    const int D = 1 << k;
+    std::vector<qcomp_t> M((size_t)D * D);
+    int t[4];
+    for (int b = 0; b < k; b++) t[b] = g[b].first;
+    for (int j = 0; j < D; j++)
+        for (int c = 0; c < D; c++) {
+            cd v = 1;
+            for (int b = 0; b < k; b++) v *= g[b].second.m[((j >> b) & 1) * 2 + ((c >> b) & 1)];
+            M[(size_t)j * D + c] = qcomp_t{v.real(), v.imag()};
+        }
+    if (k == 2) return backend(qg_sv_anyCtrlTwoTargDenseMatr(q.gpuAmps, q.numQubits, nullptr, nullptr, 0, t[0], t[1], M.data(), g_stream), func);
+    return backend(qg_sv_anyCtrlAnyTargDenseMatr(q.gpuAmps, q.numQubits, nullptr, nullptr, 0, t, k, M.data(), 0, g_stream), func);
+}
+
 // applies a list of pending ops: in pairs when that pays (general superoperators first,
 // a remaining one with a channel), the rest one by one
 bool applyPendingList(const Qureg& q, std::vector<std::pair<int, PendingOp>>& todo, const char* func) {
+    if (!q.isDensityMatrix) {
+        size_t i = 0;
+        while (i < todo.size()) {
+            const int k = (int)std::min<size_t>(4, todo.size() - i);
+            if (!applySVGroup(q, &todo[i], k, func)) return false;
+            i += k;
+        }
+        return true;
+    }
     if (todo.size() >= 2 && pairSuperops(q)) {
         std::stable_partition(todo.begin(), todo.end(), [](const std::pair<int, PendingOp>& x) { return x.second.kind == PEND_GENERAL; });
         size_t i = 0;
@@ -194,6 +257,7 @@ void addPending(const Qureg& q, int qubit, const cd (&S)[16], int kind, double p
     std::lock_guard<std::mutex> lock(g_pendingMu);
     PendingSet& set = g_pending[q.gpuAmps];
     set.numQubits = q.numQubits;
+    set.dm = true;
     auto& ops = set.ops;
     auto it = ops.find(qubit);
     if (it == ops.end()) {
@@ -290,7 +354,8 @@ bool denseSV(const Qureg& q, const vector<int>& c, const vector<int>& s, const v
 
 // validateAndApplyAnyCtrlAnyTargUnitaryMatrix: operations.cpp:36-63
 void applyDense(const Qureg& q, const int* ctrls, const int* states, int nc, const int* targs, int nt, const qcomp_t* m, bool checkUnitary, const char* func) {
-    if (!checkQureg(q, func, q.isDensityMatrix != 0)) return;
+    const bool defer = deferSV(q);
+    if (!checkQureg(q, func, q.isDensityMatrix != 0 || defer)) return;
     if (!checkCtrlsTargs(q, ctrls, nc, targs, nt, func)) return;
     if (!checkStates(states, nc, func)) return;
     if (!check(nt >= 1, func, "At least one target qubit is required.")) return;
@@ -310,6 +375,16 @@ void applyDense(const Qureg& q, const int* ctrls, const int* states, int nc, con
                         k[((r1 << 1) | r0) * 4 + ((c1 << 1) | c0)] = std::conj(C(m[r1 * 2 + c1])) * C(m[r0 * 2 + c0]);
         addPending(q, t[0], k, PEND_GENERAL);
         return;
+    }
+    if (defer) {
+        if (nt == 1 && nc == 0) {
+            const cd U[4] = {C(m[0]), C(m[1]), C(m[2]), C(m[3])};
+            addPendingSV(q, t[0], U);
+            return;
+        }
+        vector<int> touched = c;          // other pending qubits commute with this gate
+        touched.insert(touched.end(), t.begin(), t.end());
+        if (!flushPending(q, &touched, func)) return;
     }
     if (q.isDensityMatrix) {
         vector<int> touched = c;
@@ -486,7 +561,7 @@ void syncQuESTEnv(void) {
         std::memset(&q, 0, sizeof(q));
         q.gpuAmps = (qcomp_t*)kv.first;
         q.numQubits = kv.second.numQubits;
-        q.isDensityMatrix = 1;
+        q.isDensityMatrix = kv.second.dm ? 1 : 0;
         std::vector<std::pair<int, PendingOp>> todo(kv.second.ops.begin(), kv.second.ops.end());
         if (!applyPendingList(q, todo, "syncQuESTEnv")) return;
     }
@@ -612,6 +687,11 @@ int isQuregHostMirrorPinned(Qureg qureg) {
     std::lock_guard<std::mutex> lock(g_mirrorMu);
     auto it = g_mirrorKind.find(qureg.cpuAmps);
     return it != g_mirrorKind.end() && it->second != MIRROR_PAGEABLE ? 1 : 0;
+}
+
+// applies the Qureg's deferred operations now, on the current stream, without waiting
+void flushQuregDeferredOps(Qureg q) {
+    checkQureg(q, "flushQuregDeferredOps");
 }
 
 void syncQuregToGpu(Qureg q) {
