@@ -173,6 +173,13 @@ int qg_sv_anyCtrlTwoTargDenseMatr(void* amps, int numQubits, const int* ctrls, c
 /* gpu_statevec_anyCtrlAnyTargDenseMatr_sub<NumCtrls,NumTargs,ApplyConj> (gpu_subroutines.hpp:64;
  * gpu_subroutines.cpp:396-507).  matr: 2^k x 2^k row-major HOST elements; matrix
  * index bit i is targs[i].  applyConj conjugates every element. */
+/* One step of the quantum Fourier transform on contiguous targets lowTarget..target
+ * (lowTarget + numLowBits == target): the Hadamard on `target`, then, for every amplitude
+ * whose bit `target` is set, the phase exp(i pi L / 2^numLowBits) with L = (index >>
+ * lowTarget) & (2^numLowBits - 1) -- the target's controlled phases of
+ * applyQuantumFourierTransform (operations.cpp:1934-1952), one pass instead of
+ * numLowBits + 1.  Fixed-point products (Inf/NaN and extreme scales in FP64). */
+int qg_sv_qftStep(void* amps, int numQubits, int target, int lowTarget, int numLowBits, void* stream);
 int qg_sv_anyCtrlAnyTargDenseMatr(void* amps, int numQubits, const int* ctrls, const int* ctrlStates, int numCtrls,
                                   const int* targs, int numTargs, const qg_cplx* matr, int applyConj, void* stream);
 

@@ -1,0 +1,138 @@
+// One step of the quantum Fourier transform on a statevector as one pass: the Hadamard on
+// target t followed by its controlled phases.  QuEST's applyQuantumFourierTransform
+// (quest/src/api/operations.cpp:1934-1952) applies, for each target t[n] from the top,
+// applyHadamard(t[n]) and then applyTwoQubitPhaseShift(t[n], t[n-m-1], pi / 2^(m+1)) for
+// m < n: one pass per gate, n + 1 passes for this step.  For contiguous targets
+// t[j] = t0 + j those phases multiply every amplitude whose bit t[n] is set by
+//     exp(i pi sum_{m<n} x_{t[n-m-1]} / 2^(m+1)) = exp(i pi L / 2^n),
+// L = (index >> t0) & (2^n - 1), so the step is a radix-2 butterfly with a twiddle:
+//     out0 = (a0 + a1) / sqrt2,   out1 = w^L (a0 - a1) / sqrt2,   w = exp(i pi / 2^n),
+// for each pair (a0, a1) of amplitudes that differ in bit t[n] only.
+//
+// Products in 60-bit block-floating fixed point on the integer pipes (as the one-target
+// kernels of qg_fixed.cuh; GB300's FP64 rate would bound the twiddle products): the pair's
+// four reals share the largest exponent and become integers below 2^60, sums and
+// differences are exact, the twiddle w^L / sqrt2 is the product of four tables of 256
+// values at scale 2^62 (indices: the four bytes of L), and each output is the top 64 bits
+// of its products, converted to double with the scale added to the exponent field.  Error
+// per output: a few units of 2^-57 of the pair's largest |amplitude|.  Pairs holding
+// Inf/NaN or with scales near the ends of the double range are evaluated in FP64.
+#include "qg_common.cuh"
+#include "qg_fixed.cuh"
+
+#include <cmath>
+
+struct QftTables {
+    long long t[4][256][2];     // table k, entry j: exp(i pi j 2^(8k) / 2^n) (k = 0: / sqrt2), (re, im) x 2^62
+};
+
+__device__ __forceinline__ long long mulhi(long long a, long long b) { return __mul64hi(a, b); }
+
+// (a * b) for complex values at scale 2^62 (|a|, |b| <= 1): the product at scale 2^62
+__device__ __forceinline__ void cmul62(long long ar, long long ai, long long br, long long bi, long long& cr, long long& ci) {
+    cr = (mulhi(ar, br) - mulhi(ai, bi)) * 4;
+    ci = (mulhi(ar, bi) + mulhi(ai, br)) * 4;
+}
+
+// v (bits u) at the pair scale eb: mant * 2^(7 + eff - eb), below 2^60 in magnitude
+__device__ __forceinline__ long long qft_fixed(uint64_t u, int eb) {
+    const int ei = (int)((u >> 52) & 0x7FF);
+    const uint64_t mant = (u & 0xFFFFFFFFFFFFFull) | (ei ? (1ull << 52) : 0ull);
+    const int d = eb - (ei + (ei == 0));
+    const uint64_t x = d < 64 ? (mant << 7) >> d : 0ull;
+    return (u >> 63) ? -(long long)x : (long long)x;
+}
+
+// Y * 2^t as a double (t = eb - 1080 keeps every nonzero output normal for 58 <= eb <= 2043)
+__device__ __forceinline__ double qft_double(long long Y, int t) {
+    if (Y == 0) return 0.0;
+    const double d = __ll2double_rn(Y);
+    return __hiloint2double(__double2hiint(d) + t * (1 << 20), __double2loint(d));
+}
+
+#define QFT_THREADS 256
+#define QFT_C (3260954456333195553LL)    // round(2^62 / sqrt2)
+
+__global__ void __launch_bounds__(QFT_THREADS) k_qft_step(double2* __restrict__ a, qidx numPairs, int tb, int lb, qidx lmask,
+                                                          int numTables, const __grid_constant__ QftTables T) {
+    __shared__ long long sT[4][256][2];
+    for (int e = threadIdx.x; e < numTables * 512; e += QFT_THREADS) (&sT[0][0][0])[e] = (&T.t[0][0][0])[e];
+    __syncthreads();
+    const qidx stride = (qidx)gridDim.x * QFT_THREADS;
+    const qidx lowMask = ((qidx)1 << tb) - 1;
+    for (qidx p = blockIdx.x * (qidx)QFT_THREADS + threadIdx.x; p < numPairs; p += stride) {
+        const qidx i0 = ((p & ~lowMask) << 1) | (p & lowMask), i1 = i0 | ((qidx)1 << tb);
+        const double2 v0 = ld_amp(a + i0), v1 = ld_amp(a + i1);
+        // the twiddle w^L / sqrt2 at scale 2^62
+        const qidx L = (i0 >> lb) & lmask;
+        long long wr = sT[0][L & 255][0], wi = sT[0][L & 255][1];
+        for (int k = 1; k < numTables; k++) {
+            const int j = (int)((L >> (8 * k)) & 255);
+            cmul62(wr, wi, sT[k][j][0], sT[k][j][1], wr, wi);
+        }
+        const uint64_t u[4] = {qgfx::f64_bits(v0.x), qgfx::f64_bits(v0.y), qgfx::f64_bits(v1.x), qgfx::f64_bits(v1.y)};
+        int eb = 1;
+        uint64_t any = 0;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const int ei = (int)((u[k] >> 52) & 0x7FF);
+            eb = max(eb, ei + (ei == 0));
+            any |= u[k] << 1;
+        }
+        double2 o0, o1;
+        if (any == 0) {
+            o0 = make_double2(0.0, 0.0);
+            o1 = o0;
+        } else if (eb >= 58 && eb <= 2043) {
+            const long long x0r = qft_fixed(u[0], eb), x0i = qft_fixed(u[1], eb);
+            const long long x1r = qft_fixed(u[2], eb), x1i = qft_fixed(u[3], eb);
+            const long long sr = x0r + x1r, si = x0i + x1i, dr = x0r - x1r, di = x0i - x1i;
+            // values * 2^(1082 - eb) / 4: (a0 + a1) / sqrt2 and w^L (a0 - a1) / sqrt2
+            const long long y0r = mulhi(sr, QFT_C), y0i = mulhi(si, QFT_C);
+            const long long y1r = mulhi(dr, wr) - mulhi(di, wi), y1i = mulhi(dr, wi) + mulhi(di, wr);
+            const int t = eb - 1080;
+            o0 = make_double2(qft_double(y0r, t), qft_double(y0i, t));
+            o1 = make_double2(qft_double(y1r, t), qft_double(y1i, t));
+        } else {
+            // FP64: Inf/NaN, or scales near the ends of the range
+            const double s = 0.70710678118654752440;
+            const double cr = (double)wr * 0x1p-62 / s, ci = (double)wi * 0x1p-62 / s;   // w^L
+            o0 = make_double2((v0.x + v1.x) * s, (v0.y + v1.y) * s);
+            const double dr = (v0.x - v1.x) * s, di = (v0.y - v1.y) * s;
+            o1 = make_double2(fma(dr, cr, -di * ci), fma(dr, ci, di * cr));
+        }
+        st_amp(a + i0, o0);
+        st_amp(a + i1, o1);
+    }
+}
+
+extern "C" {
+
+// One QFT step on a statevector: Hadamard on `target`, then for every amplitude whose bit
+// `target` is set the phase exp(i pi L / 2^numLowBits), L = (index >> lowTarget) &
+// (2^numLowBits - 1), with lowTarget + numLowBits == target (the step of
+// applyQuantumFourierTransform on the contiguous targets lowTarget..target).
+int qg_sv_qftStep(void* amps, int numQubits, int target, int lowTarget, int numLowBits, void* stream) {
+    QG_TRY(qg_check_amps(amps, numQubits));
+    if (target < 0 || target >= numQubits || lowTarget < 0 || numLowBits < 0 || lowTarget + numLowBits != target || numLowBits > 32)
+        return qg_fail(QG_ERR_ARG, "qftStep: target %d, low target %d, %d low bits", target, lowTarget, numLowBits);
+    QftTables T;
+    const int numTables = numLowBits <= 8 ? 1 : (numLowBits + 7) / 8;
+    const long double PI = 3.141592653589793238462643383279502884L;
+    for (int k = 0; k < numTables; k++)
+        for (int j = 0; j < 256; j++) {
+            // exp(i pi j 2^(8k) / 2^n), the first table with 1/sqrt2
+            const long double ang = PI * std::ldexp((long double)j, 8 * k - numLowBits);
+            const long double sc = (k == 0 ? 1.0L / std::sqrt(2.0L) : 1.0L) * 4611686018427387904.0L;   // 2^62
+            T.t[k][j][0] = (long long)std::llroundl(std::cos(ang) * sc);
+            T.t[k][j][1] = (long long)std::llroundl(std::sin(ang) * sc);
+        }
+    const qidx numPairs = (qidx)1 << (numQubits - 1);
+    const qidx lmask = numLowBits >= 63 ? -1 : (((qidx)1 << numLowBits) - 1);
+    const unsigned grid = (unsigned)std::min<qidx>((numPairs + QFT_THREADS - 1) / QFT_THREADS, (qidx)qg_num_sms() * 8);
+    k_qft_step<<<grid, QFT_THREADS, 0, qg_stream(stream)>>>((double2*)amps, numPairs, target, lowTarget, lmask, numTables, T);
+    qg_note_launch();
+    return qg_check_launch("k_qft_step");
+}
+
+}  // extern "C"

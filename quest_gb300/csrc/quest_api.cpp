@@ -1068,6 +1068,15 @@ void applyTwoQubitPhaseFlip(Qureg q, int t1, int t2) { qcomp_t d[2] = {{1, 0}, {
 void applyQuantumFourierTransform(Qureg q, int* t, int nt) {
     const char* func = "applyQuantumFourierTransform";
     if (!checkQureg(q, func) || !checkQubits(q, t, nt, func, "target qubits")) return;
+    bool contiguous = true;
+    for (int j = 1; j < nt; j++) contiguous = contiguous && t[j] == t[0] + j;
+    if (!q.isDensityMatrix && contiguous && qg_fp64_products_mode() == 0) {
+        // each step (Hadamard on t[n], then its n controlled phases) as one pass
+        for (int n = nt - 1; n >= 0; n--)
+            if (!backend(qg_sv_qftStep(q.gpuAmps, q.numQubits, t[n], t[0], n, g_stream), func)) return;
+        for (int n = 0; n < nt / 2; n++) applySwap(q, t[n], t[nt - 1 - n]);
+        return;
+    }
     const double PI = 3.141592653589793238462643383279502884;
     for (int n = nt - 1; n >= 0; n--) {
         applyHadamard(q, t[n]);

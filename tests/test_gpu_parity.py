@@ -402,3 +402,26 @@ def test_tiled_pauli_batch_string_shapes(env, nq, style):
         Q.destroyQureg(q)
     assert np.max(np.abs(np.array(list(got)) - want)) <= TOL
     assert bytes(got) == bytes(again)       # deterministic
+
+
+@pytest.mark.parametrize("nq,text", [
+    (12, "FQFT\n"),
+    (21, "FQFT\nTOTALPROB\n"),
+    (14, "QFT 5 3 4 5 6 7\n"),            # contiguous targets above qubit 0: one pass per step
+    (14, "QFT 4 9 2 12 5\n"),             # not contiguous: the gate-by-gate form
+    (10, "X 0\nFQFT\nFQFT\n"),
+])
+def test_qft_steps_vs_oracle(env, nq, text):
+    """The quantum Fourier transform with each step (Hadamard and its controlled phases)
+    as one fixed-point pass, in both product modes (IEEE FP64 keeps the gate-by-gate form)."""
+    from quest_gb300._lib import lib
+    amps = qc.random_statevector(nq, nq + 3)
+    want, wres, _ = qc.oracle().run(text, nq, 0, amps)
+    try:
+        for mode in (0, 1):
+            assert lib().qg_set_fp64_products(mode) == 0
+            got, res, _ = run_gpu(env, text, nq, 0, amps)
+            assert np.max(np.abs(got - want)) <= TOL
+            assert np.max(np.abs(res - wres), initial=0) <= TOL
+    finally:
+        lib().qg_set_fp64_products(0)
