@@ -173,6 +173,11 @@ int qg_sv_anyCtrlTwoTargDenseMatr(void* amps, int numQubits, const int* ctrls, c
 /* gpu_statevec_anyCtrlAnyTargDenseMatr_sub<NumCtrls,NumTargs,ApplyConj> (gpu_subroutines.hpp:64;
  * gpu_subroutines.cpp:396-507).  matr: 2^k x 2^k row-major HOST elements; matrix
  * index bit i is targs[i].  applyConj conjugates every element. */
+/* A set of controlled phases: every amplitude whose index has all bits of masks[f] set is
+ * multiplied by factors[f] (|factors[f]| = 1), f < num <= 32, in one pass (the phases
+ * commute); statevectors of at least 8 qubits.  Products in fixed point; the API defers
+ * CPhase, CZ, phase shifts, S, T and Z on large statevectors and applies them with this. */
+int qg_sv_phaseSet(void* amps, int numQubits, const int64_t* masks, const qg_cplx* factors, int num, void* stream);
 /* One step of the quantum Fourier transform on contiguous targets lowTarget..target
  * (lowTarget + numLowBits == target): the Hadamard on `target`, then, for every amplitude
  * whose bit `target` is set, the phase exp(i pi L / 2^numLowBits) with L = (index >>

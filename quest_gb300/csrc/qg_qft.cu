@@ -14,19 +14,42 @@
 // four reals share the largest exponent and become integers below 2^60, sums and
 // differences are exact, the twiddle w^L / sqrt2 is the product of four tables of 256
 // values at scale 2^62 (indices: the four bytes of L), and each output is the top 64 bits
-// of its products, converted to double with the scale added to the exponent field.  Error
-// per output: a few units of 2^-57 of the pair's largest |amplitude|.  Pairs holding
+// of its products (from 32-bit limbs), converted to double with the scale added to the
+// exponent field.  Error per output: a few units of 2^-57 of the pair's largest |amplitude|.  Pairs holding
 // Inf/NaN or with scales near the ends of the double range are evaluated in FP64.
+//
+// The same fixed-point steps apply a set of controlled phases in one pass (k_phase_set):
+// phase gates commute, so the API defers them (diagonal gates whose only factor != 1 is on
+// the all-ones state of their qubits: CPhase, CZ, phase shifts, S, T, Z) and applies a set
+// of up to 32 at once, each amplitude multiplied by the product of the factors whose mask
+// it contains.  The products of every subset of 8 factors are tables of 256 values at
+// scale 2^62, so an amplitude takes one table value per 8 factors.  Statevectors of at
+// least 8 qubits (the API defers phases from 19 qubits on).
 #include "qg_common.cuh"
 #include "qg_fixed.cuh"
 
 #include <cmath>
+#include <complex>
+#include <vector>
 
 struct QftTables {
     long long t[4][256][2];     // table k, entry j: exp(i pi j 2^(8k) / 2^n) (k = 0: / sqrt2), (re, im) x 2^62
 };
 
-__device__ __forceinline__ long long mulhi(long long a, long long b) { return __mul64hi(a, b); }
+// the top 64 bits of a * b (signed), to within 2 units: balanced 32-bit limbs a = ah 2^32 + al
+// (al in [-2^31, 2^31)), three 32 x 32 -> 64 products, the low x low one dropped (a full
+// 64-bit high product takes several times the instructions on the integer pipe)
+__device__ __forceinline__ void limbs(long long a, int& h, int& l) {
+    l = (int)(unsigned)a;
+    h = (int)((a - (long long)l) >> 32);
+}
+__device__ __forceinline__ long long mulhi(long long a, long long b) {
+    int ah, al, bh, bl;
+    limbs(a, ah, al);
+    limbs(b, bh, bl);
+    const long long mid = (long long)ah * bl + (long long)al * bh;
+    return (long long)ah * bh + (mid >> 32);
+}
 
 // (a * b) for complex values at scale 2^62 (|a|, |b| <= 1): the product at scale 2^62
 __device__ __forceinline__ void cmul62(long long ar, long long ai, long long br, long long bi, long long& cr, long long& ci) {
@@ -53,9 +76,12 @@ __device__ __forceinline__ double qft_double(long long Y, int t) {
 #define QFT_THREADS 256
 #define QFT_C (3260954456333195553LL)    // round(2^62 / sqrt2)
 
+// NT tables (compile time, so that every loop over them unrolls)
+template <int NT>
 __global__ void __launch_bounds__(QFT_THREADS) k_qft_step(double2* __restrict__ a, qidx numPairs, int tb, int lb, qidx lmask,
-                                                          int numTables, const __grid_constant__ QftTables T) {
-    __shared__ long long sT[4][256][2];
+                                                          const __grid_constant__ QftTables T) {
+    constexpr int numTables = NT;
+    __shared__ long long sT[NT][256][2];
     for (int e = threadIdx.x; e < numTables * 512; e += QFT_THREADS) (&sT[0][0][0])[e] = (&T.t[0][0][0])[e];
     __syncthreads();
     const qidx stride = (qidx)gridDim.x * QFT_THREADS;
@@ -66,6 +92,7 @@ __global__ void __launch_bounds__(QFT_THREADS) k_qft_step(double2* __restrict__ 
         // the twiddle w^L / sqrt2 at scale 2^62
         const qidx L = (i0 >> lb) & lmask;
         long long wr = sT[0][L & 255][0], wi = sT[0][L & 255][1];
+#pragma unroll
         for (int k = 1; k < numTables; k++) {
             const int j = (int)((L >> (8 * k)) & 255);
             cmul62(wr, wi, sT[k][j][0], sT[k][j][1], wr, wi);
@@ -106,7 +133,116 @@ __global__ void __launch_bounds__(QFT_THREADS) k_qft_step(double2* __restrict__ 
     }
 }
 
+struct PhaseSet {
+    long long t[4][256][2];     // table g, entry j: product of the factors 8g + k with bit k of j set, x 2^62
+    qidx mask[32];              // the qubits of factor i (all must be 1)
+};
+
+// NT tables of 8 factors.  A warp takes chunks of 256 consecutive amplitudes (lane l, round
+// r: amplitude 256 c + 32 r + l).  Whether factor f applies, (index & mask_f) == mask_f,
+// splits into the bits above 8 (the same for the whole chunk: lane f tests them once per
+// chunk and a ballot gathers the 32 answers) and the 8 low bits (fixed per lane and round:
+// computed once per thread); their AND gives, byte g, the index into table g.
+template <int NT>
+__global__ void __launch_bounds__(QFT_THREADS) k_phase_set(double2* __restrict__ a, qidx numChunks, int num,
+                                                           const __grid_constant__ PhaseSet P) {
+    constexpr int numTables = NT;
+    __shared__ long long sT[NT][256][2];
+    for (int e = threadIdx.x; e < numTables * 512; e += QFT_THREADS) (&sT[0][0][0])[e] = (&P.t[0][0][0])[e];
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const qidx myHigh = lane < num ? (P.mask[lane] & ~(qidx)255) : 0;     // lane f: factor f's bits above 8
+    uint32_t low[8];                                                      // round r: the factors whose low bits hold
+#pragma unroll
+    for (int r = 0; r < 8; r++) {
+        uint32_t w = 0;
+        const int lo = 32 * r + lane;
+        for (int f = 0; f < num; f++) {
+            const int m = (int)(P.mask[f] & 255);
+            if ((lo & m) == m) w |= 1u << f;
+        }
+        low[r] = w;
+    }
+    const qidx warps = (qidx)gridDim.x * (QFT_THREADS / 32);
+    for (qidx c = blockIdx.x * (qidx)(QFT_THREADS / 32) + (threadIdx.x >> 5); c < numChunks; c += warps) {
+        const qidx base = c << 8;
+        const uint32_t high = __ballot_sync(0xffffffffu, lane < num && (base & myHigh) == myHigh);
+#pragma unroll
+        for (int r = 0; r < 8; r++) {
+            const uint32_t j4 = high & low[r];
+            if (j4 == 0) continue;                   // every factor is 1 here: nothing to write
+            const qidx i = base + 32 * r + lane;
+            long long wr = sT[0][j4 & 255][0], wi = sT[0][j4 & 255][1];
+#pragma unroll
+            for (int g = 1; g < numTables; g++) {
+                const uint32_t j = (j4 >> (8 * g)) & 255;
+                cmul62(wr, wi, sT[g][j][0], sT[g][j][1], wr, wi);
+            }
+            const double2 v = ld_amp(a + i);
+            const uint64_t u0 = qgfx::f64_bits(v.x), u1 = qgfx::f64_bits(v.y);
+            const int e0 = (int)((u0 >> 52) & 0x7FF), e1 = (int)((u1 >> 52) & 0x7FF);
+            const int eb = max(max(e0 + (e0 == 0), e1 + (e1 == 0)), 1);
+            double2 o;
+            if (((u0 | u1) << 1) == 0) {
+                o = v;
+            } else if (eb >= 58 && eb <= 2043) {
+                const long long xr = qft_fixed(u0, eb), xi = qft_fixed(u1, eb);
+                // value * 2^(1082 - eb) / 4
+                const long long yr = mulhi(xr, wr) - mulhi(xi, wi), yi = mulhi(xr, wi) + mulhi(xi, wr);
+                const int t = eb - 1080;
+                o = make_double2(qft_double(yr, t), qft_double(yi, t));
+            } else {
+                const double cr = (double)wr * 0x1p-62, ci = (double)wi * 0x1p-62;
+                o = make_double2(fma(v.x, cr, -v.y * ci), fma(v.x, ci, v.y * cr));
+            }
+            st_amp(a + i, o);
+        }
+    }
+}
+
 extern "C" {
+
+// A set of controlled phases on a statevector: every amplitude whose index contains
+// masks[f] (all those bits 1) is multiplied by factors[f], for each f < num (num <= 32;
+// each |factors[f]| = 1).  The phases commute, so their order does not matter.
+int qg_sv_phaseSet(void* amps, int numQubits, const int64_t* masks, const qg_cplx* factors, int num, void* stream) {
+    QG_TRY(qg_check_amps(amps, numQubits));
+    if (num < 0 || num > 32 || (num > 0 && (!masks || !factors)))
+        return qg_fail(QG_ERR_ARG, "phaseSet: %d phases (at most 32)", num);
+    if (num == 0) return QG_OK;
+    PhaseSet P;
+    const qidx all = ((qidx)1 << numQubits) - 1;
+    for (int f = 0; f < num; f++) {
+        if (masks[f] <= 0 || (masks[f] & ~all) != 0) return qg_fail(QG_ERR_ARG, "phaseSet: mask %lld", (long long)masks[f]);
+        const double m = std::hypot(factors[f].re, factors[f].im);
+        if (!(std::fabs(m - 1.0) < 1e-6)) return qg_fail(QG_ERR_ARG, "phaseSet: a factor of modulus %g (must be 1)", m);
+        P.mask[f] = masks[f];
+    }
+    for (int f = num; f < 32; f++) P.mask[f] = 0;
+    const int numTables = (num + 7) / 8;
+    for (int g = 0; g < numTables; g++)
+        for (int j = 0; j < 256; j++) {
+            std::complex<long double> prod(1.0L, 0.0L);
+            for (int k = 0; k < 8; k++)
+                if ((j >> k) & 1 && 8 * g + k < num)
+                    prod *= std::complex<long double>(factors[8 * g + k].re, factors[8 * g + k].im);
+            P.t[g][j][0] = (long long)std::llroundl(prod.real() * 4611686018427387904.0L);
+            P.t[g][j][1] = (long long)std::llroundl(prod.imag() * 4611686018427387904.0L);
+        }
+    if (numQubits < 8) return qg_fail(QG_ERR_ARG, "phaseSet: at least 8 qubits (chunks of 256 amplitudes)");
+    const qidx numChunks = ((qidx)1 << numQubits) >> 8;
+    const unsigned grid = (unsigned)std::min<qidx>((numChunks + QFT_THREADS / 32 - 1) / (QFT_THREADS / 32), (qidx)qg_num_sms() * 8);
+    double2* A = (double2*)amps;
+    cudaStream_t st = qg_stream(stream);
+    switch (numTables) {
+        case 1: k_phase_set<1><<<grid, QFT_THREADS, 0, st>>>(A, numChunks, num, P); break;
+        case 2: k_phase_set<2><<<grid, QFT_THREADS, 0, st>>>(A, numChunks, num, P); break;
+        case 3: k_phase_set<3><<<grid, QFT_THREADS, 0, st>>>(A, numChunks, num, P); break;
+        default: k_phase_set<4><<<grid, QFT_THREADS, 0, st>>>(A, numChunks, num, P); break;
+    }
+    qg_note_launch();
+    return qg_check_launch("k_phase_set");
+}
 
 // One QFT step on a statevector: Hadamard on `target`, then for every amplitude whose bit
 // `target` is set the phase exp(i pi L / 2^numLowBits), L = (index >> lowTarget) &
@@ -130,7 +266,14 @@ int qg_sv_qftStep(void* amps, int numQubits, int target, int lowTarget, int numL
     const qidx numPairs = (qidx)1 << (numQubits - 1);
     const qidx lmask = numLowBits >= 63 ? -1 : (((qidx)1 << numLowBits) - 1);
     const unsigned grid = (unsigned)std::min<qidx>((numPairs + QFT_THREADS - 1) / QFT_THREADS, (qidx)qg_num_sms() * 8);
-    k_qft_step<<<grid, QFT_THREADS, 0, qg_stream(stream)>>>((double2*)amps, numPairs, target, lowTarget, lmask, numTables, T);
+    double2* A = (double2*)amps;
+    cudaStream_t st = qg_stream(stream);
+    switch (numTables) {
+        case 1: k_qft_step<1><<<grid, QFT_THREADS, 0, st>>>(A, numPairs, target, lowTarget, lmask, T); break;
+        case 2: k_qft_step<2><<<grid, QFT_THREADS, 0, st>>>(A, numPairs, target, lowTarget, lmask, T); break;
+        case 3: k_qft_step<3><<<grid, QFT_THREADS, 0, st>>>(A, numPairs, target, lowTarget, lmask, T); break;
+        default: k_qft_step<4><<<grid, QFT_THREADS, 0, st>>>(A, numPairs, target, lowTarget, lmask, T); break;
+    }
     qg_note_launch();
     return qg_check_launch("k_qft_step");
 }

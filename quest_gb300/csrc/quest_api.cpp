@@ -92,6 +92,9 @@ struct PendingSet {
     int numQubits;                      // the Qureg's (ket) qubits
     bool dm;                            // a density matrix (else a statevector: PEND_SV ops)
     std::map<int, PendingOp> ops;       // ket qubit -> its pending op
+    // statevectors: pending controlled phases (qubit mask, factor), which commute with one
+    // another; every pending one-qubit op acts on a qubit outside all of their masks
+    std::vector<std::pair<long long, cd>> phases;
 };
 std::map<const void*, PendingSet> g_pending;   // keyed by gpuAmps
 std::mutex g_pendingMu;
@@ -124,7 +127,7 @@ bool applyPendingOp(const Qureg& q, int qubit, const PendingOp& op, const char* 
 // one-qubit superoperator does, so when that kernel runs (product mode 0, registers of at
 // least one tile per SM) pairs of pending qubits are applied together.
 bool pairSuperops(const Qureg& q) {
-    return q.isDensityMatrix && q.numQubits >= 3 && qg_fp64_products_mode() == 0 &&
+    return q.isDensityMatrix && q.numQubits >= 3 && q.numQubits <= QG_MAX_QUBITS_API / 2 && qg_fp64_products_mode() == 0 &&
            qg_dense_tc_wanted((long long)1 << (2 * q.numQubits - 4));
 }
 
@@ -150,7 +153,7 @@ void kronPair(const cd (&Sa)[16], const cd (&Sb)[16], cd (&M)[256]) {
 // pending qubits are applied four at a time as the Kronecker product of their unitaries
 // (one pass instead of four), then three, two or one.
 bool deferSV(const Qureg& q) {
-    return !q.isDensityMatrix && q.numQubits >= 5 && qg_fp64_products_mode() == 0 &&
+    return !q.isDensityMatrix && q.numQubits >= 5 && q.numQubits <= QG_MAX_QUBITS_API && qg_fp64_products_mode() == 0 &&
            qg_dense_tc_wanted((long long)1 << (q.numQubits - 4));
 }
 
@@ -224,15 +227,39 @@ bool applyPendingList(const Qureg& q, std::vector<std::pair<int, PendingOp>>& to
 }
 
 // applies the pending ops of the listed ket qubits (all of them when `qubits` is null)
+// applies a set of pending phases, 32 per pass
+bool applyPhases(const Qureg& q, const std::vector<std::pair<long long, cd>>& ph, const char* func) {
+    for (size_t i = 0; i < ph.size(); i += 32) {
+        const int num = (int)std::min<size_t>(32, ph.size() - i);
+        int64_t masks[32];
+        qcomp_t f[32];
+        for (int k = 0; k < num; k++) {
+            masks[k] = ph[i + k].first;
+            f[k] = qcomp_t{ph[i + k].second.real(), ph[i + k].second.imag()};
+        }
+        if (!backend(qg_sv_phaseSet(q.gpuAmps, q.numQubits, masks, f, num, g_stream), func)) return false;
+    }
+    return true;
+}
+
+// applies the pending ops of the listed ket qubits (all of them when `qubits` is null); a
+// statevector's pending phases go first, all of them, when any involves a listed qubit
 bool flushPending(const Qureg& q, const std::vector<int>* qubits, const char* func) {
     std::vector<std::pair<int, PendingOp>> todo;
+    std::vector<std::pair<long long, cd>> phases;
     {
         std::lock_guard<std::mutex> lock(g_pendingMu);
         auto it = g_pending.find(q.gpuAmps);
         if (it == g_pending.end()) return true;
+        long long touched = 0;
+        if (qubits)
+            for (int b : *qubits) touched |= 1LL << b;
+        bool phasesHit = !qubits;
+        for (auto& ph : it->second.phases) phasesHit = phasesHit || (ph.first & touched) != 0;
+        if (phasesHit) phases.swap(it->second.phases);
         if (!qubits) {
             for (auto& kv : it->second.ops) todo.push_back(kv);
-            g_pending.erase(it);
+            it->second.ops.clear();
         } else {
             for (int b : *qubits) {
                 auto jt = it->second.ops.find(b);
@@ -240,10 +267,44 @@ bool flushPending(const Qureg& q, const std::vector<int>* qubits, const char* fu
                 todo.push_back(*jt);
                 it->second.ops.erase(jt);
             }
-            if (it->second.ops.empty()) g_pending.erase(it);
         }
+        if (it->second.ops.empty() && it->second.phases.empty()) g_pending.erase(it);
+    }
+    if (!applyPhases(q, phases, func)) return false;
+    return applyPendingList(q, todo, func);
+}
+
+// applies every pending one-qubit op of a statevector, keeping its pending phases
+bool flushPendingOps(const Qureg& q, const char* func) {
+    std::vector<std::pair<int, PendingOp>> todo;
+    {
+        std::lock_guard<std::mutex> lock(g_pendingMu);
+        auto it = g_pending.find(q.gpuAmps);
+        if (it == g_pending.end()) return true;
+        for (auto& kv : it->second.ops) todo.push_back(kv);
+        it->second.ops.clear();
+        if (it->second.phases.empty()) g_pending.erase(it);
     }
     return applyPendingList(q, todo, func);
+}
+
+// a pending phase on a statevector involves this qubit
+bool phasePendingOn(const Qureg& q, int qubit) {
+    std::lock_guard<std::mutex> lock(g_pendingMu);
+    auto it = g_pending.find(q.gpuAmps);
+    if (it == g_pending.end()) return false;
+    for (auto& ph : it->second.phases)
+        if ((ph.first >> qubit) & 1) return true;
+    return false;
+}
+
+// defers a controlled phase of a statevector (after its pending one-qubit ops are applied)
+void addPendingPhase(const Qureg& q, long long mask, cd factor) {
+    std::lock_guard<std::mutex> lock(g_pendingMu);
+    PendingSet& set = g_pending[q.gpuAmps];
+    set.numQubits = q.numQubits;
+    set.dm = false;
+    set.phases.push_back({mask, factor});
 }
 
 // forgets the pending ops of a Qureg whose state is about to be overwritten or freed
@@ -378,6 +439,11 @@ void applyDense(const Qureg& q, const int* ctrls, const int* states, int nc, con
     }
     if (defer) {
         if (nt == 1 && nc == 0) {
+            // pending phases on this qubit come first
+            if (phasePendingOn(q, t[0])) {
+                const vector<int> one = {t[0]};
+                if (!flushPending(q, &one, func)) return;
+            }
             const cd U[4] = {C(m[0]), C(m[1]), C(m[2]), C(m[3])};
             addPendingSV(q, t[0], U);
             return;
@@ -419,12 +485,24 @@ bool diagSV(const Qureg& q, const vector<int>& c, const vector<int>& s, const ve
 
 void applyDiag(const Qureg& q, const int* ctrls, const int* states, int nc, const int* targs, int nt, const qcomp_t* d,
                const qcomp_t* ex, bool anyTarg, const char* func) {
-    if (!checkQureg(q, func)) return;
+    // a controlled phase (one target, factor 1 on |0>, every control state 1) on a
+    // statevector that defers one-qubit gates is deferred too
+    bool phase = !q.isDensityMatrix && !ex && !anyTarg && nt == 1 && d[0].re == 1 && d[0].im == 0 && deferSV(q);
+    for (int i = 0; phase && states && i < nc; i++) phase = states[i] == 1;
+    if (!checkQureg(q, func, phase)) return;
     if (!checkCtrlsTargs(q, ctrls, nc, targs, nt, func)) return;
     if (!checkStates(states, nc, func)) return;
     if (!check(nt >= 1, func, "At least one target qubit is required.")) return;
     if (!check(isUnitaryDiag(d, (qindex)1 << nt), func, "The given matrix was not (approximately) unitary.")) return;
     if (ex && !check(std::abs(ex->im) <= g_eps, func, "The exponent of a unitary diagonal matrix must be real.")) return;
+    if (phase) {
+        // pending one-qubit ops come first; the phases then wait with the other pending phases
+        if (!flushPendingOps(q, func)) return;
+        long long mask = 1LL << targs[0];
+        for (int i = 0; i < nc; i++) mask |= 1LL << ctrls[i];
+        if (!(d[1].re == 1 && d[1].im == 0)) addPendingPhase(q, mask, C(d[1]));
+        return;
+    }
     vector<int> c = V(ctrls, nc), s = V(states, nc), t = V(targs, nt);
     if (!diagSV(q, c, s, t, d, false, ex, anyTarg, func)) return;
     if (!q.isDensityMatrix) return;
@@ -554,7 +632,6 @@ void syncQuESTEnv(void) {
     {
         std::lock_guard<std::mutex> lock(g_pendingMu);
         for (auto& kv : g_pending) all.push_back(kv);
-        g_pending.clear();
     }
     for (auto& kv : all) {
         Qureg q;
@@ -562,8 +639,7 @@ void syncQuESTEnv(void) {
         q.gpuAmps = (qcomp_t*)kv.first;
         q.numQubits = kv.second.numQubits;
         q.isDensityMatrix = kv.second.dm ? 1 : 0;
-        std::vector<std::pair<int, PendingOp>> todo(kv.second.ops.begin(), kv.second.ops.end());
-        if (!applyPendingList(q, todo, "syncQuESTEnv")) return;
+        if (!flushPending(q, nullptr, "syncQuESTEnv")) return;
     }
     backend(qg_sync(), "syncQuESTEnv");
 }
@@ -1053,7 +1129,7 @@ void applyPhaseGadget(Qureg q, int* t, int nt, qreal angle) { applyMultiStateCon
 // applyMultiQubitPhaseShift: a (n-1)-controlled DiagMatr1 {1, e^(i angle)} (operations.cpp:1605-1613)
 void applyMultiQubitPhaseShift(Qureg q, int* t, int nt, qreal angle) {
     const char* func = "applyMultiQubitPhaseShift";
-    if (!checkQureg(q, func) || !checkQubits(q, t, nt, func, "target qubits")) return;
+    if (!checkQureg(q, func, true) || !checkQubits(q, t, nt, func, "target qubits")) return;
     if (!check(nt >= 1, func, "At least one target qubit is required.")) return;
     cd e = std::exp(cd(0, 1) * angle);
     qcomp_t d[2] = {{1, 0}, Q(e)};

@@ -254,3 +254,43 @@ def test_flush_before_reading_the_device_amplitudes(env):
         assert np.max(np.abs(out - want)) <= TOL
     finally:
         Q.destroyQureg(q)
+
+
+@pytest.mark.parametrize("seed", [11, 12])
+def test_deferred_phases_and_gates(env, seed):
+    """Controlled phases (CPhase, CZ, phase shifts, S, T, Z) on a 20-qubit statevector are
+    deferred as a set and applied in one pass, one-qubit gates four per pass; they
+    interleave on shared qubits (a gate on a qubit with a pending phase applies the phases
+    first), with more than 32 phases pending at once, a controlled gate, a QFT and
+    reductions: within 1e-12 of the oracle in both product modes."""
+    nq = 20
+    rng = np.random.default_rng(seed)
+    lines = []
+    for layer in range(5):
+        for t in rng.permutation(nq)[: int(rng.integers(8, nq + 1))]:
+            lines.append(f"U1 {int(t)} {qc.mat_tokens(qc.haar_unitary(2, rng))}")
+        for _ in range(int(rng.integers(10, 40))):
+            a, b = (int(v) for v in rng.choice(nq, 2, replace=False))
+            kind = int(rng.integers(6))
+            lines.append([f"CPS {a} {b} {rng.uniform(-3, 3)}", f"CZ {a} {b}", f"PS {a} {rng.uniform(-3, 3)}",
+                          f"S {a}", f"T {a}", f"Z {a}"][kind])
+        a, b, c = (int(v) for v in rng.choice(nq, 3, replace=False))
+        lines.append(f"CU1 1 {a} 1 {b} {qc.mat_tokens(qc.haar_unitary(2, rng))}")
+        lines.append(f"H {c}")
+        if layer == 3:
+            lines.append("TOTALPROB")
+            lines.append(f"PROBQ {int(rng.integers(nq))} 0")
+    lines.append("FQFT")
+    lines.append("TOTALPROB")
+    text = "\n".join(lines) + "\n"
+    amps = qc.random_statevector(nq, seed + 100)
+    want, wres, _ = qc.oracle().run(text, nq, 0, amps)
+    from quest_gb300._lib import lib
+    try:
+        for mode in (0, 1):
+            assert lib().qg_set_fp64_products(mode) == 0
+            got, res = run_gpu(env, text, nq, amps)
+            assert np.max(np.abs(got - want)) <= TOL
+            assert np.max(np.abs(res - wres)) <= TOL
+    finally:
+        lib().qg_set_fp64_products(0)
