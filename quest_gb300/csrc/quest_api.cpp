@@ -200,6 +200,11 @@ bool applySVGroup(const Qureg& q, const std::pair<int, PendingOp>* g, int k, con
 // a remaining one with a channel), the rest one by one
 bool applyPendingList(const Qureg& q, std::vector<std::pair<int, PendingOp>>& todo, const char* func) {
     if (!q.isDensityMatrix) {
+        // qubit 0 last, so that it falls into the remainder group when there is one: a
+        // four-qubit pass without qubit 0 takes the faster (staged) tensor-core form
+        std::stable_sort(todo.begin(), todo.end(), [](const std::pair<int, PendingOp>& x, const std::pair<int, PendingOp>& y) {
+            return (x.first == 0 ? 1 : 0) < (y.first == 0 ? 1 : 0);
+        });
         size_t i = 0;
         while (i < todo.size()) {
             const int k = (int)std::min<size_t>(4, todo.size() - i);
