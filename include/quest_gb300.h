@@ -339,7 +339,7 @@ int qg_circuit_get_block(const qg_circuit* circuit, int i, int* targs, int* numT
  * full: every 5-qubit block launch gives up after about 2 s and leaves the register untouched).
  * Asynchronous.  A tensor-core launch whose bounded wait runs out sets the device's error flag;
  * the next qg_sv32_apply_circuit or qg_graph_launch on that device returns QG_ERR_TIMEOUT for
- * it (and clears the flag) before launching anything.  Callers that need the verdict of their
+ * it (and clears the flag) before launching anything.  Callers that need the outcome of their
  * own launches synchronise the stream and read qg_tc_get_error_flag. */
 int qg_sv32_apply_circuit(qg_circuit* circuit, void* amps32, int numQubits, int impl, void* stream);
 /* the current device's flag: 1 if a tensor-core launch gave up a bounded wait since it was

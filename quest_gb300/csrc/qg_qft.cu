@@ -133,6 +133,70 @@ __global__ void __launch_bounds__(QFT_THREADS) k_qft_step(double2* __restrict__ 
     }
 }
 
+// The same step for targets from qubit 0 (lb = 0) and tb >= 8: a warp takes chunks of 256
+// consecutive pairs (lane l, round r: pair 256 c + 32 r + l), whose twiddle index L keeps its
+// bytes above the lowest across the chunk, so their product H is formed once per chunk and
+// each pair takes one complex product T0[L & 255] H instead of NT - 1.
+template <int NT>
+__global__ void __launch_bounds__(QFT_THREADS) k_qft_step_chunks(double2* __restrict__ a, qidx numChunks, int tb, qidx lmask,
+                                                                 const __grid_constant__ QftTables T) {
+    __shared__ long long sT[NT][256][2];
+    for (int e = threadIdx.x; e < NT * 512; e += QFT_THREADS) (&sT[0][0][0])[e] = (&T.t[0][0][0])[e];
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const qidx lowMask = ((qidx)1 << tb) - 1;
+    const qidx warps = (qidx)gridDim.x * (QFT_THREADS / 32);
+    for (qidx c = blockIdx.x * (qidx)(QFT_THREADS / 32) + (threadIdx.x >> 5); c < numChunks; c += warps) {
+        const qidx Lh = (c << 8) & lmask;                       // L's bytes above the lowest
+        long long hr = sT[1][(Lh >> 8) & 255][0], hi = sT[1][(Lh >> 8) & 255][1];
+#pragma unroll
+        for (int k = 2; k < NT; k++) {
+            const int j = (int)((Lh >> (8 * k)) & 255);
+            cmul62(hr, hi, sT[k][j][0], sT[k][j][1], hr, hi);
+        }
+#pragma unroll 2
+        for (int r = 0; r < 8; r++) {
+            const int k0 = 32 * r + lane;                       // L & 255
+            const qidx p = (c << 8) + k0;
+            const qidx i0 = ((p & ~lowMask) << 1) | (p & lowMask), i1 = i0 | ((qidx)1 << tb);
+            const double2 v0 = ld_amp(a + i0), v1 = ld_amp(a + i1);
+            long long wr, wi;
+            cmul62(sT[0][k0][0], sT[0][k0][1], hr, hi, wr, wi);
+            const uint64_t u[4] = {qgfx::f64_bits(v0.x), qgfx::f64_bits(v0.y), qgfx::f64_bits(v1.x), qgfx::f64_bits(v1.y)};
+            int eb = 1;
+            uint64_t any = 0;
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const int ei = (int)((u[k] >> 52) & 0x7FF);
+                eb = max(eb, ei + (ei == 0));
+                any |= u[k] << 1;
+            }
+            double2 o0, o1;
+            if (any == 0) {
+                o0 = make_double2(0.0, 0.0);
+                o1 = o0;
+            } else if (eb >= 58 && eb <= 2043) {
+                const long long x0r = qft_fixed(u[0], eb), x0i = qft_fixed(u[1], eb);
+                const long long x1r = qft_fixed(u[2], eb), x1i = qft_fixed(u[3], eb);
+                const long long sr = x0r + x1r, si = x0i + x1i, dr = x0r - x1r, di = x0i - x1i;
+                const long long y0r = mulhi(sr, QFT_C), y0i = mulhi(si, QFT_C);
+                const long long y1r = mulhi(dr, wr) - mulhi(di, wi), y1i = mulhi(dr, wi) + mulhi(di, wr);
+                const int t = eb - 1080;
+                o0 = make_double2(qft_double(y0r, t), qft_double(y0i, t));
+                o1 = make_double2(qft_double(y1r, t), qft_double(y1i, t));
+            } else {
+                const double s = 0.70710678118654752440;
+                const double cr = (double)wr * 0x1p-62 / s, ci = (double)wi * 0x1p-62 / s;
+                o0 = make_double2((v0.x + v1.x) * s, (v0.y + v1.y) * s);
+                const double dr = (v0.x - v1.x) * s, di = (v0.y - v1.y) * s;
+                o1 = make_double2(fma(dr, cr, -di * ci), fma(dr, ci, di * cr));
+            }
+            st_amp(a + i0, o0);
+            st_amp(a + i1, o1);
+        }
+    }
+}
+
 struct PhaseSet {
     long long t[4][256][2];     // table g, entry j: product of the factors 8g + k with bit k of j set, x 2^62
     qidx mask[32];              // the qubits of factor i (all must be 1)
@@ -268,6 +332,14 @@ int qg_sv_qftStep(void* amps, int numQubits, int target, int lowTarget, int numL
     const unsigned grid = (unsigned)std::min<qidx>((numPairs + QFT_THREADS - 1) / QFT_THREADS, (qidx)qg_num_sms() * 8);
     double2* A = (double2*)amps;
     cudaStream_t st = qg_stream(stream);
+    if (lowTarget == 0 && target >= 8 && numTables >= 3) {
+        const qidx numChunks = numPairs >> 8;
+        const unsigned g2 = (unsigned)std::min<qidx>((numChunks + QFT_THREADS / 32 - 1) / (QFT_THREADS / 32), (qidx)qg_num_sms() * 8);
+        if (numTables == 3) k_qft_step_chunks<3><<<g2, QFT_THREADS, 0, st>>>(A, numChunks, target, lmask, T);
+        else k_qft_step_chunks<4><<<g2, QFT_THREADS, 0, st>>>(A, numChunks, target, lmask, T);
+        qg_note_launch();
+        return qg_check_launch("k_qft_step_chunks");
+    }
     switch (numTables) {
         case 1: k_qft_step<1><<<grid, QFT_THREADS, 0, st>>>(A, numPairs, target, lowTarget, lmask, T); break;
         case 2: k_qft_step<2><<<grid, QFT_THREADS, 0, st>>>(A, numPairs, target, lowTarget, lmask, T); break;
