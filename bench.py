@@ -467,8 +467,8 @@ def run_gb300(args, world, rank, local, dist):
         traffic = round(63.55 * (1 << (nq - 1)))
         traffic_src = "ncu capture at 28 qubits (63.55 B per amplitude pair) scaled to this size"
     if fused:
-        kname = ("k_dense_tc (deferred one-qubit gates, four per pass, as one 16x16 operator: exact 8-bit "
-                 "slices on the fp16 tensor cores)")
+        kname = ("k_dense_tc (deferred one-qubit gates, four per pass, as one 16x16 operator with the layer's "
+                 "controlled phases on those qubits folded in: exact 8-bit slices on the fp16 tensor cores)")
     elif args.fp64_products == "fixed":
         kname = "k_dense1_fx (applyCompMatr1, general complex 2x2, FP64 storage, fixed-point products)"
     else:
@@ -495,7 +495,8 @@ def run_gb300(args, world, rank, local, dist):
         "vs_baseline": None,
         "dtype": "f64" if args.fp64_products == "fp64" else
                  "f64 (storage and all other ops; general 2x2 products in 60-bit block-floating fixed point, "
-                 "deferred one-qubit gates four per pass as exact 8-bit slices on the fp16 tensor cores)",
+                 "deferred one-qubit gates four per pass, with the controlled phases among them folded in, as "
+                 "exact 8-bit slices on the fp16 tensor cores)",
         "data": "synthetic (seeded Gaussian state, seeded Haar gates)",
         "config": {"workload": f"{nq}-qubit FP64 statevector (16 GiB at 30 qubits), depth {args.depth} Haar 1q "
                                f"+ 15 CPhase per layer, then full QFT", "qubits": nq, "depth": args.depth,

@@ -944,6 +944,9 @@ bool Runner::run(const std::string& text) {
         } else if (op == "CPS") {        /* applyTwoQubitPhaseShift: operations.cpp:1596-1613 */
             int t1, t2; double th; is >> t1 >> t2 >> th; cplx e = std::exp(cplx(0, 1) * th);
             diag({t2}, {}, {t1}, {1, 0, e.real(), e.imag()}, nullptr);
+        } else if (op == "MPS") {        /* applyMultiQubitPhaseShift: operations.cpp:1605-1613 */
+            int k; is >> k; auto t = rdInts(is, k); double th; is >> th; cplx e = std::exp(cplx(0, 1) * th);
+            diag(vector<int>(t.begin() + 1, t.end()), {}, {t[0]}, {1, 0, e.real(), e.imag()}, nullptr);
         } else if (op == "CX") {         /* applyControlledPauliX: operations.cpp:911-916 */
             int c, t; is >> c >> t; vector<int> codes(t + 1, 0); codes[t] = 1; pauliStr({c}, {}, codes);
         } else if (op == "CZ") {         /* applyControlledPauliZ: operations.cpp:927-932 */

@@ -102,6 +102,7 @@ extern "C" int ref_run_circuit(const char* text, int numQubits, int isDensMatr, 
         else if (op == "CRZ") { int c, t; double a; is >> c >> t >> a; applyControlledRotateZ(q, c, t, a); }
         else if (op == "PS") { int t; double a; is >> t >> a; applyPhaseShift(q, t, a); }
         else if (op == "CPS") { int a, b; double th; is >> a >> b >> th; applyTwoQubitPhaseShift(q, a, b, th); }
+        else if (op == "MPS") { int k; is >> k; auto t = rdInts(is, k); double a; is >> a; applyMultiQubitPhaseShift(q, t.data(), k, a); }
         else if (op == "CX") { int c, t; is >> c >> t; applyControlledPauliX(q, c, t); }
         else if (op == "CZ") { int c, t; is >> c >> t; applyControlledPauliZ(q, c, t); }
         else if (op == "SWAP") { int a, b; is >> a >> b; applySwap(q, a, b); }

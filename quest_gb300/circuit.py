@@ -43,6 +43,9 @@ def run_text(text, qureg):
             Q.applyPhaseShift(qureg, int(a[0]), float(a[1]))
         elif op == "CPS":
             Q.applyTwoQubitPhaseShift(qureg, int(a[0]), int(a[1]), float(a[2]))
+        elif op == "MPS":
+            k = int(a[0])
+            Q.applyMultiQubitPhaseShift(qureg, ints(a[1:1 + k]), k, float(a[1 + k]))
         elif op == "CX":
             Q.applyControlledPauliX(qureg, int(a[0]), int(a[1]))
         elif op == "CZ":

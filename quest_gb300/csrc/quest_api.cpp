@@ -93,7 +93,8 @@ struct PendingSet {
     bool dm;                            // a density matrix (else a statevector: PEND_SV ops)
     std::map<int, PendingOp> ops;       // ket qubit -> its pending op
     // statevectors: pending controlled phases (qubit mask, factor), which commute with one
-    // another; every pending one-qubit op acts on a qubit outside all of their masks
+    // another and come after every pending one-qubit op (a one-qubit gate on a qubit of a
+    // pending phase applies everything pending first)
     std::vector<std::pair<long long, cd>> phases;
 };
 std::map<const void*, PendingSet> g_pending;   // keyed by gpuAmps
@@ -178,40 +179,151 @@ void addPendingSV(const Qureg& q, int qubit, const cd (&U)[4]) {
     P[0] = r0; P[1] = r1; P[2] = r2; P[3] = r3;
 }
 
-// pending unitaries of k statevector qubits as one 2^k x 2^k matrix (bit b of an index =
-// qubit b of the group), applied in one pass
-bool applySVGroup(const Qureg& q, const std::pair<int, PendingOp>* g, int k, const char* func) {
-    if (k == 1) return applyPendingOp(q, g[0].first, g[0].second, func);
-    const int D = 1 << k;
+typedef std::vector<std::pair<long long, cd>> PhaseList;
+
+// Groups of at most four pending statevector qubits (indices into `todo`), one pass each.
+// A pending phase whose qubits all have pending ops and fall into one group is folded into
+// that group's matrix (it acts after the group's unitaries and commutes with every other
+// group), which saves the phase pass when all of them fold.  So the qubits joined by such
+// phases (clusters of at most four) are packed into the groups first-fit, largest first,
+// into as many groups as the plain split needs (n/4 groups of four and one of n % 4); the
+// cluster holding qubit 0 goes to the smaller group when it fits there, since a four-qubit
+// pass without qubit 0 takes the faster (staged) tensor-core form.  When the clusters do not
+// pack into that many groups, the plain split is used: qubits in ascending order, qubit 0
+// last.
+std::vector<std::vector<int>> groupSV(const std::vector<std::pair<int, PendingOp>>& todo, const PhaseList& phases) {
+    const int n = (int)todo.size();
+    std::vector<std::vector<int>> plain;
+    {
+        std::vector<int> order(n);
+        for (int i = 0; i < n; i++) order[i] = i;
+        std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return (todo[x].first == 0) < (todo[y].first == 0); });
+        for (int i = 0; i < n; i += 4) plain.push_back(std::vector<int>(order.begin() + i, order.begin() + std::min(n, i + 4)));
+    }
+    if (phases.empty() || n < 2) return plain;
+    long long pendingMask = 0;
+    int at[64];
+    for (int i = 0; i < n; i++) {
+        pendingMask |= 1LL << todo[i].first;
+        at[todo[i].first] = i;
+    }
+    std::vector<int> parent(n);
+    for (int i = 0; i < n; i++) parent[i] = i;
+    auto find = [&](int i) {
+        while (parent[i] != i) i = parent[i] = parent[parent[i]];
+        return i;
+    };
+    for (auto& ph : phases) {
+        const long long m = ph.first;
+        if ((m & ~pendingMask) != 0 || __builtin_popcountll((unsigned long long)m) > 4) continue;
+        int first = -1;
+        for (int b = 0; b < 64; b++) {
+            if (!((m >> b) & 1)) continue;
+            if (first < 0) first = find(at[b]);
+            else parent[find(at[b])] = first;
+        }
+    }
+    std::map<int, std::vector<int>> byRoot;
+    for (int i = 0; i < n; i++) byRoot[find(i)].push_back(i);
+    std::vector<std::vector<int>> items;
+    for (auto& kv : byRoot) {
+        if (kv.second.size() <= 4) items.push_back(kv.second);
+        else for (int i : kv.second) items.push_back({i});
+    }
+    const int numFull = n / 4, rem = n % 4;
+    std::vector<std::vector<int>> groups(numFull + (rem ? 1 : 0));
+    std::vector<int> room(groups.size(), 4);
+    if (rem) room.back() = rem;
+    auto holdsZero = [&](const std::vector<int>& it) {
+        for (int i : it)
+            if (todo[i].first == 0) return true;
+        return false;
+    };
+    std::stable_sort(items.begin(), items.end(), [](const std::vector<int>& x, const std::vector<int>& y) { return x.size() > y.size(); });
+    for (size_t k = 0; k < items.size(); k++)
+        if (rem && holdsZero(items[k]) && (int)items[k].size() <= rem) {
+            groups.back() = items[k];
+            room.back() -= (int)items[k].size();
+            items.erase(items.begin() + k);
+            break;
+        }
+    for (auto& it : items) {
+        size_t g = 0;
+        while (g < groups.size() && room[g] < (int)it.size()) g++;
+        if (g == groups.size()) return plain;
+        groups[g].insert(groups[g].end(), it.begin(), it.end());
+        room[g] -= (int)it.size();
+    }
+    for (auto& g : groups) std::sort(g.begin(), g.end(), [&](int x, int y) { return todo[x].first < todo[y].first; });
+    return groups;
+}
+
+// the pending unitaries of k statevector qubits as one 2^k x 2^k matrix (bit b of an index
+// = qubit b of the group), with the not yet applied phases that lie inside the group folded
+// in (a phase multiplies the rows whose bits of its mask are all set), applied in one pass
+bool applySVGroup(const Qureg& q, const std::vector<const std::pair<int, PendingOp>*>& g, const PhaseList& phases,
+                  std::vector<char>& applied, const char* func) {
+    const int k = (int)g.size(), D = 1 << k;
+    long long groupMask = 0;
+    for (int b = 0; b < k; b++) groupMask |= 1LL << g[b]->first;
+    std::vector<cd> rowFactor(D, cd(1));
+    bool folded = false;
+    for (size_t p = 0; p < phases.size(); p++) {
+        if (applied[p] || (phases[p].first & ~groupMask) != 0) continue;
+        int local = 0;
+        for (int b = 0; b < k; b++)
+            if ((phases[p].first >> g[b]->first) & 1) local |= 1 << b;
+        for (int j = 0; j < D; j++)
+            if ((j & local) == local) rowFactor[j] *= phases[p].second;
+        applied[p] = 1;
+        folded = true;
+    }
+    if (k == 1 && !folded) return applyPendingOp(q, g[0]->first, g[0]->second, func);
     std::vector<qcomp_t> M((size_t)D * D);
     int t[4];
-    for (int b = 0; b < k; b++) t[b] = g[b].first;
+    for (int b = 0; b < k; b++) t[b] = g[b]->first;
     for (int j = 0; j < D; j++)
         for (int c = 0; c < D; c++) {
-            cd v = 1;
-            for (int b = 0; b < k; b++) v *= g[b].second.m[((j >> b) & 1) * 2 + ((c >> b) & 1)];
+            cd v = rowFactor[j];
+            for (int b = 0; b < k; b++) v *= g[b]->second.m[((j >> b) & 1) * 2 + ((c >> b) & 1)];
             M[(size_t)j * D + c] = qcomp_t{v.real(), v.imag()};
         }
+    if (k == 1) return backend(qg_sv_anyCtrlOneTargDenseMatr(q.gpuAmps, q.numQubits, nullptr, nullptr, 0, t[0], M.data(), g_stream), func);
     if (k == 2) return backend(qg_sv_anyCtrlTwoTargDenseMatr(q.gpuAmps, q.numQubits, nullptr, nullptr, 0, t[0], t[1], M.data(), g_stream), func);
     return backend(qg_sv_anyCtrlAnyTargDenseMatr(q.gpuAmps, q.numQubits, nullptr, nullptr, 0, t, k, M.data(), 0, g_stream), func);
 }
 
-// applies a list of pending ops: in pairs when that pays (general superoperators first,
-// a remaining one with a channel), the rest one by one
-bool applyPendingList(const Qureg& q, std::vector<std::pair<int, PendingOp>>& todo, const char* func) {
-    if (!q.isDensityMatrix) {
-        // qubit 0 last, so that it falls into the remainder group when there is one: a
-        // four-qubit pass without qubit 0 takes the faster (staged) tensor-core form
-        std::stable_sort(todo.begin(), todo.end(), [](const std::pair<int, PendingOp>& x, const std::pair<int, PendingOp>& y) {
-            return (x.first == 0 ? 1 : 0) < (y.first == 0 ? 1 : 0);
-        });
-        size_t i = 0;
-        while (i < todo.size()) {
-            const int k = (int)std::min<size_t>(4, todo.size() - i);
-            if (!applySVGroup(q, &todo[i], k, func)) return false;
-            i += k;
+// applies a set of pending phases, 32 per pass
+bool applyPhases(const Qureg& q, const PhaseList& ph, const char* func) {
+    for (size_t i = 0; i < ph.size(); i += 32) {
+        const int num = (int)std::min<size_t>(32, ph.size() - i);
+        int64_t masks[32];
+        qcomp_t f[32];
+        for (int k = 0; k < num; k++) {
+            masks[k] = ph[i + k].first;
+            f[k] = qcomp_t{ph[i + k].second.real(), ph[i + k].second.imag()};
         }
-        return true;
+        if (!backend(qg_sv_phaseSet(q.gpuAmps, q.numQubits, masks, f, num, g_stream), func)) return false;
+    }
+    return true;
+}
+
+// applies a list of pending ops, then (statevectors) the pending phases that come after
+// them: density matrices in pairs when that pays (general superoperators first, a remaining
+// one with a channel), the rest one by one; statevectors in the groups of groupSV, with the
+// phases that fit in a group folded into its pass and the others applied together after
+bool applyPendingList(const Qureg& q, std::vector<std::pair<int, PendingOp>>& todo, const PhaseList& phases, const char* func) {
+    if (!q.isDensityMatrix) {
+        std::vector<char> applied(phases.size(), 0);
+        for (auto& grp : groupSV(todo, phases)) {
+            std::vector<const std::pair<int, PendingOp>*> g;
+            for (int i : grp) g.push_back(&todo[i]);
+            if (!applySVGroup(q, g, phases, applied, func)) return false;
+        }
+        PhaseList rest;
+        for (size_t p = 0; p < phases.size(); p++)
+            if (!applied[p]) rest.push_back(phases[p]);
+        return applyPhases(q, rest, func);
     }
     if (todo.size() >= 2 && pairSuperops(q)) {
         std::stable_partition(todo.begin(), todo.end(), [](const std::pair<int, PendingOp>& x) { return x.second.kind == PEND_GENERAL; });
@@ -231,27 +343,12 @@ bool applyPendingList(const Qureg& q, std::vector<std::pair<int, PendingOp>>& to
     return true;
 }
 
-// applies the pending ops of the listed ket qubits (all of them when `qubits` is null)
-// applies a set of pending phases, 32 per pass
-bool applyPhases(const Qureg& q, const std::vector<std::pair<long long, cd>>& ph, const char* func) {
-    for (size_t i = 0; i < ph.size(); i += 32) {
-        const int num = (int)std::min<size_t>(32, ph.size() - i);
-        int64_t masks[32];
-        qcomp_t f[32];
-        for (int k = 0; k < num; k++) {
-            masks[k] = ph[i + k].first;
-            f[k] = qcomp_t{ph[i + k].second.real(), ph[i + k].second.imag()};
-        }
-        if (!backend(qg_sv_phaseSet(q.gpuAmps, q.numQubits, masks, f, num, g_stream), func)) return false;
-    }
-    return true;
-}
-
-// applies the pending ops of the listed ket qubits (all of them when `qubits` is null); a
-// statevector's pending phases go first, all of them, when any involves a listed qubit
+// applies the pending ops of the listed ket qubits (all of them when `qubits` is null); when
+// a statevector's pending phase involves a listed qubit, everything pending is applied
+// (the phases come after the pending ops of their qubits)
 bool flushPending(const Qureg& q, const std::vector<int>* qubits, const char* func) {
     std::vector<std::pair<int, PendingOp>> todo;
-    std::vector<std::pair<long long, cd>> phases;
+    PhaseList phases;
     {
         std::lock_guard<std::mutex> lock(g_pendingMu);
         auto it = g_pending.find(q.gpuAmps);
@@ -259,10 +356,10 @@ bool flushPending(const Qureg& q, const std::vector<int>* qubits, const char* fu
         long long touched = 0;
         if (qubits)
             for (int b : *qubits) touched |= 1LL << b;
-        bool phasesHit = !qubits;
-        for (auto& ph : it->second.phases) phasesHit = phasesHit || (ph.first & touched) != 0;
-        if (phasesHit) phases.swap(it->second.phases);
-        if (!qubits) {
+        bool all = !qubits;
+        for (auto& ph : it->second.phases) all = all || (ph.first & touched) != 0;
+        if (all) {
+            phases.swap(it->second.phases);
             for (auto& kv : it->second.ops) todo.push_back(kv);
             it->second.ops.clear();
         } else {
@@ -275,22 +372,7 @@ bool flushPending(const Qureg& q, const std::vector<int>* qubits, const char* fu
         }
         if (it->second.ops.empty() && it->second.phases.empty()) g_pending.erase(it);
     }
-    if (!applyPhases(q, phases, func)) return false;
-    return applyPendingList(q, todo, func);
-}
-
-// applies every pending one-qubit op of a statevector, keeping its pending phases
-bool flushPendingOps(const Qureg& q, const char* func) {
-    std::vector<std::pair<int, PendingOp>> todo;
-    {
-        std::lock_guard<std::mutex> lock(g_pendingMu);
-        auto it = g_pending.find(q.gpuAmps);
-        if (it == g_pending.end()) return true;
-        for (auto& kv : it->second.ops) todo.push_back(kv);
-        it->second.ops.clear();
-        if (it->second.phases.empty()) g_pending.erase(it);
-    }
-    return applyPendingList(q, todo, func);
+    return applyPendingList(q, todo, phases, func);
 }
 
 // a pending phase on a statevector involves this qubit
@@ -303,7 +385,7 @@ bool phasePendingOn(const Qureg& q, int qubit) {
     return false;
 }
 
-// defers a controlled phase of a statevector (after its pending one-qubit ops are applied)
+// defers a controlled phase of a statevector (it acts after the pending one-qubit ops)
 void addPendingPhase(const Qureg& q, long long mask, cd factor) {
     std::lock_guard<std::mutex> lock(g_pendingMu);
     PendingSet& set = g_pending[q.gpuAmps];
@@ -490,9 +572,11 @@ bool diagSV(const Qureg& q, const vector<int>& c, const vector<int>& s, const ve
 
 void applyDiag(const Qureg& q, const int* ctrls, const int* states, int nc, const int* targs, int nt, const qcomp_t* d,
                const qcomp_t* ex, bool anyTarg, const char* func) {
-    // a controlled phase (one target, factor 1 on |0>, every control state 1) on a
-    // statevector that defers one-qubit gates is deferred too
-    bool phase = !q.isDensityMatrix && !ex && !anyTarg && nt == 1 && d[0].re == 1 && d[0].im == 0 && deferSV(q);
+    // a controlled phase (one target, factor 1 on |0>, a factor of modulus 1 on |1>, every
+    // control state 1) on a statevector of at least 8 qubits that defers one-qubit gates is
+    // deferred too
+    bool phase = !q.isDensityMatrix && !ex && !anyTarg && nt == 1 && d[0].re == 1 && d[0].im == 0 &&
+                 std::fabs(std::abs(C(d[1])) - 1.0) < 1e-9 && q.numQubits >= 8 && deferSV(q);
     for (int i = 0; phase && states && i < nc; i++) phase = states[i] == 1;
     if (!checkQureg(q, func, phase)) return;
     if (!checkCtrlsTargs(q, ctrls, nc, targs, nt, func)) return;
@@ -501,8 +585,7 @@ void applyDiag(const Qureg& q, const int* ctrls, const int* states, int nc, cons
     if (!check(isUnitaryDiag(d, (qindex)1 << nt), func, "The given matrix was not (approximately) unitary.")) return;
     if (ex && !check(std::abs(ex->im) <= g_eps, func, "The exponent of a unitary diagonal matrix must be real.")) return;
     if (phase) {
-        // pending one-qubit ops come first; the phases then wait with the other pending phases
-        if (!flushPendingOps(q, func)) return;
+        // waits with the other pending phases, after the pending one-qubit ops
         long long mask = 1LL << targs[0];
         for (int i = 0; i < nc; i++) mask |= 1LL << ctrls[i];
         if (!(d[1].re == 1 && d[1].im == 0)) addPendingPhase(q, mask, C(d[1]));

@@ -185,6 +185,7 @@ def every_op_circuit(nq, is_dm, seed, with_measure=True):
     L.append(f"CPSTR 1 {c} 1 {pauli_text(codes)}")
     L.append(f"CPG 1 {c} 0 {pauli_text(codes)} {ang()}")
     t = distinct(min(3, nq)); L.append(f"PHG {len(t)} {' '.join(map(str, t))} {ang()}")
+    t = distinct(min(3, nq)); L.append(f"MPS {len(t)} {' '.join(map(str, t))} {ang()}")
     t = distinct(min(4, nq)); L.append(f"QFT {len(t)} {' '.join(map(str, t))}")
     L.append("FQFT")
     if is_dm:

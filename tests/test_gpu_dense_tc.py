@@ -294,3 +294,92 @@ def test_deferred_phases_and_gates(env, seed):
             assert np.max(np.abs(res - wres)) <= TOL
     finally:
         lib().qg_set_fp64_products(0)
+
+
+def _pair_layer(nq, rng, phases=True):
+    lines = [f"U1 {t} {qc.mat_tokens(qc.haar_unitary(2, rng))}" for t in range(nq)]
+    if phases:
+        perm = rng.permutation(nq)
+        lines += [f"CPS {int(perm[2 * p])} {int(perm[2 * p + 1])} {rng.uniform(-3, 3)}" for p in range(nq // 2)]
+    return "\n".join(lines) + "\n"
+
+
+def test_pair_layer_takes_no_phase_pass(env):
+    """A one-qubit gate on every qubit of a 22-qubit statevector, then controlled phases on
+    disjoint random pairs: the pairs are packed into the four-qubit passes and their phases
+    folded into those passes, so the layer launches exactly as many kernels as the same
+    layer without phases (no phase pass), and matches the oracle within 1e-12."""
+    from quest_gb300.circuit import run_text
+    nq = 22
+    rng = np.random.default_rng(404)
+    Q = env.Q
+    q = Q.createQureg(nq)
+    try:
+        amps = qc.random_statevector(nq, 405)
+        env.set_amps(q, amps)
+        counts = {}
+        text = ""
+        for rep in range(2):
+            for phases in (False, True):
+                layer = _pair_layer(nq, rng, phases)
+                text += layer
+                before = ctypes.c_int64(0)
+                assert _lib().qg_get_launch_count(ctypes.byref(before)) == 0
+                run_text(layer, q)
+                Q.flushQuregDeferredOps(q)
+                after = ctypes.c_int64(0)
+                assert _lib().qg_get_launch_count(ctypes.byref(after)) == 0
+                counts[(rep, phases)] = after.value - before.value
+        got = env.get_amps(q)
+    finally:
+        Q.destroyQureg(q)
+    # 5 four-qubit passes (each with the tensor-core error-flag check) + 1 two-qubit pass
+    assert counts[(1, True)] == counts[(1, False)] <= 11, counts
+    want, _, _ = qc.oracle().run(text, nq, 0, amps)
+    assert np.max(np.abs(got - want)) <= TOL
+    assert _flag() == 0
+
+
+@pytest.mark.parametrize("seed", [21, 22])
+def test_phases_folded_into_gate_groups(env, seed):
+    """Deferred phases folded into the passes of the deferred one-qubit gates, on a 22-qubit
+    statevector: pair layers, three-qubit phase shifts, one-qubit phases on qubits with a
+    pending gate, a chain of phases joining more than four qubits (not packed together: the
+    phases left out go to the phase pass), phases on qubits with no pending gate, and layers
+    on a subset of the qubits: within 1e-12 of the oracle in both product modes."""
+    nq = 22
+    rng = np.random.default_rng(seed)
+    lines = []
+    for layer in range(6):
+        qubits = range(nq) if layer % 3 != 2 else sorted(int(v) for v in rng.choice(nq, 13, replace=False))
+        for t in qubits:
+            lines.append(f"U1 {t} {qc.mat_tokens(qc.haar_unitary(2, rng))}")
+        perm = [int(v) for v in rng.permutation(nq)]
+        for p in range(int(rng.integers(3, nq // 2 + 1))):
+            lines.append(f"CPS {perm[2 * p]} {perm[2 * p + 1]} {rng.uniform(-3, 3)}")
+        if layer == 1:
+            a, b, c, d = (int(v) for v in rng.choice(nq, 4, replace=False))
+            lines.append(f"MPS 3 {a} {b} {c} {rng.uniform(-3, 3)}")
+            lines.append(f"PS {d} {rng.uniform(-3, 3)}")
+            lines.append(f"T {a}")
+            lines.append(f"CZ {b} {d}")
+        if layer == 3:
+            chain = [int(v) for v in rng.choice(nq, 7, replace=False)]
+            for i in range(6):
+                lines.append(f"CPS {chain[i]} {chain[i + 1]} {rng.uniform(-3, 3)}")
+            lines.append(f"MPS 4 {chain[0]} {chain[2]} {chain[4]} {chain[6]} {rng.uniform(-3, 3)}")
+        if layer == 4:
+            lines.append("TOTALPROB")
+    lines.append("TOTALPROB")
+    text = "\n".join(lines) + "\n"
+    amps = qc.random_statevector(nq, seed + 300)
+    want, wres, _ = qc.oracle().run(text, nq, 0, amps)
+    try:
+        for mode in (0, 1):
+            assert _lib().qg_set_fp64_products(mode) == 0
+            got, res = run_gpu(env, text, nq, amps)
+            assert np.max(np.abs(got - want)) <= TOL
+            assert np.max(np.abs(res - wres)) <= TOL
+    finally:
+        _lib().qg_set_fp64_products(0)
+    assert _flag() == 0
