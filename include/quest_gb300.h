@@ -173,6 +173,8 @@ int qg_sv_anyCtrlTwoTargDenseMatr(void* amps, int numQubits, const int* ctrls, c
 /* gpu_statevec_anyCtrlAnyTargDenseMatr_sub<NumCtrls,NumTargs,ApplyConj> (gpu_subroutines.hpp:64;
  * gpu_subroutines.cpp:396-507).  matr: 2^k x 2^k row-major HOST elements; matrix
  * index bit i is targs[i].  applyConj conjugates every element. */
+int qg_sv_anyCtrlAnyTargDenseMatr(void* amps, int numQubits, const int* ctrls, const int* ctrlStates, int numCtrls,
+                                  const int* targs, int numTargs, const qg_cplx* matr, int applyConj, void* stream);
 /* A set of controlled phases: every amplitude whose index has all bits of masks[f] set is
  * multiplied by factors[f] (|factors[f]| = 1), f < num <= 32, in one pass (the phases
  * commute); statevectors of at least 8 qubits.  Products in fixed point; the API defers
@@ -183,10 +185,18 @@ int qg_sv_phaseSet(void* amps, int numQubits, const int64_t* masks, const qg_cpl
  * whose bit `target` is set, the phase exp(i pi L / 2^numLowBits) with L = (index >>
  * lowTarget) & (2^numLowBits - 1) -- the target's controlled phases of
  * applyQuantumFourierTransform (operations.cpp:1934-1952), one pass instead of
- * numLowBits + 1.  Fixed-point products (Inf/NaN and extreme scales in FP64). */
+ * numLowBits + 1.  numLowBits <= 40.  Fixed-point products (Inf/NaN and extreme scales in FP64). */
 int qg_sv_qftStep(void* amps, int numQubits, int target, int lowTarget, int numLowBits, void* stream);
-int qg_sv_anyCtrlAnyTargDenseMatr(void* amps, int numQubits, const int* ctrls, const int* ctrlStates, int numCtrls,
-                                  const int* targs, int numTargs, const qg_cplx* matr, int applyConj, void* stream);
+/* The QFT steps of `target` and then `target` - 1 on contiguous targets from qubit 0
+ * (qg_sv_qftStep(target, 0, target) followed by qg_sv_qftStep(target - 1, 0, target - 1)) in
+ * one pass over quadruples of amplitudes: 2 * target + 1 gates of
+ * applyQuantumFourierTransform (operations.cpp:1934-1949).  1 <= target <= 40. */
+int qg_sv_qftTwoSteps(void* amps, int numQubits, int target, void* stream);
+/* The closing swaps of a quantum Fourier transform on the targets 0..numBits-1 (qubit j
+ * with qubit numBits-1-j, j < numBits/2: applySwap in applyQuantumFourierTransform,
+ * operations.cpp:1950-1952) as one in-place pass: every amplitude index has its low numBits
+ * bits reversed.  10 <= numBits <= numQubits.  A permutation: bit-exact. */
+int qg_sv_reverseLowBits(void* amps, int numQubits, int numBits, void* stream);
 
 /* gpu_statevec_anyCtrlOneTargDiagMatr_sub (gpu_subroutines.hpp:71; gpu_subroutines.cpp:516-572) */
 int qg_sv_anyCtrlOneTargDiagMatr(void* amps, int numQubits, const int* ctrls, const int* ctrlStates, int numCtrls,

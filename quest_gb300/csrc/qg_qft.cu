@@ -32,8 +32,9 @@
 #include <complex>
 #include <vector>
 
+#define QFT_MAX_TABLES 5         // twiddle index L of up to 40 bits
 struct QftTables {
-    long long t[4][256][2];     // table k, entry j: exp(i pi j 2^(8k) / 2^n) (k = 0: / sqrt2), (re, im) x 2^62
+    long long t[QFT_MAX_TABLES][256][2];   // table k, entry j: exp(i pi j 2^(8k) / 2^n) (k = 0: / sqrt2), (re, im) x 2^62
 };
 
 // the top 64 bits of a * b (signed), to within 2 units: balanced 32-bit limbs a = ah 2^32 + al
@@ -76,6 +77,44 @@ __device__ __forceinline__ double qft_double(long long Y, int t) {
 #define QFT_THREADS 256
 #define QFT_C (3260954456333195553LL)    // round(2^62 / sqrt2)
 
+// One butterfly at the pair's own scale: o0 = (v0 + v1) / sqrt2, o1 = w (v0 - v1), with
+// (wr, wi) = w at scale 2^62 (the 1/sqrt2 included, |w| <= 1/sqrt2).  The pair's four reals
+// share the largest exponent eb and become integers below 2^60; sums and differences are
+// exact and each output is the top 64 bits of its products.  Pairs holding Inf/NaN or with
+// scales near the ends of the double range are evaluated in FP64.
+__device__ __forceinline__ void qft_butterfly(const double2 v0, const double2 v1, long long wr, long long wi, double2& o0,
+                                              double2& o1) {
+    const uint64_t u[4] = {qgfx::f64_bits(v0.x), qgfx::f64_bits(v0.y), qgfx::f64_bits(v1.x), qgfx::f64_bits(v1.y)};
+    int eb = 1;
+    uint64_t any = 0;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const int ei = (int)((u[k] >> 52) & 0x7FF);
+        eb = max(eb, ei + (ei == 0));
+        any |= u[k] << 1;
+    }
+    if (any == 0) {
+        o0 = make_double2(0.0, 0.0);
+        o1 = o0;
+    } else if (eb >= 58 && eb <= 2043) {
+        const long long x0r = qft_fixed(u[0], eb), x0i = qft_fixed(u[1], eb);
+        const long long x1r = qft_fixed(u[2], eb), x1i = qft_fixed(u[3], eb);
+        const long long sr = x0r + x1r, si = x0i + x1i, dr = x0r - x1r, di = x0i - x1i;
+        // values * 2^(1082 - eb) / 4: (a0 + a1) / sqrt2 and w (a0 - a1)
+        const long long y0r = mulhi(sr, QFT_C), y0i = mulhi(si, QFT_C);
+        const long long y1r = mulhi(dr, wr) - mulhi(di, wi), y1i = mulhi(dr, wi) + mulhi(di, wr);
+        const int t = eb - 1080;
+        o0 = make_double2(qft_double(y0r, t), qft_double(y0i, t));
+        o1 = make_double2(qft_double(y1r, t), qft_double(y1i, t));
+    } else {
+        const double s = 0.70710678118654752440;
+        const double cr = (double)wr * 0x1p-62 / s, ci = (double)wi * 0x1p-62 / s;   // w sqrt2
+        o0 = make_double2((v0.x + v1.x) * s, (v0.y + v1.y) * s);
+        const double dr = (v0.x - v1.x) * s, di = (v0.y - v1.y) * s;
+        o1 = make_double2(fma(dr, cr, -di * ci), fma(dr, ci, di * cr));
+    }
+}
+
 // NT tables (compile time, so that every loop over them unrolls)
 template <int NT>
 __global__ void __launch_bounds__(QFT_THREADS) k_qft_step(double2* __restrict__ a, qidx numPairs, int tb, int lb, qidx lmask,
@@ -97,37 +136,8 @@ __global__ void __launch_bounds__(QFT_THREADS) k_qft_step(double2* __restrict__ 
             const int j = (int)((L >> (8 * k)) & 255);
             cmul62(wr, wi, sT[k][j][0], sT[k][j][1], wr, wi);
         }
-        const uint64_t u[4] = {qgfx::f64_bits(v0.x), qgfx::f64_bits(v0.y), qgfx::f64_bits(v1.x), qgfx::f64_bits(v1.y)};
-        int eb = 1;
-        uint64_t any = 0;
-#pragma unroll
-        for (int k = 0; k < 4; k++) {
-            const int ei = (int)((u[k] >> 52) & 0x7FF);
-            eb = max(eb, ei + (ei == 0));
-            any |= u[k] << 1;
-        }
         double2 o0, o1;
-        if (any == 0) {
-            o0 = make_double2(0.0, 0.0);
-            o1 = o0;
-        } else if (eb >= 58 && eb <= 2043) {
-            const long long x0r = qft_fixed(u[0], eb), x0i = qft_fixed(u[1], eb);
-            const long long x1r = qft_fixed(u[2], eb), x1i = qft_fixed(u[3], eb);
-            const long long sr = x0r + x1r, si = x0i + x1i, dr = x0r - x1r, di = x0i - x1i;
-            // values * 2^(1082 - eb) / 4: (a0 + a1) / sqrt2 and w^L (a0 - a1) / sqrt2
-            const long long y0r = mulhi(sr, QFT_C), y0i = mulhi(si, QFT_C);
-            const long long y1r = mulhi(dr, wr) - mulhi(di, wi), y1i = mulhi(dr, wi) + mulhi(di, wr);
-            const int t = eb - 1080;
-            o0 = make_double2(qft_double(y0r, t), qft_double(y0i, t));
-            o1 = make_double2(qft_double(y1r, t), qft_double(y1i, t));
-        } else {
-            // FP64: Inf/NaN, or scales near the ends of the range
-            const double s = 0.70710678118654752440;
-            const double cr = (double)wr * 0x1p-62 / s, ci = (double)wi * 0x1p-62 / s;   // w^L
-            o0 = make_double2((v0.x + v1.x) * s, (v0.y + v1.y) * s);
-            const double dr = (v0.x - v1.x) * s, di = (v0.y - v1.y) * s;
-            o1 = make_double2(fma(dr, cr, -di * ci), fma(dr, ci, di * cr));
-        }
+        qft_butterfly(v0, v1, wr, wi, o0, o1);
         st_amp(a + i0, o0);
         st_amp(a + i1, o1);
     }
@@ -162,38 +172,97 @@ __global__ void __launch_bounds__(QFT_THREADS) k_qft_step_chunks(double2* __rest
             const double2 v0 = ld_amp(a + i0), v1 = ld_amp(a + i1);
             long long wr, wi;
             cmul62(sT[0][k0][0], sT[0][k0][1], hr, hi, wr, wi);
-            const uint64_t u[4] = {qgfx::f64_bits(v0.x), qgfx::f64_bits(v0.y), qgfx::f64_bits(v1.x), qgfx::f64_bits(v1.y)};
-            int eb = 1;
-            uint64_t any = 0;
-#pragma unroll
-            for (int k = 0; k < 4; k++) {
-                const int ei = (int)((u[k] >> 52) & 0x7FF);
-                eb = max(eb, ei + (ei == 0));
-                any |= u[k] << 1;
-            }
             double2 o0, o1;
-            if (any == 0) {
-                o0 = make_double2(0.0, 0.0);
-                o1 = o0;
-            } else if (eb >= 58 && eb <= 2043) {
-                const long long x0r = qft_fixed(u[0], eb), x0i = qft_fixed(u[1], eb);
-                const long long x1r = qft_fixed(u[2], eb), x1i = qft_fixed(u[3], eb);
-                const long long sr = x0r + x1r, si = x0i + x1i, dr = x0r - x1r, di = x0i - x1i;
-                const long long y0r = mulhi(sr, QFT_C), y0i = mulhi(si, QFT_C);
-                const long long y1r = mulhi(dr, wr) - mulhi(di, wi), y1i = mulhi(dr, wi) + mulhi(di, wr);
-                const int t = eb - 1080;
-                o0 = make_double2(qft_double(y0r, t), qft_double(y0i, t));
-                o1 = make_double2(qft_double(y1r, t), qft_double(y1i, t));
-            } else {
-                const double s = 0.70710678118654752440;
-                const double cr = (double)wr * 0x1p-62 / s, ci = (double)wi * 0x1p-62 / s;
-                o0 = make_double2((v0.x + v1.x) * s, (v0.y + v1.y) * s);
-                const double dr = (v0.x - v1.x) * s, di = (v0.y - v1.y) * s;
-                o1 = make_double2(fma(dr, cr, -di * ci), fma(dr, ci, di * cr));
-            }
+            qft_butterfly(v0, v1, wr, wi, o0, o1);
             st_amp(a + i0, o0);
             st_amp(a + i1, o1);
         }
+    }
+}
+
+// Two steps in one pass, targets from qubit 0: the step of target T (twiddle index L = the
+// T bits below it) and then the step of target T - 1 (the T - 1 bits below it).  A thread
+// takes the four amplitudes a_xy that differ in bits T (x) and T - 1 (y) only; with B = their
+// index bits below T - 1 and w = exp(i pi / 2^T):
+//     step T:     pairs (a_0y, a_1y), twiddle w^(B + y 2^(T-1)) / sqrt2 = i^y W,  W = w^B / sqrt2
+//     step T - 1: pairs (x_x0, x_x1), twiddle exp(i pi B / 2^(T-1)) / sqrt2 = w^(2B) / sqrt2 = V
+// Both twiddles come from the tables of step T: W from the bytes of B and V from those of 2B.
+// Between the steps the values are rounded to double, as in two separate passes.
+//
+// T - 1 >= 8: a warp takes chunks of 256 consecutive quadruples (lane l, round r: B's low
+// byte b = 32 r + l).  B's higher bytes are fixed across the chunk, so W's product of the
+// higher tables (HW) is formed once per chunk, and V's as well: the bytes of 2B above the
+// lowest are those of 2 (B - b) with bit 8 set when b >= 128: two products (H0, H1).
+template <int NT>
+__global__ void __launch_bounds__(QFT_THREADS, 3) k_qft_two_steps_chunks(double2* __restrict__ a, qidx numChunks, int tb,
+                                                                      const __grid_constant__ QftTables T) {
+    static_assert(NT >= 2, "T - 1 >= 8 needs two tables");
+    __shared__ long long sT[NT][256][2];
+    for (int e = threadIdx.x; e < NT * 512; e += QFT_THREADS) (&sT[0][0][0])[e] = (&T.t[0][0][0])[e];
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const qidx bMask = ((qidx)1 << (tb - 1)) - 1, half = (qidx)1 << (tb - 1), top = (qidx)1 << tb;
+    const qidx warps = (qidx)gridDim.x * (QFT_THREADS / 32);
+    for (qidx c = blockIdx.x * (qidx)(QFT_THREADS / 32) + (threadIdx.x >> 5); c < numChunks; c += warps) {
+        const qidx Bh = (c << 8) & bMask;                       // B with its low byte cleared
+        const qidx B2 = Bh << 1;                                // 2 B with its low 9 bits cleared
+        long long hwr = sT[1][(Bh >> 8) & 255][0], hwi = sT[1][(Bh >> 8) & 255][1];
+        const int j1 = (int)((B2 >> 8) & 255);
+        long long h0r = sT[1][j1][0], h0i = sT[1][j1][1], h1r = sT[1][j1 | 1][0], h1i = sT[1][j1 | 1][1];
+#pragma unroll
+        for (int k = 2; k < NT; k++) {
+            const int j = (int)((Bh >> (8 * k)) & 255), j2 = (int)((B2 >> (8 * k)) & 255);
+            cmul62(hwr, hwi, sT[k][j][0], sT[k][j][1], hwr, hwi);
+            cmul62(h0r, h0i, sT[k][j2][0], sT[k][j2][1], h0r, h0i);
+            cmul62(h1r, h1i, sT[k][j2][0], sT[k][j2][1], h1r, h1i);
+        }
+#pragma unroll 1
+        for (int r = 0; r < 8; r++) {
+            const int b = 32 * r + lane;                        // B & 255
+            const qidx qd = (c << 8) + b;
+            const qidx i00 = ((qd & ~bMask) << 2) | (qd & bMask);
+            const double2 v00 = ld_amp(a + i00), v01 = ld_amp(a + i00 + half);
+            const double2 v10 = ld_amp(a + i00 + top), v11 = ld_amp(a + i00 + top + half);
+            long long wr, wi, vr, vi;
+            cmul62(sT[0][b][0], sT[0][b][1], hwr, hwi, wr, wi);
+            const bool hi = r >= 4;                             // b >= 128: bit 8 of 2B set
+            cmul62(sT[0][(2 * b) & 255][0], sT[0][(2 * b) & 255][1], hi ? h1r : h0r, hi ? h1i : h0i, vr, vi);
+            double2 x00, x10, x01, x11, y00, y01, y10, y11;
+            qft_butterfly(v00, v10, wr, wi, x00, x10);
+            qft_butterfly(v01, v11, -wi, wr, x01, x11);         // i W
+            qft_butterfly(x00, x01, vr, vi, y00, y01);
+            qft_butterfly(x10, x11, vr, vi, y10, y11);
+            st_amp(a + i00, y00);
+            st_amp(a + i00 + half, y01);
+            st_amp(a + i00 + top, y10);
+            st_amp(a + i00 + top + half, y11);
+        }
+    }
+}
+
+// The same for 1 <= T <= 8: B < 128 and 2B < 256, one table (W = T0[B], V = T0[2B]).
+__global__ void __launch_bounds__(QFT_THREADS) k_qft_two_steps_small(double2* __restrict__ a, qidx numQuads, int tb,
+                                                                     const __grid_constant__ QftTables T) {
+    __shared__ long long sT[256][2];
+    for (int e = threadIdx.x; e < 512; e += QFT_THREADS) (&sT[0][0])[e] = (&T.t[0][0][0])[e];
+    __syncthreads();
+    const qidx bMask = ((qidx)1 << (tb - 1)) - 1, half = (qidx)1 << (tb - 1), top = (qidx)1 << tb;
+    const qidx stride = (qidx)gridDim.x * QFT_THREADS;
+    for (qidx qd = blockIdx.x * (qidx)QFT_THREADS + threadIdx.x; qd < numQuads; qd += stride) {
+        const int b = (int)(qd & bMask);
+        const qidx i00 = ((qd & ~bMask) << 2) | (qidx)b;
+        const double2 v00 = ld_amp(a + i00), v01 = ld_amp(a + i00 + half);
+        const double2 v10 = ld_amp(a + i00 + top), v11 = ld_amp(a + i00 + top + half);
+        const long long wr = sT[b][0], wi = sT[b][1], vr = sT[2 * b][0], vi = sT[2 * b][1];
+        double2 x00, x10, x01, x11, y00, y01, y10, y11;
+        qft_butterfly(v00, v10, wr, wi, x00, x10);
+        qft_butterfly(v01, v11, -wi, wr, x01, x11);
+        qft_butterfly(x00, x01, vr, vi, y00, y01);
+        qft_butterfly(x10, x11, vr, vi, y10, y11);
+        st_amp(a + i00, y00);
+        st_amp(a + i00 + half, y01);
+        st_amp(a + i00 + top, y10);
+        st_amp(a + i00 + top + half, y11);
     }
 }
 
@@ -264,7 +333,78 @@ __global__ void __launch_bounds__(QFT_THREADS) k_phase_set(double2* __restrict__
     }
 }
 
+// The closing swaps of a QFT on qubits 0..n-1 (n >= 10) as one in-place permutation: index
+// bits [0, n) reversed.  The index splits into o (bits above n), h (bits n-5..n-1), m (the
+// n - 10 middle bits) and l (bits 0..4); (o, h, m, l) goes to (o, rev5 l, rev m, rev5 h).  So
+// the 32 x 32 tile of (o, m) goes, transposed and with both 5-bit fields reversed, to the
+// tile of (o, rev m): a block reads a tile and its partner (one tile when m = rev m) into
+// shared memory -- rows of 32 consecutive amplitudes, 512 bytes -- and then writes both,
+// again in rows of 512 bytes.  Every tile belongs to one block, so nothing else reads or
+// writes it meanwhile.  Rows padded to 33 amplitudes: a warp reading a column of the tile
+// takes the minimum of four shared-memory wavefronts.
+// the twiddle tables of a step with n low bits: table k, entry j = exp(i pi j 2^(8k) / 2^n)
+// at scale 2^62, table 0 with 1/sqrt2; returns the number of tables (at least one)
+static int qft_tables(int n, QftTables& T) {
+    const int numTables = n <= 8 ? 1 : (n + 7) / 8;
+    const long double PI = 3.141592653589793238462643383279502884L;
+    for (int k = 0; k < numTables; k++)
+        for (int j = 0; j < 256; j++) {
+            const long double ang = PI * std::ldexp((long double)j, 8 * k - n);
+            const long double sc = (k == 0 ? 1.0L / std::sqrt(2.0L) : 1.0L) * 4611686018427387904.0L;   // 2^62
+            T.t[k][j][0] = (long long)std::llroundl(std::cos(ang) * sc);
+            T.t[k][j][1] = (long long)std::llroundl(std::sin(ang) * sc);
+        }
+    return numTables;
+}
+
+#define REV_THREADS 256
+__global__ void __launch_bounds__(REV_THREADS) k_reverse_low_bits(double2* __restrict__ a, qidx numTiles, int n) {
+    __shared__ double2 s[2][32][33];
+    const int midBits = n - 10;
+    const int lane = threadIdx.x & 31, row0 = threadIdx.x >> 5;
+    const int rl = (int)(__brev((unsigned)lane) >> 27);               // rev5(lane)
+    const qidx rowStride = (qidx)1 << (n - 5);
+    for (qidx tile = blockIdx.x; tile < numTiles; tile += gridDim.x) {
+        const qidx o = tile >> midBits, m = tile & (((qidx)1 << midBits) - 1);
+        const qidx rm = midBits ? (qidx)(__brevll((unsigned long long)m) >> (64 - midBits)) : 0;
+        if (rm < m) continue;                                            // the partner's tile does this pair
+        const bool two = rm != m;
+        const qidx baseM = (o << n) | (m << 5), baseR = (o << n) | (rm << 5);
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const int h = row0 + 8 * k;
+            s[0][h][lane] = ld_amp(a + baseM + h * rowStride + lane);
+            if (two) s[1][h][lane] = ld_amp(a + baseR + h * rowStride + lane);
+        }
+        __syncthreads();
+        // destination row r (= rev5 of the source's l), column lane (= rev5 of its h)
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const int r = row0 + 8 * k;
+            const int sl = (int)(__brev((unsigned)r) >> 27);
+            st_amp(a + baseR + r * rowStride + lane, s[0][rl][sl]);
+            if (two) st_amp(a + baseM + r * rowStride + lane, s[1][rl][sl]);
+        }
+        __syncthreads();
+    }
+}
+
 extern "C" {
+
+// Reverses the low numBits bits of every amplitude index (the closing swaps of a QFT on
+// qubits 0..numBits-1), in place, in one pass.
+int qg_sv_reverseLowBits(void* amps, int numQubits, int numBits, void* stream) {
+    QG_TRY(qg_check_amps(amps, numQubits));
+    if (numBits < 10 || numBits > numQubits)
+        return qg_fail(QG_ERR_ARG, "reverseLowBits: %d bits of a %d-qubit register (10 <= bits <= qubits)", numBits, numQubits);
+    const qidx numTiles = (qidx)1 << (numQubits - 10);
+    int perSm = 0;
+    QG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, k_reverse_low_bits, REV_THREADS, 0));
+    const unsigned grid = (unsigned)std::min<qidx>(numTiles, (qidx)qg_num_sms() * std::max(1, perSm));
+    k_reverse_low_bits<<<grid, REV_THREADS, 0, qg_stream(stream)>>>((double2*)amps, numTiles, numBits);
+    qg_note_launch();
+    return qg_check_launch("k_reverse_low_bits");
+}
 
 // A set of controlled phases on a statevector: every amplitude whose index contains
 // masks[f] (all those bits 1) is multiplied by factors[f], for each f < num (num <= 32;
@@ -314,19 +454,11 @@ int qg_sv_phaseSet(void* amps, int numQubits, const int64_t* masks, const qg_cpl
 // applyQuantumFourierTransform on the contiguous targets lowTarget..target).
 int qg_sv_qftStep(void* amps, int numQubits, int target, int lowTarget, int numLowBits, void* stream) {
     QG_TRY(qg_check_amps(amps, numQubits));
-    if (target < 0 || target >= numQubits || lowTarget < 0 || numLowBits < 0 || lowTarget + numLowBits != target || numLowBits > 32)
+    if (target < 0 || target >= numQubits || lowTarget < 0 || numLowBits < 0 || lowTarget + numLowBits != target ||
+        numLowBits > 8 * QFT_MAX_TABLES)
         return qg_fail(QG_ERR_ARG, "qftStep: target %d, low target %d, %d low bits", target, lowTarget, numLowBits);
     QftTables T;
-    const int numTables = numLowBits <= 8 ? 1 : (numLowBits + 7) / 8;
-    const long double PI = 3.141592653589793238462643383279502884L;
-    for (int k = 0; k < numTables; k++)
-        for (int j = 0; j < 256; j++) {
-            // exp(i pi j 2^(8k) / 2^n), the first table with 1/sqrt2
-            const long double ang = PI * std::ldexp((long double)j, 8 * k - numLowBits);
-            const long double sc = (k == 0 ? 1.0L / std::sqrt(2.0L) : 1.0L) * 4611686018427387904.0L;   // 2^62
-            T.t[k][j][0] = (long long)std::llroundl(std::cos(ang) * sc);
-            T.t[k][j][1] = (long long)std::llroundl(std::sin(ang) * sc);
-        }
+    const int numTables = qft_tables(numLowBits, T);
     const qidx numPairs = (qidx)1 << (numQubits - 1);
     const qidx lmask = numLowBits >= 63 ? -1 : (((qidx)1 << numLowBits) - 1);
     const unsigned grid = (unsigned)std::min<qidx>((numPairs + QFT_THREADS - 1) / QFT_THREADS, (qidx)qg_num_sms() * 8);
@@ -336,7 +468,8 @@ int qg_sv_qftStep(void* amps, int numQubits, int target, int lowTarget, int numL
         const qidx numChunks = numPairs >> 8;
         const unsigned g2 = (unsigned)std::min<qidx>((numChunks + QFT_THREADS / 32 - 1) / (QFT_THREADS / 32), (qidx)qg_num_sms() * 8);
         if (numTables == 3) k_qft_step_chunks<3><<<g2, QFT_THREADS, 0, st>>>(A, numChunks, target, lmask, T);
-        else k_qft_step_chunks<4><<<g2, QFT_THREADS, 0, st>>>(A, numChunks, target, lmask, T);
+        else if (numTables == 4) k_qft_step_chunks<4><<<g2, QFT_THREADS, 0, st>>>(A, numChunks, target, lmask, T);
+        else k_qft_step_chunks<5><<<g2, QFT_THREADS, 0, st>>>(A, numChunks, target, lmask, T);
         qg_note_launch();
         return qg_check_launch("k_qft_step_chunks");
     }
@@ -344,10 +477,41 @@ int qg_sv_qftStep(void* amps, int numQubits, int target, int lowTarget, int numL
         case 1: k_qft_step<1><<<grid, QFT_THREADS, 0, st>>>(A, numPairs, target, lowTarget, lmask, T); break;
         case 2: k_qft_step<2><<<grid, QFT_THREADS, 0, st>>>(A, numPairs, target, lowTarget, lmask, T); break;
         case 3: k_qft_step<3><<<grid, QFT_THREADS, 0, st>>>(A, numPairs, target, lowTarget, lmask, T); break;
-        default: k_qft_step<4><<<grid, QFT_THREADS, 0, st>>>(A, numPairs, target, lowTarget, lmask, T); break;
+        case 4: k_qft_step<4><<<grid, QFT_THREADS, 0, st>>>(A, numPairs, target, lowTarget, lmask, T); break;
+        default: k_qft_step<5><<<grid, QFT_THREADS, 0, st>>>(A, numPairs, target, lowTarget, lmask, T); break;
     }
     qg_note_launch();
     return qg_check_launch("k_qft_step");
+}
+
+// The QFT steps of targets `target` and then `target` - 1 on the contiguous targets from
+// qubit 0 (qg_sv_qftStep(target, 0, target), then qg_sv_qftStep(target - 1, 0, target - 1))
+// in one pass.
+int qg_sv_qftTwoSteps(void* amps, int numQubits, int target, void* stream) {
+    QG_TRY(qg_check_amps(amps, numQubits));
+    if (target < 1 || target >= numQubits || target > 8 * QFT_MAX_TABLES)
+        return qg_fail(QG_ERR_ARG, "qftTwoSteps: target %d of %d qubits", target, numQubits);
+    QftTables T;
+    const int numTables = qft_tables(target, T);
+    const qidx numQuads = (qidx)1 << (numQubits - 2);
+    double2* A = (double2*)amps;
+    cudaStream_t st = qg_stream(stream);
+    if (target <= 8) {
+        const unsigned grid = (unsigned)std::min<qidx>((numQuads + QFT_THREADS - 1) / QFT_THREADS, (qidx)qg_num_sms() * 8);
+        k_qft_two_steps_small<<<grid, QFT_THREADS, 0, st>>>(A, numQuads, target, T);
+        qg_note_launch();
+        return qg_check_launch("k_qft_two_steps_small");
+    }
+    const qidx numChunks = numQuads >> 8;
+    const unsigned grid = (unsigned)std::min<qidx>((numChunks + QFT_THREADS / 32 - 1) / (QFT_THREADS / 32), (qidx)qg_num_sms() * 8);
+    switch (numTables) {
+        case 2: k_qft_two_steps_chunks<2><<<grid, QFT_THREADS, 0, st>>>(A, numChunks, target, T); break;
+        case 3: k_qft_two_steps_chunks<3><<<grid, QFT_THREADS, 0, st>>>(A, numChunks, target, T); break;
+        case 4: k_qft_two_steps_chunks<4><<<grid, QFT_THREADS, 0, st>>>(A, numChunks, target, T); break;
+        default: k_qft_two_steps_chunks<5><<<grid, QFT_THREADS, 0, st>>>(A, numChunks, target, T); break;
+    }
+    qg_note_launch();
+    return qg_check_launch("k_qft_two_steps_chunks");
 }
 
 }  // extern "C"

@@ -1235,9 +1235,20 @@ void applyQuantumFourierTransform(Qureg q, int* t, int nt) {
     bool contiguous = true;
     for (int j = 1; j < nt; j++) contiguous = contiguous && t[j] == t[0] + j;
     if (!q.isDensityMatrix && contiguous && qg_fp64_products_mode() == 0) {
-        // each step (Hadamard on t[n], then its n controlled phases) as one pass
-        for (int n = nt - 1; n >= 0; n--)
+        // each step (Hadamard on t[n], then its n controlled phases) as one pass, or for
+        // targets from qubit 0 two steps per pass; their closing swaps as one permutation pass
+        for (int n = nt - 1; n >= 0; n--) {
+            if (t[0] == 0 && n >= 1) {
+                if (!backend(qg_sv_qftTwoSteps(q.gpuAmps, q.numQubits, t[n], g_stream), func)) return;
+                n--;
+                continue;
+            }
             if (!backend(qg_sv_qftStep(q.gpuAmps, q.numQubits, t[n], t[0], n, g_stream), func)) return;
+        }
+        if (t[0] == 0 && nt >= 10) {
+            backend(qg_sv_reverseLowBits(q.gpuAmps, q.numQubits, nt, g_stream), func);
+            return;
+        }
         for (int n = 0; n < nt / 2; n++) applySwap(q, t[n], t[nt - 1 - n]);
         return;
     }

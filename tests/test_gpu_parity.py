@@ -410,6 +410,8 @@ def test_tiled_pauli_batch_string_shapes(env, nq, style):
     (14, "QFT 5 3 4 5 6 7\n"),            # contiguous targets above qubit 0: one pass per step
     (14, "QFT 4 9 2 12 5\n"),             # not contiguous: the gate-by-gate form
     (10, "X 0\nFQFT\nFQFT\n"),
+    (16, "QFT 11 0 1 2 3 4 5 6 7 8 9 10\n"),   # from qubit 0, below the top: closing swaps in one pass
+    (14, "QFT 9 0 1 2 3 4 5 6 7 8\n"),        # fewer than 10 targets: the swaps one by one
 ])
 def test_qft_steps_vs_oracle(env, nq, text):
     """The quantum Fourier transform with each step (Hadamard and its controlled phases)
@@ -425,3 +427,61 @@ def test_qft_steps_vs_oracle(env, nq, text):
             assert np.max(np.abs(res - wres), initial=0) <= TOL
     finally:
         lib().qg_set_fp64_products(0)
+
+
+@pytest.mark.parametrize("nq,nb", [(10, 10), (11, 10), (13, 13), (16, 12), (20, 20), (21, 15)])
+def test_reverse_low_bits_bit_exact(env, nq, nb):
+    """The closing swaps of a QFT on qubits 0..nb-1 as one permutation pass: every index has
+    its low nb bits reversed, bit for bit (a permutation of the amplitudes)."""
+    import ctypes
+    from quest_gb300._lib import lib
+    amps = qc.random_statevector(nq, 7 * nq + nb)
+    idx = np.arange(1 << nq, dtype=np.int64)
+    low = idx & ((1 << nb) - 1)
+    rev = np.zeros_like(low)
+    for b in range(nb):
+        rev |= ((low >> b) & 1) << (nb - 1 - b)
+    want = np.empty_like(amps)
+    want[(idx & ~((1 << nb) - 1)) | rev] = amps
+    Q = env.Q
+    q = Q.createQureg(nq)
+    try:
+        env.set_amps(q, amps)
+        assert lib().qg_sync() == 0
+        assert lib().qg_sv_reverseLowBits(ctypes.cast(q.gpuAmps, ctypes.c_void_p), nq, nb, None) == 0
+        assert lib().qg_sync() == 0
+        got = env.get_amps(q)
+    finally:
+        Q.destroyQureg(q)
+    assert got.tobytes() == want.tobytes()
+
+
+def test_qft_two_steps_match_single_steps(env):
+    """Two QFT steps in one pass (targets T and T - 1 from qubit 0) against the two single-step
+    passes, on a 26-qubit state, for T from 25 (four twiddle tables) down to 1: the same values
+    to 1e-14 of the largest amplitude (the step of T on the pairs whose bit T - 1 is set takes
+    its twiddle as i W, which the single step forms from its tables)."""
+    import ctypes
+    from quest_gb300._lib import lib
+    L = lib()
+    nq = 26
+    nbytes = 16 << nq
+    bufs = [ctypes.c_void_p(), ctypes.c_void_p()]
+    for b in bufs:
+        assert L.qg_alloc(ctypes.byref(b), nbytes) == 0
+    try:
+        for T in (25, 24, 17, 16, 9, 8, 3, 1):
+            for b in bufs:
+                assert L.qg_sv_initDebugState(b, nq, None) == 0
+            assert L.qg_sv_qftTwoSteps(bufs[0], nq, T, None) == 0
+            assert L.qg_sv_qftStep(bufs[1], nq, T, 0, T, None) == 0
+            assert L.qg_sv_qftStep(bufs[1], nq, T - 1, 0, T - 1, None) == 0
+            out = [np.empty(1 << nq, dtype=np.complex128) for _ in bufs]
+            for o, b in zip(out, bufs):
+                assert L.qg_copy_d2h(o.ctypes.data_as(ctypes.c_void_p), b, nbytes, None) == 0
+            assert L.qg_sync() == 0
+            scale = np.max(np.abs(out[1]))
+            assert np.max(np.abs(out[0] - out[1])) <= 1e-14 * scale, T
+    finally:
+        for b in bufs:
+            L.qg_free(b)
