@@ -88,14 +88,19 @@ struct PendingOp {
     double p[3];      // the channel's parameters when kind is not PEND_GENERAL
     cd m[16];         // the product of the qubit's pending superoperators, row-major
 };
+typedef std::vector<std::pair<long long, cd>> PhaseList;
 struct PendingSet {
     int numQubits;                      // the Qureg's (ket) qubits
     bool dm;                            // a density matrix (else a statevector: PEND_SV ops)
     std::map<int, PendingOp> ops;       // ket qubit -> its pending op
     // statevectors: pending controlled phases (qubit mask, factor), which commute with one
-    // another and come after every pending one-qubit op (a one-qubit gate on a qubit of a
-    // pending phase applies everything pending first)
-    std::vector<std::pair<long long, cd>> phases;
+    // another and come after every pending one-qubit op and the block (a one-qubit gate on
+    // a qubit of a pending phase applies everything pending first)
+    PhaseList phases;
+    // statevectors: a pending two-qubit unitary (blockQ[0] < blockQ[1], -1 when none; 4x4,
+    // index bit i = qubit blockQ[i]), whose qubits have no entry in `ops`
+    int blockQ[2] = {-1, -1};
+    cd block[16];
 };
 std::map<const void*, PendingSet> g_pending;   // keyed by gpuAmps
 std::mutex g_pendingMu;
@@ -158,12 +163,28 @@ bool deferSV(const Qureg& q) {
            qg_dense_tc_wanted((long long)1 << (q.numQubits - 4));
 }
 
-// U applied after the qubit's pending unitary: pending = U * pending
+// U applied after the qubit's pending unitary: pending = U * pending (the block's, when the
+// qubit is one of the pending two-qubit block's)
 void addPendingSV(const Qureg& q, int qubit, const cd (&U)[4]) {
     std::lock_guard<std::mutex> lock(g_pendingMu);
     PendingSet& set = g_pending[q.gpuAmps];
     set.numQubits = q.numQubits;
     set.dm = false;
+    if (qubit == set.blockQ[0] || qubit == set.blockQ[1]) {
+        const int bit = qubit == set.blockQ[0] ? 0 : 1;
+        cd nb[16];
+        for (int r = 0; r < 4; r++)
+            for (int c = 0; c < 4; c++) {
+                cd acc = 0;
+                for (int v = 0; v < 2; v++) {
+                    const int sr = (r & ~(1 << bit)) | (v << bit);     // r with its `bit` set to v
+                    acc += U[((r >> bit) & 1) * 2 + v] * set.block[sr * 4 + c];
+                }
+                nb[r * 4 + c] = acc;
+            }
+        for (int i = 0; i < 16; i++) set.block[i] = nb[i];
+        return;
+    }
     auto it = set.ops.find(qubit);
     if (it == set.ops.end()) {
         PendingOp op;
@@ -179,36 +200,57 @@ void addPendingSV(const Qureg& q, int qubit, const cd (&U)[4]) {
     P[0] = r0; P[1] = r1; P[2] = r2; P[3] = r3;
 }
 
-typedef std::vector<std::pair<long long, cd>> PhaseList;
+// a pending statevector unitary on one qubit or on two (q[0] < q[1]; 2^k x 2^k, index bit i
+// = qubit q[i])
+struct SVUnit {
+    int k;
+    int q[2];
+    cd m[16];
+};
 
-// Groups of at most four pending statevector qubits (indices into `todo`), one pass each.
-// A pending phase whose qubits all have pending ops and fall into one group is folded into
-// that group's matrix (it acts after the group's unitaries and commutes with every other
-// group), which saves the phase pass when all of them fold.  So the qubits joined by such
-// phases (clusters of at most four) are packed into the groups first-fit, largest first,
-// into as many groups as the plain split needs (n/4 groups of four and one of n % 4); the
-// cluster holding qubit 0 goes to the smaller group when it fits there, since a four-qubit
-// pass without qubit 0 takes the faster (staged) tensor-core form.  When the clusters do not
-// pack into that many groups, the plain split is used: qubits in ascending order, qubit 0
-// last.
-std::vector<std::vector<int>> groupSV(const std::vector<std::pair<int, PendingOp>>& todo, const PhaseList& phases) {
-    const int n = (int)todo.size();
+// Groups of at most four pending statevector qubits (indices into `units`, whose units
+// stay whole), one pass each.  A pending phase whose qubits all have pending units and fall
+// into one group is folded into that group's matrix (it acts after the group's unitaries and
+// commutes with every other group), which saves the phase pass when all of them fold.  So
+// the units joined by such phases (clusters of at most four qubits) are packed into the
+// groups first-fit, largest first, into as many groups as the plain split needs (n/4 groups
+// of four qubits and one of n % 4); the cluster holding qubit 0 goes to the smaller group
+// when it fits there, since a four-qubit pass without qubit 0 takes the faster (staged)
+// tensor-core form.  When the clusters do not pack into that many groups, the units are
+// packed in ascending order of their qubits, qubit 0 last.
+std::vector<std::vector<int>> groupSV(const std::vector<SVUnit>& units, const PhaseList& phases) {
+    const int nu = (int)units.size();
+    int n = 0;
+    for (auto& u : units) n += u.k;
+    auto holdsZero = [&](int i) { return units[i].q[0] == 0 || (units[i].k == 2 && units[i].q[1] == 0); };
     std::vector<std::vector<int>> plain;
     {
-        std::vector<int> order(n);
-        for (int i = 0; i < n; i++) order[i] = i;
-        std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return (todo[x].first == 0) < (todo[y].first == 0); });
-        for (int i = 0; i < n; i += 4) plain.push_back(std::vector<int>(order.begin() + i, order.begin() + std::min(n, i + 4)));
+        std::vector<int> order(nu);
+        for (int i = 0; i < nu; i++) order[i] = i;
+        std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+            if (holdsZero(x) != holdsZero(y)) return holdsZero(y);
+            return units[x].q[0] < units[y].q[0];
+        });
+        int room = 0;
+        for (int i : order) {
+            if (room < units[i].k) {
+                plain.emplace_back();
+                room = 4;
+            }
+            plain.back().push_back(i);
+            room -= units[i].k;
+        }
     }
-    if (phases.empty() || n < 2) return plain;
+    if (phases.empty() || nu < 2) return plain;
     long long pendingMask = 0;
     int at[64];
-    for (int i = 0; i < n; i++) {
-        pendingMask |= 1LL << todo[i].first;
-        at[todo[i].first] = i;
-    }
-    std::vector<int> parent(n);
-    for (int i = 0; i < n; i++) parent[i] = i;
+    for (int i = 0; i < nu; i++)
+        for (int b = 0; b < units[i].k; b++) {
+            pendingMask |= 1LL << units[i].q[b];
+            at[units[i].q[b]] = i;
+        }
+    std::vector<int> parent(nu);
+    for (int i = 0; i < nu; i++) parent[i] = i;
     auto find = [&](int i) {
         while (parent[i] != i) i = parent[i] = parent[parent[i]];
         return i;
@@ -224,73 +266,99 @@ std::vector<std::vector<int>> groupSV(const std::vector<std::pair<int, PendingOp
         }
     }
     std::map<int, std::vector<int>> byRoot;
-    for (int i = 0; i < n; i++) byRoot[find(i)].push_back(i);
-    std::vector<std::vector<int>> items;
+    for (int i = 0; i < nu; i++) byRoot[find(i)].push_back(i);
+    struct Item {
+        std::vector<int> members;
+        int size;
+    };
+    std::vector<Item> items;
     for (auto& kv : byRoot) {
-        if (kv.second.size() <= 4) items.push_back(kv.second);
-        else for (int i : kv.second) items.push_back({i});
+        int size = 0;
+        for (int i : kv.second) size += units[i].k;
+        if (size <= 4) items.push_back({kv.second, size});
+        else for (int i : kv.second) items.push_back({{i}, units[i].k});
     }
     const int numFull = n / 4, rem = n % 4;
     std::vector<std::vector<int>> groups(numFull + (rem ? 1 : 0));
     std::vector<int> room(groups.size(), 4);
     if (rem) room.back() = rem;
-    auto holdsZero = [&](const std::vector<int>& it) {
-        for (int i : it)
-            if (todo[i].first == 0) return true;
-        return false;
-    };
-    std::stable_sort(items.begin(), items.end(), [](const std::vector<int>& x, const std::vector<int>& y) { return x.size() > y.size(); });
-    for (size_t k = 0; k < items.size(); k++)
-        if (rem && holdsZero(items[k]) && (int)items[k].size() <= rem) {
-            groups.back() = items[k];
-            room.back() -= (int)items[k].size();
+    std::stable_sort(items.begin(), items.end(), [](const Item& x, const Item& y) { return x.size > y.size; });
+    for (size_t k = 0; k < items.size(); k++) {
+        bool zero = false;
+        for (int i : items[k].members) zero = zero || holdsZero(i);
+        if (rem && zero && items[k].size <= rem) {
+            groups.back() = items[k].members;
+            room.back() -= items[k].size;
             items.erase(items.begin() + k);
             break;
         }
+    }
     for (auto& it : items) {
         size_t g = 0;
-        while (g < groups.size() && room[g] < (int)it.size()) g++;
+        while (g < groups.size() && room[g] < it.size) g++;
         if (g == groups.size()) return plain;
-        groups[g].insert(groups[g].end(), it.begin(), it.end());
-        room[g] -= (int)it.size();
+        groups[g].insert(groups[g].end(), it.members.begin(), it.members.end());
+        room[g] -= it.size;
     }
-    for (auto& g : groups) std::sort(g.begin(), g.end(), [&](int x, int y) { return todo[x].first < todo[y].first; });
     return groups;
 }
 
-// the pending unitaries of k statevector qubits as one 2^k x 2^k matrix (bit b of an index
-// = qubit b of the group), with the not yet applied phases that lie inside the group folded
-// in (a phase multiplies the rows whose bits of its mask are all set), applied in one pass
-bool applySVGroup(const Qureg& q, const std::vector<const std::pair<int, PendingOp>*>& g, const PhaseList& phases,
-                  std::vector<char>& applied, const char* func) {
-    const int k = (int)g.size(), D = 1 << k;
+// The matrix of a group of units (qubits ascending; bit b of an index = the group's b-th
+// qubit), with the not yet applied phases that lie inside the group folded in (a phase
+// multiplies the rows whose bits of its mask are all set).
+struct SVGroupOp {
+    int k;
+    int t[4];
+    std::vector<cd> m;
+};
+SVGroupOp svGroupOp(const std::vector<SVUnit>& units, const std::vector<int>& grp, const PhaseList& phases,
+                    std::vector<char>& applied) {
+    SVGroupOp g;
+    g.k = 0;
+    for (int i : grp)
+        for (int b = 0; b < units[i].k; b++) g.t[g.k++] = units[i].q[b];
+    std::sort(g.t, g.t + g.k);
+    int pos[64];
     long long groupMask = 0;
-    for (int b = 0; b < k; b++) groupMask |= 1LL << g[b]->first;
+    for (int b = 0; b < g.k; b++) {
+        pos[g.t[b]] = b;
+        groupMask |= 1LL << g.t[b];
+    }
+    const int D = 1 << g.k;
     std::vector<cd> rowFactor(D, cd(1));
-    bool folded = false;
     for (size_t p = 0; p < phases.size(); p++) {
         if (applied[p] || (phases[p].first & ~groupMask) != 0) continue;
         int local = 0;
-        for (int b = 0; b < k; b++)
-            if ((phases[p].first >> g[b]->first) & 1) local |= 1 << b;
+        for (int b = 0; b < g.k; b++)
+            if ((phases[p].first >> g.t[b]) & 1) local |= 1 << b;
         for (int j = 0; j < D; j++)
             if ((j & local) == local) rowFactor[j] *= phases[p].second;
         applied[p] = 1;
-        folded = true;
     }
-    if (k == 1 && !folded) return applyPendingOp(q, g[0]->first, g[0]->second, func);
-    std::vector<qcomp_t> M((size_t)D * D);
-    int t[4];
-    for (int b = 0; b < k; b++) t[b] = g[b]->first;
+    g.m.assign((size_t)D * D, cd(0));
     for (int j = 0; j < D; j++)
         for (int c = 0; c < D; c++) {
             cd v = rowFactor[j];
-            for (int b = 0; b < k; b++) v *= g[b]->second.m[((j >> b) & 1) * 2 + ((c >> b) & 1)];
-            M[(size_t)j * D + c] = qcomp_t{v.real(), v.imag()};
+            for (int i : grp) {
+                const SVUnit& u = units[i];
+                int jj = 0, cc = 0;
+                for (int b = 0; b < u.k; b++) {
+                    jj |= ((j >> pos[u.q[b]]) & 1) << b;
+                    cc |= ((c >> pos[u.q[b]]) & 1) << b;
+                }
+                v *= u.m[jj * (1 << u.k) + cc];
+            }
+            g.m[(size_t)j * D + c] = v;
         }
-    if (k == 1) return backend(qg_sv_anyCtrlOneTargDenseMatr(q.gpuAmps, q.numQubits, nullptr, nullptr, 0, t[0], M.data(), g_stream), func);
-    if (k == 2) return backend(qg_sv_anyCtrlTwoTargDenseMatr(q.gpuAmps, q.numQubits, nullptr, nullptr, 0, t[0], t[1], M.data(), g_stream), func);
-    return backend(qg_sv_anyCtrlAnyTargDenseMatr(q.gpuAmps, q.numQubits, nullptr, nullptr, 0, t, k, M.data(), 0, g_stream), func);
+    return g;
+}
+
+bool applySVGroupOp(const Qureg& q, const SVGroupOp& g, const char* func) {
+    std::vector<qcomp_t> M(g.m.size());
+    for (size_t i = 0; i < g.m.size(); i++) M[i] = qcomp_t{g.m[i].real(), g.m[i].imag()};
+    if (g.k == 1) return backend(qg_sv_anyCtrlOneTargDenseMatr(q.gpuAmps, q.numQubits, nullptr, nullptr, 0, g.t[0], M.data(), g_stream), func);
+    if (g.k == 2) return backend(qg_sv_anyCtrlTwoTargDenseMatr(q.gpuAmps, q.numQubits, nullptr, nullptr, 0, g.t[0], g.t[1], M.data(), g_stream), func);
+    return backend(qg_sv_anyCtrlAnyTargDenseMatr(q.gpuAmps, q.numQubits, nullptr, nullptr, 0, g.t, g.k, M.data(), 0, g_stream), func);
 }
 
 // applies a set of pending phases, 32 per pass
@@ -308,23 +376,52 @@ bool applyPhases(const Qureg& q, const PhaseList& ph, const char* func) {
     return true;
 }
 
-// applies a list of pending ops, then (statevectors) the pending phases that come after
-// them: density matrices in pairs when that pays (general superoperators first, a remaining
-// one with a channel), the rest one by one; statevectors in the groups of groupSV, with the
-// phases that fit in a group folded into its pass and the others applied together after
-bool applyPendingList(const Qureg& q, std::vector<std::pair<int, PendingOp>>& todo, const PhaseList& phases, const char* func) {
-    if (!q.isDensityMatrix) {
-        std::vector<char> applied(phases.size(), 0);
-        for (auto& grp : groupSV(todo, phases)) {
-            std::vector<const std::pair<int, PendingOp>*> g;
-            for (int i : grp) g.push_back(&todo[i]);
-            if (!applySVGroup(q, g, phases, applied, func)) return false;
-        }
-        PhaseList rest;
-        for (size_t p = 0; p < phases.size(); p++)
-            if (!applied[p]) rest.push_back(phases[p]);
-        return applyPhases(q, rest, func);
+// Applies a statevector's pending units in the groups of groupSV, with the phases that fit
+// in a group folded into its pass, then the other phases together.  With `keepLast`, a last
+// group of one or two qubits that no remaining phase touches is not applied but stays
+// pending (as the two-qubit block, or a one-qubit op): the next flush packs it with the
+// units that later phases join it to, which saves a pass per flush when the qubit count is
+// not a multiple of four (the gates of the next layer on its qubits join it meanwhile).
+bool applySVUnits(const Qureg& q, const std::vector<SVUnit>& units, const PhaseList& phases, bool keepLast, const char* func) {
+    std::vector<char> applied(phases.size(), 0);
+    std::vector<std::vector<int>> groups = groupSV(units, phases);
+    std::vector<SVGroupOp> ops;
+    for (auto& grp : groups) ops.push_back(svGroupOp(units, grp, phases, applied));
+    bool keep = keepLast && !ops.empty() && ops.back().k <= 2;
+    if (keep) {
+        long long lastMask = 0;
+        for (int b = 0; b < ops.back().k; b++) lastMask |= 1LL << ops.back().t[b];
+        for (size_t p = 0; p < phases.size(); p++) keep = keep && (applied[p] || (phases[p].first & lastMask) == 0);
     }
+    for (size_t i = 0; i + (keep ? 1 : 0) < ops.size(); i++)
+        if (!applySVGroupOp(q, ops[i], func)) return false;
+    if (keep) {
+        const SVGroupOp& g = ops.back();
+        std::lock_guard<std::mutex> lock(g_pendingMu);
+        PendingSet& set = g_pending[q.gpuAmps];
+        set.numQubits = q.numQubits;
+        set.dm = false;
+        if (g.k == 2) {
+            set.blockQ[0] = g.t[0];
+            set.blockQ[1] = g.t[1];
+            for (int i = 0; i < 16; i++) set.block[i] = g.m[i];
+        } else {
+            PendingOp op;
+            op.kind = PEND_SV;
+            op.p[0] = op.p[1] = op.p[2] = 0;
+            for (int i = 0; i < 16; i++) op.m[i] = i < 4 ? g.m[i] : cd(0);
+            set.ops[g.t[0]] = op;
+        }
+    }
+    PhaseList rest;
+    for (size_t p = 0; p < phases.size(); p++)
+        if (!applied[p]) rest.push_back(phases[p]);
+    return applyPhases(q, rest, func);
+}
+
+// applies a density matrix's pending ops: in pairs when that pays (general superoperators
+// first, a remaining one with a channel), the rest one by one
+bool applyPendingList(const Qureg& q, std::vector<std::pair<int, PendingOp>>& todo, const char* func) {
     if (todo.size() >= 2 && pairSuperops(q)) {
         std::stable_partition(todo.begin(), todo.end(), [](const std::pair<int, PendingOp>& x) { return x.second.kind == PEND_GENERAL; });
         size_t i = 0;
@@ -345,34 +442,59 @@ bool applyPendingList(const Qureg& q, std::vector<std::pair<int, PendingOp>>& to
 
 // applies the pending ops of the listed ket qubits (all of them when `qubits` is null); when
 // a statevector's pending phase involves a listed qubit, everything pending is applied
-// (the phases come after the pending ops of their qubits)
-bool flushPending(const Qureg& q, const std::vector<int>* qubits, const char* func) {
+// (the phases come after the pending ops of their qubits); `keepLast` as in applySVUnits
+bool flushPending(const Qureg& q, const std::vector<int>* qubits, const char* func, bool keepLast = false) {
     std::vector<std::pair<int, PendingOp>> todo;
     PhaseList phases;
+    std::vector<SVUnit> units;
+    bool dm = true;
     {
         std::lock_guard<std::mutex> lock(g_pendingMu);
         auto it = g_pending.find(q.gpuAmps);
         if (it == g_pending.end()) return true;
+        PendingSet& set = it->second;
+        dm = set.dm;
         long long touched = 0;
         if (qubits)
             for (int b : *qubits) touched |= 1LL << b;
         bool all = !qubits;
-        for (auto& ph : it->second.phases) all = all || (ph.first & touched) != 0;
+        for (auto& ph : set.phases) all = all || (ph.first & touched) != 0;
+        bool takeBlock = set.blockQ[0] >= 0 && (all || ((touched >> set.blockQ[0]) & 1) || ((touched >> set.blockQ[1]) & 1));
         if (all) {
-            phases.swap(it->second.phases);
-            for (auto& kv : it->second.ops) todo.push_back(kv);
-            it->second.ops.clear();
+            phases.swap(set.phases);
+            for (auto& kv : set.ops) todo.push_back(kv);
+            set.ops.clear();
         } else {
             for (int b : *qubits) {
-                auto jt = it->second.ops.find(b);
-                if (jt == it->second.ops.end()) continue;
+                auto jt = set.ops.find(b);
+                if (jt == set.ops.end()) continue;
                 todo.push_back(*jt);
-                it->second.ops.erase(jt);
+                set.ops.erase(jt);
             }
         }
-        if (it->second.ops.empty() && it->second.phases.empty()) g_pending.erase(it);
+        if (!dm) {
+            for (auto& kv : todo) {
+                SVUnit u;
+                u.k = 1;
+                u.q[0] = kv.first;
+                u.q[1] = -1;
+                for (int i = 0; i < 16; i++) u.m[i] = kv.second.m[i];
+                units.push_back(u);
+            }
+            if (takeBlock) {
+                SVUnit u;
+                u.k = 2;
+                u.q[0] = set.blockQ[0];
+                u.q[1] = set.blockQ[1];
+                for (int i = 0; i < 16; i++) u.m[i] = set.block[i];
+                units.push_back(u);
+                set.blockQ[0] = set.blockQ[1] = -1;
+            }
+        }
+        if (set.ops.empty() && set.phases.empty() && set.blockQ[0] < 0) g_pending.erase(it);
     }
-    return applyPendingList(q, todo, phases, func);
+    if (dm) return applyPendingList(q, todo, func);
+    return applySVUnits(q, units, phases, keepLast, func);
 }
 
 // a pending phase on a statevector involves this qubit
@@ -526,10 +648,11 @@ void applyDense(const Qureg& q, const int* ctrls, const int* states, int nc, con
     }
     if (defer) {
         if (nt == 1 && nc == 0) {
-            // pending phases on this qubit come first
+            // pending phases on this qubit come first (a last group of one or two qubits may
+            // stay pending: the gate then joins it)
             if (phasePendingOn(q, t[0])) {
                 const vector<int> one = {t[0]};
-                if (!flushPending(q, &one, func)) return;
+                if (!flushPending(q, &one, func, true)) return;
             }
             const cd U[4] = {C(m[0]), C(m[1]), C(m[2]), C(m[3])};
             addPendingSV(q, t[0], U);
