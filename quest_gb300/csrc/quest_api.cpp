@@ -215,9 +215,9 @@ struct SVUnit {
 // the units joined by such phases (clusters of at most four qubits) are packed into the
 // groups first-fit, largest first, into as many groups as the plain split needs (n/4 groups
 // of four qubits and one of n % 4); the cluster holding qubit 0 goes to the smaller group
-// when it fits there, since a four-qubit pass without qubit 0 takes the faster (staged)
-// tensor-core form.  When the clusters do not pack into that many groups, the units are
-// packed in ascending order of their qubits, qubit 0 last.
+// when it fits there and the rest still packs, since a four-qubit pass without qubit 0 takes
+// the faster (staged) tensor-core form.  When the clusters do not pack into that many
+// groups, the units are packed in ascending order of their qubits, qubit 0 last.
 std::vector<std::vector<int>> groupSV(const std::vector<SVUnit>& units, const PhaseList& phases) {
     const int nu = (int)units.size();
     int n = 0;
@@ -279,28 +279,37 @@ std::vector<std::vector<int>> groupSV(const std::vector<SVUnit>& units, const Ph
         else for (int i : kv.second) items.push_back({{i}, units[i].k});
     }
     const int numFull = n / 4, rem = n % 4;
-    std::vector<std::vector<int>> groups(numFull + (rem ? 1 : 0));
-    std::vector<int> room(groups.size(), 4);
-    if (rem) room.back() = rem;
     std::stable_sort(items.begin(), items.end(), [](const Item& x, const Item& y) { return x.size > y.size; });
-    for (size_t k = 0; k < items.size(); k++) {
-        bool zero = false;
-        for (int i : items[k].members) zero = zero || holdsZero(i);
-        if (rem && zero && items[k].size <= rem) {
-            groups.back() = items[k].members;
-            room.back() -= items[k].size;
-            items.erase(items.begin() + k);
-            break;
+    // first-fit, largest first; with `zeroLast`, the item holding qubit 0 goes first to the
+    // smaller group
+    auto pack = [&](bool zeroLast, std::vector<std::vector<int>>& groups) {
+        groups.assign(numFull + (rem ? 1 : 0), std::vector<int>());
+        std::vector<int> room(groups.size(), 4);
+        if (rem) room.back() = rem;
+        std::vector<char> placed(items.size(), 0);
+        for (size_t k = 0; zeroLast && k < items.size(); k++) {
+            bool zero = false;
+            for (int i : items[k].members) zero = zero || holdsZero(i);
+            if (rem && zero && items[k].size <= rem) {
+                groups.back() = items[k].members;
+                room.back() -= items[k].size;
+                placed[k] = 1;
+                break;
+            }
         }
-    }
-    for (auto& it : items) {
-        size_t g = 0;
-        while (g < groups.size() && room[g] < it.size) g++;
-        if (g == groups.size()) return plain;
-        groups[g].insert(groups[g].end(), it.members.begin(), it.members.end());
-        room[g] -= it.size;
-    }
-    return groups;
+        for (size_t k = 0; k < items.size(); k++) {
+            if (placed[k]) continue;
+            size_t g = 0;
+            while (g < groups.size() && room[g] < items[k].size) g++;
+            if (g == groups.size()) return false;
+            groups[g].insert(groups[g].end(), items[k].members.begin(), items[k].members.end());
+            room[g] -= items[k].size;
+        }
+        return true;
+    };
+    std::vector<std::vector<int>> groups;
+    if (pack(true, groups) || pack(false, groups)) return groups;
+    return plain;
 }
 
 // The matrix of a group of units (qubits ascending; bit b of an index = the group's b-th

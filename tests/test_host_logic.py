@@ -60,3 +60,29 @@ def test_api_without_env_reports_error(api):
         pytest.skip("environment already initialised in this process")
     with pytest.raises(api.QuESTError):
         api.Q.createQureg(3)
+
+
+def test_deferred_statevector_gates_on_the_host(built_lib, tmp_path):
+    """The API's deferral of one-qubit gates and controlled phases on statevectors
+    (tests/deferral_check.cpp): the API source compiled against CPU stand-ins of the pass
+    kernels, random layered circuits through the public calls equal the gate-by-gate product,
+    and benchmark-shaped layers take the expected number of passes and no phase pass."""
+    import os
+    import shutil
+    import subprocess
+    from quest_gb300 import build
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("g++ not available")
+    here = os.path.dirname(os.path.abspath(__file__))
+    root = os.path.dirname(here)
+    libdir = os.path.dirname(built_lib)
+    cuda = build._cuda_home()
+    exe = str(tmp_path / "deferral_check")
+    subprocess.run([gxx, "-O2", "-std=c++17", "-I", os.path.join(root, "include"), "-I", os.path.join(root, "quest_gb300", "csrc"),
+                    "-I", os.path.join(cuda, "include"), os.path.join(here, "deferral_check.cpp"), "-o", exe,
+                    "-L", libdir, "-lquest_gb300", "-L", os.path.join(cuda, "lib64"), "-lcudart",
+                    "-Wl,-rpath," + libdir], check=True)
+    out = subprocess.run([exe], capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stdout[-3000:]
+    assert out.stdout.strip().splitlines()[-1].startswith("OK")
