@@ -40,7 +40,6 @@
 #include <vector>
 
 #define DT_WAIT_NS 2000000000ull   // a tile takes microseconds; 2 s means it never completes
-#define DT_STAGE_MIN_BIT 1         // staged inputs when the lowest target or control is at least this qubit
 #define DT_SKIP INT_MIN            // epilogue: nothing to store for this group (else the scale << 20)
 
 // KR reals per group; STG: the producers' inputs pass through a shared-memory stage
@@ -222,9 +221,8 @@ __global__ void __launch_bounds__(DtShape<KR, STG>::THREADS, 1) k_dense_tc(const
         // tiles ahead; each thread reads back only what it copied, so one wait_group per
         // tile orders them (one commit per tile, empty past the last).  Otherwise the loads of
         // tile i + 1 go into the registers of a k-core of tile i as soon as its digits are
-        // formed.  (Staging gains where consecutive groups are adjacent amplitudes; with qubit
-        // 0 among the targets or controls, a thread's own loads share sectors, which the
-        // register loads take from L1 and the L2-only copies do not.)
+        // formed.  (Staging gains where a warp's loads cover consecutive amplitudes and
+        // qubit 0 is neither a target nor a control.)
         auto issue = [&](qidx i) {
             if (i < nLocal && (first + i * step) * 128 + row < args.numIts) {
                 const double2* src = args.amps + (tile_base(i) + rowOff);
@@ -459,6 +457,32 @@ int qg_dense_tc_launch(double2* amps, qidx numIts, const Ins& ins, qidx mask, co
     constexpr int KR = 2 << K, D = 1 << K;
     using S = DtShape<KR, false>;
     *used = false;
+    // A target on qubit 0 becomes the matrix's top index bit (the operator and the offsets
+    // permuted to match): the two threads of a group then hold its halves with qubit 0 clear
+    // and set, so lanes l and l + 16 read adjacent amplitudes (4-8 % faster than qubit 0 as the
+    // lowest index bit for targets 0..3 and 0, 3, 4, 17 at 28 qubits; within 2 % elsewhere).
+    int zb = -1;
+    for (int b = 0; b < K; b++)
+        if (off[1 << b] == 1) zb = b;
+    std::vector<double2> mp(m, m + D * D);
+    std::vector<qidx> op(off, off + D);
+    if (zb >= 0 && zb != K - 1) {
+        int oldBit[K], k2 = 0;
+        for (int b = 0; b < K; b++)
+            if (b != zb) oldBit[k2++] = b;
+        oldBit[K - 1] = zb;
+        auto oldIndex = [&](int jn) {
+            int jo = 0;
+            for (int b = 0; b < K; b++) jo |= ((jn >> b) & 1) << oldBit[b];
+            return jo;
+        };
+        for (int jn = 0; jn < D; jn++) {
+            op[jn] = off[oldIndex(jn)];
+            for (int cn = 0; cn < D; cn++) mp[jn * D + cn] = m[oldIndex(jn) * D + oldIndex(cn)];
+        }
+        m = mp.data();
+        off = op.data();
+    }
     std::vector<double> u(2 * D * D), R(KR * KR);
     for (int i = 0; i < D * D; i++) { u[2 * i] = m[i].x; u[2 * i + 1] = m[i].y; }
     qgfx::real_form(u.data(), D, R.data());
@@ -486,8 +510,6 @@ int qg_dense_tc_launch(double2* amps, qidx numIts, const Ins& ins, qidx mask, co
                 bt[dt_core_offset(j * KR + n, k, S::B_ROWS) / 2] = qgsl::digit_half(dig[(j * KR + n) * KR + k]);
     std::memcpy(a->bops, bt.data(), S::B_BYTES);
     const unsigned grid = (unsigned)std::min<qidx>(a->numTiles, (qidx)qg_num_sms());
-    // staged inputs for four targets when qubits 0..DT_STAGE_MIN_BIT-1 are neither targets
-    // nor controls (ins.low[0] = 2^p - 1 for the lowest of them, p)
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     {
         std::lock_guard<std::mutex> lock(g_timeMu);
@@ -500,7 +522,10 @@ int qg_dense_tc_launch(double2* amps, qidx numIts, const Ins& ins, qidx mask, co
     }
     bool staged = false;
     if constexpr (KR == 32) {
-        staged = ins.num == 0 || ins.low[0] >= ((qidx)1 << DT_STAGE_MIN_BIT) - 1;
+        // qubit 0 neither a target nor a control: with a control there, a warp's loads take
+        // every other amplitude; with a target there (the top index bit), the staged form
+        // measured 2-4 % slower than the register form on most placements at 28 qubits
+        staged = ins.num == 0 || ins.low[0] != 0;
         if (staged) {
             QG_TRY((dt_set_attr<KR, true>()));
             k_dense_tc<KR, true><<<grid, DtShape<KR, true>::THREADS, DtShape<KR, true>::SMEM, st>>>(*a);
