@@ -333,15 +333,6 @@ __global__ void __launch_bounds__(QFT_THREADS) k_phase_set(double2* __restrict__
     }
 }
 
-// The closing swaps of a QFT on qubits 0..n-1 (n >= 10) as one in-place permutation: index
-// bits [0, n) reversed.  The index splits into o (bits above n), h (bits n-5..n-1), m (the
-// n - 10 middle bits) and l (bits 0..4); (o, h, m, l) goes to (o, rev5 l, rev m, rev5 h).  So
-// the 32 x 32 tile of (o, m) goes, transposed and with both 5-bit fields reversed, to the
-// tile of (o, rev m): a block reads a tile and its partner (one tile when m = rev m) into
-// shared memory -- rows of 32 consecutive amplitudes, 512 bytes -- and then writes both,
-// again in rows of 512 bytes.  Every tile belongs to one block, so nothing else reads or
-// writes it meanwhile.  Rows padded to 33 amplitudes: a warp reading a column of the tile
-// takes the minimum of four shared-memory wavefronts.
 // the twiddle tables of a step with n low bits: table k, entry j = exp(i pi j 2^(8k) / 2^n)
 // at scale 2^62, table 0 with 1/sqrt2; returns the number of tables (at least one)
 static int qft_tables(int n, QftTables& T) {
@@ -357,9 +348,19 @@ static int qft_tables(int n, QftTables& T) {
     return numTables;
 }
 
+// The closing swaps of a QFT on qubits 0..n-1 (n >= 10) as one in-place permutation: index
+// bits [0, n) reversed.  The index splits into o (bits above n), h (bits n-5..n-1), m (the
+// n - 10 middle bits) and l (bits 0..4); (o, h, m, l) goes to (o, rev5 l, rev m, rev5 h).  So
+// the 32 x 32 tile of (o, m) goes, transposed and with both 5-bit fields reversed, to the
+// tile of (o, rev m): a block reads a tile and its partner (one tile when m = rev m) into
+// shared memory -- rows of 32 consecutive amplitudes, 512 bytes -- and then writes both,
+// again in rows of 512 bytes.  Every tile belongs to one block, so nothing else reads or
+// writes it meanwhile.  In shared memory, element (h, l) sits in column l ^ (rev5(h) & 7):
+// the eight lanes of a 16-byte access phase then hit eight distinct bank groups both when a
+// row is written (l = the lane) and when a column is read back (h = rev5 of the lane).
 #define REV_THREADS 256
-__global__ void __launch_bounds__(REV_THREADS) k_reverse_low_bits(double2* __restrict__ a, qidx numTiles, int n) {
-    __shared__ double2 s[2][32][33];
+__global__ void __launch_bounds__(REV_THREADS, 6) k_reverse_low_bits(double2* __restrict__ a, qidx numTiles, int n) {
+    __shared__ double2 s[2][32][32];
     const int midBits = n - 10;
     const int lane = threadIdx.x & 31, row0 = threadIdx.x >> 5;
     const int rl = (int)(__brev((unsigned)lane) >> 27);               // rev5(lane)
@@ -373,8 +374,9 @@ __global__ void __launch_bounds__(REV_THREADS) k_reverse_low_bits(double2* __res
 #pragma unroll
         for (int k = 0; k < 4; k++) {
             const int h = row0 + 8 * k;
-            s[0][h][lane] = ld_amp(a + baseM + h * rowStride + lane);
-            if (two) s[1][h][lane] = ld_amp(a + baseR + h * rowStride + lane);
+            const int col = lane ^ (int)((__brev((unsigned)h) >> 27) & 7);
+            s[0][h][col] = ld_amp(a + baseM + h * rowStride + lane);
+            if (two) s[1][h][col] = ld_amp(a + baseR + h * rowStride + lane);
         }
         __syncthreads();
         // destination row r (= rev5 of the source's l), column lane (= rev5 of its h)
@@ -382,8 +384,9 @@ __global__ void __launch_bounds__(REV_THREADS) k_reverse_low_bits(double2* __res
         for (int k = 0; k < 4; k++) {
             const int r = row0 + 8 * k;
             const int sl = (int)(__brev((unsigned)r) >> 27);
-            st_amp(a + baseR + r * rowStride + lane, s[0][rl][sl]);
-            if (two) st_amp(a + baseM + r * rowStride + lane, s[1][rl][sl]);
+            const int col = sl ^ (lane & 7);                             // rev5(rl) & 7 = lane & 7
+            st_amp(a + baseR + r * rowStride + lane, s[0][rl][col]);
+            if (two) st_amp(a + baseM + r * rowStride + lane, s[1][rl][col]);
         }
         __syncthreads();
     }
