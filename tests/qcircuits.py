@@ -350,3 +350,19 @@ def fullstate_diag_circuit(nq, is_dm, seed):
     L.append(f"FSD 1 1 {fmt(rng.uniform(0.5, 1.5))} {fmt(rng.uniform(-0.5, 0.5))} {mat_tokens(elems('general'))}")
     L.append("TOTALPROB")
     return "\n".join(L) + "\n"
+
+
+def benchmark_circuit_text(nq, depth, seed):
+    """The 30-qubit benchmark's circuit at nq qubits: per layer a Haar 2x2 on every qubit
+    and a controlled phase of random angle on 15 disjoint random pairs, then the QFT."""
+    rng = np.random.default_rng(seed)
+    L = []
+    for _ in range(depth):
+        for t in range(nq):
+            L.append(f"U1 {t} {mat_tokens(haar_unitary(2, rng))}")
+        perm = rng.permutation(nq)
+        for p in range(min(15, nq // 2)):
+            L.append(f"CPS {int(perm[2 * p])} {int(perm[2 * p + 1])} {fmt(rng.uniform(0, 2 * np.pi))}")
+    L.append("FQFT")
+    L.append("TOTALPROB")
+    return "\n".join(L) + "\n"
