@@ -115,6 +115,87 @@ __device__ __forceinline__ void qft_butterfly(const double2 v0, const double2 v1
     }
 }
 
+// The butterfly kept in fixed point, for a second step that follows in the same pass.
+// qft_fly_fx: a pair of doubles in, y = (o0.re, o0.im, o1.re, o1.im) out as integers at the
+// pair's scale, value = y 2^(eb - 1080) (|y| < 2^59); eb = 0 for an all-zero pair; false
+// when the pair needs FP64.  qft_fly_int: the same on integer inputs below 2^59 at one
+// scale, outputs at that scale divided by 4.
+__device__ __forceinline__ bool qft_fly_fx(const double2 v0, const double2 v1, long long wr, long long wi, long long (&y)[4],
+                                           int& eb) {
+    const uint64_t u[4] = {qgfx::f64_bits(v0.x), qgfx::f64_bits(v0.y), qgfx::f64_bits(v1.x), qgfx::f64_bits(v1.y)};
+    eb = 1;
+    uint64_t any = 0;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const int ei = (int)((u[k] >> 52) & 0x7FF);
+        eb = max(eb, ei + (ei == 0));
+        any |= u[k] << 1;
+    }
+    if (any == 0) {
+        eb = 0;
+        y[0] = y[1] = y[2] = y[3] = 0;
+        return true;
+    }
+    if (eb < 58 || eb > 2043) return false;
+    const long long x0r = qft_fixed(u[0], eb), x0i = qft_fixed(u[1], eb);
+    const long long x1r = qft_fixed(u[2], eb), x1i = qft_fixed(u[3], eb);
+    const long long sr = x0r + x1r, si = x0i + x1i, dr = x0r - x1r, di = x0i - x1i;
+    y[0] = mulhi(sr, QFT_C);
+    y[1] = mulhi(si, QFT_C);
+    y[2] = mulhi(dr, wr) - mulhi(di, wi);
+    y[3] = mulhi(dr, wi) + mulhi(di, wr);
+    return true;
+}
+__device__ __forceinline__ void qft_fly_int(long long x0r, long long x0i, long long x1r, long long x1i, long long wr, long long wi,
+                                            long long (&y)[4]) {
+    const long long sr = x0r + x1r, si = x0i + x1i, dr = x0r - x1r, di = x0i - x1i;
+    y[0] = mulhi(sr, QFT_C);
+    y[1] = mulhi(si, QFT_C);
+    y[2] = mulhi(dr, wr) - mulhi(di, wi);
+    y[3] = mulhi(dr, wi) + mulhi(di, wr);
+}
+__device__ __forceinline__ long long qft_align(long long y, int shift) { return shift >= 63 ? 0 : (y >> shift); }
+
+// the two steps in FP64 butterflies, for a quadruple with a pair that needs them (out of
+// line: it is rare, and inlined it took registers from the fixed-point path)
+__device__ __noinline__ void qft_two_flies_fp64(const double2 v00, const double2 v01, const double2 v10, const double2 v11,
+                                                long long wr, long long wi, long long vr, long long vi, double2& y00,
+                                                double2& y01, double2& y10, double2& y11) {
+    double2 x00, x01, x10, x11;
+    qft_butterfly(v00, v10, wr, wi, x00, x10);
+    qft_butterfly(v01, v11, -wi, wr, x01, x11);
+    qft_butterfly(x00, x01, vr, vi, y00, y01);
+    qft_butterfly(x10, x11, vr, vi, y10, y11);
+}
+
+// Two steps on one quadruple (v_xy: bit T = x, bit T - 1 = y): step T on the pairs
+// (v_0y, v_1y) with twiddles W and i W, then step T - 1 on (x_x0, x_x1) with twiddle V.
+// The values stay in fixed point between the steps: the second step takes the first's
+// integer outputs, aligned to the larger of the two pairs' scales (an arithmetic shift of
+// the smaller), so the quadruple is converted from and to double once.  A quadruple with a
+// pair that needs FP64 takes four FP64 butterflies.
+__device__ __forceinline__ void qft_two_flies(const double2 v00, const double2 v01, const double2 v10, const double2 v11,
+                                              long long wr, long long wi, long long vr, long long vi, double2& y00,
+                                              double2& y01, double2& y10, double2& y11) {
+    long long ya[4], yb[4];
+    int ea, eb;
+    const bool okA = qft_fly_fx(v00, v10, wr, wi, ya, ea);
+    const bool okB = qft_fly_fx(v01, v11, -wi, wr, yb, eb);
+    if (okA && okB) {
+        const int e = max(ea, eb), sa = e - ea, sb = e - eb;
+        long long z0[4], z1[4];
+        qft_fly_int(qft_align(ya[0], sa), qft_align(ya[1], sa), qft_align(yb[0], sb), qft_align(yb[1], sb), vr, vi, z0);
+        qft_fly_int(qft_align(ya[2], sa), qft_align(ya[3], sa), qft_align(yb[2], sb), qft_align(yb[3], sb), vr, vi, z1);
+        const int t = e - 1078;      // value = z 2^(e - 1078)
+        y00 = make_double2(qft_double(z0[0], t), qft_double(z0[1], t));
+        y01 = make_double2(qft_double(z0[2], t), qft_double(z0[3], t));
+        y10 = make_double2(qft_double(z1[0], t), qft_double(z1[1], t));
+        y11 = make_double2(qft_double(z1[2], t), qft_double(z1[3], t));
+    } else {
+        qft_two_flies_fp64(v00, v01, v10, v11, wr, wi, vr, vi, y00, y01, y10, y11);
+    }
+}
+
 // NT tables (compile time, so that every loop over them unrolls)
 template <int NT>
 __global__ void __launch_bounds__(QFT_THREADS) k_qft_step(double2* __restrict__ a, qidx numPairs, int tb, int lb, qidx lmask,
@@ -187,14 +268,14 @@ __global__ void __launch_bounds__(QFT_THREADS) k_qft_step_chunks(double2* __rest
 //     step T:     pairs (a_0y, a_1y), twiddle w^(B + y 2^(T-1)) / sqrt2 = i^y W,  W = w^B / sqrt2
 //     step T - 1: pairs (x_x0, x_x1), twiddle exp(i pi B / 2^(T-1)) / sqrt2 = w^(2B) / sqrt2 = V
 // Both twiddles come from the tables of step T: W from the bytes of B and V from those of 2B.
-// Between the steps the values are rounded to double, as in two separate passes.
+// Between the steps the values stay in fixed point (qft_two_flies).
 //
 // T - 1 >= 8: a warp takes chunks of 256 consecutive quadruples (lane l, round r: B's low
 // byte b = 32 r + l).  B's higher bytes are fixed across the chunk, so W's product of the
 // higher tables (HW) is formed once per chunk, and V's as well: the bytes of 2B above the
 // lowest are those of 2 (B - b) with bit 8 set when b >= 128: two products (H0, H1).
 template <int NT>
-__global__ void __launch_bounds__(QFT_THREADS, 3) k_qft_two_steps_chunks(double2* __restrict__ a, qidx numChunks, int tb,
+__global__ void __launch_bounds__(QFT_THREADS, 2) k_qft_two_steps_chunks(double2* __restrict__ a, qidx numChunks, int tb,
                                                                       const __grid_constant__ QftTables T) {
     static_assert(NT >= 2, "T - 1 >= 8 needs two tables");
     __shared__ long long sT[NT][256][2];
@@ -227,11 +308,8 @@ __global__ void __launch_bounds__(QFT_THREADS, 3) k_qft_two_steps_chunks(double2
             cmul62(sT[0][b][0], sT[0][b][1], hwr, hwi, wr, wi);
             const bool hi = r >= 4;                             // b >= 128: bit 8 of 2B set
             cmul62(sT[0][(2 * b) & 255][0], sT[0][(2 * b) & 255][1], hi ? h1r : h0r, hi ? h1i : h0i, vr, vi);
-            double2 x00, x10, x01, x11, y00, y01, y10, y11;
-            qft_butterfly(v00, v10, wr, wi, x00, x10);
-            qft_butterfly(v01, v11, -wi, wr, x01, x11);         // i W
-            qft_butterfly(x00, x01, vr, vi, y00, y01);
-            qft_butterfly(x10, x11, vr, vi, y10, y11);
+            double2 y00, y01, y10, y11;
+            qft_two_flies(v00, v01, v10, v11, wr, wi, vr, vi, y00, y01, y10, y11);
             st_amp(a + i00, y00);
             st_amp(a + i00 + half, y01);
             st_amp(a + i00 + top, y10);
@@ -254,11 +332,8 @@ __global__ void __launch_bounds__(QFT_THREADS) k_qft_two_steps_small(double2* __
         const double2 v00 = ld_amp(a + i00), v01 = ld_amp(a + i00 + half);
         const double2 v10 = ld_amp(a + i00 + top), v11 = ld_amp(a + i00 + top + half);
         const long long wr = sT[b][0], wi = sT[b][1], vr = sT[2 * b][0], vi = sT[2 * b][1];
-        double2 x00, x10, x01, x11, y00, y01, y10, y11;
-        qft_butterfly(v00, v10, wr, wi, x00, x10);
-        qft_butterfly(v01, v11, -wi, wr, x01, x11);
-        qft_butterfly(x00, x01, vr, vi, y00, y01);
-        qft_butterfly(x10, x11, vr, vi, y10, y11);
+        double2 y00, y01, y10, y11;
+        qft_two_flies(v00, v01, v10, v11, wr, wi, vr, vi, y00, y01, y10, y11);
         st_amp(a + i00, y00);
         st_amp(a + i00 + half, y01);
         st_amp(a + i00 + top, y10);

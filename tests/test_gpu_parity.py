@@ -485,3 +485,54 @@ def test_qft_two_steps_match_single_steps(env):
     finally:
         for b in bufs:
             L.qg_free(b)
+
+
+@pytest.mark.parametrize("T", [11, 5])
+def test_qft_two_steps_special_values(env, T):
+    """Two QFT steps in one pass on a 12-qubit state holding zeros, denormals, values near
+    the top of the double range, Inf and NaN in some quadruples (the FP64 butterflies) next
+    to ordinary ones (fixed point): against two single-step passes, the same non-finite
+    outputs and every finite output within 1e-13 of its quadruple's largest input."""
+    import ctypes
+    from quest_gb300._lib import lib
+    L = lib()
+    nq = 12
+    rng = np.random.default_rng(T)
+    amps = (rng.standard_normal(1 << nq) + 1j * rng.standard_normal(1 << nq)) * 1e-2
+    idx = rng.choice(1 << nq, 40, replace=False)
+    specials = [0.0, 5e-324, 3e-310, 1.7e308, 1e300, np.inf, -np.inf, np.nan, 1e-300]
+    for k, i in enumerate(idx):
+        amps[i] = complex(specials[k % len(specials)], 0.0 if k % 2 else 1e-3)
+    amps[:64] = 0.0                                            # all-zero quadruples
+    nbytes = 16 << nq
+    bufs = [ctypes.c_void_p(), ctypes.c_void_p()]
+    for b in bufs:
+        assert L.qg_alloc(ctypes.byref(b), nbytes) == 0
+    try:
+        src = np.ascontiguousarray(amps)
+        for b in bufs:
+            assert L.qg_copy_h2d(b, src.ctypes.data_as(ctypes.c_void_p), nbytes, None) == 0
+        assert L.qg_sync() == 0
+        assert L.qg_sv_qftTwoSteps(bufs[0], nq, T, None) == 0
+        assert L.qg_sv_qftStep(bufs[1], nq, T, 0, T, None) == 0
+        assert L.qg_sv_qftStep(bufs[1], nq, T - 1, 0, T - 1, None) == 0
+        out = [np.empty(1 << nq, dtype=np.complex128) for _ in bufs]
+        for o, b in zip(out, bufs):
+            assert L.qg_copy_d2h(o.ctypes.data_as(ctypes.c_void_p), b, nbytes, None) == 0
+        assert L.qg_sync() == 0
+    finally:
+        for b in bufs:
+            L.qg_free(b)
+    fused, single = out
+    # largest input magnitude of each amplitude's quadruple (bits T and T - 1)
+    i = np.arange(1 << nq)
+    base = i & ~((1 << T) | (1 << (T - 1)))
+    mags = np.abs(np.nan_to_num(amps, nan=0.0, posinf=1.8e308, neginf=1.8e308))
+    qmax = np.zeros(1 << nq)
+    for off in (0, 1 << (T - 1), 1 << T, (1 << T) | (1 << (T - 1))):
+        qmax = np.maximum(qmax, mags[base | off])
+    for part in (np.real, np.imag):
+        a, b = part(fused), part(single)
+        assert np.array_equal(np.isfinite(a), np.isfinite(b))
+        fin = np.isfinite(a)
+        assert np.all(np.abs(a[fin] - b[fin]) <= 1e-13 * qmax[fin])
