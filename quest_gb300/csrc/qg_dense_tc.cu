@@ -536,8 +536,7 @@ int qg_dense_tc_launch(double2* amps, qidx numIts, const Ins& ins, qidx mask, co
         k_dense_tc<KR, false><<<grid, S::THREADS, S::SMEM, st>>>(*a);
     }
     if (ev1) QG_CUDA(cudaEventRecord(ev1, st));
-    qg_note_launch();
-    *used = true;
+    *used = true;      // the launch is counted by the caller (qg_sv_anyCtrlAnyTargDenseMatr), once per call
     return qg_check_launch("k_dense_tc");
 }
 
