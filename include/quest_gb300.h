@@ -192,6 +192,10 @@ int qg_sv_qftStep(void* amps, int numQubits, int target, int lowTarget, int numL
  * one pass over quadruples of amplitudes: 2 * target + 1 gates of
  * applyQuantumFourierTransform (operations.cpp:1934-1949).  1 <= target <= 40. */
 int qg_sv_qftTwoSteps(void* amps, int numQubits, int target, void* stream);
+/* The QFT steps of `target`, `target` - 1 and `target` - 2 on contiguous targets from qubit 0
+ * in one pass over octets of amplitudes (3 * target gates of applyQuantumFourierTransform).
+ * 2 <= target <= 8 or 10 <= target <= 40. */
+int qg_sv_qftThreeSteps(void* amps, int numQubits, int target, void* stream);
 /* The closing swaps of a quantum Fourier transform on the targets 0..numBits-1 (qubit j
  * with qubit numBits-1-j, j < numBits/2: applySwap in applyQuantumFourierTransform,
  * operations.cpp:1950-1952) as one in-place pass: every amplitude index has its low numBits

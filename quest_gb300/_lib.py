@@ -81,6 +81,7 @@ ABI = {
     "qg_sv_qftStep": [vp, I, I, I, I, vp],
     "qg_sv_reverseLowBits": [vp, I, I, vp],
     "qg_sv_qftTwoSteps": [vp, I, I, vp],
+    "qg_sv_qftThreeSteps": [vp, I, I, vp],
     "qg_sv_phaseSet": [vp, I, ctypes.POINTER(ctypes.c_int64), c_cplx_p, I, vp],
     "qg_sv_anyCtrlOneTargDiagMatr": [vp, I, c_int_p, c_int_p, I, I, c_cplx_p, vp],
     "qg_sv_anyCtrlTwoTargDiagMatr": [vp, I, c_int_p, c_int_p, I, I, I, c_cplx_p, vp],

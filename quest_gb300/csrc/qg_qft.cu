@@ -341,6 +341,168 @@ __global__ void __launch_bounds__(QFT_THREADS) k_qft_two_steps_small(double2* __
     }
 }
 
+// Three steps in one pass, targets from qubit 0: the steps of T, T - 1 and T - 2 on the
+// eight amplitudes a_pqr that differ in bits T (p), T - 1 (q) and T - 2 (r) only.  With B =
+// their index bits below T - 2 and w = exp(i pi / 2^T):
+//     step T:     pairs over p, twiddle w^(B + r 2^(T-2) + q 2^(T-1)) / sqrt2 = W omega^r i^q,
+//                 W = w^B / sqrt2, omega = exp(i pi / 4)
+//     step T - 1: pairs over q, twiddle exp(i pi (B + r 2^(T-2)) / 2^(T-1)) / sqrt2 = V i^r,
+//                 V = w^(2B) / sqrt2
+//     step T - 2: pairs over r, twiddle U = w^(4B) / sqrt2
+// All from the tables of step T.  The first step's four pairs are converted at their own
+// scales; their outputs are aligned to the largest and the next two steps run on integers
+// at that one scale (each halving it twice: the outputs are converted with 2^(e - 1076)).
+// An octet with a pair that needs FP64, or whose scale would leave no headroom for the
+// double conversion at the end, takes twelve FP64 butterflies.
+__device__ __noinline__ void qft_three_flies_fp64(double2* __restrict__ p, qidx quarter, long long w0r, long long w0i,
+                                                  long long w1r, long long w1i, long long vr, long long vi, long long ur,
+                                                  long long ui) {
+    double2 v[8], x[8];
+#pragma unroll
+    for (int o = 0; o < 8; o++) v[o] = ld_amp(p + o * quarter);
+#pragma unroll
+    for (int qr = 0; qr < 4; qr++) {        // step T: pairs (0qr, 1qr), twiddle W omega^r i^q
+        const int q = qr >> 1, r = qr & 1;
+        const long long wr = r ? w1r : w0r, wi = r ? w1i : w0i;
+        qft_butterfly(v[qr], v[4 + qr], q ? -wi : wr, q ? wr : wi, x[qr], x[4 + qr]);
+    }
+#pragma unroll
+    for (int pr = 0; pr < 4; pr++) {        // step T - 1: pairs (p0r, p1r), twiddle V i^r
+        const int pp = pr >> 1, r = pr & 1, o = 4 * pp + r;
+        qft_butterfly(x[o], x[o + 2], r ? -vi : vr, r ? vr : vi, v[o], v[o + 2]);
+    }
+#pragma unroll
+    for (int pq = 0; pq < 4; pq++) {        // step T - 2: pairs (pq0, pq1), twiddle U
+        qft_butterfly(v[2 * pq], v[2 * pq + 1], ur, ui, x[2 * pq], x[2 * pq + 1]);
+        st_amp(p + 2 * pq * quarter, x[2 * pq]);
+        st_amp(p + (2 * pq + 1) * quarter, x[2 * pq + 1]);
+    }
+}
+
+// The octet at p (amplitude o = 4p + 2q + r at p + o * quarter), its values already in v:
+// the three steps in fixed point, written back; with twiddles W, W omega, V, U.  An octet
+// that needs FP64 goes to qft_three_flies_fp64, which reads it again.
+__device__ __forceinline__ void qft_three_flies(double2* __restrict__ p, qidx quarter, const double2 (&v)[8], long long w0r,
+                                                long long w0i, long long w1r, long long w1i, long long vr, long long vi,
+                                                long long ur, long long ui) {
+    long long y[4][4];
+    int e[4];
+    bool ok = true;
+#pragma unroll
+    for (int qr = 0; qr < 4; qr++) {
+        const int q = qr >> 1, r = qr & 1;
+        const long long wr = r ? w1r : w0r, wi = r ? w1i : w0i;
+        ok = qft_fly_fx(v[qr], v[4 + qr], q ? -wi : wr, q ? wr : wi, y[qr], e[qr]) && ok;
+    }
+    const int em = max(max(e[0], e[1]), max(e[2], e[3]));
+    if (!ok || em > 2041) {
+        qft_three_flies_fp64(p, quarter, w0r, w0i, w1r, w1i, vr, vi, ur, ui);
+        return;
+    }
+    // z[4p + 2q + r] (re, im) at scale em
+    long long z[8][2];
+#pragma unroll
+    for (int qr = 0; qr < 4; qr++) {
+        const int sh = em - e[qr];
+        z[qr][0] = qft_align(y[qr][0], sh);
+        z[qr][1] = qft_align(y[qr][1], sh);
+        z[4 + qr][0] = qft_align(y[qr][2], sh);
+        z[4 + qr][1] = qft_align(y[qr][3], sh);
+    }
+#pragma unroll
+    for (int pr = 0; pr < 4; pr++) {        // step T - 1: pairs (p0r, p1r), twiddle V i^r
+        const int pp = pr >> 1, r = pr & 1, o = 4 * pp + r;
+        long long out[4];
+        qft_fly_int(z[o][0], z[o][1], z[o + 2][0], z[o + 2][1], r ? -vi : vr, r ? vr : vi, out);
+        z[o][0] = out[0];
+        z[o][1] = out[1];
+        z[o + 2][0] = out[2];
+        z[o + 2][1] = out[3];
+    }
+    const int t = em - 1076;
+#pragma unroll
+    for (int pq = 0; pq < 4; pq++) {        // step T - 2: pairs (pq0, pq1), twiddle U
+        long long out[4];
+        qft_fly_int(z[2 * pq][0], z[2 * pq][1], z[2 * pq + 1][0], z[2 * pq + 1][1], ur, ui, out);
+        st_amp(p + 2 * pq * quarter, make_double2(qft_double(out[0], t), qft_double(out[1], t)));
+        st_amp(p + (2 * pq + 1) * quarter, make_double2(qft_double(out[2], t), qft_double(out[3], t)));
+    }
+}
+
+// T - 2 >= 8: a warp takes chunks of 256 consecutive octets (B's low byte b = 32 r + lane);
+// the products of the higher tables are formed once per chunk, by seven lanes, into shared
+// memory: for W (the bytes of B), for V (those of 2B: bit 8 from b's bit 7, two variants) and
+// for U (those of 4B: bits 8-9 from b's bits 6-7, four variants).
+template <int NT>
+__global__ void __launch_bounds__(QFT_THREADS, 2) k_qft_three_steps_chunks(double2* __restrict__ a, qidx numChunks, int tb,
+                                                                        const __grid_constant__ QftTables T) {
+    static_assert(NT >= 2, "T - 2 >= 8 needs two tables");
+    __shared__ long long sT[NT][256][2];
+    __shared__ long long sH[QFT_THREADS / 32][8][2];        // per warp: HW, HV[2], HU[4] of its chunk
+    for (int e = threadIdx.x; e < NT * 512; e += QFT_THREADS) (&sT[0][0][0])[e] = (&T.t[0][0][0])[e];
+    __syncthreads();
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const qidx bMask = ((qidx)1 << (tb - 2)) - 1, quarter = (qidx)1 << (tb - 2);
+    const qidx warps = (qidx)gridDim.x * (QFT_THREADS / 32);
+    for (qidx c = blockIdx.x * (qidx)(QFT_THREADS / 32) + wid; c < numChunks; c += warps) {
+        // lane k < 7 forms product k: 0 for W (the bytes of B), 1-2 for V (those of 2B, bit 8
+        // = 0 or 1), 3-6 for U (those of 4B, bits 8-9 = 0..3); the low 8, 9 and 10 bits of B,
+        // 2B and 4B are clear here
+        if (lane < 7) {
+            const qidx Bh = (c << 8) & bMask;
+            const qidx X = lane == 0 ? Bh : lane < 3 ? Bh << 1 : Bh << 2;
+            const int low = lane == 0 ? 0 : lane < 3 ? lane - 1 : lane - 3;
+            const int j = (int)((X >> 8) & 255) | low;
+            long long hr = sT[1][j][0], hi = sT[1][j][1];
+#pragma unroll
+            for (int k = 2; k < NT; k++) {
+                const int jk = (int)((X >> (8 * k)) & 255);
+                cmul62(hr, hi, sT[k][jk][0], sT[k][jk][1], hr, hi);
+            }
+            sH[wid][lane][0] = hr;
+            sH[wid][lane][1] = hi;
+        }
+        __syncwarp();
+#pragma unroll 1
+        for (int r = 0; r < 8; r++) {
+            const int b = 32 * r + lane;                        // B & 255
+            const qidx oc = (c << 8) + b;
+            const qidx i0 = ((oc & ~bMask) << 3) | (oc & bMask);
+            double2 v[8];
+#pragma unroll
+            for (int o = 0; o < 8; o++) v[o] = ld_amp(a + i0 + o * quarter);
+            long long w0r, w0i, w1r, w1i, vr, vi, ur, ui;
+            const int hv = 1 + (r >> 2), hu = 3 + (r >> 1);    // b's bit 7; b's bits 6-7
+            cmul62(sT[0][b][0], sT[0][b][1], sH[wid][0][0], sH[wid][0][1], w0r, w0i);
+            cmul62(w0r, w0i, QFT_C, QFT_C, w1r, w1i);                                           // W omega
+            cmul62(sT[0][(2 * b) & 255][0], sT[0][(2 * b) & 255][1], sH[wid][hv][0], sH[wid][hv][1], vr, vi);
+            cmul62(sT[0][(4 * b) & 255][0], sT[0][(4 * b) & 255][1], sH[wid][hu][0], sH[wid][hu][1], ur, ui);
+            qft_three_flies(a + i0, quarter, v, w0r, w0i, w1r, w1i, vr, vi, ur, ui);
+        }
+        __syncwarp();                                           // sH is rewritten for the next chunk
+    }
+}
+
+// The same for 2 <= T <= 8: B < 64 and 4B < 256, one table (W = T0[B], V = T0[2B], U = T0[4B]).
+__global__ void __launch_bounds__(QFT_THREADS, 2) k_qft_three_steps_small(double2* __restrict__ a, qidx numOctets, int tb,
+                                                                       const __grid_constant__ QftTables T) {
+    __shared__ long long sT[256][2];
+    for (int e = threadIdx.x; e < 512; e += QFT_THREADS) (&sT[0][0])[e] = (&T.t[0][0][0])[e];
+    __syncthreads();
+    const qidx bMask = ((qidx)1 << (tb - 2)) - 1, quarter = (qidx)1 << (tb - 2);
+    const qidx stride = (qidx)gridDim.x * QFT_THREADS;
+    for (qidx oc = blockIdx.x * (qidx)QFT_THREADS + threadIdx.x; oc < numOctets; oc += stride) {
+        const int b = (int)(oc & bMask);
+        const qidx i0 = ((oc & ~bMask) << 3) | (qidx)b;
+        double2 v[8];
+#pragma unroll
+        for (int o = 0; o < 8; o++) v[o] = ld_amp(a + i0 + o * quarter);
+        long long w1r, w1i;
+        cmul62(sT[b][0], sT[b][1], QFT_C, QFT_C, w1r, w1i);
+        qft_three_flies(a + i0, quarter, v, sT[b][0], sT[b][1], w1r, w1i, sT[2 * b][0], sT[2 * b][1], sT[4 * b][0], sT[4 * b][1]);
+    }
+}
+
 struct PhaseSet {
     long long t[4][256][2];     // table g, entry j: product of the factors 8g + k with bit k of j set, x 2^62
     qidx mask[32];              // the qubits of factor i (all must be 1)
@@ -590,6 +752,35 @@ int qg_sv_qftTwoSteps(void* amps, int numQubits, int target, void* stream) {
     }
     qg_note_launch();
     return qg_check_launch("k_qft_two_steps_chunks");
+}
+
+// The QFT steps of `target`, `target` - 1 and `target` - 2 on the contiguous targets from
+// qubit 0 in one pass: 2 <= target <= 8 or 10 <= target <= 40.
+int qg_sv_qftThreeSteps(void* amps, int numQubits, int target, void* stream) {
+    QG_TRY(qg_check_amps(amps, numQubits));
+    if (target < 2 || target >= numQubits || target == 9 || target > 8 * QFT_MAX_TABLES)
+        return qg_fail(QG_ERR_ARG, "qftThreeSteps: target %d of %d qubits (2..8 or 10..40)", target, numQubits);
+    QftTables T;
+    const int numTables = qft_tables(target, T);
+    const qidx numOctets = (qidx)1 << (numQubits - 3);
+    double2* A = (double2*)amps;
+    cudaStream_t st = qg_stream(stream);
+    if (target <= 8) {
+        const unsigned grid = (unsigned)std::min<qidx>((numOctets + QFT_THREADS - 1) / QFT_THREADS, (qidx)qg_num_sms() * 8);
+        k_qft_three_steps_small<<<grid, QFT_THREADS, 0, st>>>(A, numOctets, target, T);
+        qg_note_launch();
+        return qg_check_launch("k_qft_three_steps_small");
+    }
+    const qidx numChunks = numOctets >> 8;
+    const unsigned grid = (unsigned)std::min<qidx>((numChunks + QFT_THREADS / 32 - 1) / (QFT_THREADS / 32), (qidx)qg_num_sms() * 8);
+    switch (numTables) {
+        case 2: k_qft_three_steps_chunks<2><<<grid, QFT_THREADS, 0, st>>>(A, numChunks, target, T); break;
+        case 3: k_qft_three_steps_chunks<3><<<grid, QFT_THREADS, 0, st>>>(A, numChunks, target, T); break;
+        case 4: k_qft_three_steps_chunks<4><<<grid, QFT_THREADS, 0, st>>>(A, numChunks, target, T); break;
+        default: k_qft_three_steps_chunks<5><<<grid, QFT_THREADS, 0, st>>>(A, numChunks, target, T); break;
+    }
+    qg_note_launch();
+    return qg_check_launch("k_qft_three_steps_chunks");
 }
 
 }  // extern "C"

@@ -1368,8 +1368,14 @@ void applyQuantumFourierTransform(Qureg q, int* t, int nt) {
     for (int j = 1; j < nt; j++) contiguous = contiguous && t[j] == t[0] + j;
     if (!q.isDensityMatrix && contiguous && qg_fp64_products_mode() == 0) {
         // each step (Hadamard on t[n], then its n controlled phases) as one pass, or for
-        // targets from qubit 0 two steps per pass; their closing swaps as one permutation pass
+        // targets from qubit 0 three steps per pass (two where three do not fit: the pass
+        // of three takes targets 2..8 and 10..40); their closing swaps as one permutation
         for (int n = nt - 1; n >= 0; n--) {
+            if (t[0] == 0 && n >= 2 && n != 9) {
+                if (!backend(qg_sv_qftThreeSteps(q.gpuAmps, q.numQubits, t[n], g_stream), func)) return;
+                n -= 2;
+                continue;
+            }
             if (t[0] == 0 && n >= 1) {
                 if (!backend(qg_sv_qftTwoSteps(q.gpuAmps, q.numQubits, t[n], g_stream), func)) return;
                 n--;

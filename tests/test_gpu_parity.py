@@ -536,3 +536,86 @@ def test_qft_two_steps_special_values(env, T):
         assert np.array_equal(np.isfinite(a), np.isfinite(b))
         fin = np.isfinite(a)
         assert np.all(np.abs(a[fin] - b[fin]) <= 1e-13 * qmax[fin])
+
+
+def test_qft_three_steps_match_single_steps(env):
+    """Three QFT steps in one pass (targets T, T - 1, T - 2 from qubit 0) against three
+    single-step passes, on a 26-qubit state, for T from 25 (four twiddle tables) down to 2:
+    the same values to 1e-14 of the largest amplitude."""
+    import ctypes
+    from quest_gb300._lib import lib
+    L = lib()
+    nq = 26
+    nbytes = 16 << nq
+    bufs = [ctypes.c_void_p(), ctypes.c_void_p()]
+    for b in bufs:
+        assert L.qg_alloc(ctypes.byref(b), nbytes) == 0
+    try:
+        for T in (25, 24, 18, 17, 10, 8, 5, 2):
+            for b in bufs:
+                assert L.qg_sv_initDebugState(b, nq, None) == 0
+            assert L.qg_sv_qftThreeSteps(bufs[0], nq, T, None) == 0
+            for k in range(3):
+                assert L.qg_sv_qftStep(bufs[1], nq, T - k, 0, T - k, None) == 0
+            out = [np.empty(1 << nq, dtype=np.complex128) for _ in bufs]
+            for o, b in zip(out, bufs):
+                assert L.qg_copy_d2h(o.ctypes.data_as(ctypes.c_void_p), b, nbytes, None) == 0
+            assert L.qg_sync() == 0
+            scale = np.max(np.abs(out[1]))
+            assert np.max(np.abs(out[0] - out[1])) <= 1e-14 * scale, T
+        assert L.qg_sv_qftThreeSteps(bufs[0], nq, 9, None) != 0       # 9: not a pass of three
+    finally:
+        for b in bufs:
+            L.qg_free(b)
+
+
+@pytest.mark.parametrize("T", [12, 6])
+def test_qft_three_steps_special_values(env, T):
+    """Three QFT steps in one pass on a 13-qubit state holding zeros, denormals, values near
+    the top of the double range, Inf and NaN beside ordinary octets: against three
+    single-step passes, non-finite outputs in the same places and every finite output
+    within 1e-13 of its octet's largest input."""
+    import ctypes
+    from quest_gb300._lib import lib
+    L = lib()
+    nq = 13
+    rng = np.random.default_rng(T + 50)
+    amps = (rng.standard_normal(1 << nq) + 1j * rng.standard_normal(1 << nq)) * 1e-2
+    idx = rng.choice(1 << nq, 60, replace=False)
+    specials = [0.0, 5e-324, 3e-310, 1.7e308, 1e300, np.inf, -np.inf, np.nan, 1e-300]
+    for k, i in enumerate(idx):
+        amps[i] = complex(specials[k % len(specials)], 0.0 if k % 2 else 1e-3)
+    amps[:64] = 0.0
+    nbytes = 16 << nq
+    bufs = [ctypes.c_void_p(), ctypes.c_void_p()]
+    for b in bufs:
+        assert L.qg_alloc(ctypes.byref(b), nbytes) == 0
+    try:
+        src = np.ascontiguousarray(amps)
+        for b in bufs:
+            assert L.qg_copy_h2d(b, src.ctypes.data_as(ctypes.c_void_p), nbytes, None) == 0
+        assert L.qg_sync() == 0
+        assert L.qg_sv_qftThreeSteps(bufs[0], nq, T, None) == 0
+        for k in range(3):
+            assert L.qg_sv_qftStep(bufs[1], nq, T - k, 0, T - k, None) == 0
+        out = [np.empty(1 << nq, dtype=np.complex128) for _ in bufs]
+        for o, b in zip(out, bufs):
+            assert L.qg_copy_d2h(o.ctypes.data_as(ctypes.c_void_p), b, nbytes, None) == 0
+        assert L.qg_sync() == 0
+    finally:
+        for b in bufs:
+            L.qg_free(b)
+    fused, single = out
+    i = np.arange(1 << nq)
+    m3 = (1 << T) | (1 << (T - 1)) | (1 << (T - 2))
+    base = i & ~m3
+    mags = np.abs(np.nan_to_num(amps, nan=0.0, posinf=1.8e308, neginf=1.8e308))
+    omax = np.zeros(1 << nq)
+    for o in range(8):
+        off = ((o >> 2) & 1) << T | ((o >> 1) & 1) << (T - 1) | (o & 1) << (T - 2)
+        omax = np.maximum(omax, mags[base | off])
+    for part in (np.real, np.imag):
+        a, b = part(fused), part(single)
+        assert np.array_equal(np.isfinite(a), np.isfinite(b))
+        fin = np.isfinite(a)
+        assert np.all(np.abs(a[fin] - b[fin]) <= 1e-13 * omax[fin])
