@@ -154,6 +154,40 @@ void kronPair(const cd (&Sa)[16], const cd (&Sb)[16], cd (&M)[256]) {
         }
 }
 
+// A two-qubit superoperator M (16x16 on (a, b, a + N, b + N)) applied after the pending
+// one-qubit superoperators of ket qubits a and b: those are taken out of the pending set
+// and multiplied in (M <- M (Sa (x) Sb), a missing one the identity), so that the qubits'
+// pending work costs no pass of its own.  Other pending qubits commute with M.
+void composePendingPair(const Qureg& q, int a, int b, cd (&M)[256]) {
+    cd S[2][16];
+    bool any = false;
+    {
+        std::lock_guard<std::mutex> lock(g_pendingMu);
+        auto it = g_pending.find(q.gpuAmps);
+        for (int i = 0; i < 2; i++) {
+            for (int e = 0; e < 16; e++) S[i][e] = (e % 5 == 0) ? cd(1) : cd(0);
+            if (it == g_pending.end()) continue;
+            auto jt = it->second.ops.find(i == 0 ? a : b);
+            if (jt == it->second.ops.end()) continue;
+            for (int e = 0; e < 16; e++) S[i][e] = jt->second.m[e];
+            it->second.ops.erase(jt);
+            any = true;
+        }
+        if (it != g_pending.end() && it->second.ops.empty() && it->second.phases.empty() && it->second.blockQ[0] < 0)
+            g_pending.erase(it);
+    }
+    if (!any) return;
+    cd P[256], R[256];
+    kronPair(S[0], S[1], P);
+    for (int j = 0; j < 16; j++)
+        for (int k = 0; k < 16; k++) {
+            cd acc = 0;
+            for (int m = 0; m < 16; m++) acc += M[j * 16 + m] * P[m * 16 + k];
+            R[j * 16 + k] = acc;
+        }
+    for (int i = 0; i < 256; i++) M[i] = R[i];
+}
+
 // Statevectors: one-qubit dense unitaries are deferred the same way (a pending 2x2 per
 // qubit, composed on the host) when the tensor-core kernel runs for four targets, and the
 // pending qubits are applied four at a time as the Kronecker product of their unitaries
@@ -672,19 +706,21 @@ void applyDense(const Qureg& q, const int* ctrls, const int* states, int nc, con
         if (!flushPending(q, &touched, func)) return;
     }
     if (q.isDensityMatrix) {
-        vector<int> touched = c;
-        touched.insert(touched.end(), t.begin(), t.end());
-        if (!flushPending(q, &touched, func)) return;
         if (nt == 2 && nc == 0 && pairSuperops(q)) {
             // U rho U^dagger in one pass: conj(U) (x) U on (t0, t1, t0 + N, t1 + N), the
-            // reference's two passes (ket, then conjugated bra) as one superoperator
+            // reference's two passes (ket, then conjugated bra) as one superoperator, with
+            // the pending superoperators of t0 and t1 multiplied in
             cd M[256];
             for (int j = 0; j < 16; j++)
                 for (int k = 0; k < 16; k++)
                     M[j * 16 + k] = C(m[(j & 3) * 4 + (k & 3)]) * std::conj(C(m[(j >> 2) * 4 + (k >> 2)]));
+            composePendingPair(q, t[0], t[1], M);
             applyPairOp(q, t[0], t[1], M, func);
             return;
         }
+        vector<int> touched = c;
+        touched.insert(touched.end(), t.begin(), t.end());
+        if (!flushPending(q, &touched, func)) return;
     }
     if (!denseSV(q, c, s, t, m, false, func)) return;
     if (!q.isDensityMatrix) return;
@@ -1584,6 +1620,14 @@ void mixKrausMap(Qureg q, int* qubits, int n, KrausMap map) {
         cd S[16];
         for (int i = 0; i < 16; i++) S[i] = C(map.superop.cpuElemsFlat[i]);
         addPending(q, qubits[0], S, PEND_GENERAL);
+        return;
+    }
+    if (n == 2 && pairSuperops(q)) {
+        // the superoperator with the pending superoperators of its two qubits multiplied in
+        cd M[256];
+        for (int i = 0; i < 256; i++) M[i] = C(map.superop.cpuElemsFlat[i]);
+        composePendingPair(q, qubits[0], qubits[1], M);
+        applyPairOp(q, qubits[0], qubits[1], M, func);
         return;
     }
     vector<int> touched(qubits, qubits + n);

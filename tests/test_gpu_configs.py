@@ -176,13 +176,15 @@ def test_pauli_str_sum_validation(env):
         Q.destroyQureg(q)
 
 
-@pytest.mark.parametrize("nq,seed", [(3, 1), (6, 2), (9, 3)])
-def test_deferred_density_matrix_superoperators(env, nq, seed):
+@pytest.mark.parametrize("nq,seed,slices", [(3, 1, 1), (6, 2, 1), (9, 3, 1), (3, 4, 2), (6, 5, 2), (9, 6, 2)])
+def test_deferred_density_matrix_superoperators(env, nq, seed, slices):
     """One-qubit unitaries and channels on a density matrix are multiplied into one
     pending superoperator per qubit and applied when something needs the state; random
     interleavings with two-qubit operations (which apply only the qubits they touch),
     controlled gates, rotations and reductions in between, against the oracle applying
-    every operation at once."""
+    every operation at once.  With the tensor-core kernel forced (slices = 2) the pending
+    qubits pair up, and a two-qubit unitary or Kraus map takes its qubits' pending
+    superoperators into its own pass."""
     rng = np.random.default_rng(900 + seed)
     L = []
     for step in range(60):
@@ -223,7 +225,15 @@ def test_deferred_density_matrix_superoperators(env, nq, seed):
     text = "\n".join(L) + "\n"
     amps = qc.random_density_matrix(nq, 950 + seed)
     a1, r1, _ = qc.oracle().run(text, nq, 1, amps)
-    a2, r2, _ = run_gpu(env, text, nq, 1, amps)
+    from quest_gb300 import _lib
+    L = _lib.lib()
+    before = ctypes.c_int(1)
+    _lib.check(L.qg_get_tensor_slices(ctypes.byref(before)))
+    _lib.check(L.qg_set_tensor_slices(slices))
+    try:
+        a2, r2, _ = run_gpu(env, text, nq, 1, amps)
+    finally:
+        _lib.check(L.qg_set_tensor_slices(before.value))
     assert np.max(np.abs(a1 - a2)) <= TOL
     assert np.max(np.abs(r1 - r2)) <= TOL
 
