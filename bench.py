@@ -894,7 +894,7 @@ def run_gates(args, world, rank, local, dist):
     """Per-gate-kind timing on one FP64 register: 1- to 4-target dense unitaries, a
     controlled phase and a swap, in both product modes (fixed point, FP64 FMAs), after
     the launch-shape autotuner, and the API's fused passes (a set of controlled phases,
-    one and two QFT steps, the QFT's closing swaps); then density-matrix channels on a
+    one, two and three QFT steps, the QFT's closing swaps); then density-matrix channels on a
     register of half the qubits (the same bytes).  ms per call from CUDA events over
     `--steps` calls."""
     import ctypes as C
@@ -966,8 +966,8 @@ def run_gates(args, world, rank, local, dist):
     rows.append({"gate": "swap (half of the amplitudes)", "products": "none", "ms": round(ms, 4),
                  "gbs": round(2 * state_bytes / 2 / ms / 1e6, 1)})
     # the fused passes of the API (fixed point): a set of 15 controlled phases, one QFT step
-    # (Hadamard and its controlled phases), two QFT steps, the QFT's closing swaps; GB/s of
-    # one read and one write of the whole state
+    # (Hadamard and its controlled phases), two and three QFT steps, the QFT's closing swaps;
+    # GB/s of one read and one write of the whole state
     npairs = min(15, n // 2)
     pairs = rng.permutation(n)[:2 * npairs].reshape(npairs, 2)
     masks = (C.c_int64 * npairs)(*[(1 << int(a)) | (1 << int(b)) for a, b in pairs])
@@ -980,6 +980,8 @@ def run_gates(args, world, rank, local, dist):
                       lambda: _lib.check(L.qg_sv_qftStep(p, n, T, 0, T, None))),
                      (f"QFT steps of qubits {T} and {T - 1} in one pass",
                       lambda: _lib.check(L.qg_sv_qftTwoSteps(p, n, T, None))),
+                     (f"QFT steps of qubits {T}, {T - 1} and {T - 2} in one pass",
+                      lambda: _lib.check(L.qg_sv_qftThreeSteps(p, n, T, None))),
                      (f"QFT closing swaps ({n // 2} swaps) as one bit-reversal pass",
                       lambda: _lib.check(L.qg_sv_reverseLowBits(p, n, n, None)))):
         ms = timed(fn)
