@@ -1320,6 +1320,139 @@ def run_dm(args, world, rank, local, dist, emit=True):
     return line
 
 
+def c1_gates(nq, layers, seed, num_expec=16):
+    """The plain method (C1): `layers` x (H on every qubit; RX, RY, RZ on every qubit with
+    angles uniform in [0, 2 pi); a CNOT ladder q -> q + 1), then the total probability and
+    `num_expec` Pauli expectation values, the codes I/X/Y/Z uniform per qubit.  The same
+    draws as the parity tests' text form of this circuit."""
+    rng = np.random.default_rng(seed)
+    gates = []
+    for _ in range(layers):
+        gates += [("H", t) for t in range(nq)]
+        for t in range(nq):
+            for op in ("RX", "RY", "RZ"):
+                gates.append((op, t, float(rng.uniform(0, 2 * np.pi))))
+        gates += [("CX", t, t + 1) for t in range(nq - 1)]
+    codes = [[int(v) for v in rng.integers(0, 4, size=nq)] for _ in range(num_expec)]
+    return gates, codes
+
+
+def run_c1(args, world, rank, local, dist):
+    """The plain method (C1) at 20 qubits (16 MiB: the state fits in L2) through the
+    QuEST-named API: 10 layers of H, RX/RY/RZ on every qubit and a CNOT ladder, then
+    calcTotalProb and 16 Pauli expectation values; one step is the whole circuit from the
+    same input (a device copy), ending with the reductions (a host read).  Reports the wall
+    time per circuit, the time of each gate kind alone, and the CPU oracle on the whole
+    circuit with its results beside the GPU's."""
+    import ctypes as C
+    from quest_gb300 import _lib, api
+    from quest_gb300.api import Q
+    L = _lib.lib()
+    _lib.check(L.qg_init(local))
+    api.init_env()
+    nq = args.qubits if "--qubits" in sys.argv else 20
+    layers = args.depth if "--depth" in sys.argv else 10
+    seed = 0x5155455354 + 1
+    gates, codes = c1_gates(nq, layers, seed)
+    state = random_state(nq, seed)
+    strs = (api.PauliStr * len(codes))(*[api.pauli_str(c) for c in codes])
+    vals = (C.c_double * len(codes))()
+    nbytes = 16 << nq
+    q = Q.createQureg(nq)
+    api.set_amps(q, state)
+    src = C.c_void_p()
+    _lib.check(L.qg_alloc(C.byref(src), nbytes))
+    _lib.check(L.qg_copy_d2d(src, C.cast(q.gpuAmps, C.c_void_p), nbytes, None))
+
+    def apply(g):
+        if g[0] == "H":
+            Q.applyHadamard(q, g[1])
+        elif g[0] == "RX":
+            Q.applyRotateX(q, g[1], g[2])
+        elif g[0] == "RY":
+            Q.applyRotateY(q, g[1], g[2])
+        elif g[0] == "RZ":
+            Q.applyRotateZ(q, g[1], g[2])
+        else:
+            Q.applyControlledPauliX(q, g[1], g[2])
+
+    def step():
+        _lib.check(L.qg_copy_d2d(C.cast(q.gpuAmps, C.c_void_p), src, nbytes, None))
+        for g in gates:
+            apply(g)
+        prob = Q.calcTotalProb(q)
+        Q.calcExpecPauliStrs(vals, q, strs, len(codes))
+        return prob
+
+    for _ in range(args.warmup):
+        step()
+    L.qg_sync()
+    launches0 = C.c_int64(0)
+    L.qg_get_launch_count(C.byref(launches0))
+    with ClockSampler(local) as clocks:
+        barrier(dist)
+        L.qg_sync()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            prob = step()
+        L.qg_sync()
+        wall = max_over_ranks(dist, time.perf_counter() - t0)
+        barrier(dist)
+    launches1 = C.c_int64(0)
+    L.qg_get_launch_count(C.byref(launches1))
+    got = [prob] + list(vals)
+    # each gate kind alone: 20 calls, then flushQuregDeferredOps (deferred kinds are applied there)
+    e0, e1, ms = C.c_void_p(), C.c_void_p(), C.c_float(0)
+    L.qg_event_create(C.byref(e0))
+    L.qg_event_create(C.byref(e1))
+    per_kind = {}
+    amp_bytes = {"H": 2 * nbytes, "RX": 2 * nbytes, "RY": 2 * nbytes, "RZ": 2 * nbytes, "CX": nbytes}
+    for kind in ("H", "RX", "RY", "RZ", "CX"):
+        sample = [g for g in gates if g[0] == kind][:20]
+        L.qg_sync()
+        L.qg_event_record(e0, None)
+        for g in sample:
+            apply(g)
+        Q.flushQuregDeferredOps(q)
+        L.qg_event_record(e1, None)
+        L.qg_event_elapsed_ms(e0, e1, C.byref(ms))
+        per = ms.value / len(sample)
+        per_kind[kind] = {"ms_per_gate": round(per, 5), "gbs": round(amp_bytes[kind] / per / 1e6, 1)}
+    Q.destroyQureg(q)
+    L.qg_free(src)
+    alg_bytes = sum(amp_bytes[g[0]] for g in gates) + nbytes * (1 + len(codes))
+    cpu = None
+    if rank == 0 and args.cpu_sample > 0:
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import qcircuits as qc
+        text = qc.config1_circuit(nq, layers, seed, len(codes))
+        orc = qc.oracle()
+        threads = host_threads()
+        orc.lib.orc_set_num_threads(threads)
+        t0 = time.perf_counter()
+        _, want, _ = orc.run(text, nq, 0, state)
+        secs = time.perf_counter() - t0
+        cpu = {"value": round(secs * 1e3, 2), "unit": "ms per circuit", "cores": threads, "kind": "port",
+               "sample": f"the whole circuit ({len(gates)} gates and {1 + len(codes)} reductions) on {threads} host "
+                         f"threads with the OpenMP oracle",
+               "max_abs_diff_of_results": float(np.max(np.abs(np.array(got) - np.array(want[:len(got)]))))}
+    line = {"metric": "plain method (C1): wall time per 20-qubit circuit", "value": round(wall / args.steps * 1e3, 3),
+            "unit": "ms per circuit", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(wall / args.steps * 1e3, 3), "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64 (storage; products in block-floating fixed point, one-qubit gates deferred)",
+            "data": "synthetic (seeded Gaussian state, seeded angles and Pauli codes)",
+            "config": {"workload": f"{nq}-qubit FP64 statevector, {layers} x (H on every qubit, RX/RY/RZ on every "
+                                   f"qubit, CNOT ladder), then calcTotalProb and {len(codes)} Pauli expectations",
+                       "qubits": nq, "layers": layers, "gates": len(gates),
+                       "l2": "the 16 MiB state fits in L2 (no flush: the reference's own size)",
+                       "start": "each step from a device copy of the input state; wall time includes the host reads of the results"},
+            "algorithmic_gbs": round(alg_bytes * args.steps / wall / 1e9, 1), "per_gate_kind": per_kind,
+            "gpu_launches": int(launches1.value - launches0.value), "results": got[:3],
+            "cpu_baseline": cpu, "clocks": clocks.summary()}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def run_blocks(args, world, rank, local, dist):
     """Per-target-set timing of one fused 5-qubit block on an FP32 register through the
     tensor-core kernel (`Circuit` API, impl = tc): ms per apply from CUDA events over
@@ -1396,11 +1529,12 @@ def main():
     ap.add_argument("--depth", type=int, default=20)
     ap.add_argument("--cpu-sample", type=int, default=45, help="gates of the circuit timed on the host CPU")
     ap.add_argument("--traffic", type=float, default=None, help="ncu DRAM bytes per dense launch, if captured")
-    ap.add_argument("--config", default="plain", choices=["plain", "precision", "serve", "gates", "blocks", "expec", "dm"],
+    ap.add_argument("--config", default="plain", choices=["plain", "precision", "serve", "gates", "blocks", "expec", "dm", "c1"],
                     help="plain: the 30-qubit FP64 per-gate circuit (default); precision: FP32 fused blocks; "
                          "serve: request stream, served vs plain; gates: per-gate-kind timing (28 qubits); "
                          "blocks: one FP32 5-qubit block per target set; expec: 16 Pauli strings per call (28 qubits); "
-                         "dm: the density-matrix method (14-qubit density matrix, 30 layers)")
+                         "dm: the density-matrix method (14-qubit density matrix, 30 layers); "
+                         "c1: the plain method (20 qubits, 10 layers, reductions) as wall time per circuit")
     ap.add_argument("--block-targets", default="", help="blocks: target sets, e.g. '0,1,2,3,4;5,6,7,8,9'")
     ap.add_argument("--requests", type=int, default=48)
     ap.add_argument("--min-qubits", type=int, default=8)
@@ -1425,6 +1559,8 @@ def main():
         run_blocks(args, world, rank, local, dist)
     elif args.config == "expec":
         run_expec(args, world, rank, local, dist)
+    elif args.config == "c1":
+        run_c1(args, world, rank, local, dist)
     elif args.config == "dm":
         args.dm_qubits = args.qubits if "--qubits" in sys.argv else 14
         args.dm_layers = args.depth if "--depth" in sys.argv else 30

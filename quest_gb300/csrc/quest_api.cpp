@@ -1363,9 +1363,23 @@ void applyMultiStateControlledPauliGadget(Qureg q, int* c, int* s, int nc, Pauli
 }
 void applyPauliGadget(Qureg q, PauliStr str, qreal angle) { applyMultiStateControlledPauliGadget(q, nullptr, nullptr, 0, str, angle); }
 
-void applyRotateX(Qureg q, int t, qreal a) { if (!checkQureg(q, "applyRotateX") || !checkQubits(q, &t, 1, "applyRotateX", "target qubits")) return; int p = 1; applyPauliGadget(q, getPauliStrFromCodes(&p, &t, 1), a); }
-void applyRotateY(Qureg q, int t, qreal a) { if (!checkQureg(q, "applyRotateY") || !checkQubits(q, &t, 1, "applyRotateY", "target qubits")) return; int p = 2; applyPauliGadget(q, getPauliStrFromCodes(&p, &t, 1), a); }
-void applyRotateZ(Qureg q, int t, qreal a) { if (!checkQureg(q, "applyRotateZ") || !checkQubits(q, &t, 1, "applyRotateZ", "target qubits")) return; int p = 3; applyPauliGadget(q, getPauliStrFromCodes(&p, &t, 1), a); }
+// A one-target rotation exp(-i angle/2 P) (operations.cpp:1283-1310: a Pauli gadget) as its
+// 2x2 unitary through applyDense where one-qubit gates are deferred -- statevectors that
+// defer them, and density matrices -- so that it joins the qubit's pending unitary (or
+// superoperator) instead of taking a pass of its own.  False where the gadget applies.
+bool rotationDeferred(const Qureg& q, int t, qreal a, int pauli, const char* func) {
+    if (!(q.isDensityMatrix ? q.gpuAmps != nullptr : deferSV(q))) return false;
+    const double c = std::cos(a / 2), s = std::sin(a / 2);
+    qcomp_t m[4];
+    if (pauli == 1) { m[0] = {c, 0}; m[1] = {0, -s}; m[2] = {0, -s}; m[3] = {c, 0}; }
+    else if (pauli == 2) { m[0] = {c, 0}; m[1] = {-s, 0}; m[2] = {s, 0}; m[3] = {c, 0}; }
+    else { m[0] = {c, -s}; m[1] = {0, 0}; m[2] = {0, 0}; m[3] = {c, s}; }
+    applyDense(q, nullptr, nullptr, 0, &t, 1, m, false, func);
+    return true;
+}
+void applyRotateX(Qureg q, int t, qreal a) { if (rotationDeferred(q, t, a, 1, "applyRotateX")) return; if (!checkQureg(q, "applyRotateX") || !checkQubits(q, &t, 1, "applyRotateX", "target qubits")) return; int p = 1; applyPauliGadget(q, getPauliStrFromCodes(&p, &t, 1), a); }
+void applyRotateY(Qureg q, int t, qreal a) { if (rotationDeferred(q, t, a, 2, "applyRotateY")) return; if (!checkQureg(q, "applyRotateY") || !checkQubits(q, &t, 1, "applyRotateY", "target qubits")) return; int p = 2; applyPauliGadget(q, getPauliStrFromCodes(&p, &t, 1), a); }
+void applyRotateZ(Qureg q, int t, qreal a) { if (rotationDeferred(q, t, a, 3, "applyRotateZ")) return; if (!checkQureg(q, "applyRotateZ") || !checkQubits(q, &t, 1, "applyRotateZ", "target qubits")) return; int p = 3; applyPauliGadget(q, getPauliStrFromCodes(&p, &t, 1), a); }
 void applyControlledRotateX(Qureg q, int c, int t, qreal a) { if (!checkQureg(q, "applyControlledRotateX") || !checkCtrlsTargs(q, &c, 1, &t, 1, "applyControlledRotateX")) return; int p = 1; applyMultiStateControlledPauliGadget(q, &c, nullptr, 1, getPauliStrFromCodes(&p, &t, 1), a); }
 void applyControlledRotateY(Qureg q, int c, int t, qreal a) { if (!checkQureg(q, "applyControlledRotateY") || !checkCtrlsTargs(q, &c, 1, &t, 1, "applyControlledRotateY")) return; int p = 2; applyMultiStateControlledPauliGadget(q, &c, nullptr, 1, getPauliStrFromCodes(&p, &t, 1), a); }
 void applyControlledRotateZ(Qureg q, int c, int t, qreal a) { if (!checkQureg(q, "applyControlledRotateZ") || !checkCtrlsTargs(q, &c, 1, &t, 1, "applyControlledRotateZ")) return; int p = 3; applyMultiStateControlledPauliGadget(q, &c, nullptr, 1, getPauliStrFromCodes(&p, &t, 1), a); }
