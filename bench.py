@@ -549,7 +549,7 @@ def extras_summary(args, world, rank, local, dist):
         sl = run_serve(sa, world, rank, local, dist, emit=False)
         serving = {"requests": sa.requests, "data": sl["data"], "saturation": sl["saturation"],
                    "poisson": sl["poisson"], "max_abs_expec_err_served_vs_fp64": sl["max_abs_expec_err_served_vs_fp64"],
-                   "plain_registers": sl["plain_registers"]}
+                   "plain_registers": sl["plain_registers"], "plain_path": sl["plain_path"]}
     except Exception as e:          # noqa: BLE001
         serving = {"error": f"{type(e).__name__}: {e}"}
     try:
@@ -776,6 +776,15 @@ def run_serve(args, world, rank, local, dist, emit=True):
         plain_regs[n] = Q.createQureg(n)
 
     def plain_one(n, ops, codes):
+        # per gate: the API's deferral of one-qubit gates into tensor-core passes is off
+        # for this arm (it follows the tensor-slice switch), so every gate is one pass
+        _lib.check(L.qg_set_tensor_slices(0))
+        try:
+            return plain_gates(n, ops, codes)
+        finally:
+            _lib.check(L.qg_set_tensor_slices(1))
+
+    def plain_gates(n, ops, codes):
         q = plain_regs[n]
         Q.initZeroState(q)
         for op in ops:
@@ -882,7 +891,8 @@ def run_serve(args, world, rank, local, dist, emit=True):
                         "served_p50_ms": round(pct(lat_s, 50), 2), "served_p99_ms": round(pct(lat_s, 99), 2),
                         "plain_p50_ms": round(pct(lat_p, 50), 2), "plain_p99_ms": round(pct(lat_p, 99), 2)},
             "max_abs_expec_err_served_vs_fp64": err,
-            "plain_registers": "one pre-created register per qubit count, reset to |0> per request"}
+            "plain_registers": "one pre-created register per qubit count, reset to |0> per request",
+            "plain_path": "one pass per gate (fixed-point FP64 products; the API's deferral of one-qubit gates off)"}
     for r in plain_regs.values():
         Q.destroyQureg(r)
     if rank == 0 and emit:
@@ -1522,7 +1532,7 @@ def run_blocks(args, world, rank, local, dist):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--qubits", type=int, default=30)
