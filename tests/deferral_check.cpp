@@ -2,9 +2,14 @@
 // the API file is compiled here with the pass kernels it calls replaced by plain CPU loops
 // (one-, two- and k-target dense matrices, phase sets), and random layers of one-qubit
 // unitaries (on every qubit, or on a subset), two-qubit phase shifts on disjoint pairs (or on
-// a few pairs), three-qubit and one-qubit phase shifts, on 8 to 14 qubits, go through the
-// public calls (applyCompMatr1, applyTwoQubitPhaseShift, applyMultiQubitPhaseShift,
-// applyPhaseShift, flushQuregDeferredOps).  The state must equal the gate-by-gate product to
+// a few pairs), one-target rotations, three-qubit and one-qubit phase shifts, on 8 to 14
+// qubits, go through the public calls (applyCompMatr1, applyRotateX/Y/Z,
+// applyTwoQubitPhaseShift, applyMultiQubitPhaseShift, applyPhaseShift,
+// flushQuregDeferredOps); and random sequences of one- and two-qubit unitaries,
+// depolarising and two-qubit Kraus maps on density matrices of 3 to 6 qubits (one-qubit
+// operations deferred per qubit, two-qubit ones taking their qubits' pending
+// superoperators into their own pass) against the Choi-vector product, in fewer passes
+// than operations.  The state must equal the gate-by-gate product to
 // 1e-12 of its largest amplitude, and the circuits shaped like the benchmark layers (a gate
 // on every qubit, phases on disjoint pairs covering all of them) must take no phase pass and
 // ceil(n / 4) passes per layer, the last partial group staying pending to the next layer
@@ -51,6 +56,15 @@ int qg_sv_anyCtrlAnyTargDenseMatr(void* amps, int n, const int*, const int*, int
     if (nc || conj) { printf("FAIL: unexpected controls\n"); exit(2); }
     g_passes++; applyK((cx*)amps, n, t, k, (const qcomp_t*)m); return 0;
 }
+int qg_dm_oneQubitDepolarising(void* amps, int numKet, int qubit, double p, void*) {
+    g_passes++;
+    const double c1 = 1 - 2 * p / 3, c2 = 2 * p / 3, c3 = 1 - 4 * p / 3;
+    qcomp_t S[16] = {};
+    S[0] = {c1, 0}; S[3] = {c2, 0}; S[5] = {c3, 0}; S[10] = {c3, 0}; S[12] = {c2, 0}; S[15] = {c1, 0};
+    const int t[2] = {qubit, qubit + numKet};
+    applyK((cx*)amps, 2 * numKet, t, 2, S);
+    return 0;
+}
 int qg_sv_phaseSet(void* amps, int n, const int64_t* masks, const qg_cplx* f, int num, void*) {
     g_passes++; g_phasePasses++;
     cx* a = (cx*)amps;
@@ -93,6 +107,16 @@ int main() {
                 qcomp_t mm[4] = {m.elems[0][0], m.elems[0][1], m.elems[1][0], m.elems[1][1]};
                 applyK(ref.data(), n, &t, 1, mm);
                 gates++;
+                if (trial % 2 == 0 && (g() % 2)) {     // a rotation after it: joins the pending unitary
+                    const int kind = (int)(g() % 3);
+                    const double th = nd(g), c = std::cos(th / 2), sn = std::sin(th / 2);
+                    qcomp_t r[4];
+                    if (kind == 0) { applyRotateX(q, t, th); r[0] = {c, 0}; r[1] = {0, -sn}; r[2] = {0, -sn}; r[3] = {c, 0}; }
+                    else if (kind == 1) { applyRotateY(q, t, th); r[0] = {c, 0}; r[1] = {-sn, 0}; r[2] = {sn, 0}; r[3] = {c, 0}; }
+                    else { applyRotateZ(q, t, th); r[0] = {c, -sn}; r[1] = {0, 0}; r[2] = {0, 0}; r[3] = {c, sn}; }
+                    applyK(ref.data(), n, &t, 1, r);
+                    gates++;
+                }
             }
             // phases: disjoint pairs, sometimes a 3-qubit one and a single
             std::vector<int> perm(n);
@@ -139,6 +163,103 @@ int main() {
         if (!ok) bad++;
         printf("n=%2d trial=%2d gates=%lld passes=%ld (phase passes %ld) err/max=%.2e %s\n", n, trial, gates, g_passes, g_phasePasses, err / mx, ok ? "" : "FAIL");
     }
-    printf("%s %d circuits\n", bad ? "FAIL" : "OK", 40);
+    // density matrices: one-qubit unitaries and depolarising deferred per qubit, two-qubit
+    // unitaries and Kraus maps taking their qubits' pending superoperators into their pass
+    auto haar2 = [&](int D, std::vector<cx>& u) {     // a random D x D unitary (Gram-Schmidt)
+        u.assign(D * D, 0);
+        for (auto& z : u) z = cx(nd(g), nd(g));
+        for (int c = 0; c < D; c++) {
+            for (int p_ = 0; p_ < c; p_++) {
+                cx dot = 0;
+                for (int r = 0; r < D; r++) dot += std::conj(u[r * D + p_]) * u[r * D + c];
+                for (int r = 0; r < D; r++) u[r * D + c] -= dot * u[r * D + p_];
+            }
+            double nr = 0;
+            for (int r = 0; r < D; r++) nr += std::norm(u[r * D + c]);
+            for (int r = 0; r < D; r++) u[r * D + c] /= std::sqrt(nr);
+        }
+    };
+    auto onKetBra = [&](std::vector<cx>& v, int nk, const std::vector<int>& t, const std::vector<cx>& u) {
+        const int k = (int)t.size(), D = 1 << k;
+        std::vector<qcomp_t> m(D * D), mc(D * D);
+        for (int i = 0; i < D * D; i++) { m[i] = {u[i].real(), u[i].imag()}; mc[i] = {u[i].real(), -u[i].imag()}; }
+        std::vector<int> tb(t);
+        for (auto& x : tb) x += nk;
+        applyK(v.data(), 2 * nk, t.data(), k, m.data());
+        applyK(v.data(), 2 * nk, tb.data(), k, mc.data());
+    };
+    int dmBad = 0;
+    for (int trial = 0; trial < 12; trial++) {
+        const int nk = 3 + trial % 4;                // 3..6 qubits: Choi vectors of 6..12 qubits
+        const long long NA = 1LL << (2 * nk);
+        std::vector<cx> st(NA), ref;
+        for (auto& v : st) v = cx(nd(g), nd(g));
+        ref = st;
+        Qureg q{};
+        q.numQubits = nk; q.isDensityMatrix = 1; q.numAmps = NA; q.gpuAmps = (qcomp_t*)st.data();
+        g_passes = 0;
+        int ops = 0;
+        for (int step = 0; step < 40; step++) {
+            const int kind = (int)(g() % 4), a = (int)(g() % nk);
+            int b = (int)(g() % (nk - 1));
+            if (b >= a) b++;
+            std::vector<cx> u;
+            if (kind == 0) {
+                haar2(2, u);
+                CompMatr1 m{};
+                m.numQubits = 1; m.numRows = 2;
+                for (int i = 0; i < 4; i++) m.elems[i / 2][i % 2] = {u[i].real(), u[i].imag()};
+                applyCompMatr1(q, a, m);
+                onKetBra(ref, nk, {a}, u);
+            } else if (kind == 1) {
+                const double p = 0.3 * std::fabs(nd(g)) / 3;
+                mixDepolarising(q, a, p > 0.7 ? 0.7 : p);
+                const double pp = p > 0.7 ? 0.7 : p, c1 = 1 - 2 * pp / 3, c2 = 2 * pp / 3, c3 = 1 - 4 * pp / 3;
+                qcomp_t S[16] = {};
+                S[0] = {c1, 0}; S[3] = {c2, 0}; S[5] = {c3, 0}; S[10] = {c3, 0}; S[12] = {c2, 0}; S[15] = {c1, 0};
+                const int t[2] = {a, a + nk};
+                applyK(ref.data(), 2 * nk, t, 2, S);
+            } else if (kind == 2) {
+                haar2(4, u);
+                CompMatr2 m{};
+                m.numQubits = 2; m.numRows = 4;
+                for (int i = 0; i < 16; i++) m.elems[i / 4][i % 4] = {u[i].real(), u[i].imag()};
+                applyCompMatr2(q, a, b, m);
+                onKetBra(ref, nk, {a, b}, u);
+            } else {
+                // K0 = sqrt(1 - p) Ua, K1 = sqrt(p) Ub: completely positive and trace preserving
+                std::vector<cx> ua, ub;
+                haar2(4, ua);
+                haar2(4, ub);
+                const double p = 0.25;
+                std::vector<qcomp_t> flat(32);
+                for (int i = 0; i < 16; i++) {
+                    const cx x = std::sqrt(1 - p) * ua[i], y = std::sqrt(p) * ub[i];
+                    flat[i] = {x.real(), x.imag()};
+                    flat[16 + i] = {y.real(), y.imag()};
+                }
+                KrausMap km = createKrausMap(2, 2);
+                setKrausMapFlat(km, flat.data());
+                int tq[2] = {a, b};
+                mixKrausMap(q, tq, 2, km);
+                destroyKrausMap(km);
+                std::vector<cx> r0 = ref, r1 = ref;
+                std::vector<cx> k0(16), k1(16);
+                for (int i = 0; i < 16; i++) { k0[i] = std::sqrt(1 - p) * ua[i]; k1[i] = std::sqrt(p) * ub[i]; }
+                onKetBra(r0, nk, {a, b}, k0);
+                onKetBra(r1, nk, {a, b}, k1);
+                for (long long i = 0; i < NA; i++) ref[i] = r0[i] + r1[i];
+            }
+            ops++;
+        }
+        flushQuregDeferredOps(q);
+        double err = 0, mx = 0;
+        for (long long i = 0; i < NA; i++) { err = std::max(err, std::abs(st[i] - ref[i])); mx = std::max(mx, std::abs(ref[i])); }
+        const bool ok = err <= 1e-12 * mx && g_passes < ops;
+        if (!ok) dmBad++;
+        printf("dm n=%d trial=%2d ops=%d passes=%ld err/max=%.2e %s\n", nk, trial, ops, g_passes, err / mx, ok ? "" : "FAIL");
+    }
+    bad += dmBad;
+    printf("%s %d circuits\n", bad ? "FAIL" : "OK", 52);
     return bad != 0;
 }
