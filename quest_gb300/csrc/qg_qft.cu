@@ -380,34 +380,50 @@ __device__ __noinline__ void qft_three_flies_fp64(double2* __restrict__ p, qidx 
 }
 
 // The octet at p (amplitude o = 4p + 2q + r at p + o * quarter), its values already in v:
-// the three steps in fixed point, written back; with twiddles W, W omega, V, U.  An octet
-// that needs FP64 goes to qft_three_flies_fp64, which reads it again.
+// the three steps in fixed point, written back; with twiddles W, W omega, V, U.  The
+// octet's sixteen reals share one scale, the largest exponent among them (block floating
+// point over the octet: each output's error is a few units of 2^-56 of the octet's largest
+// |amplitude|), so they are converted once and every butterfly runs on integers.  An octet
+// that needs FP64 (Inf/NaN, or scales near the ends of the range) goes to
+// qft_three_flies_fp64, which reads it again.
 __device__ __forceinline__ void qft_three_flies(double2* __restrict__ p, qidx quarter, const double2 (&v)[8], long long w0r,
                                                 long long w0i, long long w1r, long long w1i, long long vr, long long vi,
                                                 long long ur, long long ui) {
-    long long y[4][4];
-    int e[4];
-    bool ok = true;
+    int eb = 1;
+    uint64_t any = 0;
 #pragma unroll
-    for (int qr = 0; qr < 4; qr++) {
-        const int q = qr >> 1, r = qr & 1;
-        const long long wr = r ? w1r : w0r, wi = r ? w1i : w0i;
-        ok = qft_fly_fx(v[qr], v[4 + qr], q ? -wi : wr, q ? wr : wi, y[qr], e[qr]) && ok;
+    for (int o = 0; o < 8; o++) {
+        const uint64_t ux = qgfx::f64_bits(v[o].x), uy = qgfx::f64_bits(v[o].y);
+        const int ex = (int)((ux >> 52) & 0x7FF), ey = (int)((uy >> 52) & 0x7FF);
+        eb = max(eb, max(ex + (ex == 0), ey + (ey == 0)));
+        any |= (ux << 1) | (uy << 1);
     }
-    const int em = max(max(e[0], e[1]), max(e[2], e[3]));
-    if (!ok || em > 2041) {
+    if (any == 0) {
+#pragma unroll
+        for (int o = 0; o < 8; o++) st_amp(p + o * quarter, make_double2(0.0, 0.0));
+        return;
+    }
+    if (eb < 58 || eb > 2040) {
         qft_three_flies_fp64(p, quarter, w0r, w0i, w1r, w1i, vr, vi, ur, ui);
         return;
     }
-    // z[4p + 2q + r] (re, im) at scale em
+    // z[4p + 2q + r] (re, im), values x 2^(1082 - eb) below 2^60
     long long z[8][2];
 #pragma unroll
-    for (int qr = 0; qr < 4; qr++) {
-        const int sh = em - e[qr];
-        z[qr][0] = qft_align(y[qr][0], sh);
-        z[qr][1] = qft_align(y[qr][1], sh);
-        z[4 + qr][0] = qft_align(y[qr][2], sh);
-        z[4 + qr][1] = qft_align(y[qr][3], sh);
+    for (int o = 0; o < 8; o++) {
+        z[o][0] = qft_fixed(qgfx::f64_bits(v[o].x), eb);
+        z[o][1] = qft_fixed(qgfx::f64_bits(v[o].y), eb);
+    }
+#pragma unroll
+    for (int qr = 0; qr < 4; qr++) {        // step T: pairs (0qr, 1qr), twiddle W omega^r i^q
+        const int q = qr >> 1, r = qr & 1;
+        const long long wr = r ? w1r : w0r, wi = r ? w1i : w0i;
+        long long out[4];
+        qft_fly_int(z[qr][0], z[qr][1], z[4 + qr][0], z[4 + qr][1], q ? -wi : wr, q ? wr : wi, out);
+        z[qr][0] = out[0];
+        z[qr][1] = out[1];
+        z[4 + qr][0] = out[2];
+        z[4 + qr][1] = out[3];
     }
 #pragma unroll
     for (int pr = 0; pr < 4; pr++) {        // step T - 1: pairs (p0r, p1r), twiddle V i^r
@@ -419,7 +435,7 @@ __device__ __forceinline__ void qft_three_flies(double2* __restrict__ p, qidx qu
         z[o + 2][0] = out[2];
         z[o + 2][1] = out[3];
     }
-    const int t = em - 1076;
+    const int t = eb - 1076;                 // value = z 2^(eb - 1076) after three steps (2^-2 each)
 #pragma unroll
     for (int pq = 0; pq < 4; pq++) {        // step T - 2: pairs (pq0, pq1), twiddle U
         long long out[4];
