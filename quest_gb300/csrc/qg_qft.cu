@@ -1,4 +1,4 @@
-// One step of the quantum Fourier transform on a statevector as one pass: the Hadamard on
+// Steps of the quantum Fourier transform on a statevector in one pass: the Hadamard on
 // target t followed by its controlled phases.  QuEST's applyQuantumFourierTransform
 // (quest/src/api/operations.cpp:1934-1952) applies, for each target t[n] from the top,
 // applyHadamard(t[n]) and then applyTwoQubitPhaseShift(t[n], t[n-m-1], pi / 2^(m+1)) for
@@ -12,11 +12,18 @@
 // Products in 60-bit block-floating fixed point on the integer pipes (as the one-target
 // kernels of qg_fixed.cuh; GB300's FP64 rate would bound the twiddle products): the pair's
 // four reals share the largest exponent and become integers below 2^60, sums and
-// differences are exact, the twiddle w^L / sqrt2 is the product of four tables of 256
-// values at scale 2^62 (indices: the four bytes of L), and each output is the top 64 bits
+// differences are exact, the twiddle w^L / sqrt2 is the product of up to five tables of
+// 256 values at scale 2^62 (indices: the bytes of L), and each output is the top 64 bits
 // of its products (from 32-bit limbs), converted to double with the scale added to the
-// exponent field.  Error per output: a few units of 2^-57 of the pair's largest |amplitude|.  Pairs holding
-// Inf/NaN or with scales near the ends of the double range are evaluated in FP64.
+// exponent field.  Error per output: a few units of 2^-57 of the pair's largest
+// |amplitude|.  Pairs holding Inf/NaN or with scales near the ends of the double range
+// are evaluated in FP64.
+//
+// Targets from qubit 0 take two or three steps per pass (k_qft_two_steps_*,
+// k_qft_three_steps_*): a thread holds the 4 or 8 amplitudes that differ in the steps'
+// target bits, every twiddle of the steps comes from the first step's tables, and the
+// values stay in fixed point between the steps.  The transform's closing swaps on qubits
+// 0..n-1 are one in-place bit-reversal pass (k_reverse_low_bits).
 //
 // The same fixed-point steps apply a set of controlled phases in one pass (k_phase_set):
 // phase gates commute, so the API defers them (diagonal gates whose only factor != 1 is on
