@@ -114,11 +114,8 @@ bool applyPendingOp(const Qureg& q, int qubit, const PendingOp& op, const char* 
         case PEND_DEPHASE: return backend(qg_dm_oneQubitDephasing(q.gpuAmps, N, qubit, op.p[0], g_stream), func);
         case PEND_DAMP: return backend(qg_dm_oneQubitDamping(q.gpuAmps, N, qubit, op.p[0], g_stream), func);
         case PEND_PAULIS: return backend(qg_dm_oneQubitPauliChannel(q.gpuAmps, N, qubit, op.p[0], op.p[1], op.p[2], g_stream), func);
-        case PEND_SV: {
-            const qcomp_t k[4] = {qcomp_t{op.m[0].real(), op.m[0].imag()}, qcomp_t{op.m[1].real(), op.m[1].imag()},
-                                  qcomp_t{op.m[2].real(), op.m[2].imag()}, qcomp_t{op.m[3].real(), op.m[3].imag()}};
-            return backend(qg_sv_anyCtrlOneTargDenseMatr(q.gpuAmps, N, nullptr, nullptr, 0, qubit, k, g_stream), func);
-        }
+        case PEND_SV:       // statevector ops are applied in groups (applySVUnits), never here
+            return check(false, func, "Internal error: a statevector's pending gate reached the density-matrix path.");
         default: {
             qcomp_t k[16];
             for (int i = 0; i < 16; i++) k[i] = qcomp_t{op.m[i].real(), op.m[i].imag()};
