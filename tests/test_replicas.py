@@ -72,3 +72,37 @@ def test_reference_arm_runs_on_rank_zero_only(capsys):
 
     b.run_reference(Args, 2, 1, None)        # rank 1 of 2: no work, no output
     assert capsys.readouterr().out == ""
+
+
+def test_benchmark_circuits_match_the_parity_tests():
+    """The circuits bench.py times are the ones the parity tests hold against the oracle:
+    the plain method (c1) draws the same angles and Pauli codes as the tests' text form
+    (and its CPU baseline runs that text), and the 30-qubit circuit has the stated
+    1380 gates (600 Haar 2x2, 300 controlled phases on disjoint pairs, the QFT)."""
+    import numpy as np
+    import qcircuits as qc
+    b = _bench()
+    nq, layers, seed = 20, 10, 0x5155455354 + 1
+    gates, codes = b.c1_gates(nq, layers, seed)
+    text = qc.config1_circuit(nq, layers, seed, len(codes)).splitlines()
+    ops = [l.split() for l in text]
+    gate_lines = [o for o in ops if o[0] in ("H", "RX", "RY", "RZ", "CX")]
+    assert len(gate_lines) == len(gates) == layers * (nq + 3 * nq + nq - 1)
+    for g, o in zip(gates, gate_lines):
+        assert g[0] == o[0] and g[1] == int(o[1])
+        if g[0] in ("RX", "RY", "RZ"):
+            assert g[2] == float(o[2])
+        if g[0] == "CX":
+            assert g[2] == int(o[2])
+    expec = [o for o in ops if o[0] == "EXPEC"]
+    assert [qc.pauli_text(c) for c in codes] == [o[1] for o in expec]
+    circ = b.make_circuit(30, 20, 7)
+    assert b.num_gates(circ, 30) == 1380
+    us = [g for g in circ if g[0] == "U"]
+    cps = [g for g in circ if g[0] == "CP"]
+    assert len(us) == 600 and len(cps) == 300 and circ[-1] == ("QFT",)
+    for layer in range(20):
+        pairs = cps[15 * layer:15 * layer + 15]
+        qubits = [q for g in pairs for q in g[1:3]]
+        assert len(set(qubits)) == 30                      # disjoint pairs covering every qubit
+        assert all(np.allclose(u[2] @ u[2].conj().T, np.eye(2)) for u in us[30 * layer:30 * layer + 30])
